@@ -1,0 +1,343 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 scattering-amplitude hot path (one JSON line on rank 0).
+
+Workload (default): coherent dynamic S(q,t) — 10,000 atoms in a 50 A box, 1,024 frames of
+Gaussian random walk (sigma 0.05 A) with a harmonic pull (RMSD ~1 A), H/C/N/O/S coherent
+lengths, 20 shells 0.05-3.0 1/A x 500 directions, FFT autocorrelation (padded length
+2,048). Seeded synthetic data. A "step" is the whole computation: phase sum over
+1.024e11 atom.q.frame terms, correlation, orientational average.
+
+  value      terms/s of the chosen (FP32) path, inputs resident in HBM, CUDA events on
+             the plan's stream (coordinates 164 MB > 129 MB L2: inputs larger than L2).
+  e2e        the same through the C ABI with host buffers: pinned host coordinates,
+             sub-vectors and factors copied in and S(q,t)/fq/fq2 copied out every step.
+  roofline   phase-sum kernel: terms/s against the SFU ceiling measured live by
+             sass_probe_pipes (2 SFU results per term), and FP32 FMA rate for reference.
+  plain      the plain FP64 path on the same GPU (same terms), its time, and the FP32
+             path's max relative error in S(q,t) against it (time-to-1e-3 comparison).
+  cpu_baseline  the CPU oracle (FP64 restatement of the reference, all host threads) on
+             a bounded sample of the same workload.
+
+--impl reference times that CPU restatement (the reference itself cannot be built:
+MPI, Boost, FFTW3, HDF5 and libxml2 are absent) and prints its own line.
+Multi-GPU: replicas only — every rank runs the full workload on its own GPU (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "atom*q*frame terms/s; time to 1e-3 rel err in S(q,t), chosen vs plain, same GPU"
+UNIT = "terms/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="coherent_sqt")
+    ap.add_argument("--plain-shells", type=int, default=2,
+                    help="shells of the plain FP64 comparison run (time scaled by terms)")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    return ap.parse_args()
+
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x):
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region (median SM clock, throttle reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(name):
+    from sassena_gb300 import synth
+    return synth.WORKLOADS[name]()
+
+
+def cpu_sample(w, seconds, nthreads):
+    """Time the oracle on one shell x m directions (m grown until ~`seconds`)."""
+    import oracle
+    s = w.nq // 2
+    m = 1
+    fac = w.factors()[s:s + 1]
+    while True:
+        sv = w.shells[s] * w.directions[:m]
+        offs = np.array([0, m], dtype=np.uintp)
+        t0 = time.perf_counter()
+        oracle.all_vectors(w.coords, offs, sv, fac, 0, 0, nthreads) if w.scattering == "all" \
+            else oracle.self_vectors(w.coords, offs, sv, fac, 0, 0, nthreads)
+        dt = time.perf_counter() - t0
+        terms = w.na * m * w.nf
+        if dt >= seconds * 0.4 or m >= w.nm:
+            return {"value": terms / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+                    "sample": "oracle (FP64 restatement) on shell %d/%d x %d of %d directions, "
+                              "all %d atoms x %d frames (%.3g terms, %.1f s)"
+                              % (s, w.nq, m, w.nm, w.na, w.nf, terms, dt)}
+        m = min(w.nm, max(m * 2, int(m * seconds * 0.6 / max(dt, 1e-3))))
+
+
+def run_reference(args, dist):
+    if dist.rank != 0:
+        return
+    w = make_workload(args.workload)
+    nthreads = os.cpu_count() or 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(w, args.cpu_seconds / max(1, args.steps), nthreads)
+        if i >= args.warmup:
+            vals.append(r["value"])
+    v = statistics.median(vals)
+    cfg = {"workload": args.workload, "na": w.na, "nf": w.nf, "nq": w.nq, "nm": w.nm,
+           "terms_per_step": w.terms(), "dsp": w.dsp, "scattering": w.scattering}
+    print(json.dumps({"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT,
+                      "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": w.terms() / v * 1e3, "higher_is_better": True,
+                      "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                      "data": "synthetic (seeded)", "config": cfg,
+                      "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads,
+                                       "kind": "port", "sample": r["sample"]},
+                      "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0},
+                      "note": "reference unbuildable here (MPI/Boost/FFTW3/HDF5/libxml2 absent);"
+                              " timed its CPU restatement, ms_per_step extrapolated by terms"}))
+
+
+def run_ours(args, dist):
+    import torch
+
+    from sassena_gb300 import abi
+
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    w = make_workload(args.workload)
+    stream = torch.cuda.current_stream()
+    nclass = len(w.class_names)
+    terms = w.terms()
+    plan = abi.Plan(w.na, w.nf, nclass, w.scattering, w.dsp, "fftw", "fp32", device=dev,
+                    stream=stream.cuda_stream)
+    plan.stage(w.coords)
+    plan.set_classes(w.atom_class)
+    offs = w.sub_offsets()
+    sv = torch.from_numpy(w.subvectors()).cuda()
+    cf = torch.from_numpy(np.ascontiguousarray(w.class_factors)).cuda()
+    fqt = torch.zeros((w.nq, w.nf, 2), dtype=torch.float64, device="cuda")
+    fq = torch.zeros((w.nq, 2), dtype=torch.float64, device="cuda")
+    fq2 = torch.zeros((w.nq, 2), dtype=torch.float64, device="cuda")
+
+    def step():
+        plan.compute_device(offs, sv.data_ptr(), cf.data_ptr(), fqt.data_ptr(), fq.data_ptr(),
+                            fq2.data_ptr())
+        return plan.timing()
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(dev)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    phase_ms, corr_ms, launches = [], [], 0
+    e0.record(stream)
+    for _ in range(args.steps):
+        t = step()
+        phase_ms.append(t["phase_ms"])
+        corr_ms.append(t["corr_ms"] + t["finalize_ms"])
+        launches += t["kernel_launches"]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    dist.barrier()
+    ms = dist.max(e0.elapsed_time(e1) / args.steps)
+    value = terms * dist.world / (ms * 1e-3)
+
+    # ---- end to end through the C ABI with host buffers ------------------------------
+    lib = abi.load()
+    nbytes = w.coords.nbytes
+    hp = lib.sass_host_alloc(nbytes)
+    host_coords = np.ctypeslib.as_array((np.ctypeslib.ctypes.c_float * w.coords.size)
+                                        .from_address(hp)).reshape(w.coords.shape)
+    host_coords[...] = w.coords
+    sv_h = w.subvectors()
+    cf_h = np.ascontiguousarray(w.class_factors)
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        plan.stage(host_coords)
+        res = plan.compute(offs, sv_h, cf_h)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    lib.sass_host_free(hp)
+    e2e_step = dist.max(statistics.median(e2e_ms))
+    h2d = nbytes + sv_h.nbytes + cf_h.nbytes
+    d2h = w.nq * (w.nf + 2) * 16
+
+    # ---- roofline of the dominant kernel (phase sum) ------------------------------------
+    sfu, fma = abi.probe_pipes(dev)
+    ph = statistics.median(phase_ms)
+    achieved = terms / (ph * 1e-3)
+    peak_terms = sfu / 2.0
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "phase_sum_coherent_sqt.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+    roof = {"bound": "sfu", "achieved": achieved, "peak": peak_terms, "unit": "terms/s",
+            "frac": achieved / peak_terms, "traffic": traffic,
+            "kernel": "phase_sum_fp32_kernel", "kernel_ms": ph,
+            "peak_source": "measured live: sass_probe_pipes SFU %.4g results/s / 2 per term"
+                           % sfu,
+            "fp32_fma_per_s": fma, "fp32_frac": (achieved * 6) / fma}
+    corr = statistics.median(corr_ms)
+    corr_bytes = (w.nq * w.nm * w.nf * 16) + (w.nq * w.nf * 16)
+    roof_corr = {"bound": "hbm", "kernel": "corr_fft_kernel+finalize", "ms": corr,
+                 "achieved": corr_bytes / (corr * 1e-3) / 1e9, "unit": "GB/s"}
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
+           "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded random walk, %s)" % w.name,
+           "config": {"workload": w.name, "na": w.na, "nf": w.nf, "nq": w.nq, "nm": w.nm,
+                      "terms_per_step": terms, "dsp": w.dsp, "scattering": w.scattering,
+                      "fft_length": 1 << max(2, int(np.ceil(np.log2(2 * w.nf)))),
+                      "l2": "inputs larger than L2 (coordinates %.0f MB)" % (w.na * w.nf * 16 / 1e6),
+                      "parallelism": "replicas x%d" % dist.world},
+           "e2e": {"value": terms * dist.world / (e2e_step * 1e-3), "unit": UNIT,
+                   "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_step},
+           "roofline": roof, "roofline_correlation": roof_corr,
+           "gpu_launches": int(launches), "clocks": clk}
+
+    # ---- plain FP64 path on the same GPU, and the FP32 error against it -------------------
+    if not args.no_plain:
+        ns = max(1, min(args.plain_shells, w.nq))
+        idx = np.linspace(0, w.nq - 1, ns).round().astype(int)
+        sub_offs = np.arange(ns + 1, dtype=np.uintp) * w.nm
+        sub_sv = (w.shells[idx, None, None] * w.directions[None]).reshape(-1, 3)
+        sub_cf = w.class_factors[idx]
+        with abi.Plan(w.na, w.nf, nclass, w.scattering, w.dsp, "fftw", "fp64", device=dev) as p64:
+            p64.stage(w.coords)
+            p64.set_classes(w.atom_class)
+            ref = p64.compute(sub_offs, sub_sv, sub_cf)
+            t64 = p64.timing()
+        fp32_sub = plan.compute(sub_offs, sub_sv, sub_cf)
+        t32 = plan.timing()
+        err = (np.abs(fp32_sub[0] - ref[0]).max(axis=1) / np.abs(ref[0][:, 0])).max()
+        sub_terms = w.na * w.nf * w.nm * ns
+        plain_tps = sub_terms / (t64["total_ms"] * 1e-3)
+        out["plain_fp64"] = {"value": plain_tps, "unit": UNIT, "shells_run": ns,
+                             "ms_full_workload_extrapolated": terms / plain_tps * 1e3,
+                             "fp32_max_rel_err_vs_fp64": float(err),
+                             "speedup_same_gpu": (terms / plain_tps * 1e3) / ms,
+                             "fp32_ms_same_shells": t32["total_ms"]}
+
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_sample(w, args.cpu_seconds, os.cpu_count() or 1)
+    if dist.rank == 0:
+        print(json.dumps(out))
+    plan.close()
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,156 @@
+/*
+ * sassena_gb300 — C ABI of the GB300 scattering-amplitude hot path.
+ *
+ * The reference (Sassena 1.4.2) computes, per q-vector, the orientational average
+ * of the autocorrelated (or squared, or plain) scattering amplitude
+ *     A(q,t) = sum_j b_j(|q|) exp(i q . r_j(t))
+ * inside its scatter devices. This header is the thin C layer under the C++ host
+ * devices (sassena_gb300/host/): plain pointers and sizes, int status codes, no
+ * exceptions, no CUDA or C++ types in the signatures.
+ *
+ * Reference interfaces replaced (paths inside the reference project):
+ *   plan create      ScatterDeviceFactory::create, src/scatter_devices/scatter_device_factory.cpp:23-210
+ *                    (device choice by scattering.type :145-201), device ctors
+ *                    all_vectors_scatter_device.cpp:32-55, self_vectors_scatter_device.cpp:40-57
+ *   stage frames     DataStagerByFrame::stage, src/stager/data_stager.cpp:72-118
+ *                    (DataStagerByAtom::stage :214-338 for the incoherent device)
+ *   atom classes     ScatterFactors::set_selection / update, src/scatter_devices/scatter_factors.cpp:56-94
+ *   compute          AbstractScatterDevice::runner's per-q compute(), abstract_scatter_device.cpp:145-175,
+ *                    AllVectorsScatterDevice::compute all_vectors_scatter_device.cpp:238-361,
+ *                    SelfVectorsScatterDevice::compute self_vectors_scatter_device.cpp:145-239;
+ *                    outputs are the rows HDF5WriterClient::write receives,
+ *                    src/services/file_writer_service.cpp:504-531 (fq0 = fqt[0])
+ *   amplitudes       AllVectorsScatterDevice::scatter, all_vectors_scatter_device.cpp:388-439
+ *   errors           Err::Inst()->write + throw (e.g. all_vectors_scatter_device.cpp:217-227),
+ *                    ram_check limits (:57-125) -> status codes + sass_plan_error()
+ *
+ * Threading: a plan is used by one host thread at a time; distinct plans are
+ * independent. All device work of a plan runs on the plan's CUDA stream.
+ */
+#ifndef SASSENA_GB300_H
+#define SASSENA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define SASS_OK 0
+#define SASS_ERR_ARG 1          /* invalid argument or shape */
+#define SASS_ERR_OOM 2          /* device or host allocation failed */
+#define SASS_ERR_UNSUPPORTED 3  /* configuration outside this build (e.g. NF > 4096 with FFT) */
+#define SASS_ERR_CUDA 4         /* CUDA runtime error */
+#define SASS_ERR_TIMEOUT 5      /* a bounded device-side wait gave up */
+#define SASS_ERR_STATE 6        /* call out of order (e.g. compute before staging) */
+
+/* scattering.type (parameters.cpp:372) */
+#define SASS_SCATTERING_ALL 0   /* coherent: AllVectorsScatterDevice */
+#define SASS_SCATTERING_SELF 1  /* incoherent: SelfVectorsScatterDevice */
+
+/* scattering.dsp.type (parameters.cpp:375) */
+#define SASS_DSP_AUTOCORRELATE 0
+#define SASS_DSP_SQUARE 1
+#define SASS_DSP_PLAIN 2
+
+/* scattering.dsp.method (parameters.cpp:376): fftw maps to this library's FFT */
+#define SASS_METHOD_FFTW 0
+#define SASS_METHOD_DIRECT 1
+
+/* Arithmetic of the phase sum. FP64 reproduces the reference's FP64 sums;
+ * FP32 is the fast form (FP32 phase, Kahan, FP64 cross-block reductions). */
+#define SASS_PRECISION_FP64 0
+#define SASS_PRECISION_FP32 1
+
+typedef struct sass_plan sass_plan;
+
+typedef struct sass_plan_desc {
+    int scattering;       /* SASS_SCATTERING_* */
+    int dsp_type;         /* SASS_DSP_* */
+    int dsp_method;       /* SASS_METHOD_* */
+    int precision;        /* SASS_PRECISION_* */
+    size_t na;            /* atoms of the target selection (stager.target) */
+    size_t nf;            /* frames */
+    size_t nclass;        /* distinct scattering classes (b depends only on class and |q|) */
+    int device;           /* CUDA device ordinal */
+    void* stream;         /* cudaStream_t to run on; NULL: the plan creates its own */
+    size_t amplitude_budget_bytes; /* cap on the amplitude buffer; 0: 4 GiB */
+} sass_plan_desc;
+
+/* Per-call device timings (CUDA events on the plan's stream, milliseconds). */
+typedef struct sass_timing {
+    double phase_ms;      /* phase-sum kernels (coherent) */
+    double corr_ms;       /* correlation / store / incoherent fused kernels */
+    double finalize_ms;   /* per-shell FP64 finalisation */
+    double h2d_ms;        /* host-to-device copies inside sass_compute */
+    double d2h_ms;        /* device-to-host copies inside sass_compute */
+    double total_ms;      /* whole sass_compute call on the stream */
+    uint64_t kernel_launches; /* kernels this library launched in the call */
+    uint64_t phase_launches;  /* of which phase-sum kernels */
+    uint64_t h2d_bytes, d2h_bytes;
+} sass_timing;
+
+/* Create a plan (device buffers, FFT tables, stream). Replaces the factory +
+ * device constructor pair. */
+int sass_plan_create(const sass_plan_desc* desc, sass_plan** plan);
+void sass_plan_destroy(sass_plan* plan);
+
+/* Last error message of the plan ("" if none); valid until the next call. */
+const char* sass_plan_error(const sass_plan* plan);
+/* Name of a status code. */
+const char* sass_status_name(int status);
+
+/* Stage the trajectory: frame-major float32 [nf][na][3] (the reference's coor_t
+ * buffer). coords_on_device != 0 means `coords` is a device pointer. */
+int sass_stage_frames(sass_plan* plan, const float* coords, int coords_on_device);
+
+/* Class index per atom of the selection, int32 [na], each in [0, nclass). */
+int sass_set_atom_classes(sass_plan* plan, const int32_t* atom_class, int on_device);
+
+/* Compute nq q-vectors ("shells" here: one q and its orientation sub-vectors).
+ *   sub_offsets   [nq+1] host array: sub-vectors of q i are [sub_offsets[i], sub_offsets[i+1])
+ *   subvectors    [sub_offsets[nq]][3] FP64 (|q| * orientation, or q itself)
+ *   class_factors [nq][nclass] FP64, b_class(|q_i|)
+ *   fqt           [nq][nf][2] FP64 out  (orientational average of C(t))
+ *   fq, fq2       [nq][2] FP64 out      (afinal, a2final after 1/NM)
+ * io_on_device != 0: subvectors, class_factors, fqt, fq, fq2 are device pointers
+ * (sub_offsets is always a host array). */
+int sass_compute(sass_plan* plan, size_t nq, const size_t* sub_offsets, const double* subvectors,
+                 const double* class_factors, double* fqt, double* fq, double* fq2,
+                 int io_on_device);
+
+/* Raw coherent amplitudes (no dsp): out [nsub][nf][2] FP64 for the given
+ * sub-vectors; sub_shell [nsub] selects the row of class_factors [nshell][nclass]. */
+int sass_amplitudes(sass_plan* plan, size_t nsub, const double* subvectors,
+                    const int32_t* sub_shell, size_t nshell, const double* class_factors,
+                    double* out);
+
+/* Timings of the last sass_compute / sass_amplitudes call. */
+int sass_last_timing(const sass_plan* plan, sass_timing* out);
+
+/* Tile shape of the phase sum (q per lane, warps = frames per CTA, atoms per
+ * stage, atom splits; 0 = automatic). Returns SASS_ERR_UNSUPPORTED for shapes
+ * this build does not instantiate. */
+int sass_set_phase_tile(sass_plan* plan, int q_per_lane, int warps, int atoms, int atom_splits);
+
+/* Frame centre used by the FP32 form (frame-0 bounding-box midpoint). */
+int sass_frame_center(const sass_plan* plan, double* center3);
+
+/* Pinned host memory for faster staging (cudaHostAlloc / cudaFreeHost). */
+void* sass_host_alloc(size_t bytes);
+void sass_host_free(void* p);
+
+/* Measure the SFU (sin/cos results per second) and FP32 FMA (per second)
+ * throughput of `device` with pipe microbenchmarks; the phase sum's roofline. */
+int sass_probe_pipes(int device, double* sfu_ops_per_s, double* fp32_fma_per_s);
+
+/* Library version string. */
+const char* sass_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SASSENA_GB300_H */

@@ -1,0 +1,164 @@
+"""CPU oracle for Sassena's scattering-amplitude hot path (test infrastructure).
+
+Only tests/, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
+import this package, and only as the checker. The product package
+``sassena_gb300`` never imports it.
+
+Parity status: parity unpinned. The reference has no golden vectors for this
+path and cannot be built in this environment, so the C++ restatement
+(``cpu_oracle.cpp``) is pinned by analytic known answers and by the independent
+numpy restatement in ``numpy_oracle.py``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+DSP_AUTOCORRELATE, DSP_SQUARE, DSP_PLAIN = 0, 1, 2
+METHOD_FFTW, METHOD_DIRECT = 0, 1
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_fp = ctypes.POINTER(ctypes.c_float)
+_sp = ctypes.POINTER(ctypes.c_size_t)
+
+
+def build() -> str:
+    """Compile the oracle library with its Makefile (idempotent)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(
+            os.path.join(_HERE, "cpu_oracle.cpp")
+        ):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        for name in ("oracle_all_vectors", "oracle_self_vectors"):
+            f = getattr(L, name)
+            f.restype = ctypes.c_int
+            f.argtypes = [_fp, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t, _sp, _dp, _dp,
+                          ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
+        L.oracle_amplitudes.restype = ctypes.c_int
+        L.oracle_amplitudes.argtypes = [_fp, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t,
+                                        _dp, _sp, _dp, ctypes.c_int, _dp]
+        L.oracle_dft.argtypes = [_dp, ctypes.c_size_t, ctypes.c_int]
+        L.oracle_autocorrelate_fftw.argtypes = [_dp, ctypes.c_size_t]
+        L.oracle_autocorrelate_direct.argtypes = [_dp, ctypes.c_size_t]
+        L.oracle_sfactor.restype = ctypes.c_double
+        L.oracle_sfactor.argtypes = [ctypes.c_int, _dp, ctypes.c_size_t, ctypes.c_double]
+        L.oracle_volume.restype = ctypes.c_double
+        L.oracle_volume.argtypes = [ctypes.c_int, _dp, ctypes.c_size_t]
+        L.oracle_exclusion.restype = ctypes.c_double
+        L.oracle_exclusion.argtypes = [ctypes.c_int, _dp, ctypes.c_size_t, ctypes.c_double,
+                                       ctypes.c_double]
+        L.oracle_scan.restype = ctypes.c_size_t
+        L.oracle_scan.argtypes = [_dp, ctypes.c_double, ctypes.c_double, ctypes.c_size_t,
+                                  ctypes.c_double, _dp]
+        _lib = L
+    return _lib
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(t)
+
+
+def _vectors(kind, coords, sub_offsets, subvectors, factors, dsp_type, dsp_method, nthreads):
+    coords = np.ascontiguousarray(coords, dtype=np.float32)
+    nf, na = coords.shape[0], coords.shape[1]
+    sub_offsets = np.ascontiguousarray(sub_offsets, dtype=np.uintp)
+    subvectors = np.ascontiguousarray(subvectors, dtype=np.float64).reshape(-1, 3)
+    nq = len(sub_offsets) - 1
+    factors = np.ascontiguousarray(factors, dtype=np.float64).reshape(nq, na)
+    fqt = np.zeros((nq, nf, 2))
+    fq = np.zeros((nq, 2))
+    fq2 = np.zeros((nq, 2))
+    fn = getattr(lib(), "oracle_%s_vectors" % kind)
+    rc = fn(_ptr(coords, _fp), nf, na, nq, _ptr(sub_offsets, _sp), _ptr(subvectors, _dp),
+            _ptr(factors, _dp), dsp_type, dsp_method, nthreads, _ptr(fqt, _dp), _ptr(fq, _dp),
+            _ptr(fq2, _dp))
+    if rc != 0:
+        raise ValueError("oracle_%s_vectors rejected its arguments" % kind)
+    return fqt, fq, fq2
+
+
+def all_vectors(coords, sub_offsets, subvectors, factors, dsp_type=DSP_AUTOCORRELATE,
+                dsp_method=METHOD_FFTW, nthreads=None):
+    """Coherent S(q,t) per q: returns (fqt [nq,nf,2], fq [nq,2], fq2 [nq,2])."""
+    return _vectors("all", coords, sub_offsets, subvectors, factors, dsp_type, dsp_method,
+                    nthreads or os.cpu_count())
+
+
+def self_vectors(coords, sub_offsets, subvectors, factors, dsp_type=DSP_AUTOCORRELATE,
+                 dsp_method=METHOD_FFTW, nthreads=None):
+    """Incoherent F(q,t) per q: returns (fqt [nq,nf,2], fq [nq,2], fq2 [nq,2])."""
+    return _vectors("self", coords, sub_offsets, subvectors, factors, dsp_type, dsp_method,
+                    nthreads or os.cpu_count())
+
+
+def amplitudes(coords, subvectors, sub_shell, factors, nthreads=None):
+    """A[m, f] = sum_j b_j(shell(m)) exp(i q_m . r_j(f)) as complex128 [nsub, nf]."""
+    coords = np.ascontiguousarray(coords, dtype=np.float32)
+    nf, na = coords.shape[0], coords.shape[1]
+    subvectors = np.ascontiguousarray(subvectors, dtype=np.float64).reshape(-1, 3)
+    sub_shell = np.ascontiguousarray(sub_shell, dtype=np.uintp)
+    factors = np.ascontiguousarray(factors, dtype=np.float64).reshape(-1, na)
+    out = np.zeros((len(subvectors), nf, 2))
+    lib().oracle_amplitudes(_ptr(coords, _fp), nf, na, len(subvectors), _ptr(subvectors, _dp),
+                            _ptr(sub_shell, _sp), _ptr(factors, _dp), nthreads or os.cpu_count(),
+                            _ptr(out, _dp))
+    return out[..., 0] + 1j * out[..., 1]
+
+
+def autocorrelate_fftw(a):
+    nf = len(a)
+    buf = np.zeros((2 * nf, 2))
+    buf[:nf, 0] = np.real(a)
+    buf[:nf, 1] = np.imag(a)
+    lib().oracle_autocorrelate_fftw(_ptr(buf, _dp), nf)
+    return buf[:nf, 0] + 1j * buf[:nf, 1]
+
+
+def autocorrelate_direct(a):
+    nf = len(a)
+    buf = np.stack([np.real(a), np.imag(a)], axis=1).astype(np.float64).copy()
+    lib().oracle_autocorrelate_direct(_ptr(buf, _dp), nf)
+    return buf[:, 0] + 1j * buf[:, 1]
+
+
+def dft(a, sign=-1):
+    n = len(a)
+    buf = np.stack([np.real(a), np.imag(a)], axis=1).astype(np.float64).copy()
+    lib().oracle_dft(_ptr(buf, _dp), n, sign)
+    return buf[:, 0] + 1j * buf[:, 1]
+
+
+def sfactor(ftype, params, q):
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    return lib().oracle_sfactor(ftype, _ptr(p, _dp), len(p), q)
+
+
+def volume(ftype, params):
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    return lib().oracle_volume(ftype, _ptr(p, _dp), len(p))
+
+
+def exclusion(ftype, params, effvolume, q):
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    return lib().oracle_exclusion(ftype, _ptr(p, _dp), len(p), effvolume, q)
+
+
+def scan(base, frm, to, points, exponent=1.0):
+    base = np.ascontiguousarray(base, dtype=np.float64)
+    out = np.zeros((max(points, 1), 3))
+    n = lib().oracle_scan(_ptr(base, _dp), frm, to, points, exponent, _ptr(out, _dp))
+    return out[:n]

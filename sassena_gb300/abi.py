@@ -1,0 +1,223 @@
+"""ctypes binding of the C ABI in include/sassena_gb300.h.
+
+The library is loaded from the package's in-tree build directory. There is no
+fallback: if the shared library is missing or a CUDA device is absent, the calls
+raise. Numpy arrays are passed as plain pointers; results come back as numpy arrays.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_lib", "libsassena_gb300.so")
+
+SASS_OK = 0
+STATUS = {0: "SASS_OK", 1: "SASS_ERR_ARG", 2: "SASS_ERR_OOM", 3: "SASS_ERR_UNSUPPORTED",
+          4: "SASS_ERR_CUDA", 5: "SASS_ERR_TIMEOUT", 6: "SASS_ERR_STATE"}
+
+SCATTERING = {"all": 0, "self": 1}
+DSP = {"autocorrelate": 0, "square": 1, "plain": 2}
+METHOD = {"fftw": 0, "direct": 1}
+PRECISION = {"fp64": 0, "fp32": 1}
+
+# Every symbol the header declares (checked by the CPU tests).
+EXPORTS = [
+    "sass_plan_create", "sass_plan_destroy", "sass_plan_error", "sass_status_name",
+    "sass_stage_frames", "sass_set_atom_classes", "sass_compute", "sass_amplitudes",
+    "sass_last_timing", "sass_set_phase_tile", "sass_frame_center", "sass_host_alloc",
+    "sass_host_free", "sass_probe_pipes", "sass_version",
+]
+
+
+class SassError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (STATUS.get(code, code), msg))
+        self.code = code
+
+
+class PlanDesc(ctypes.Structure):
+    _fields_ = [("scattering", ctypes.c_int), ("dsp_type", ctypes.c_int),
+                ("dsp_method", ctypes.c_int), ("precision", ctypes.c_int),
+                ("na", ctypes.c_size_t), ("nf", ctypes.c_size_t), ("nclass", ctypes.c_size_t),
+                ("device", ctypes.c_int), ("stream", ctypes.c_void_p),
+                ("amplitude_budget_bytes", ctypes.c_size_t)]
+
+
+class Timing(ctypes.Structure):
+    _fields_ = [("phase_ms", ctypes.c_double), ("corr_ms", ctypes.c_double),
+                ("finalize_ms", ctypes.c_double), ("h2d_ms", ctypes.c_double),
+                ("d2h_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
+                ("kernel_launches", ctypes.c_uint64), ("phase_launches", ctypes.c_uint64),
+                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+_vp = ctypes.c_void_p
+_dp = ctypes.POINTER(ctypes.c_double)
+_sz = ctypes.c_size_t
+
+
+def load(path=LIB_PATH):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OSError("sassena_gb300 native library not built: %s (run __graft_entry__.build())"
+                      % path)
+    L = ctypes.CDLL(path)
+    L.sass_plan_create.argtypes = [ctypes.POINTER(PlanDesc), ctypes.POINTER(_vp)]
+    L.sass_plan_destroy.argtypes = [_vp]
+    L.sass_plan_destroy.restype = None
+    L.sass_plan_error.argtypes = [_vp]
+    L.sass_plan_error.restype = ctypes.c_char_p
+    L.sass_status_name.argtypes = [ctypes.c_int]
+    L.sass_status_name.restype = ctypes.c_char_p
+    L.sass_stage_frames.argtypes = [_vp, _vp, ctypes.c_int]
+    L.sass_set_atom_classes.argtypes = [_vp, _vp, ctypes.c_int]
+    L.sass_compute.argtypes = [_vp, _sz, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int]
+    L.sass_amplitudes.argtypes = [_vp, _sz, _vp, _vp, _sz, _vp, _vp]
+    L.sass_last_timing.argtypes = [_vp, ctypes.POINTER(Timing)]
+    L.sass_set_phase_tile.argtypes = [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.sass_frame_center.argtypes = [_vp, _dp]
+    L.sass_host_alloc.argtypes = [_sz]
+    L.sass_host_alloc.restype = _vp
+    L.sass_host_free.argtypes = [_vp]
+    L.sass_host_free.restype = None
+    L.sass_version.restype = ctypes.c_char_p
+    L.sass_probe_pipes.argtypes = [ctypes.c_int, _dp, _dp]
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_vp) if isinstance(a, np.ndarray) else _vp(a)
+
+
+class Plan:
+    """One scatter-device computation (a sass_plan) for fixed NA, NF and settings."""
+
+    def __init__(self, na, nf, nclass, scattering="all", dsp="autocorrelate", method="fftw",
+                 precision="fp64", device=0, stream=None, amplitude_budget_bytes=0):
+        self.lib = load()
+        self.na, self.nf, self.nclass = int(na), int(nf), int(nclass)
+        d = PlanDesc(SCATTERING[scattering], DSP[dsp], METHOD[method], PRECISION[precision],
+                     self.na, self.nf, self.nclass, device, stream or 0, amplitude_budget_bytes)
+        h = _vp()
+        rc = self.lib.sass_plan_create(ctypes.byref(d), ctypes.byref(h))
+        self._h = h
+        if rc != SASS_OK:
+            msg = self.error()
+            self.close()
+            raise SassError(rc, msg)
+
+    def error(self):
+        if not self._h:
+            return ""
+        return self.lib.sass_plan_error(self._h).decode()
+
+    def _check(self, rc):
+        if rc != SASS_OK:
+            raise SassError(rc, self.error())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.sass_plan_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def stage(self, coords, on_device=False):
+        """coords: float32 [nf, na, 3] numpy array, or a device pointer (int)."""
+        if on_device:
+            return self._check(self.lib.sass_stage_frames(self._h, _vp(coords), 1))
+        c = np.ascontiguousarray(coords, dtype=np.float32)
+        if c.shape != (self.nf, self.na, 3):
+            raise ValueError("coords must be [nf, na, 3]")
+        self._check(self.lib.sass_stage_frames(self._h, _ptr(c), 0))
+
+    def set_classes(self, atom_class):
+        c = np.ascontiguousarray(atom_class, dtype=np.int32)
+        if c.shape != (self.na,):
+            raise ValueError("atom_class must be [na]")
+        self._check(self.lib.sass_set_atom_classes(self._h, _ptr(c), 0))
+
+    def set_tile(self, q_per_lane=0, warps=0, atoms=0, atom_splits=0):
+        self._check(self.lib.sass_set_phase_tile(self._h, q_per_lane, warps, atoms, atom_splits))
+
+    def compute(self, sub_offsets, subvectors, class_factors):
+        """Host in/out: returns (fqt [nq, nf] complex, fq [nq] complex, fq2 [nq] complex)."""
+        offs = np.ascontiguousarray(sub_offsets, dtype=np.uintp)
+        nq = len(offs) - 1
+        sv = np.ascontiguousarray(subvectors, dtype=np.float64).reshape(-1, 3)
+        cf = np.ascontiguousarray(class_factors, dtype=np.float64).reshape(nq, self.nclass)
+        fqt = np.zeros((nq, self.nf, 2))
+        fq = np.zeros((nq, 2))
+        fq2 = np.zeros((nq, 2))
+        self._check(self.lib.sass_compute(self._h, nq, _ptr(offs), _ptr(sv), _ptr(cf), _ptr(fqt),
+                                          _ptr(fq), _ptr(fq2), 0))
+        return (fqt[..., 0] + 1j * fqt[..., 1], fq[:, 0] + 1j * fq[:, 1],
+                fq2[:, 0] + 1j * fq2[:, 1])
+
+    def compute_device(self, sub_offsets, d_subvectors, d_class_factors, d_fqt, d_fq, d_fq2):
+        """All array arguments except sub_offsets are device pointers (ints)."""
+        offs = np.ascontiguousarray(sub_offsets, dtype=np.uintp)
+        self._check(self.lib.sass_compute(self._h, len(offs) - 1, _ptr(offs), _vp(d_subvectors),
+                                          _vp(d_class_factors), _vp(d_fqt), _vp(d_fq), _vp(d_fq2),
+                                          1))
+
+    def amplitudes(self, subvectors, sub_shell, class_factors):
+        sv = np.ascontiguousarray(subvectors, dtype=np.float64).reshape(-1, 3)
+        sh = np.ascontiguousarray(sub_shell, dtype=np.int32)
+        cf = np.ascontiguousarray(class_factors, dtype=np.float64).reshape(-1, self.nclass)
+        out = np.zeros((len(sv), self.nf, 2))
+        self._check(self.lib.sass_amplitudes(self._h, len(sv), _ptr(sv), _ptr(sh), len(cf),
+                                             _ptr(cf), _ptr(out)))
+        return out[..., 0] + 1j * out[..., 1]
+
+    def timing(self):
+        t = Timing()
+        self._check(self.lib.sass_last_timing(self._h, ctypes.byref(t)))
+        return t.as_dict()
+
+    def center(self):
+        c = np.zeros(3)
+        self._check(self.lib.sass_frame_center(self._h, c.ctypes.data_as(_dp)))
+        return c
+
+
+def probe_pipes(device=0):
+    """Measured (sfu_ops_per_s, fp32_fma_per_s) of the device."""
+    L = load()
+    a, b = ctypes.c_double(), ctypes.c_double()
+    rc = L.sass_probe_pipes(device, ctypes.byref(a), ctypes.byref(b))
+    if rc != SASS_OK:
+        raise SassError(rc, "sass_probe_pipes failed")
+    return a.value, b.value
+
+
+def compute_workload(w, precision="fp64", method="fftw", device=0, tile=None):
+    """Run a synth.Workload through the C ABI; returns (fqt, fq, fq2)."""
+    with Plan(w.na, w.nf, len(w.class_names), w.scattering, w.dsp, method, precision,
+              device) as p:
+        p.stage(w.coords)
+        p.set_classes(w.atom_class)
+        if tile:
+            p.set_tile(*tile)
+        return p.compute(w.sub_offsets(), w.subvectors(), w.class_factors)

@@ -1,0 +1,658 @@
+// Correlation, store and orientational-average kernels.
+//
+// Replaces, per sub-vector, alignpad + dsp + store of the reference
+// (src/scatter_devices/all_vectors_scatter_device.cpp:186-236, smath.cpp:141-247)
+// and the 1/NM normalisation (:355-360), and the whole incoherent series loop of
+// SelfVectorsScatterDevice (self_vectors_scatter_device.cpp:145-239, 288-322).
+//
+// The reference computes, per sub-vector v, C_v = IFFT(|FFT(pad(A_v))|^2)/(2NF(NF-tau)),
+// then accumulates atfinal += C_v, afinal += mean(C_v), a2final += |mean(C_v)|^2.
+// Both sums over v are linear in the power spectrum P_v = |X_v|^2, so here:
+//   * one forward FFT per series (cuFFT-free radix-2 DIF in shared memory, input
+//     natural order, output bit-reversed; the zero upper half of the padded series
+//     folds the first stage into the load),
+//   * P_v is accumulated per shell (Kahan FP32 or FP64 per CTA, FP64 across CTAs),
+//   * mean_tau C_v = sum_w P_v(w) K(w) with a precomputed kernel K (so no per-series
+//     inverse transform is needed for afinal/a2final),
+//   * ONE inverse FFT per shell (FP64 radix-2 DIT taking the bit-reversed spectrum,
+//     output natural order) gives sum_v C_v, normalised in FP64.
+// The padded length L is the next power of two >= 2NF; the linear correlation for
+// tau < NF is the same for any L >= 2NF-1, and the normalisation uses L.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace sassgpu {
+
+namespace {
+
+template <class T2>
+__device__ __forceinline__ T2 zero2();
+template <>
+__device__ __forceinline__ float2 zero2<float2>() {
+    return make_float2(0.f, 0.f);
+}
+template <>
+__device__ __forceinline__ double2 zero2<double2>() {
+    return make_double2(0.0, 0.0);
+}
+
+__device__ __forceinline__ void conv(float2& d, double2 s) { d = make_float2((float)s.x, (float)s.y); }
+__device__ __forceinline__ void conv(double2& d, double2 s) { d = s; }
+__device__ __forceinline__ void conv(float2& d, float2 s) { d = s; }
+__device__ __forceinline__ double2 to_d2(float2 a) { return make_double2(a.x, a.y); }
+__device__ __forceinline__ double2 to_d2(double2 a) { return a; }
+
+// Remaining DIF stages (half-size L/4 .. 1) after the folded first stage.
+template <class T2, int NT>
+__device__ void dif_tail(T2* buf, const T2* tw, int lg) {
+    const int half = 1 << (lg - 1);
+    for (int lh = lg - 2; lh >= 0; --lh) {
+        const int h = 1 << lh;
+        const int sh = lg - 1 - lh;
+        for (int b = threadIdx.x; b < half; b += NT) {
+            const int p = b & (h - 1);
+            const int i0 = ((b >> lh) << (lh + 1)) + p;
+            T2 u = buf[i0], w = buf[i0 + h];
+            buf[i0] = cadd(u, w);
+            buf[i0 + h] = cmul(csub(u, w), tw[p << sh]);
+        }
+        __syncthreads();
+    }
+}
+
+// Unnormalised inverse DIT FFT: bit-reversed input, natural output, twiddles conj(tw).
+template <int NT>
+__device__ void dit_inverse(double2* buf, const double2* __restrict__ tw, int lg) {
+    const int half = 1 << (lg - 1);
+    for (int lh = 0; lh < lg; ++lh) {
+        const int h = 1 << lh;
+        const int sh = lg - 1 - lh;
+        for (int b = threadIdx.x; b < half; b += NT) {
+            const int p = b & (h - 1);
+            const int i0 = ((b >> lh) << (lh + 1)) + p;
+            double2 u = buf[i0];
+            double2 w = cmulc(buf[i0 + h], __ldg(tw + (p << sh)));
+            buf[i0] = cadd(u, w);
+            buf[i0 + h] = csub(u, w);
+        }
+        __syncthreads();
+    }
+}
+
+// Sum of a double2 over the CTA; valid in thread 0. Ends with a barrier so the
+// caller may reuse shared memory afterwards.
+template <int NT>
+__device__ double2 block_sum(double2 v, double2* red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double2 s = make_double2(0.0, 0.0);
+    if (threadIdx.x == 0)
+        for (int w = 0; w < NT / 32; ++w) {
+            s.x += red[w].x;
+            s.y += red[w].y;
+        }
+    __syncthreads();
+    return s;
+}
+
+// Per-thread power-spectrum accumulator: Kahan FP32 (FP32 path) or plain FP64.
+template <class T, int MAXR>
+struct PowerAcc;
+
+template <int MAXR>
+struct PowerAcc<float, MAXR> {
+    float s[MAXR], c[MAXR];
+    __device__ void clear() {
+#pragma unroll
+        for (int r = 0; r < MAXR; ++r) s[r] = c[r] = 0.f;
+    }
+    __device__ __forceinline__ void add(int r, float p) {
+        float y = __fsub_rn(p, c[r]);
+        float t = __fadd_rn(s[r], y);
+        c[r] = __fsub_rn(__fsub_rn(t, s[r]), y);
+        s[r] = t;
+    }
+    __device__ double get(int r) const { return (double)s[r] - (double)c[r]; }
+};
+
+template <int MAXR>
+struct PowerAcc<double, MAXR> {
+    double s[MAXR];
+    __device__ void clear() {
+#pragma unroll
+        for (int r = 0; r < MAXR; ++r) s[r] = 0.0;
+    }
+    __device__ __forceinline__ void add(int r, double p) { s[r] += p; }
+    __device__ double get(int r) const { return s[r]; }
+};
+
+// Series generation for the incoherent path: b * exp(i q . r(t)).
+__device__ __forceinline__ double2 self_term(double b, float4 r, double qx, double qy, double qz) {
+    // p1 = x1*qx+y1*qy+z1*qz, rounded as self_vectors_scatter_device.cpp:312 writes it
+    double p = __dadd_rn(__dadd_rn(__dmul_rn((double)r.x, qx), __dmul_rn((double)r.y, qy)),
+                         __dmul_rn((double)r.z, qz));
+    double s, c;
+    sincos(p, &s, &c);
+    return make_double2(__dmul_rn(b, c), __dmul_rn(b, s));
+}
+__device__ __forceinline__ float2 self_term(float b, float4 r, float qx, float qy, float qz) {
+    float u = fmaf(r.z, qz, fmaf(r.y, qy, r.x * qx));  // revolutions, centred coordinates
+    float n = __fsub_rn(__fadd_rn(u, 12582912.0f), 12582912.0f);
+    float s, c;
+    __sincosf(__fsub_rn(u, n) * 6.28318530717958647692f, &s, &c);
+    return make_float2(b * c, b * s);
+}
+
+// Shared memory of the FFT accumulate kernels:
+//   buf [L] T2 | tw [L/2] T2 (FP32 only; FP64 twiddles are read through L1) |
+//   red [NT/32] double2 | rj [nf] float4 (incoherent only)
+template <class T>
+struct FftSmem {
+    static size_t bytes(int lg, int nt, int nf, bool self) {
+        size_t L = (size_t)1 << lg;
+        size_t b = L * sizeof(typename cplx<T>::type);
+        if (sizeof(T) == 4) b += (L / 2) * sizeof(typename cplx<T>::type);
+        b += (nt / 32) * sizeof(double2);
+        if (self) b += (size_t)nf * sizeof(float4);
+        return b;
+    }
+};
+
+// Power spectrum of the series in buf (bit-reversed order): accumulate P and
+// return this thread's part of sum_w P(w) K(w).
+template <class T, int NT, int MAXR>
+__device__ __forceinline__ double2 absorb_power(const typename cplx<T>::type* buf, int L,
+                                                const typename cplx<T>::type* __restrict__ kbr,
+                                                PowerAcc<T, MAXR>& acc) {
+    typedef typename cplx<T>::type T2;
+    T ax = 0, ay = 0;
+#pragma unroll
+    for (int r = 0; r < MAXR; ++r) {
+        const int i = threadIdx.x + r * NT;
+        if (i < L) {
+            T2 X = buf[i];
+            T P = X.x * X.x + X.y * X.y;
+            acc.add(r, P);
+            T2 k = kbr[i];
+            ax += P * k.x;
+            ay += P * k.y;
+        }
+    }
+    return make_double2((double)ax, (double)ay);
+}
+
+template <class T, int NT, int MAXR>
+__device__ __forceinline__ void write_power(const PowerAcc<T, MAXR>& acc, int L, double* dst) {
+#pragma unroll
+    for (int r = 0; r < MAXR; ++r) {
+        const int i = threadIdx.x + r * NT;
+        if (i < L) dst[i] = acc.get(r);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Coherent autocorrelation: one CTA per chunk of series of one shell.
+// ---------------------------------------------------------------------------
+template <class T, int NT, int MAXR>
+__global__ void __launch_bounds__(NT)
+    corr_fft_kernel(const double2* __restrict__ A, int nf, int lg, const void* tw_,
+                    const void* kbr_, const SeriesChunk* __restrict__ chunks,
+                    double* __restrict__ ppart, double2* __restrict__ apart,
+                    double* __restrict__ a2part) {
+    typedef typename cplx<T>::type T2;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int L = 1 << lg, half = L >> 1;
+    const T2* twg = reinterpret_cast<const T2*>(tw_);
+    const T2* kbr = reinterpret_cast<const T2*>(kbr_);
+    T2* buf = reinterpret_cast<T2*>(smem);
+    const T2* tw;
+    double2* red;
+    if (sizeof(T) == 4) {
+        T2* tws = buf + L;
+        for (int i = threadIdx.x; i < half; i += NT) tws[i] = twg[i];
+        tw = tws;
+        red = reinterpret_cast<double2*>(tws + half);
+    } else {
+        tw = twg;
+        red = reinterpret_cast<double2*>(buf + L);
+    }
+    const SeriesChunk c = chunks[blockIdx.x];
+    PowerAcc<T, MAXR> acc;
+    acc.clear();
+    double2 asum = make_double2(0.0, 0.0);
+    double a2sum = 0.0;
+    __syncthreads();
+    for (int v = c.v_begin; v < c.v_end; ++v) {
+        const double2* src = A + (size_t)v * nf;
+        for (int p = threadIdx.x; p < half; p += NT) {
+            T2 x = zero2<T2>();
+            if (p < nf) conv(x, src[p]);
+            buf[p] = x;
+            buf[p + half] = cmul(x, tw[p]);
+        }
+        __syncthreads();
+        dif_tail<T2, NT>(buf, tw, lg);
+        double2 av = block_sum<NT>(absorb_power<T, NT, MAXR>(buf, L, kbr, acc), red);
+        if (threadIdx.x == 0) {
+            asum.x += av.x;
+            asum.y += av.y;
+            a2sum += av.x * av.x + av.y * av.y;
+        }
+    }
+    write_power<T, NT, MAXR>(acc, L, ppart + (size_t)c.slot * L);
+    if (threadIdx.x == 0) {
+        apart[c.slot] = asum;
+        a2part[c.slot] = a2sum;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Incoherent autocorrelation: one CTA per chunk of atoms of one shell; for each
+// atom its trajectory is staged once and reused for every direction of the shell.
+// ---------------------------------------------------------------------------
+template <class T, int NT, int MAXR>
+__global__ void __launch_bounds__(NT)
+    self_fft_kernel(const float4* __restrict__ xyz, int na_pad, int nf, int lg,
+                    const double* __restrict__ qv, const T* __restrict__ bfac,
+                    const int* __restrict__ shell_v, const void* tw_, const void* kbr_,
+                    const AtomChunk* __restrict__ chunks, double* __restrict__ ppart,
+                    double2* __restrict__ apart, double* __restrict__ a2part) {
+    typedef typename cplx<T>::type T2;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int L = 1 << lg, half = L >> 1;
+    const T2* twg = reinterpret_cast<const T2*>(tw_);
+    const T2* kbr = reinterpret_cast<const T2*>(kbr_);
+    T2* buf = reinterpret_cast<T2*>(smem);
+    const T2* tw;
+    double2* red;
+    if (sizeof(T) == 4) {
+        T2* tws = buf + L;
+        for (int i = threadIdx.x; i < half; i += NT) tws[i] = twg[i];
+        tw = tws;
+        red = reinterpret_cast<double2*>(tws + half);
+    } else {
+        tw = twg;
+        red = reinterpret_cast<double2*>(buf + L);
+    }
+    float4* rj = reinterpret_cast<float4*>(red + NT / 32);
+    const AtomChunk c = chunks[blockIdx.x];
+    const int v0 = shell_v[c.shell], v1 = shell_v[c.shell + 1];
+    PowerAcc<T, MAXR> acc;
+    acc.clear();
+    double2 asum = make_double2(0.0, 0.0);
+    double a2sum = 0.0;
+    const double inv2pi = 0.15915494309189533577;
+    for (int j = c.j_begin; j < c.j_end; ++j) {
+        __syncthreads();  // previous atom's series fully consumed
+        for (int t = threadIdx.x; t < nf; t += NT) rj[t] = xyz[(size_t)t * na_pad + j];
+        const T b = bfac[(size_t)c.shell * na_pad + j];
+        __syncthreads();
+        for (int v = v0; v < v1; ++v) {
+            const double* q = qv + 3 * (size_t)v;
+            T qx, qy, qz;
+            if (sizeof(T) == 4) {
+                qx = (T)(q[0] * inv2pi);
+                qy = (T)(q[1] * inv2pi);
+                qz = (T)(q[2] * inv2pi);
+            } else {
+                qx = (T)q[0];
+                qy = (T)q[1];
+                qz = (T)q[2];
+            }
+            for (int p = threadIdx.x; p < half; p += NT) {
+                T2 x = zero2<T2>();
+                if (p < nf) x = self_term(b, rj[p], qx, qy, qz);
+                buf[p] = x;
+                buf[p + half] = cmul(x, tw[p]);
+            }
+            __syncthreads();
+            dif_tail<T2, NT>(buf, tw, lg);
+            double2 av = block_sum<NT>(absorb_power<T, NT, MAXR>(buf, L, kbr, acc), red);
+            if (threadIdx.x == 0) {
+                asum.x += av.x;
+                asum.y += av.y;
+                a2sum += av.x * av.x + av.y * av.y;
+            }
+        }
+    }
+    write_power<T, NT, MAXR>(acc, L, ppart + (size_t)c.slot * L);
+    if (threadIdx.x == 0) {
+        apart[c.slot] = asum;
+        a2part[c.slot] = a2sum;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// dsp = square | plain (no transform): C_v(t) = |A_v(t)|^2 or A_v(t) * exp(i q_v.c).
+// Partials are complex per frame: ppart as double2 [slot][nf].
+// ---------------------------------------------------------------------------
+template <int NT, int MAXT>
+__global__ void __launch_bounds__(NT)
+    corr_direct_kernel(const double2* __restrict__ A, int nf, int square, const double* __restrict__ qv,
+                       double cx, double cy, double cz, int restore, const SeriesChunk* __restrict__ chunks,
+                       double2* __restrict__ ppart, double2* __restrict__ apart,
+                       double* __restrict__ a2part) {
+    __shared__ double2 red[NT / 32];
+    const SeriesChunk c = chunks[blockIdx.x];
+    double2 acc[MAXT];
+#pragma unroll
+    for (int r = 0; r < MAXT; ++r) acc[r] = make_double2(0.0, 0.0);
+    double2 asum = make_double2(0.0, 0.0);
+    double a2sum = 0.0;
+    for (int v = c.v_begin; v < c.v_end; ++v) {
+        double2 ph = make_double2(1.0, 0.0);
+        if (!square && restore) {
+            const double* q = qv + 3 * (size_t)v;
+            sincos(q[0] * cx + q[1] * cy + q[2] * cz, &ph.y, &ph.x);
+        }
+        double2 part = make_double2(0.0, 0.0);
+#pragma unroll
+        for (int r = 0; r < MAXT; ++r) {
+            const int t = threadIdx.x + r * NT;
+            if (t < nf) {
+                double2 a = A[(size_t)v * nf + t];
+                double2 cv = square ? make_double2(a.x * a.x + a.y * a.y, 0.0) : cmul(a, ph);
+                acc[r].x += cv.x;
+                acc[r].y += cv.y;
+                part.x += cv.x;
+                part.y += cv.y;
+            }
+        }
+        double2 s = block_sum<NT>(part, red);
+        if (threadIdx.x == 0) {
+            double2 av = make_double2(s.x * (1.0 / nf), s.y * (1.0 / nf));
+            asum.x += av.x;
+            asum.y += av.y;
+            a2sum += av.x * av.x + av.y * av.y;
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < MAXT; ++r) {
+        const int t = threadIdx.x + r * NT;
+        if (t < nf) ppart[(size_t)c.slot * nf + t] = acc[r];
+    }
+    if (threadIdx.x == 0) {
+        apart[c.slot] = asum;
+        a2part[c.slot] = a2sum;
+    }
+}
+
+template <class T, int NT, int MAXT>
+__global__ void __launch_bounds__(NT)
+    self_direct_kernel(const float4* __restrict__ xyz, int na_pad, int nf, int square,
+                       const double* __restrict__ qv, const T* __restrict__ bfac,
+                       const int* __restrict__ shell_v, double cx, double cy, double cz,
+                       int restore, const AtomChunk* __restrict__ chunks,
+                       double2* __restrict__ ppart, double2* __restrict__ apart,
+                       double* __restrict__ a2part) {
+    typedef typename cplx<T>::type T2;
+    __shared__ double2 red[NT / 32];
+    const AtomChunk c = chunks[blockIdx.x];
+    const int v0 = shell_v[c.shell], v1 = shell_v[c.shell + 1];
+    const double inv2pi = 0.15915494309189533577;
+    double2 acc[MAXT];
+#pragma unroll
+    for (int r = 0; r < MAXT; ++r) acc[r] = make_double2(0.0, 0.0);
+    double2 asum = make_double2(0.0, 0.0);
+    double a2sum = 0.0;
+    for (int j = c.j_begin; j < c.j_end; ++j) {
+        const T b = bfac[(size_t)c.shell * na_pad + j];
+        for (int v = v0; v < v1; ++v) {
+            const double* q = qv + 3 * (size_t)v;
+            double2 ph = make_double2(1.0, 0.0);
+            if (!square && restore) sincos(q[0] * cx + q[1] * cy + q[2] * cz, &ph.y, &ph.x);
+            T qx, qy, qz;
+            if (sizeof(T) == 4) {
+                qx = (T)(q[0] * inv2pi);
+                qy = (T)(q[1] * inv2pi);
+                qz = (T)(q[2] * inv2pi);
+            } else {
+                qx = (T)q[0];
+                qy = (T)q[1];
+                qz = (T)q[2];
+            }
+            double2 part = make_double2(0.0, 0.0);
+#pragma unroll
+            for (int r = 0; r < MAXT; ++r) {
+                const int t = threadIdx.x + r * NT;
+                if (t < nf) {
+                    T2 x = self_term(b, xyz[(size_t)t * na_pad + j], qx, qy, qz);
+                    double2 xd = to_d2(x);
+                    double2 cv = square ? make_double2(xd.x * xd.x + xd.y * xd.y, 0.0) : cmul(xd, ph);
+                    acc[r].x += cv.x;
+                    acc[r].y += cv.y;
+                    part.x += cv.x;
+                    part.y += cv.y;
+                }
+            }
+            double2 s = block_sum<NT>(part, red);
+            if (threadIdx.x == 0) {
+                double2 av = make_double2(s.x * (1.0 / nf), s.y * (1.0 / nf));
+                asum.x += av.x;
+                asum.y += av.y;
+                a2sum += av.x * av.x + av.y * av.y;
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < MAXT; ++r) {
+        const int t = threadIdx.x + r * NT;
+        if (t < nf) ppart[(size_t)c.slot * nf + t] = acc[r];
+    }
+    if (threadIdx.x == 0) {
+        apart[c.slot] = asum;
+        a2part[c.slot] = a2sum;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-shell finalisation in FP64: sum partial slots, inverse FFT (autocorrelate),
+// normalise by 1/(L (NF - tau)) and 1/NM, conjugate for dsp.method = direct.
+// ---------------------------------------------------------------------------
+template <int NT>
+__global__ void __launch_bounds__(NT) finalize_kernel(FinalizeArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int s = blockIdx.x;
+    const int sb = a.slot_begin[s], se = a.slot_begin[s + 1];
+    const int nf = a.nf;
+    const double inv_nm = a.inv_nm[s];
+    const double sgn = a.conj_out ? -1.0 : 1.0;
+    double2* out = a.fqt + (size_t)s * nf;
+    if (a.dsp == DSP_AUTOCORRELATE) {
+        const int L = 1 << a.lg;
+        double2* buf = reinterpret_cast<double2*>(smem);
+        for (int i = threadIdx.x; i < L; i += NT) {
+            double p = 0.0;
+            for (int k = sb; k < se; ++k) p += a.ppart[(size_t)k * L + i];
+            buf[i] = make_double2(p, 0.0);
+        }
+        __syncthreads();
+        dit_inverse<NT>(buf, a.tw, a.lg);
+        for (int t = threadIdx.x; t < nf; t += NT) {
+            double f = (1.0 / ((double)L * (double)(nf - t))) * inv_nm;
+            out[t] = make_double2(buf[t].x * f, sgn * buf[t].y * f);
+        }
+    } else {
+        const double2* pp = reinterpret_cast<const double2*>(a.ppart);
+        for (int t = threadIdx.x; t < nf; t += NT) {
+            double2 v = make_double2(0.0, 0.0);
+            for (int k = sb; k < se; ++k) {
+                double2 x = pp[(size_t)k * nf + t];
+                v.x += x.x;
+                v.y += x.y;
+            }
+            out[t] = make_double2(v.x * inv_nm, sgn * v.y * inv_nm);
+        }
+    }
+    if (threadIdx.x == 0) {
+        double2 as = make_double2(0.0, 0.0);
+        double a2 = 0.0;
+        for (int k = sb; k < se; ++k) {
+            as.x += a.apart[k].x;
+            as.y += a.apart[k].y;
+            a2 += a.a2part[k];
+        }
+        a.fq[s] = make_double2(as.x * inv_nm, sgn * as.y * inv_nm);
+        a.fq2[s] = make_double2(a2 * inv_nm, 0.0);
+    }
+}
+
+__global__ void stage_kernel(const float* __restrict__ raw, int nf, int na, int na_pad, double cx,
+                             double cy, double cz, int center, float4* __restrict__ xyz) {
+    const size_t n = (size_t)nf * na_pad;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const size_t f = idx / na_pad;
+        const int j = (int)(idx - f * na_pad);
+        float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (j < na) {
+            const float* p = raw + (f * na + j) * 3;
+            if (center) {
+                r.x = (float)((double)p[0] - cx);
+                r.y = (float)((double)p[1] - cy);
+                r.z = (float)((double)p[2] - cz);
+            } else {
+                r.x = p[0];
+                r.y = p[1];
+                r.z = p[2];
+            }
+        }
+        xyz[idx] = r;
+    }
+}
+
+template <class T>
+__global__ void expand_factors_kernel(const double* __restrict__ cf, int nclass, int nshell,
+                                      const int* __restrict__ cls, int na_pad, T* __restrict__ b) {
+    const size_t n = (size_t)nshell * na_pad;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const size_t s = idx / na_pad;
+        const int j = (int)(idx - s * na_pad);
+        const int c = cls[j];
+        b[idx] = (c >= 0 && c < nclass) ? (T)cf[s * nclass + c] : (T)0;
+    }
+}
+
+int grid_for(size_t n, int threads) {
+    size_t b = (n + threads - 1) / threads;
+    if (b > 152 * 32) b = 152 * 32;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+template <class K>
+cudaError_t set_smem(K k, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <class T, int NT, int MAXR>
+cudaError_t launch_corr_fft(const CorrArgs& a, cudaStream_t st) {
+    size_t sm = FftSmem<T>::bytes(a.lg, NT, a.nf, false);
+    auto k = corr_fft_kernel<T, NT, MAXR>;
+    cudaError_t e = set_smem(k, sm);
+    if (e != cudaSuccess) return e;
+    k<<<a.nchunks, NT, sm, st>>>(a.A, a.nf, a.lg, a.tw, a.kbr, a.chunks, a.ppart, a.apart,
+                                 a.a2part);
+    return cudaGetLastError();
+}
+
+template <class T, int NT, int MAXR>
+cudaError_t launch_self_fft(const CorrArgs& a, cudaStream_t st) {
+    size_t sm = FftSmem<T>::bytes(a.lg, NT, a.nf, true);
+    auto k = self_fft_kernel<T, NT, MAXR>;
+    cudaError_t e = set_smem(k, sm);
+    if (e != cudaSuccess) return e;
+    k<<<a.nchunks, NT, sm, st>>>(a.xyz, a.na_pad, a.nf, a.lg, a.qv, (const T*)a.bfac, a.shell_v,
+                                 a.tw, a.kbr, a.achunks, a.ppart, a.apart, a.a2part);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t fft_smem_bytes(int precision, int lg, int nf, bool self) {
+    const int nt = lg <= 9 ? 64 : 256;
+    return precision == PREC_FP32 ? FftSmem<float>::bytes(lg, nt, nf, self)
+                                  : FftSmem<double>::bytes(lg, nt, nf, self);
+}
+
+cudaError_t launch_corr_accumulate(const CorrArgs& a, int dsp, cudaStream_t st) {
+    if (a.nchunks == 0) return cudaSuccess;
+    if (dsp == DSP_AUTOCORRELATE) {
+        if (a.lg < 2 || a.lg > 13) return cudaErrorInvalidValue;
+        if (a.precision == PREC_FP32)
+            return a.lg <= 9 ? launch_corr_fft<float, 64, 8>(a, st)
+                             : launch_corr_fft<float, 256, 32>(a, st);
+        return a.lg <= 9 ? launch_corr_fft<double, 64, 8>(a, st)
+                         : launch_corr_fft<double, 256, 32>(a, st);
+    }
+    if (a.nf > 256 * 16) return cudaErrorInvalidValue;
+    corr_direct_kernel<256, 16><<<a.nchunks, 256, 0, st>>>(
+        a.A, a.nf, dsp == DSP_SQUARE, a.qv, a.cx, a.cy, a.cz, a.restore_phase, a.chunks,
+        reinterpret_cast<double2*>(a.ppart), a.apart, a.a2part);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_self_accumulate(const CorrArgs& a, int dsp, cudaStream_t st) {
+    if (a.nchunks == 0) return cudaSuccess;
+    if (dsp == DSP_AUTOCORRELATE) {
+        if (a.lg < 2 || a.lg > 13) return cudaErrorInvalidValue;
+        if (a.precision == PREC_FP32)
+            return a.lg <= 9 ? launch_self_fft<float, 64, 8>(a, st)
+                             : launch_self_fft<float, 256, 32>(a, st);
+        return a.lg <= 9 ? launch_self_fft<double, 64, 8>(a, st)
+                         : launch_self_fft<double, 256, 32>(a, st);
+    }
+    if (a.nf > 256 * 16) return cudaErrorInvalidValue;
+    if (a.precision == PREC_FP32)
+        self_direct_kernel<float, 256, 16><<<a.nchunks, 256, 0, st>>>(
+            a.xyz, a.na_pad, a.nf, dsp == DSP_SQUARE, a.qv, (const float*)a.bfac, a.shell_v, a.cx,
+            a.cy, a.cz, a.restore_phase, a.achunks, reinterpret_cast<double2*>(a.ppart), a.apart,
+            a.a2part);
+    else
+        self_direct_kernel<double, 256, 16><<<a.nchunks, 256, 0, st>>>(
+            a.xyz, a.na_pad, a.nf, dsp == DSP_SQUARE, a.qv, (const double*)a.bfac, a.shell_v, a.cx,
+            a.cy, a.cz, a.restore_phase, a.achunks, reinterpret_cast<double2*>(a.ppart), a.apart,
+            a.a2part);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const FinalizeArgs& a, cudaStream_t st) {
+    if (a.nshell == 0) return cudaSuccess;
+    size_t sm = a.dsp == DSP_AUTOCORRELATE ? ((size_t)1 << a.lg) * sizeof(double2) : 0;
+    auto k = finalize_kernel<256>;
+    cudaError_t e = set_smem(k, sm);
+    if (e != cudaSuccess) return e;
+    k<<<a.nshell, 256, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stage(const float* raw, int nf, int na, int na_pad, double cx, double cy,
+                         double cz, int center, float4* xyz, cudaStream_t st) {
+    size_t n = (size_t)nf * na_pad;
+    stage_kernel<<<grid_for(n, 256), 256, 0, st>>>(raw, nf, na, na_pad, cx, cy, cz, center, xyz);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_expand_factors(const double* class_factors, int nclass, int nshell,
+                                  const int* cls, int na_pad, int precision, void* b,
+                                  cudaStream_t st) {
+    size_t n = (size_t)nshell * na_pad;
+    if (n == 0) return cudaSuccess;
+    if (precision == PREC_FP32)
+        expand_factors_kernel<float><<<grid_for(n, 256), 256, 0, st>>>(
+            class_factors, nclass, nshell, cls, na_pad, (float*)b);
+    else
+        expand_factors_kernel<double><<<grid_for(n, 256), 256, 0, st>>>(
+            class_factors, nclass, nshell, cls, na_pad, (double*)b);
+    return cudaGetLastError();
+}
+
+}  // namespace sassgpu

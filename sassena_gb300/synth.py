@@ -1,0 +1,218 @@
+"""Seeded synthetic trajectories and scattering set-ups for the benchmark workloads.
+
+No public dataset is involved: every workload is generated from a seed with numpy's
+PCG64. Coordinates are float32 frame-major ``[nf, na, 3]``, the layout the reference's
+``DataStagerByFrame`` produces (src/stager/data_stager.cpp:110-114).
+
+Workloads (sizes as named in the benchmark definitions):
+  * ``incoherent_fqt``   1,000 atoms, 30 A box, 128 frames, Gaussian steps sigma=0.1 A per
+                         axis, H/C/N/O 50/30/10/10 with incoherent lengths, 10 shells
+                         0.1-2.0 1/A, 100 directions per shell.
+  * ``coherent_sqt``     10,000 atoms, 50 A box, 1,024 frames, sigma=0.05 A steps plus a
+                         harmonic pull (3-D RMSD saturating near 1 A), H/C/N/O/S coherent
+                         lengths, 20 shells 0.05-3.0 1/A, 500 directions per shell.
+  * ``static_xray``      20,000-bead random coil (bond 1.5 A) + 80,000 solvent atoms in a
+                         110 A box, 64 frames, four-Gaussian form factors with seeded
+                         coefficients, 200 shells 0.01-0.5 1/A, 2,000 directions.
+Directions on the sphere come from normalised Gaussian triples (the project's own
+generator; the reference's Boost mt19937/uniform_on_sphere stream is not reproduced).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# Neutron scattering lengths in fm. Coherent: NIST b_c. Incoherent: sqrt(sigma_inc/4pi).
+COHERENT_FM = {"H": -3.7390, "C": 6.6460, "N": 9.3600, "O": 5.8030, "S": 2.8470}
+INCOHERENT_FM = {"H": 25.274, "C": 0.089, "N": 1.990, "O": 0.080, "S": 0.236}
+
+
+@dataclass
+class Workload:
+    """One scattering calculation: trajectory, atom classes, shells and directions."""
+
+    name: str
+    coords: np.ndarray            # float32 [nf, na, 3]
+    atom_class: np.ndarray        # int32 [na]; class c has factor class_factors[s, c]
+    class_names: list
+    class_factors: np.ndarray     # float64 [nq, nclass], b_c(|q_s|)
+    shells: np.ndarray            # float64 [nq], |q|
+    directions: np.ndarray        # float64 [nm, 3], unit vectors shared by all shells
+    scattering: str = "all"       # "all" (coherent) or "self" (incoherent)
+    dsp: str = "autocorrelate"    # autocorrelate | square | plain
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def nf(self):
+        return self.coords.shape[0]
+
+    @property
+    def na(self):
+        return self.coords.shape[1]
+
+    @property
+    def nq(self):
+        return len(self.shells)
+
+    @property
+    def nm(self):
+        return len(self.directions)
+
+    def terms(self):
+        """atom x q-vector x frame terms of the phase sum."""
+        return self.na * self.nq * self.nm * self.nf
+
+    def sub_offsets(self):
+        return np.arange(self.nq + 1, dtype=np.uintp) * self.nm
+
+    def subvectors(self):
+        """[nq*nm, 3]: |q_s| * u_m, shell-major (init_subvectors order)."""
+        return (self.shells[:, None, None] * self.directions[None, :, :]).reshape(-1, 3)
+
+    def factors(self):
+        """Per-atom factors [nq, na] expanded from the classes."""
+        return self.class_factors[:, self.atom_class]
+
+
+def sphere_directions(n, seed):
+    rng = np.random.default_rng(np.random.PCG64(seed))
+    v = rng.standard_normal((n, 3))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    return v
+
+
+def fibonacci_sphere(n):
+    """Deterministic near-uniform points (spherical Fibonacci lattice)."""
+    i = np.arange(n) + 0.5
+    z = 1.0 - 2.0 * i / n
+    r = np.sqrt(np.maximum(0.0, 1.0 - z * z))
+    phi = i * math.pi * (3.0 - math.sqrt(5.0))
+    return np.stack([r * np.cos(phi), r * np.sin(phi), z], axis=1)
+
+
+def _types(rng, na, names, ratios):
+    counts = np.floor(np.asarray(ratios, dtype=float) / sum(ratios) * na).astype(int)
+    counts[0] += na - counts.sum()
+    t = np.repeat(np.arange(len(names)), counts)
+    rng.shuffle(t)
+    return t.astype(np.int32)
+
+
+def random_walk(rng, r0, nf, sigma, k=0.0, chunk=64):
+    """Frames r_{t+1} = r_t + sigma*xi - k (r_t - r_0); float32 [nf, na, 3]."""
+    na = r0.shape[0]
+    out = np.empty((nf, na, 3), dtype=np.float32)
+    r = r0.astype(np.float64).copy()
+    out[0] = r
+    t = 1
+    while t < nf:
+        m = min(chunk, nf - t)
+        steps = rng.standard_normal((m, na, 3)) * sigma
+        for i in range(m):
+            r += steps[i]
+            if k:
+                r -= k * (r - r0)
+            out[t + i] = r
+        t += m
+    return out
+
+
+def incoherent_fqt(seed=1, na=1000, nf=128, box=30.0, sigma=0.1, nq=10, qmin=0.1, qmax=2.0,
+                   nm=100):
+    rng = np.random.default_rng(np.random.PCG64(seed))
+    names = ["H", "C", "N", "O"]
+    cls = _types(rng, na, names, [50, 30, 10, 10])
+    r0 = rng.uniform(0.0, box, (na, 3))
+    coords = random_walk(rng, r0, nf, sigma)
+    shells = np.linspace(qmin, qmax, nq)
+    b = np.array([INCOHERENT_FM[n] for n in names])
+    return Workload("incoherent_fqt", coords, cls, names, np.tile(b, (nq, 1)), shells,
+                    sphere_directions(nm, seed + 1000), scattering="self",
+                    meta=dict(box=box, sigma=sigma, seed=seed))
+
+
+def coherent_sqt(seed=2, na=10000, nf=1024, box=50.0, sigma=0.05, rmsd=1.0, nq=20, qmin=0.05,
+                 qmax=3.0, nm=500):
+    rng = np.random.default_rng(np.random.PCG64(seed))
+    names = ["H", "C", "N", "O", "S"]
+    cls = _types(rng, na, names, [50, 30, 8, 10, 2])
+    r0 = rng.uniform(0.0, box, (na, 3))
+    # OU stationary per-axis variance sigma^2/(2k-k^2); 3-D MSD = rmsd^2.
+    c = 3.0 * sigma * sigma / (rmsd * rmsd)
+    k = 1.0 - math.sqrt(1.0 - c)
+    coords = random_walk(rng, r0, nf, sigma, k=k)
+    shells = np.linspace(qmin, qmax, nq)
+    b = np.array([COHERENT_FM[n] for n in names])
+    return Workload("coherent_sqt", coords, cls, names, np.tile(b, (nq, 1)), shells,
+                    sphere_directions(nm, seed + 1000), scattering="all",
+                    meta=dict(box=box, sigma=sigma, k=k, seed=seed))
+
+
+def xray_form_factor_params(rng, ntypes):
+    """Four-Gaussian + constant coefficients: a_k in [0.5,3], b_k in [0.5,50], c in [0,1].
+
+    Returned as the database's sfactor type-2 parameter vector
+    v = (a1, b1/16pi^2, a2, b2/16pi^2, a3, b3/16pi^2, a4, b4/16pi^2, c), because the
+    reference evaluates v0*exp(-v1 q^2)+... (database.cpp:513-523) while the
+    form factor is a_k exp(-b_k q^2/16pi^2).
+    """
+    out = []
+    for _ in range(ntypes):
+        a = rng.uniform(0.5, 3.0, 4)
+        bb = rng.uniform(0.5, 50.0, 4) / (16.0 * math.pi ** 2)
+        c = rng.uniform(0.0, 1.0)
+        v = np.empty(9)
+        v[0:8:2] = a
+        v[1:8:2] = bb
+        v[8] = c
+        out.append(v)
+    return np.array(out)
+
+
+def sfactor_type2(v, q):
+    return (v[0] * np.exp(-v[1] * q * q) + v[2] * np.exp(-v[3] * q * q)
+            + v[4] * np.exp(-v[5] * q * q) + v[6] * np.exp(-v[7] * q * q) + v[8])
+
+
+def static_xray(seed=3, nbeads=20000, nsolvent=80000, nf=64, box=110.0, bond=1.5, sigma=0.05,
+                nq=200, qmin=0.01, qmax=0.5, nm=2000):
+    rng = np.random.default_rng(np.random.PCG64(seed))
+    steps = rng.standard_normal((nbeads, 3))
+    steps *= bond / np.linalg.norm(steps, axis=1, keepdims=True)
+    chain = np.cumsum(steps, axis=0)
+    chain += box / 2.0 - chain.mean(axis=0)
+    solvent = rng.uniform(0.0, box, (nsolvent, 3))
+    r0 = np.concatenate([chain, solvent])
+    coords = random_walk(rng, r0, nf, sigma)
+    names = ["C", "O"]  # coil beads / solvent
+    cls = np.concatenate([np.zeros(nbeads, np.int32), np.ones(nsolvent, np.int32)])
+    params = xray_form_factor_params(rng, len(names))
+    shells = np.linspace(qmin, qmax, nq)
+    cf = np.stack([sfactor_type2(params[c], shells) for c in range(len(names))], axis=1)
+    return Workload("static_xray", coords, cls, names, cf, shells,
+                    sphere_directions(nm, seed + 1000), scattering="all", dsp="square",
+                    meta=dict(box=box, seed=seed, sfactor_params=params))
+
+
+def small(scattering="all", dsp="autocorrelate", seed=7, na=37, nf=24, nq=3, nm=5, box=12.0):
+    """A tiny random case for parity tests (ragged sizes on purpose)."""
+    rng = np.random.default_rng(np.random.PCG64(seed))
+    names = ["H", "C", "N", "O"]
+    cls = rng.integers(0, len(names), na).astype(np.int32)
+    r0 = rng.uniform(0.0, box, (na, 3))
+    coords = random_walk(rng, r0, nf, 0.2)
+    shells = np.linspace(0.3, 2.5, nq)
+    table = COHERENT_FM if scattering == "all" else INCOHERENT_FM
+    b = np.array([table[n] for n in names])
+    cf = np.tile(b, (nq, 1)) * (1.0 + 0.1 * np.arange(nq))[:, None]
+    return Workload("small", coords, cls, names, cf, shells, sphere_directions(nm, seed + 1),
+                    scattering=scattering, dsp=dsp)
+
+
+WORKLOADS = {
+    "incoherent_fqt": incoherent_fqt,
+    "coherent_sqt": coherent_sqt,
+    "static_xray": static_xray,
+}

@@ -1,0 +1,183 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+Bars (error metric rel_err = max_t |S - S_ref| / |S_ref(q,0)| per q):
+  * FP64 plain path: <= 1e-12 (the reference's FP64 results, oracle restatement);
+  * FP32 fast path:  <= 1e-3 (the accuracy target of the precision form).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from sassena_gb300 import abi, synth
+
+from helpers import cplx, rel_err_sqt, rel_err_vec
+
+pytestmark = pytest.mark.gpu
+
+DSPS = [("autocorrelate", "fftw"), ("autocorrelate", "direct"), ("square", "fftw"),
+        ("plain", "fftw")]
+DSP_ID = {"autocorrelate": 0, "square": 1, "plain": 2}
+METHOD_ID = {"fftw": 0, "direct": 1}
+TOL = {"fp64": 1e-12, "fp32": 1e-3}
+
+
+def run_oracle(w, dsp, method):
+    fn = oracle.all_vectors if w.scattering == "all" else oracle.self_vectors
+    return fn(w.coords, w.sub_offsets(), w.subvectors(), w.factors(), DSP_ID[dsp],
+              METHOD_ID[method], nthreads=8)
+
+
+def run_gpu(w, precision, method, tile=None):
+    return abi.compute_workload(w, precision=precision, method=method, tile=tile)
+
+
+def check(w, precision, method, tile=None):
+    ref_fqt, ref_fq, ref_fq2 = run_oracle(w, w.dsp, method)
+    fqt, fq, fq2 = run_gpu(w, precision, method, tile)
+    tol = TOL[precision]
+    e_t = rel_err_sqt(fqt, ref_fqt).max()
+    e_q = rel_err_vec(fq, cplx(ref_fq))
+    e_q2 = rel_err_vec(fq2, cplx(ref_fq2))
+    assert e_t <= tol, "fqt rel err %.3e > %.1e" % (e_t, tol)
+    assert e_q <= tol, "fq rel err %.3e > %.1e" % (e_q, tol)
+    assert e_q2 <= tol, "fq2 rel err %.3e > %.1e" % (e_q2, tol)
+    return e_t, e_q, e_q2
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("dsp,method", DSPS)
+def test_coherent_small(native_lib, precision, dsp, method):
+    w = synth.small("all", dsp, seed=11, na=37, nf=24, nq=3, nm=5)
+    check(w, precision, method)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("dsp,method", DSPS)
+def test_incoherent_small(native_lib, precision, dsp, method):
+    w = synth.small("self", dsp, seed=12, na=29, nf=21, nq=2, nm=4)
+    check(w, precision, method)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_coherent_ragged_medium(native_lib, precision):
+    # NA not a multiple of the 128-atom granule, NF not a power of two, NM not a
+    # multiple of 32 and shells of different sizes (CSR offsets).
+    w = synth.small("all", "autocorrelate", seed=13, na=301, nf=77, nq=4, nm=45)
+    check(w, precision, "fftw")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_incoherent_ragged_medium(native_lib, precision):
+    w = synth.small("self", "autocorrelate", seed=14, na=150, nf=100, nq=2, nm=7)
+    check(w, precision, "fftw")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_uneven_shells(native_lib, precision):
+    w = synth.small("all", "autocorrelate", seed=15, na=64, nf=33, nq=3, nm=40)
+    offs = np.array([0, 3, 40, 41, 120], dtype=np.uintp)  # 4 q-vectors, uneven sub-vector sets
+    rng = np.random.default_rng(5)
+    sv = rng.normal(size=(120, 3))
+    cf = np.tile(w.class_factors[:1], (4, 1))
+    fac = cf[:, w.atom_class]
+    ref = oracle.all_vectors(w.coords, offs, sv, fac, 0, 0, nthreads=8)
+    with abi.Plan(w.na, w.nf, len(w.class_names), "all", "autocorrelate", "fftw", precision) as p:
+        p.stage(w.coords)
+        p.set_classes(w.atom_class)
+        fqt, fq, fq2 = p.compute(offs, sv, cf)
+    assert rel_err_sqt(fqt, ref[0]).max() <= TOL[precision]
+    assert rel_err_vec(fq2, cplx(ref[2])) <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("splits", [1, 3])
+def test_amplitudes_and_atom_splits(native_lib, precision, splits):
+    w = synth.small("all", "autocorrelate", seed=16, na=700, nf=19, nq=2, nm=9)
+    sv = w.subvectors()
+    shell = np.repeat(np.arange(w.nq), w.nm).astype(np.int32)
+    ref = oracle.amplitudes(w.coords, sv, shell.astype(np.uintp), w.factors(), nthreads=8)
+    with abi.Plan(w.na, w.nf, len(w.class_names), "all", precision=precision) as p:
+        p.stage(w.coords)
+        p.set_classes(w.atom_class)
+        q = 1
+        tile = (q, 8, 128) if precision == "fp32" else (q, 4, 64)
+        p.set_tile(*tile, atom_splits=splits)
+        amp = p.amplitudes(sv, shell, w.class_factors)
+    scale = np.abs(w.factors()).sum(axis=1).max()
+    err = np.abs(amp - ref).max() / scale
+    assert err <= (1e-13 if precision == "fp64" else 2e-5), err
+
+
+def test_static_single_atom(native_lib):
+    # One static atom: |A|^2 = b^2 for every q and t (known answer).
+    nf = 16
+    coords = np.tile(np.array([[[1.5, -2.0, 0.25]]], dtype=np.float32), (nf, 1, 1))
+    b = 3.7
+    offs = np.array([0, 6], dtype=np.uintp)
+    sv = synth.sphere_directions(6, 3) * 1.3
+    for precision in ("fp64", "fp32"):
+        with abi.Plan(1, nf, 1, "all", "autocorrelate", "fftw", precision) as p:
+            p.stage(coords)
+            p.set_classes(np.zeros(1, np.int32))
+            fqt, fq, fq2 = p.compute(offs, sv, np.array([[b]]))
+        assert np.allclose(fqt.real, b * b, rtol=1e-12 if precision == "fp64" else 1e-5)
+        assert np.abs(fqt.imag).max() <= 1e-12 * b * b if precision == "fp64" else 1e-5 * b * b
+
+
+def test_two_atom_identity(native_lib):
+    # Two static atoms: |A(q u)|^2 = b1^2 + b2^2 + 2 b1 b2 cos(q u.d) per direction, exact.
+    nf = 4
+    r = np.array([[0.0, 0.0, 0.0], [1.2, -0.7, 2.1]], dtype=np.float32)
+    coords = np.tile(r[None], (nf, 1, 1))
+    b = np.array([2.0, -1.3])
+    dirs = synth.fibonacci_sphere(64)
+    q = 1.7
+    offs = np.array([0, 64], dtype=np.uintp)
+    with abi.Plan(2, nf, 2, "all", "square", "fftw", "fp64") as p:
+        p.stage(coords)
+        p.set_classes(np.array([0, 1], np.int32))
+        fqt, fq, fq2 = p.compute(offs, q * dirs, b[None, :])
+    d = (r[1] - r[0]).astype(np.float64)
+    expect = np.mean(b[0] ** 2 + b[1] ** 2 + 2 * b[0] * b[1] * np.cos(q * dirs @ d))
+    assert abs(fq[0].real - expect) <= 1e-12 * abs(expect)
+    assert np.allclose(fqt[0].real, expect, rtol=1e-12)
+
+
+def test_error_paths(native_lib):
+    with pytest.raises(abi.SassError) as e:
+        abi.Plan(10, 0, 1)
+    assert e.value.code == 1
+    with pytest.raises(abi.SassError) as e:
+        abi.Plan(10, 5000, 1, "all", "autocorrelate")
+    assert e.value.code == 3
+    with abi.Plan(4, 4, 2) as p:
+        with pytest.raises(abi.SassError) as e:
+            p.compute(np.array([0, 1], np.uintp), np.ones((1, 3)), np.ones((1, 2)))
+        assert e.value.code == 6  # compute before staging
+        p.stage(np.zeros((4, 4, 3), np.float32))
+        with pytest.raises(abi.SassError) as e:
+            p.set_classes(np.array([0, 1, 2, 0], np.int32))  # class 2 >= nclass
+        assert e.value.code == 1
+        p.set_classes(np.array([0, 1, 1, 0], np.int32))
+        with pytest.raises(abi.SassError) as e:
+            p.compute(np.array([0, 0], np.uintp), np.ones((1, 3)), np.ones((1, 2)))
+        assert e.value.code == 1  # a q-vector with no sub-vectors
+        with pytest.raises(abi.SassError) as e:
+            p.set_tile(3, 8, 128)
+        assert e.value.code == 3
+        # the plan stays usable after rejected calls
+        fqt, fq, fq2 = p.compute(np.array([0, 1], np.uintp), np.ones((1, 3)), np.ones((1, 2)))
+        assert np.isfinite(fqt).all()
+
+
+def test_single_frame(native_lib):
+    w = synth.small("all", "autocorrelate", seed=17, na=20, nf=1, nq=2, nm=3)
+    check(w, "fp64", "fftw")
+
+
+@pytest.mark.parametrize("nf", [128, 1024])
+def test_coherent_fp32_error_at_length(native_lib, nf):
+    """FP32 form at realistic trajectory lengths stays well inside 1e-3."""
+    rng = np.random.default_rng(nf)
+    w = synth.coherent_sqt(seed=21, na=500, nf=nf, nq=3, nm=8, box=20.0)
+    check(w, "fp32", "fftw")
