@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--nq", type=int, default=0, help="override the number of shells (profiling)")
+    ap.add_argument("--nf", type=int, default=0, help="override the number of frames (profiling)")
     return ap.parse_args()
 
 
@@ -139,9 +142,14 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_workload(name):
+def make_workload(name, nq=0, nf=0):
     from sassena_gb300 import synth
-    return synth.WORKLOADS[name]()
+    kw = {}
+    if nq:
+        kw["nq"] = nq
+    if nf:
+        kw["nf"] = nf
+    return synth.WORKLOADS[name](**kw)
 
 
 def cpu_sample(w, seconds, nthreads):
@@ -169,7 +177,7 @@ def cpu_sample(w, seconds, nthreads):
 def run_reference(args, dist):
     if dist.rank != 0:
         return
-    w = make_workload(args.workload)
+    w = make_workload(args.workload, args.nq, args.nf)
     nthreads = os.cpu_count() or 1
     vals = []
     for i in range(args.warmup + args.steps):
@@ -199,7 +207,7 @@ def run_ours(args, dist):
 
     dev = dist.local
     torch.cuda.set_device(dev)
-    w = make_workload(args.workload)
+    w = make_workload(args.workload, args.nq, args.nf)
     stream = torch.cuda.current_stream()
     nclass = len(w.class_names)
     terms = w.terms()
@@ -250,7 +258,7 @@ def run_ours(args, dist):
     sv_h = w.subvectors()
     cf_h = np.ascontiguousarray(w.class_factors)
     e2e_ms = []
-    for i in range(args.warmup + args.steps):
+    for i in range(0 if args.no_e2e else args.warmup + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         plan.stage(host_coords)
@@ -259,7 +267,7 @@ def run_ours(args, dist):
         if i >= args.warmup:
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
     lib.sass_host_free(hp)
-    e2e_step = dist.max(statistics.median(e2e_ms))
+    e2e_step = dist.max(statistics.median(e2e_ms) if e2e_ms else float("nan"))
     h2d = nbytes + sv_h.nbytes + cf_h.nbytes
     d2h = w.nq * (w.nf + 2) * 16
 
