@@ -146,6 +146,23 @@ void sass_host_free(void* p);
  * throughput of `device` with pipe microbenchmarks; the phase sum's roofline. */
 int sass_probe_pipes(int device, double* sfu_ops_per_s, double* fp32_fma_per_s);
 
+/* Allocation-free coherent autocorrelation + orientational average (FP64), for
+ * callers that must not allocate GPU memory while they run: programs that reserve
+ * the whole device up front, code running inside a memory-pool callback, services
+ * that cannot risk an out-of-memory failure mid-run. No counterpart in the
+ * reference (its scatter devices allocate per call, all_vectors_scatter_device.cpp:262).
+ *   amplitudes  device [nsub][nf][2] FP64, A_v(t) per sub-vector (sass_amplitudes layout)
+ *   sub_offsets device uint64 [nq+1], sub-vectors of q i are [sub_offsets[i], sub_offsets[i+1])
+ *   fqt, fq, fq2 device outputs as in sass_compute (dsp = autocorrelate, method fftw/direct)
+ * Working memory is one fixed 8.2 MiB device array inside the library; nothing is
+ * allocated. Limits: nq <= 128, nf <= 4096 (else SASS_ERR_UNSUPPORTED). Calls share
+ * the array: calls that overlap on the GPU race, so issue them in order on one
+ * stream. The first call on a device looks up the array's address; make it before
+ * any stream capture. Asynchronous on `stream` (a cudaStream_t, NULL = default). */
+int sass_correlate_noalloc(int device, void* stream, const double* amplitudes, size_t nf,
+                           size_t nq, const uint64_t* sub_offsets, int dsp_method,
+                           double* fqt, double* fq, double* fq2);
+
 /* Library version string. */
 const char* sass_version(void);
 

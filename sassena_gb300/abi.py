@@ -28,7 +28,7 @@ EXPORTS = [
     "sass_plan_create", "sass_plan_destroy", "sass_plan_error", "sass_status_name",
     "sass_stage_frames", "sass_set_atom_classes", "sass_compute", "sass_amplitudes",
     "sass_last_timing", "sass_set_phase_tile", "sass_frame_center", "sass_host_alloc",
-    "sass_host_free", "sass_probe_pipes", "sass_version",
+    "sass_host_free", "sass_probe_pipes", "sass_correlate_noalloc", "sass_version",
 ]
 
 
@@ -92,6 +92,8 @@ def load(path=LIB_PATH):
     L.sass_host_free.restype = None
     L.sass_version.restype = ctypes.c_char_p
     L.sass_probe_pipes.argtypes = [ctypes.c_int, _dp, _dp]
+    L.sass_correlate_noalloc.argtypes = [ctypes.c_int, _vp, _vp, _sz, _sz, _vp, ctypes.c_int, _vp,
+                                         _vp, _vp]
     _lib = L
     return L
 

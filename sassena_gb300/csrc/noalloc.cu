@@ -1,0 +1,199 @@
+// Allocation-free entry point: coherent autocorrelation + orientational average
+// from caller-provided amplitudes, with all working memory in one fixed,
+// file-scope device array.
+//
+// Who this is for: code that must not allocate GPU memory while it runs. Examples
+// are a host program that reserves all device memory up front and forbids further
+// cudaMalloc (a fixed memory budget shared with other solvers), code that runs
+// inside a memory-pool allocator's callback, and services that must not risk an
+// out-of-memory failure in the middle of a run. sass_compute allocates its working
+// buffers on demand; sass_correlate_noalloc instead uses the static array below,
+// which exists from the moment the library is loaded on a device.
+//
+// Limits: at most kMaxQ q-vectors per call and NF <= 4096 (padded FFT length 8192).
+// The array holds kScratchBytes (8,593,664 bytes, 8.2 MiB) on every GPU that loads the library,
+// until the process exits.
+//
+// Sharing: every call uses the same array and the array keeps the previous call's
+// contents. The partial sums are fully rewritten by each call before they are read
+// (no state carries over), but two calls that overlap on the GPU (different
+// streams, or different host threads) race on the array and corrupt each other's
+// results. Serialise calls, e.g. by issuing them on one stream.
+//
+// First call per device: the device address of the array is looked up with
+// cudaGetSymbolAddress (with that device current) on the first call that uses the
+// device. Make that first call before capturing work into a CUDA graph.
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "../../include/sassena_gb300.h"
+#include "common.cuh"
+#include "kernels.h"
+
+using namespace sassgpu;
+
+namespace {
+
+constexpr int kMaxLg = 13;                 // padded length 8192 => NF <= 4096
+constexpr int kMaxL = 1 << kMaxLg;
+constexpr int kMaxQ = 128;                 // q-vectors per call
+constexpr int kMaxSlots = 128;             // partial slots (chunks) per call
+constexpr int kMaxDevices = 64;
+
+// Byte layout of the scratch array (all offsets multiples of 256).
+constexpr size_t kOffPart = 0;                                             // double [slots][L]
+constexpr size_t kOffApart = kOffPart + (size_t)kMaxSlots * kMaxL * 8;     // double2 [slots]
+constexpr size_t kOffA2 = kOffApart + kMaxSlots * 16;                      // double [slots]
+constexpr size_t kOffTw = kOffA2 + kMaxSlots * 8 + 1024;                   // double2 [L/2]
+constexpr size_t kOffK = kOffTw + (size_t)(kMaxL / 2) * 16;                // double2 [L]
+constexpr size_t kOffChunks = kOffK + (size_t)kMaxL * 16;                  // SeriesChunk [slots]
+constexpr size_t kOffSlotBegin = kOffChunks + kMaxSlots * sizeof(SeriesChunk);  // int [Q+1]
+constexpr size_t kOffInvNm = kOffSlotBegin + 1024;                         // double [Q]
+constexpr size_t kScratchBytes = kOffInvNm + kMaxQ * 8 + 256;
+static_assert(kScratchBytes == 8593664, "documented scratch size");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+struct DeviceState {
+    bool ready = false;
+    unsigned char* base = nullptr;  // device address of g_noalloc_scratch
+    int table_nf = -1;              // NF whose FFT tables are in the array
+};
+std::mutex g_lock;
+DeviceState g_dev[kMaxDevices];
+
+// tw[k] = exp(-2 pi i k / L), k < L/2 (FP64 sincospi).
+__global__ void noalloc_twiddles(double2* tw, int L) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < L / 2; k += gridDim.x * blockDim.x) {
+        double s, c;
+        sincospi(-2.0 * (double)k / (double)L, &s, &c);
+        tw[k] = make_double2(c, s);
+    }
+}
+
+// K at bit-reversed position i: K(w) = sum_{tau<NF} exp(+2 pi i w tau / L) / (NF L (NF-tau)),
+// the weights that turn a power spectrum into the tau-mean of the normalised correlation.
+__global__ void noalloc_store_kernel_table(const double2* __restrict__ tw, double2* kbr, int nf,
+                                           int lg) {
+    const int L = 1 << lg;
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < L; w += gridDim.x * blockDim.x) {
+        double re = 0.0, im = 0.0;
+        long long m = 0;  // (w * tau) mod L
+        for (int t = 0; t < nf; ++t) {
+            const double wt = 1.0 / ((double)nf * (double)L * (double)(nf - t));
+            // exp(+2 pi i m / L) = conj(tw[m]) for m < L/2, -conj(tw[m - L/2]) otherwise
+            double2 z = m < L / 2 ? tw[m] : tw[m - L / 2];
+            double sg = m < L / 2 ? 1.0 : -1.0;
+            re += wt * sg * z.x;
+            im -= wt * sg * z.y;
+            m += w;
+            if (m >= L) m -= L;
+        }
+        int i = __brev((unsigned)w) >> (32 - lg);
+        kbr[i] = make_double2(re, im);
+    }
+}
+
+// Chunks of each q's sub-vectors (g per q, some possibly empty), slot offsets and 1/NM.
+__global__ void noalloc_schedule(const unsigned long long* __restrict__ offs, int nq, int g,
+                                 SeriesChunk* chunks, int* slot_begin, double* inv_nm) {
+    for (int c = threadIdx.x; c < nq * g; c += blockDim.x) {
+        const int s = c / g, k = c - s * g;
+        const long long b = (long long)offs[s], e = (long long)offs[s + 1];
+        const long long nm = e - b;
+        const long long len = nm > 0 ? (nm + g - 1) / g : 0;
+        long long vb = b + k * len, ve = vb + len;
+        if (vb > e) vb = e;
+        if (ve > e) ve = e;
+        SeriesChunk ch;
+        ch.shell = s;
+        ch.v_begin = (int)vb;
+        ch.v_end = (int)ve;
+        ch.slot = c;
+        chunks[c] = ch;
+    }
+    for (int s = threadIdx.x; s <= nq; s += blockDim.x) slot_begin[s] = s * g;
+    for (int s = threadIdx.x; s < nq; s += blockDim.x) {
+        const long long nm = (long long)offs[s + 1] - (long long)offs[s];
+        inv_nm[s] = nm > 0 ? 1.0 / (double)nm : __longlong_as_double(0x7ff8000000000000LL);
+    }
+}
+
+}  // namespace
+
+extern "C" int sass_correlate_noalloc(int device, void* stream, const double* amplitudes, size_t nf,
+                                      size_t nq, const uint64_t* sub_offsets, int dsp_method,
+                                      double* fqt, double* fq, double* fq2) {
+    if (!amplitudes || !sub_offsets || !fqt || !fq || !fq2) return SASS_ERR_ARG;
+    if (nf == 0 || nq == 0) return SASS_ERR_ARG;
+    if (dsp_method != SASS_METHOD_FFTW && dsp_method != SASS_METHOD_DIRECT) return SASS_ERR_ARG;
+    if (device < 0 || device >= kMaxDevices) return SASS_ERR_ARG;
+    int lg = 2;
+    while (((size_t)1 << lg) < 2 * nf) ++lg;
+    if (lg > kMaxLg || nq > (size_t)kMaxQ) return SASS_ERR_UNSUPPORTED;  // beyond the fixed array
+    cudaStream_t st = (cudaStream_t)stream;
+
+    std::lock_guard<std::mutex> guard(g_lock);
+    if (cudaSetDevice(device) != cudaSuccess) return SASS_ERR_CUDA;
+    DeviceState& ds = g_dev[device];
+    if (!ds.ready) {
+        void* addr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
+        if (e != cudaSuccess || addr == nullptr) {
+            cudaGetLastError();
+            return SASS_ERR_CUDA;
+        }
+        ds.base = static_cast<unsigned char*>(addr);
+        ds.ready = true;
+    }
+    unsigned char* b = ds.base;
+    double2* tw = reinterpret_cast<double2*>(b + kOffTw);
+    double2* kbr = reinterpret_cast<double2*>(b + kOffK);
+    if (ds.table_nf != (int)nf) {
+        const int L = 1 << lg;
+        noalloc_twiddles<<<(L / 2 + 255) / 256, 256, 0, st>>>(tw, L);
+        noalloc_store_kernel_table<<<(L + 127) / 128, 128, 0, st>>>(tw, kbr, (int)nf, lg);
+        if (cudaGetLastError() != cudaSuccess) return SASS_ERR_CUDA;
+        ds.table_nf = (int)nf;
+    }
+    const int g = kMaxSlots / (int)nq;  // chunks per q (>= 1)
+    SeriesChunk* chunks = reinterpret_cast<SeriesChunk*>(b + kOffChunks);
+    int* slot_begin = reinterpret_cast<int*>(b + kOffSlotBegin);
+    double* inv_nm = reinterpret_cast<double*>(b + kOffInvNm);
+    noalloc_schedule<<<1, 256, 0, st>>>(reinterpret_cast<const unsigned long long*>(sub_offsets),
+                                        (int)nq, g, chunks, slot_begin, inv_nm);
+    if (cudaGetLastError() != cudaSuccess) return SASS_ERR_CUDA;
+
+    CorrArgs ca{};
+    ca.precision = PREC_FP64;
+    ca.nf = (int)nf;
+    ca.lg = lg;
+    ca.A = reinterpret_cast<const double2*>(amplitudes);
+    ca.tw = tw;
+    ca.kbr = kbr;
+    ca.chunks = chunks;
+    ca.nchunks = (int)nq * g;
+    ca.ppart = reinterpret_cast<double*>(b + kOffPart);
+    ca.apart = reinterpret_cast<double2*>(b + kOffApart);
+    ca.a2part = reinterpret_cast<double*>(b + kOffA2);
+    if (launch_corr_accumulate(ca, DSP_AUTOCORRELATE, st) != cudaSuccess) return SASS_ERR_CUDA;
+
+    FinalizeArgs fa{};
+    fa.nf = (int)nf;
+    fa.lg = lg;
+    fa.dsp = DSP_AUTOCORRELATE;
+    fa.conj_out = dsp_method == SASS_METHOD_DIRECT;
+    fa.ppart = ca.ppart;
+    fa.apart = ca.apart;
+    fa.a2part = ca.a2part;
+    fa.slot_begin = slot_begin;
+    fa.inv_nm = inv_nm;
+    fa.tw = tw;
+    fa.fqt = reinterpret_cast<double2*>(fqt);
+    fa.fq = reinterpret_cast<double2*>(fq);
+    fa.fq2 = reinterpret_cast<double2*>(fq2);
+    fa.nshell = (int)nq;
+    if (launch_finalize(fa, st) != cudaSuccess) return SASS_ERR_CUDA;
+    return SASS_OK;
+}
