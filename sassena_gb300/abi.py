@@ -223,3 +223,88 @@ def compute_workload(w, precision="fp64", method="fftw", device=0, tile=None):
         if tile:
             p.set_tile(*tile)
         return p.compute(w.sub_offsets(), w.subvectors(), w.class_factors)
+
+
+# ----------------------------------------------------------------------------------------
+# Host layer (no GPU): signal-file writer/reader and configuration parsing
+# ----------------------------------------------------------------------------------------
+HOST_LIB_PATH = os.path.join(_PKG, "_lib", "libsassena_host.so")
+DRIVER_PATH = os.path.join(_PKG, "_lib", "sassena-gpu")
+_host = None
+
+
+def host():
+    global _host
+    if _host is None:
+        if not os.path.exists(HOST_LIB_PATH):
+            raise OSError("host library not built: %s" % HOST_LIB_PATH)
+        H = ctypes.CDLL(HOST_LIB_PATH)
+        H.sass_host_error.restype = ctypes.c_char_p
+        H.sass_host_signal_write.argtypes = [ctypes.c_char_p, _sz, _sz, _vp, _vp, _vp, _vp, _vp,
+                                             ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p]
+        H.sass_host_signal_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(_sz),
+                                            ctypes.POINTER(_sz), ctypes.POINTER(ctypes.c_int),
+                                            _vp, _vp, _vp, _vp, _vp]
+        H.sass_host_config_qvectors.argtypes = [ctypes.c_char_p, _vp, _sz, ctypes.POINTER(_sz)]
+        _host = H
+    return _host
+
+
+def write_signal(path, qvectors, fqt=None, fq0=None, fq=None, fq2=None, rawconfig="",
+                 database=""):
+    """Write a signal.h5 (complex arrays; None = dataset not written)."""
+    H = host()
+    q = np.ascontiguousarray(qvectors, dtype=np.float64).reshape(-1, 3)
+    nq = len(q)
+    nf = 0 if fqt is None else np.asarray(fqt).shape[1]
+
+    def ri(a, shape):
+        if a is None:
+            return None
+        a = np.asarray(a, dtype=np.complex128).reshape(shape)
+        return np.ascontiguousarray(np.stack([a.real, a.imag], axis=-1))
+
+    arrs = [ri(fqt, (nq, nf)), ri(fq0, (nq,)), ri(fq, (nq,)), ri(fq2, (nq,))]
+    flags = sum(1 << i for i, a in enumerate(arrs) if a is not None)
+    ptrs = [a.ctypes.data_as(_vp) if a is not None else None for a in arrs]
+    rc = H.sass_host_signal_write(path.encode(), nq, nf, q.ctypes.data_as(_vp), *ptrs, flags,
+                                  rawconfig.encode(), database.encode())
+    if rc:
+        raise RuntimeError(H.sass_host_error().decode())
+
+
+def read_signal(path):
+    """Read a signal.h5 with the host library: dict of complex arrays + qvectors."""
+    H = host()
+    nq, nf, flags = _sz(), _sz(), ctypes.c_int()
+    rc = H.sass_host_signal_read(path.encode(), ctypes.byref(nq), ctypes.byref(nf),
+                                 ctypes.byref(flags), None, None, None, None, None)
+    if rc:
+        raise RuntimeError(H.sass_host_error().decode())
+    q = np.zeros((nq.value, 3))
+    fqt = np.zeros((nq.value, nf.value, 2))
+    f0, f1, f2 = (np.zeros((nq.value, 2)) for _ in range(3))
+    rc = H.sass_host_signal_read(path.encode(), ctypes.byref(nq), ctypes.byref(nf),
+                                 ctypes.byref(flags), q.ctypes.data_as(_vp),
+                                 fqt.ctypes.data_as(_vp), f0.ctypes.data_as(_vp),
+                                 f1.ctypes.data_as(_vp), f2.ctypes.data_as(_vp))
+    if rc:
+        raise RuntimeError(H.sass_host_error().decode())
+    c = lambda a: a[..., 0] + 1j * a[..., 1]  # noqa: E731
+    out = {"qvectors": q}
+    for bit, name, arr in ((1, "fqt", fqt), (2, "fq0", f0), (4, "fq", f1), (8, "fq2", f2)):
+        if flags.value & bit:
+            out[name] = c(arr)
+    return out
+
+
+def config_qvectors(config_path):
+    H = host()
+    n = _sz()
+    rc = H.sass_host_config_qvectors(config_path.encode(), None, 0, ctypes.byref(n))
+    if rc:
+        raise RuntimeError(H.sass_host_error().decode())
+    out = np.zeros((n.value, 3))
+    H.sass_host_config_qvectors(config_path.encode(), out.ctypes.data_as(_vp), n.value,
+                                ctypes.byref(n))
+    return out

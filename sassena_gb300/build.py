@@ -93,8 +93,9 @@ def build(verbose=False, jobs=None):
     if _stale(LIB, objs):
         _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
     if hs:
-        if _stale(HOST_LIB, hs):
-            _run([CXX, "-shared", "-o", HOST_LIB] + hs + ["-pthread"])
+        if _stale(HOST_LIB, hs + [LIB]):
+            _run([CXX, "-shared", "-o", HOST_LIB] + hs + ["-L" + OUT, "-lsassena_gb300",
+                                                         "-Wl,-rpath,$ORIGIN", "-pthread"])
         drv_src = os.path.join(HOST, "sassena_gpu.cpp")
         if os.path.exists(drv_src) and _stale(DRIVER, [drv_src, HOST_LIB, LIB] + _deps(drv_src)):
             _run([CXX] + CXX_FLAGS + [drv_src, "-o", DRIVER, "-L" + OUT, "-lsassena_host",

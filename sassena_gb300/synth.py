@@ -216,3 +216,118 @@ WORKLOADS = {
     "coherent_sqt": coherent_sqt,
     "static_xray": static_xray,
 }
+
+
+# ----------------------------------------------------------------------------------------
+# Files for the sassena-gpu driver: PDB + DCD + db.xml + scatter.xml (+ orientation file)
+# ----------------------------------------------------------------------------------------
+PDB_NAMES = {"H": "H1", "C": "C1", "N": "N1", "O": "O1", "S": "S1"}
+
+
+def write_pdb(path, w):
+    """ATOM records whose names map through db.xml's names/pdb regexes (atoms.cpp:64-86)."""
+    with open(path, "w") as f:
+        r0 = w.coords[0]
+        for j in range(w.na):
+            nm = PDB_NAMES.get(w.class_names[w.atom_class[j]], w.class_names[w.atom_class[j]])
+            f.write("ATOM  %5d %-4s MOL A   1    %8.3f%8.3f%8.3f  1.00  0.00\n"
+                    % ((j + 1) % 100000, nm, r0[j, 0], r0[j, 1], r0[j, 2]))
+        f.write("END\n")
+
+
+def write_dcd(path, coords):
+    """CHARMM DCD as the reference's DCDCoordinateWriter lays it out (coordinate_writer.cpp:37-144):
+    84-byte header (unit-cell block flag set), empty title, natoms, then per frame a 48-byte
+    unit cell and the X, Y, Z records."""
+    import struct
+    coords = np.asarray(coords, dtype=np.float32)
+    nf, na = coords.shape[0], coords.shape[1]
+    with open(path, "wb") as f:
+        hdr = struct.pack("<i4s9if13i", 84, b"CORD", nf, 0, 1, 0, 0, 0, 0, 0, 0, 1.0,
+                          1, 0, 0, 0, 0, 0, 0, 0, 0, 24, 84, 4, 0)
+        # 84 | CORD | nf 0 1 0*6 | dt | ext1=1 ext2=0 0*7 24 | 84, then title record 4 0 4
+        f.write(hdr)
+        f.write(struct.pack("<i", 4))
+        f.write(struct.pack("<3i", 4, na, 4))
+        cell = struct.pack("<i6di", 48, 0, 0, 0, 0, 0, 0, 48)
+        rec = struct.pack("<i", 4 * na)
+        for t in range(nf):
+            f.write(cell)
+            for k in range(3):
+                f.write(rec)
+                f.write(np.ascontiguousarray(coords[t, :, k]).tobytes())
+                f.write(rec)
+
+
+def write_database(path, w, sfactor_params=None):
+    """db.xml: names/pdb regexes, masses, sizes, exclusion factors and scattering factors
+    (type 0 constants from the workload's class factors, or type 2 parameter vectors)."""
+    lines = ["<?xml version=\"1.0\"?>", "<root>", "<names><pdb>"]
+    for c in w.class_names:
+        lines.append("<element><name>%s</name><param>%s[0-9]*</param></element>" % (c, c))
+    lines.append("</pdb></names><masses>")
+    for c in w.class_names:
+        lines.append("<element><name>%s</name><param>1.0</param></element>" % c)
+    lines.append("</masses><sizes>")
+    for c in w.class_names:
+        lines.append("<element><name>%s</name><type>0</type><param>1.0</param></element>" % c)
+    lines.append("</sizes><exclusionfactors>")
+    for c in w.class_names:
+        lines.append("<element><name>%s</name><type>0</type><param>0.0</param></element>" % c)
+    lines.append("</exclusionfactors><scatterfactors>")
+    for i, c in enumerate(w.class_names):
+        if sfactor_params is not None:
+            ps = "".join("<param>%.17g</param>" % v for v in sfactor_params[i])
+            lines.append("<element><name>%s</name><type>2</type>%s</element>" % (c, ps))
+        else:
+            lines.append("<element><name>%s</name><type>0</type><param>%.17g</param></element>"
+                         % (c, w.class_factors[0, i]))
+    lines.append("</scatterfactors></root>")
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def write_files(directory, w, precision="fp64", method="fftw", qvectors_file=True,
+                signal="signal.h5", sfactor_params=None, extra=""):
+    """Write sample.pdb, sample.dcd, db.xml, qvectors.txt, orientations.txt and scatter.xml
+    for workload `w` into `directory`; returns the scatter.xml path.
+
+    q-vectors are |q_s| along x (the orientation set ignores the q direction,
+    abstract_vectors_scatter_device.cpp:123-129) and the directions come from a file
+    (vectors.type=file, parameters.cpp:932-943)."""
+    import os
+    os.makedirs(directory, exist_ok=True)
+    write_pdb(os.path.join(directory, "sample.pdb"), w)
+    write_dcd(os.path.join(directory, "sample.dcd"), w.coords)
+    write_database(os.path.join(directory, "db.xml"), w, sfactor_params)
+    with open(os.path.join(directory, "qvectors.txt"), "w") as f:
+        for q in w.shells:
+            f.write("%.17g 0 0\n" % q)
+    with open(os.path.join(directory, "orientations.txt"), "w") as f:
+        for d in w.directions:
+            f.write("%.17g %.17g %.17g\n" % tuple(d))
+    xml = """<?xml version="1.0"?>
+<root>
+  <sample>
+    <structure><file>sample.pdb</file><format>pdb</format></structure>
+    <framesets><frameset><file>sample.dcd</file><format>dcd</format></frameset></framesets>
+  </sample>
+  <database><type>file</type><file>db.xml</file></database>
+  <scattering>
+    <type>%(type)s</type>
+    <vectors><type>file</type><file>qvectors.txt</file></vectors>
+    <dsp><type>%(dsp)s</type><method>%(method)s</method></dsp>
+    <average><orientation><type>vectors</type>
+      <vectors><type>file</type><file>orientations.txt</file></vectors>
+    </orientation></average>
+    <signal><file>%(signal)s</file></signal>
+  </scattering>
+  <gpu><precision>%(precision)s</precision></gpu>
+  %(extra)s
+</root>
+""" % dict(type=w.scattering, dsp=w.dsp, method=method, signal=signal, precision=precision,
+           extra=extra)
+    path = os.path.join(directory, "scatter.xml")
+    with open(path, "w") as f:
+        f.write(xml)
+    return path

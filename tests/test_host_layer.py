@@ -1,0 +1,191 @@
+"""CPU tests of the C++ host layer: configuration, database, PDB/DCD, staging,
+scatter-factor classes, sub-vectors and the signal.h5 writer/reader (no GPU)."""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from sassena_gb300 import abi, synth
+
+import h5lite
+
+
+def run_driver(*args):
+    return subprocess.run([abi.DRIVER_PATH] + list(args), capture_output=True, text=True)
+
+
+def dry(cfg, tmp_path, *extra):
+    out = str(tmp_path / "dry.json")
+    r = run_driver("--config", cfg, "--dry-run", out, *extra)
+    assert r.returncode == 0, r.stderr
+    return json.load(open(out))
+
+
+# ---- signal.h5 ----------------------------------------------------------------------------
+def test_signal_roundtrip_and_structure(tmp_path):
+    rng = np.random.default_rng(0)
+    nq, nf = 7, 13
+    q = rng.normal(size=(nq, 3))
+    fqt = rng.normal(size=(nq, nf)) + 1j * rng.normal(size=(nq, nf))
+    fq = rng.normal(size=nq) + 1j * rng.normal(size=nq)
+    fq2 = rng.normal(size=nq) + 0j
+    path = str(tmp_path / "signal.h5")
+    abi.write_signal(path, q, fqt, fqt[:, 0], fq, fq2, rawconfig="<root>cfg</root>",
+                     database="<root>db</root>")
+    # the host reader
+    d = abi.read_signal(path)
+    assert np.array_equal(d["qvectors"], q)
+    assert np.array_equal(d["fqt"], fqt) and np.array_equal(d["fq2"], fq2)
+    # an independent reader, with structural checks
+    f = h5lite.File(path)
+    assert sorted(f.root) == ["fq", "fq0", "fq2", "fqt", "meta", "qvectors"]
+    assert np.array_equal(f.read("qvectors"), q)
+    got = f.read("fqt")
+    assert got.shape == (nq, nf, 2) and got.dtype == np.float64
+    assert np.array_equal(got[..., 0] + 1j * got[..., 1], fqt)
+    assert np.array_equal(f.read("fq0"), np.stack([fqt[:, 0].real, fqt[:, 0].imag], 1))
+    assert f.read("meta/config") == b"<root>cfg</root>"
+    assert f.read("meta/database") == b"<root>db</root>"
+    raw = f.read("meta/rawconfig")
+    assert raw.dtype == np.int8 and raw.tobytes() == b"<root>cfg</root>"
+
+
+def test_signal_optional_datasets(tmp_path):
+    path = str(tmp_path / "s.h5")
+    abi.write_signal(path, np.ones((2, 3)), fqt=None, fq0=None, fq=np.array([1 + 2j, 3]),
+                     fq2=None)
+    f = h5lite.File(path)
+    assert sorted(f.root) == ["fq", "meta", "qvectors"]
+    d = abi.read_signal(path)
+    assert "fqt" not in d and np.allclose(d["fq"], [1 + 2j, 3])
+
+
+def test_signal_reader_rejects_non_hdf5(tmp_path):
+    p = tmp_path / "x.h5"
+    p.write_bytes(b"not an hdf5 file" * 10)
+    with pytest.raises(RuntimeError):
+        abi.read_signal(str(p))
+
+
+# ---- configuration, sample, staging ---------------------------------------------------------
+@pytest.fixture
+def small_files(tmp_path):
+    w = synth.small("all", "autocorrelate", seed=21, na=23, nf=9, nq=3, nm=4)
+    cfg = synth.write_files(str(tmp_path / "run"), w)
+    return w, cfg
+
+
+def test_dry_run_matches_workload(small_files, tmp_path):
+    w, cfg = small_files
+    d = dry(cfg, tmp_path)
+    assert d["nf"] == w.nf and d["na"] == w.na
+    assert np.allclose(np.array(d["qvectors"])[:, 0], w.shells, rtol=0, atol=0)
+    # orientations from a file are normalised (parameters.cpp:932-943)
+    assert np.allclose(d["orientations"], w.directions, atol=1e-15)
+    assert np.allclose(d["subvectors_q0"], w.shells[0] * w.directions, atol=1e-15)
+    labels = d["class_labels"]
+    cls = np.array(d["atom_class"])
+    assert [labels[c] for c in cls] == [w.class_names[c] for c in w.atom_class]
+    cf = np.array(d["class_factors"])
+    order = [w.class_names.index(l) for l in labels]
+    assert np.allclose(cf, w.class_factors[0][order][None, :].repeat(w.nq, 0))
+    # DCD written in the reference's layout reads back bit-exactly (float32 staging)
+    assert d["coord_sum"] == pytest.approx(float(w.coords.astype(np.float64).sum()), rel=1e-12)
+
+
+def test_scans_follow_reference(tmp_path):
+    w = synth.small("all", seed=2, na=5, nf=3, nq=1, nm=1)
+    cfg = synth.write_files(str(tmp_path / "s"), w)
+    txt = open(cfg).read().replace(
+        "<vectors><type>file</type><file>qvectors.txt</file></vectors>",
+        "<vectors><type>scans</type><scans><scan><base><x>0.3</x><y>0.4</y><z>1.2</z></base>"
+        "<from>0.1</from><to>2.0</to><points>17</points><exponent>1.7</exponent></scan>"
+        "</scans></vectors>")
+    open(cfg, "w").write(txt)
+    q = abi.config_qvectors(cfg)
+    ref = oracle.scan([0.3, 0.4, 1.2], 0.1, 2.0, 17, 1.7)
+    assert np.array_equal(q, ref)  # float powf reproduced bit for bit
+
+
+def test_type2_form_factors_and_background(tmp_path):
+    rng = np.random.default_rng(3)
+    w = synth.small("all", "square", seed=4, na=11, nf=2, nq=4, nm=2)
+    params = synth.xray_form_factor_params(rng, len(w.class_names))
+    cfg = synth.write_files(str(tmp_path / "x"), w, sfactor_params=params)
+    d = dry(cfg, tmp_path)
+    labels = d["class_labels"]
+    cf = np.array(d["class_factors"])
+    for i, q in enumerate(w.shells):
+        for c, l in enumerate(labels):
+            v = params[w.class_names.index(l)]
+            assert cf[i, c] == pytest.approx(oracle.sfactor(2, v, q), rel=1e-15)
+
+
+def test_frameset_first_last_stride_clones(small_files, tmp_path):
+    w, cfg = small_files
+    txt = open(cfg).read().replace(
+        "<frameset><file>sample.dcd</file><format>dcd</format></frameset>",
+        "<frameset><file>sample.dcd</file><format>dcd</format><first>1</first><last>7</last>"
+        "<stride>2</stride><clones>2</clones></frameset>")
+    open(cfg, "w").write(txt)
+    d = dry(cfg, tmp_path)
+    # trim_index keeps i >= first, i <= last and i % stride == 0 (absolute index)
+    keep = [i for i in range(w.nf) if i >= 1 and i <= 7 and i % 2 == 0]
+    assert d["nf"] == 2 * len(keep)
+    expect = 2 * w.coords[keep].astype(np.float64).sum()
+    assert d["coord_sum"] == pytest.approx(expect, rel=1e-12)
+
+
+def test_target_selection_range(small_files, tmp_path):
+    w, cfg = small_files
+    txt = open(cfg).read().replace(
+        "</sample>",
+        "<selections><selection><type>range</type><name>part</name><from>3</from><to>9</to>"
+        "</selection></selections></sample><stager><target>part</target></stager>")
+    open(cfg, "w").write(txt)
+    d = dry(cfg, tmp_path)
+    assert d["na"] == 7
+    assert d["coord_sum"] == pytest.approx(float(w.coords[:, 3:10].astype(np.float64).sum()),
+                                           rel=1e-12)
+
+
+@pytest.mark.parametrize("edit,needle", [
+    (("<type>autocorrelate</type>", "<type>bogus</type>"), "DSP type not understood"),
+    (("sample.dcd</file>", "missing.dcd</file>"), "DCD"),
+    (("<file>db.xml</file>", "<file>nodb.xml</file>"), "does not exist"),
+    (("<type>vectors</type>", "<type>multipole</type>"), "multipole"),
+])
+def test_driver_errors(small_files, tmp_path, edit, needle):
+    w, cfg = small_files
+    txt = open(cfg).read().replace(*edit)
+    open(cfg, "w").write(txt)
+    r = run_driver("--config", cfg, "--dry-run", str(tmp_path / "o.json"))
+    assert r.returncode == 1
+    assert needle in r.stderr
+
+
+def test_dcd_atom_count_mismatch(small_files, tmp_path):
+    w, cfg = small_files
+    synth.write_dcd(os.path.join(os.path.dirname(cfg), "sample.dcd"), w.coords[:, :-1])
+    r = run_driver("--config", cfg, "--dry-run", str(tmp_path / "o.json"))
+    assert r.returncode == 1 and "Atom number mismatch" in r.stderr
+
+
+def test_truncated_dcd(small_files, tmp_path):
+    w, cfg = small_files
+    p = os.path.join(os.path.dirname(cfg), "sample.dcd")
+    data = open(p, "rb").read()
+    open(p, "wb").write(data[:-20])
+    r = run_driver("--config", cfg, "--dry-run", str(tmp_path / "o.json"))
+    assert r.returncode == 1 and "truncated" in r.stderr
+
+
+def test_command_line_overrides(small_files, tmp_path):
+    w, cfg = small_files
+    d = dry(cfg, tmp_path, "--scattering.signal.file=other.h5", "--gpu.precision", "fp32")
+    assert d["signal"].endswith("other.h5") and d["precision"] == "fp32"
+    r = run_driver("--config", cfg, "--dry-run", str(tmp_path / "o.json"), "--no.such=1")
+    assert r.returncode == 1 and "unknown option" in r.stderr
