@@ -390,8 +390,9 @@ int run_batch(sass_plan* p, size_t nshell, const size_t* offs, const double* d_q
 
     if (p->d.scattering == SASS_SCATTERING_ALL) {
         // --- phase sum ----------------------------------------------------------
-        CK(p, p->A.ensure(nv * p->nf * sizeof(double2)));
-        double2* dst = p->A.as<double2>();
+        const bool f32 = p->d.precision == SASS_PRECISION_FP32;
+        CK(p, p->A.ensure(nv * p->nf * (f32 ? sizeof(float2) : sizeof(double2))));
+        double2* dst = f32 ? nullptr : p->A.as<double2>();
         if (nsplit > 1) {
             CK(p, p->Apart.ensure((size_t)nsplit * nv * p->nf * sizeof(double2)));
             dst = p->Apart.as<double2>();
@@ -409,6 +410,7 @@ int run_batch(sass_plan* p, size_t nshell, const size_t* offs, const double* d_q
         size_t tiles = p->na_pad / tile.atoms;
         a.atoms_per_split = (int)(((tiles + nsplit - 1) / nsplit) * tile.atoms);
         a.out = dst;
+        a.out_f32 = (f32 && nsplit == 1) ? p->A.as<float2>() : nullptr;
         a.split_stride = nv * p->nf;
         a.err = p->err.as<unsigned>();
         a.tile = tile;
@@ -417,12 +419,13 @@ int run_batch(sass_plan* p, size_t nshell, const size_t* offs, const double* d_q
         p->timing.kernel_launches++;
         p->timing.phase_launches++;
         if (nsplit > 1) {
-            CK(p, launch_split_reduce(dst, nsplit, nv * p->nf, p->A.as<double2>(), p->st));
+            if (f32) CK(p, launch_split_reduce_f32(dst, nsplit, nv * p->nf, p->A.as<float2>(), p->st));
+            else CK(p, launch_split_reduce(dst, nsplit, nv * p->nf, p->A.as<double2>(), p->st));
             p->timing.kernel_launches++;
         }
         ev_record(p, 3);
         // --- correlation / store -------------------------------------------------
-        ca.A = p->A.as<double2>();
+        ca.A = p->A.p;
         ca.chunks = sp.chunks;
         ca.nchunks = (int)s.chunks.size();
         ev_record(p, 4);
@@ -772,8 +775,9 @@ int sass_amplitudes(sass_plan* p, size_t nsub, const double* subvectors, const i
     else if (ctas < (size_t)sm_count(p->device) * 4)
         nsplit = (int)std::min<size_t>(max_split, (sm_count(p->device) * 4 + ctas - 1) / ctas);
     nsplit = std::max(nsplit, 1);
-    CK(p, p->A.ensure(nsub * p->nf * sizeof(double2)));
-    double2* dst = p->A.as<double2>();
+    const bool f32 = p->d.precision == SASS_PRECISION_FP32;
+    CK(p, p->A.ensure(nsub * p->nf * (f32 ? sizeof(float2) : sizeof(double2))));
+    double2* dst = f32 ? nullptr : p->A.as<double2>();
     if (nsplit > 1) {
         CK(p, p->Apart.ensure((size_t)nsplit * nsub * p->nf * sizeof(double2)));
         dst = p->Apart.as<double2>();
@@ -791,16 +795,30 @@ int sass_amplitudes(sass_plan* p, size_t nsub, const double* subvectors, const i
     size_t tiles = p->na_pad / tile.atoms;
     a.atoms_per_split = (int)(((tiles + nsplit - 1) / nsplit) * tile.atoms);
     a.out = dst;
+    a.out_f32 = (f32 && nsplit == 1) ? p->A.as<float2>() : nullptr;
     a.split_stride = nsub * p->nf;
     a.err = p->err.as<unsigned>();
     a.tile = tile;
     ev_record(p, 2);
     CK(p, launch_phase_sum(a, p->st));
-    if (nsplit > 1) CK(p, launch_split_reduce(dst, nsplit, nsub * p->nf, p->A.as<double2>(), p->st));
+    if (nsplit > 1) {
+        if (f32) CK(p, launch_split_reduce_f32(dst, nsplit, nsub * p->nf, p->A.as<float2>(), p->st));
+        else CK(p, launch_split_reduce(dst, nsplit, nsub * p->nf, p->A.as<double2>(), p->st));
+    }
     ev_record(p, 3);
-    CK(p, cudaMemcpyAsync(out, p->A.p, nsub * p->nf * sizeof(double2), cudaMemcpyDeviceToHost, p->st));
+    std::vector<float2> a32;
+    if (f32) {
+        a32.resize(nsub * p->nf);
+        CK(p, cudaMemcpyAsync(a32.data(), p->A.p, a32.size() * sizeof(float2), cudaMemcpyDeviceToHost, p->st));
+    } else {
+        CK(p, cudaMemcpyAsync(out, p->A.p, nsub * p->nf * sizeof(double2), cudaMemcpyDeviceToHost, p->st));
+    }
     rc = read_device_error(p);
     if (rc) return rc;
+    for (size_t i = 0; i < a32.size(); ++i) {
+        out[2 * i] = a32[i].x;
+        out[2 * i + 1] = a32[i].y;
+    }
     p->timing.phase_ms = ev_ms(p, 2, 3);
     p->timing.phase_launches = 1;
     p->timing.kernel_launches = 2 + (nsplit > 1);

@@ -38,7 +38,6 @@ __device__ __forceinline__ double2 zero2<double2>() {
 
 __device__ __forceinline__ void conv(float2& d, double2 s) { d = make_float2((float)s.x, (float)s.y); }
 __device__ __forceinline__ void conv(double2& d, double2 s) { d = s; }
-__device__ __forceinline__ void conv(float2& d, float2 s) { d = s; }
 __device__ __forceinline__ double2 to_d2(float2 a) { return make_double2(a.x, a.y); }
 __device__ __forceinline__ double2 to_d2(double2 a) { return a; }
 
@@ -201,7 +200,7 @@ __device__ __forceinline__ void write_power(const PowerAcc<T, MAXR>& acc, int L,
 // ---------------------------------------------------------------------------
 template <class T, int NT, int MAXR>
 __global__ void __launch_bounds__(NT)
-    corr_fft_kernel(const double2* __restrict__ A, int nf, int lg, const void* tw_,
+    corr_fft_kernel(const void* __restrict__ A_, int nf, int lg, const void* tw_,
                     const void* kbr_, const SeriesChunk* __restrict__ chunks,
                     double* __restrict__ ppart, double2* __restrict__ apart,
                     double* __restrict__ a2part) {
@@ -229,10 +228,10 @@ __global__ void __launch_bounds__(NT)
     double a2sum = 0.0;
     __syncthreads();
     for (int v = c.v_begin; v < c.v_end; ++v) {
-        const double2* src = A + (size_t)v * nf;
+        const T2* src = reinterpret_cast<const T2*>(A_) + (size_t)v * nf;
         for (int p = threadIdx.x; p < half; p += NT) {
             T2 x = zero2<T2>();
-            if (p < nf) conv(x, src[p]);
+            if (p < nf) x = src[p];
             buf[p] = x;
             buf[p + half] = cmul(x, tw[p]);
         }
@@ -332,9 +331,9 @@ __global__ void __launch_bounds__(NT)
 // dsp = square | plain (no transform): C_v(t) = |A_v(t)|^2 or A_v(t) * exp(i q_v.c).
 // Partials are complex per frame: ppart as double2 [slot][nf].
 // ---------------------------------------------------------------------------
-template <int NT, int MAXT>
+template <class AT, int NT, int MAXT>
 __global__ void __launch_bounds__(NT)
-    corr_direct_kernel(const double2* __restrict__ A, int nf, int square, const double* __restrict__ qv,
+    corr_direct_kernel(const AT* __restrict__ A, int nf, int square, const double* __restrict__ qv,
                        double cx, double cy, double cz, int restore, const SeriesChunk* __restrict__ chunks,
                        double2* __restrict__ ppart, double2* __restrict__ apart,
                        double* __restrict__ a2part) {
@@ -356,7 +355,7 @@ __global__ void __launch_bounds__(NT)
         for (int r = 0; r < MAXT; ++r) {
             const int t = threadIdx.x + r * NT;
             if (t < nf) {
-                double2 a = A[(size_t)v * nf + t];
+                double2 a = to_d2(A[(size_t)v * nf + t]);
                 double2 cv = square ? make_double2(a.x * a.x + a.y * a.y, 0.0) : cmul(a, ph);
                 acc[r].x += cv.x;
                 acc[r].y += cv.y;
@@ -594,9 +593,14 @@ cudaError_t launch_corr_accumulate(const CorrArgs& a, int dsp, cudaStream_t st) 
                          : launch_corr_fft<double, 256, 32>(a, st);
     }
     if (a.nf > 256 * 16) return cudaErrorInvalidValue;
-    corr_direct_kernel<256, 16><<<a.nchunks, 256, 0, st>>>(
-        a.A, a.nf, dsp == DSP_SQUARE, a.qv, a.cx, a.cy, a.cz, a.restore_phase, a.chunks,
-        reinterpret_cast<double2*>(a.ppart), a.apart, a.a2part);
+    if (a.precision == PREC_FP32)
+        corr_direct_kernel<float2, 256, 16><<<a.nchunks, 256, 0, st>>>(
+            reinterpret_cast<const float2*>(a.A), a.nf, dsp == DSP_SQUARE, a.qv, a.cx, a.cy, a.cz,
+            a.restore_phase, a.chunks, reinterpret_cast<double2*>(a.ppart), a.apart, a.a2part);
+    else
+        corr_direct_kernel<double2, 256, 16><<<a.nchunks, 256, 0, st>>>(
+            reinterpret_cast<const double2*>(a.A), a.nf, dsp == DSP_SQUARE, a.qv, a.cx, a.cy, a.cz,
+            a.restore_phase, a.chunks, reinterpret_cast<double2*>(a.ppart), a.apart, a.a2part);
     return cudaGetLastError();
 }
 

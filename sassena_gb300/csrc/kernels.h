@@ -44,7 +44,8 @@ struct PhaseSumArgs {
     int ngroups;
     int nsplit;               // atom splits (grid z)
     int atoms_per_split;      // multiple of the tile's atom count
-    double2* out;             // [nsplit][nv_total][nf]
+    double2* out;             // FP64: [nv_total][nf]; FP32 with nsplit > 1: [nsplit][nv_total][nf]
+    float2* out_f32;          // FP32 with nsplit == 1: [nv_total][nf]
     size_t split_stride;      // elements between splits of `out`
     unsigned int* err;
     PhaseTile tile;
@@ -52,9 +53,11 @@ struct PhaseSumArgs {
 
 bool phase_tile_supported(int precision, PhaseTile t);
 cudaError_t launch_phase_sum(const PhaseSumArgs& a, cudaStream_t st);
-// out[v][f] = sum_s part[s][v][f] in split order (FP64).
+// out[v][f] = sum_s part[s][v][f] in split order (FP64), stored as double2 or float2.
 cudaError_t launch_split_reduce(const double2* part, int nsplit, size_t n, double2* out,
                                 cudaStream_t st);
+cudaError_t launch_split_reduce_f32(const double2* part, int nsplit, size_t n, float2* out,
+                                    cudaStream_t st);
 
 // Work unit of the correlation / store kernels: series [v_begin, v_end) of one
 // shell, reduced into partial slot `slot`.
@@ -70,7 +73,7 @@ struct AtomChunk {
 struct CorrArgs {
     int precision;
     int nf, lg;                 // FFT length L = 1 << lg >= 2*nf
-    const double2* A;           // [nv][nf] amplitudes (coherent)
+    const void* A;              // [nv][nf] amplitudes: float2 (FP32) or double2 (FP64)
     const void* tw;             // [L/2] exp(-2 pi i k / L), float2 (FP32) or double2 (FP64)
     const void* kbr;            // [L] bit-reversed store kernel, same type as tw
     const SeriesChunk* chunks;  // coherent chunks

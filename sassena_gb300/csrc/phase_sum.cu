@@ -62,8 +62,8 @@ __global__ void __launch_bounds__(W * 32)
     phase_sum_fp32_kernel(const float4* __restrict__ xyz, int na_pad, int nf,
                           const float* __restrict__ bfac, const double* __restrict__ qv,
                           const VecGroup* __restrict__ groups, int atoms_per_split,
-                          double2* __restrict__ out, size_t split_stride, int nv_total,
-                          unsigned int* err) {
+                          double2* __restrict__ out, float2* __restrict__ out_f32,
+                          size_t split_stride, unsigned int* err) {
     using L = PipeLayout<W, T, S, 4>;
     static_assert(S * T >= 32 * Q, "output staging must fit in the coordinate ring");
     extern __shared__ __align__(128) unsigned char smem[];
@@ -182,7 +182,18 @@ __global__ void __launch_bounds__(W * 32)
             make_double2((double)sr[k] - (double)cr[k], (double)si[k] - (double)ci[k]);
     }
     __syncthreads();
-    double2* dst = out + (size_t)blockIdx.z * split_stride;
+    if (out_f32) {  // single atom split: the result goes straight to FP32 amplitudes
+        for (int idx = threadIdx.x; idx < g.nv * W; idx += W * 32) {
+            int vl = idx / W, w = idx - vl * W;
+            int ff = blockIdx.x * W + w;
+            if (ff < nf) {
+                double2 v = so[vl * W + w];
+                out_f32[(size_t)(g.v0 + vl) * nf + ff] = make_float2((float)v.x, (float)v.y);
+            }
+        }
+        return;
+    }
+    double2* dst = out + (size_t)blockIdx.z * split_stride;  // FP64 partial of this atom split
     for (int idx = threadIdx.x; idx < g.nv * W; idx += W * 32) {
         int vl = idx / W, w = idx - vl * W;
         int ff = blockIdx.x * W + w;
@@ -195,9 +206,10 @@ __global__ void __launch_bounds__(W * 32)
     phase_sum_fp64_kernel(const float4* __restrict__ xyz, int na_pad, int nf,
                           const double* __restrict__ bfac, const double* __restrict__ qv,
                           const VecGroup* __restrict__ groups, int atoms_per_split,
-                          double2* __restrict__ out, size_t split_stride, int nv_total,
-                          unsigned int* err) {
+                          double2* __restrict__ out, float2* __restrict__ out_f32,
+                          size_t split_stride, unsigned int* err) {
     using L = PipeLayout<W, T, S, 8>;
+    (void)out_f32;
     static_assert(S * T >= 32 * Q, "output staging must fit in the coordinate ring");
     extern __shared__ __align__(128) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -297,8 +309,20 @@ __global__ void __launch_bounds__(W * 32)
     }
 }
 
+template <class OUT>
+__device__ __forceinline__ OUT store_as(double2 v);
+template <>
+__device__ __forceinline__ double2 store_as<double2>(double2 v) {
+    return v;
+}
+template <>
+__device__ __forceinline__ float2 store_as<float2>(double2 v) {
+    return make_float2((float)v.x, (float)v.y);
+}
+
+template <class OUT>
 __global__ void split_reduce_kernel(const double2* __restrict__ part, int nsplit, size_t n,
-                                    double2* __restrict__ out) {
+                                    OUT* __restrict__ out) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
          i += (size_t)gridDim.x * blockDim.x) {
         double2 a = part[i];
@@ -307,7 +331,7 @@ __global__ void split_reduce_kernel(const double2* __restrict__ part, int nsplit
             a.x += b.x;
             a.y += b.y;
         }
-        out[i] = a;
+        out[i] = store_as<OUT>(a);
     }
 }
 
@@ -339,7 +363,8 @@ cudaError_t launch_phase_sum(const PhaseSumArgs& a, cudaStream_t st) {
         for (int g0 = 0; g0 < a.ngroups; g0 += 65535) {                                         \
         dim3 grid((a.nf + W - 1) / W, min(65535, a.ngroups - g0), a.nsplit);                    \
         k<<<grid, W * 32, smem, st>>>(a.xyz, a.na_pad, a.nf, (const float*)a.bfac, a.qv,        \
-                                      a.groups + g0, a.atoms_per_split, a.out, a.split_stride, 0, \
+                                      a.groups + g0, a.atoms_per_split, a.out, a.out_f32,       \
+                                      a.split_stride,                                           \
                                       a.err);                                                   \
         }                                                                                       \
         return cudaGetLastError();                                                              \
@@ -353,7 +378,8 @@ cudaError_t launch_phase_sum(const PhaseSumArgs& a, cudaStream_t st) {
         for (int g0 = 0; g0 < a.ngroups; g0 += 65535) {                                         \
         dim3 grid((a.nf + W - 1) / W, min(65535, a.ngroups - g0), a.nsplit);                    \
         k<<<grid, W * 32, smem, st>>>(a.xyz, a.na_pad, a.nf, (const double*)a.bfac, a.qv,       \
-                                      a.groups + g0, a.atoms_per_split, a.out, a.split_stride, 0, \
+                                      a.groups + g0, a.atoms_per_split, a.out, a.out_f32,       \
+                                      a.split_stride,                                           \
                                       a.err);                                                   \
         }                                                                                       \
         return cudaGetLastError();                                                              \
@@ -373,7 +399,16 @@ cudaError_t launch_split_reduce(const double2* part, int nsplit, size_t n, doubl
     if (n == 0) return cudaSuccess;
     int blocks = (int)((n + 255) / 256);
     if (blocks > 152 * 16) blocks = 152 * 16;
-    split_reduce_kernel<<<blocks, 256, 0, st>>>(part, nsplit, n, out);
+    split_reduce_kernel<double2><<<blocks, 256, 0, st>>>(part, nsplit, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_split_reduce_f32(const double2* part, int nsplit, size_t n, float2* out,
+                                    cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    split_reduce_kernel<float2><<<blocks, 256, 0, st>>>(part, nsplit, n, out);
     return cudaGetLastError();
 }
 

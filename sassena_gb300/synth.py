@@ -296,6 +296,8 @@ def write_files(directory, w, precision="fp64", method="fftw", qvectors_file=Tru
     abstract_vectors_scatter_device.cpp:123-129) and the directions come from a file
     (vectors.type=file, parameters.cpp:932-943)."""
     import os
+    if sfactor_params is None and not np.all(w.class_factors == w.class_factors[:1]):
+        raise ValueError("type-0 database factors cannot vary with |q|; pass sfactor_params")
     os.makedirs(directory, exist_ok=True)
     write_pdb(os.path.join(directory, "sample.pdb"), w)
     write_dcd(os.path.join(directory, "sample.dcd"), w.coords)

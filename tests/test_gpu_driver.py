@@ -23,6 +23,13 @@ def run(cfg, *extra):
     return r
 
 
+def small(*a, **k):
+    """A small workload with |q|-independent factors (database type 0 constants)."""
+    w = synth.small(*a, **k)
+    w.class_factors[:] = w.class_factors[:1]
+    return w
+
+
 def reference(w, method=0):
     fn = oracle.all_vectors if w.scattering == "all" else oracle.self_vectors
     dsp = {"autocorrelate": 0, "square": 1, "plain": 2}[w.dsp]
@@ -40,7 +47,7 @@ def read_rows(path):
 @pytest.mark.parametrize("scattering,dsp", [("all", "autocorrelate"), ("self", "autocorrelate"),
                                             ("all", "square")])
 def test_driver_fp64_matches_oracle(native_lib, tmp_path, scattering, dsp):
-    w = synth.small(scattering, dsp, seed=51, na=41, nf=18, nq=3, nm=6)
+    w = small(scattering, dsp, seed=51, na=41, nf=18, nq=3, nm=6)
     cfg = synth.write_files(str(tmp_path / "run"), w, precision="fp64")
     run(cfg)
     q, fqt, fq0, fq, fq2 = read_rows(str(tmp_path / "run" / "signal.h5"))
@@ -55,7 +62,7 @@ def test_driver_fp64_matches_oracle(native_lib, tmp_path, scattering, dsp):
 
 
 def test_driver_fp32_form(native_lib, tmp_path):
-    w = synth.small("all", "autocorrelate", seed=52, na=60, nf=30, nq=2, nm=8)
+    w = small("all", "autocorrelate", seed=52, na=60, nf=30, nq=2, nm=8)
     cfg = synth.write_files(str(tmp_path / "run"), w, precision="fp32")
     run(cfg)
     q, fqt, *_ = read_rows(str(tmp_path / "run" / "signal.h5"))
@@ -65,7 +72,7 @@ def test_driver_fp32_form(native_lib, tmp_path):
 
 
 def test_driver_resume_appends(native_lib, tmp_path):
-    w = synth.small("all", "autocorrelate", seed=53, na=30, nf=12, nq=4, nm=5)
+    w = small("all", "autocorrelate", seed=53, na=30, nf=12, nq=4, nm=5)
     d = str(tmp_path / "run")
     cfg = synth.write_files(d, w, precision="fp64")
     full = open(os.path.join(d, "qvectors.txt")).read().splitlines()
@@ -93,7 +100,7 @@ def test_driver_resume_appends(native_lib, tmp_path):
 
 
 def test_driver_rejects_nf_mismatch_on_resume(native_lib, tmp_path):
-    w = synth.small("all", "autocorrelate", seed=54, na=10, nf=8, nq=2, nm=2)
+    w = small("all", "autocorrelate", seed=54, na=10, nf=8, nq=2, nm=2)
     d = str(tmp_path / "run")
     cfg = synth.write_files(d, w)
     run(cfg)

@@ -74,6 +74,7 @@ def test_signal_reader_rejects_non_hdf5(tmp_path):
 @pytest.fixture
 def small_files(tmp_path):
     w = synth.small("all", "autocorrelate", seed=21, na=23, nf=9, nq=3, nm=4)
+    w.class_factors[:] = w.class_factors[:1]  # database type-0 constants
     cfg = synth.write_files(str(tmp_path / "run"), w)
     return w, cfg
 
