@@ -127,6 +127,14 @@ int sass_amplitudes(sass_plan* plan, size_t nsub, const double* subvectors,
                     const int32_t* sub_shell, size_t nshell, const double* class_factors,
                     double* out);
 
+/* Time every instantiated phase-sum tile shape and atom-split size on this
+ * workload (the arguments of sass_compute, host arrays) and keep the fastest for the
+ * plan's later calls; the choice is cached per process by problem signature. The
+ * chosen shape is returned through the (optional) out-pointers. */
+int sass_autotune(sass_plan* plan, size_t nq, const size_t* sub_offsets, const double* subvectors,
+                  const double* class_factors, int repeats, int* q_per_lane, int* warps, int* atoms,
+                  int* split_atoms);
+
 /* Timings of the last sass_compute / sass_amplitudes call. */
 int sass_last_timing(const sass_plan* plan, sass_timing* out);
 
@@ -137,6 +145,44 @@ int sass_set_phase_tile(sass_plan* plan, int q_per_lane, int warps, int atoms, i
 
 /* Frame centre used by the FP32 form (frame-0 bounding-box midpoint). */
 int sass_frame_center(const sass_plan* plan, double* center3);
+
+/* ---- Batches: many independent systems in one graph-captured launch sequence ----
+ * Each system has its own trajectory, atom classes, q-vectors and sub-vector sets of
+ * any size. The batch stages everything once; sass_batch_run replays one CUDA graph
+ * containing the factor expansion, ONE persistent phase-sum launch over the tiles of all
+ * systems (work queue), the batched correlation and the finalisation. No counterpart in
+ * the reference, which runs one system per process invocation (sassena.cpp:132-417). */
+typedef struct sass_batch sass_batch;
+
+typedef struct sass_system {
+    size_t na, nf, nclass;
+    const float* coords;          /* host [nf][na][3] float32, frame-major */
+    const int32_t* atom_class;    /* host [na] */
+    size_t nq;                    /* q-vectors of this system */
+    const size_t* sub_offsets;    /* host [nq+1] */
+    const double* subvectors;     /* host [sub_offsets[nq]][3] */
+    const double* class_factors;  /* host [nq][nclass] */
+} sass_system;
+
+/* desc supplies scattering, dsp, method, precision, device and stream (its na, nf,
+ * nclass are ignored; each system carries its own). */
+int sass_batch_create(const sass_plan_desc* desc, size_t nsystems, const sass_system* systems,
+                      sass_batch** batch);
+/* Autotune tile shape and atom-split size over the whole batch (coherent). */
+int sass_batch_autotune(sass_batch* batch, int repeats, int* q_per_lane, int* warps, int* atoms,
+                        int* split_atoms, double* best_ms);
+/* Enqueue one replay of the batch's graph (asynchronous on the batch stream). */
+int sass_batch_run(sass_batch* batch);
+/* Wait for the last run and check the device error word. */
+int sass_batch_sync(sass_batch* batch);
+/* Copy one system's results to host arrays (fqt [nq][nf][2], fq/fq2 [nq][2]; NULL skips). */
+int sass_batch_results(sass_batch* batch, size_t system, double* fqt, double* fq, double* fq2);
+int sass_batch_timing(const sass_batch* batch, sass_timing* out);
+/* Total atom.q.frame terms, phase-sum tiles and the tile shape of the batch. */
+int sass_batch_info(const sass_batch* batch, double* terms, uint64_t* phase_tiles, int* q_per_lane,
+                    int* warps, int* atoms, int* split_atoms);
+const char* sass_batch_error(const sass_batch* batch);
+void sass_batch_destroy(sass_batch* batch);
 
 /* Pinned host memory for faster staging (cudaHostAlloc / cudaFreeHost). */
 void* sass_host_alloc(size_t bytes);

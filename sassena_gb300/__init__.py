@@ -5,6 +5,6 @@ C ABI); the C++ host devices in sassena_gb300/host drive it from the reference's
 configuration. This Python package holds the ctypes binding used by tests and the
 benchmark, the build recipe and the seeded synthetic workloads.
 """
-from .abi import Plan, SassError, compute_workload, load  # noqa: F401
+from .abi import Batch, Plan, SassError, compute_workload, load  # noqa: F401
 
-__all__ = ["Plan", "SassError", "compute_workload", "load"]
+__all__ = ["Batch", "Plan", "SassError", "compute_workload", "load"]

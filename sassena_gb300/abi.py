@@ -29,6 +29,9 @@ EXPORTS = [
     "sass_stage_frames", "sass_set_atom_classes", "sass_compute", "sass_amplitudes",
     "sass_last_timing", "sass_set_phase_tile", "sass_frame_center", "sass_host_alloc",
     "sass_host_free", "sass_probe_pipes", "sass_correlate_noalloc", "sass_version",
+    "sass_autotune", "sass_batch_create", "sass_batch_autotune", "sass_batch_run",
+    "sass_batch_sync", "sass_batch_results", "sass_batch_timing", "sass_batch_info",
+    "sass_batch_error", "sass_batch_destroy",
 ]
 
 
@@ -44,6 +47,13 @@ class PlanDesc(ctypes.Structure):
                 ("na", ctypes.c_size_t), ("nf", ctypes.c_size_t), ("nclass", ctypes.c_size_t),
                 ("device", ctypes.c_int), ("stream", ctypes.c_void_p),
                 ("amplitude_budget_bytes", ctypes.c_size_t)]
+
+
+class System(ctypes.Structure):
+    _fields_ = [("na", ctypes.c_size_t), ("nf", ctypes.c_size_t), ("nclass", ctypes.c_size_t),
+                ("coords", ctypes.c_void_p), ("atom_class", ctypes.c_void_p),
+                ("nq", ctypes.c_size_t), ("sub_offsets", ctypes.c_void_p),
+                ("subvectors", ctypes.c_void_p), ("class_factors", ctypes.c_void_p)]
 
 
 class Timing(ctypes.Structure):
@@ -92,6 +102,20 @@ def load(path=LIB_PATH):
     L.sass_host_free.restype = None
     L.sass_version.restype = ctypes.c_char_p
     L.sass_probe_pipes.argtypes = [ctypes.c_int, _dp, _dp]
+    _ip = ctypes.POINTER(ctypes.c_int)
+    L.sass_autotune.argtypes = [_vp, _sz, _vp, _vp, _vp, ctypes.c_int, _ip, _ip, _ip, _ip]
+    L.sass_batch_create.argtypes = [ctypes.POINTER(PlanDesc), _sz, ctypes.POINTER(System),
+                                    ctypes.POINTER(_vp)]
+    L.sass_batch_autotune.argtypes = [_vp, ctypes.c_int, _ip, _ip, _ip, _ip, _dp]
+    L.sass_batch_run.argtypes = [_vp]
+    L.sass_batch_sync.argtypes = [_vp]
+    L.sass_batch_results.argtypes = [_vp, _sz, _vp, _vp, _vp]
+    L.sass_batch_timing.argtypes = [_vp, ctypes.POINTER(Timing)]
+    L.sass_batch_info.argtypes = [_vp, _dp, ctypes.POINTER(ctypes.c_uint64), _ip, _ip, _ip, _ip]
+    L.sass_batch_error.argtypes = [_vp]
+    L.sass_batch_error.restype = ctypes.c_char_p
+    L.sass_batch_destroy.argtypes = [_vp]
+    L.sass_batch_destroy.restype = None
     L.sass_correlate_noalloc.argtypes = [ctypes.c_int, _vp, _vp, _sz, _sz, _vp, ctypes.c_int, _vp,
                                          _vp, _vp]
     _lib = L
@@ -198,10 +222,112 @@ class Plan:
         self._check(self.lib.sass_last_timing(self._h, ctypes.byref(t)))
         return t.as_dict()
 
+    def autotune(self, sub_offsets, subvectors, class_factors, repeats=2):
+        """Time every tile shape on this workload; the plan keeps the fastest."""
+        offs = np.ascontiguousarray(sub_offsets, dtype=np.uintp)
+        nq = len(offs) - 1
+        sv = np.ascontiguousarray(subvectors, dtype=np.float64).reshape(-1, 3)
+        cf = np.ascontiguousarray(class_factors, dtype=np.float64).reshape(nq, self.nclass)
+        out = [ctypes.c_int() for _ in range(4)]
+        self._check(self.lib.sass_autotune(self._h, nq, _ptr(offs), _ptr(sv), _ptr(cf), repeats,
+                                           *[ctypes.byref(o) for o in out]))
+        return dict(zip(("q_per_lane", "warps", "atoms", "split_atoms"), [o.value for o in out]))
+
     def center(self):
         c = np.zeros(3)
         self._check(self.lib.sass_frame_center(self._h, c.ctypes.data_as(_dp)))
         return c
+
+
+class Batch:
+    """Many systems in one graph-captured launch sequence (sass_batch_*)."""
+
+    def __init__(self, workloads, precision="fp32", method="fftw", device=0, stream=None):
+        self.lib = load()
+        w0 = workloads[0]
+        d = PlanDesc(SCATTERING[w0.scattering], DSP[w0.dsp], METHOD[method], PRECISION[precision],
+                     0, 0, 0, device, stream or 0, 0)
+        self._keep = []
+        sys = (System * len(workloads))()
+        for i, w in enumerate(workloads):
+            c = np.ascontiguousarray(w.coords, dtype=np.float32)
+            cls = np.ascontiguousarray(w.atom_class, dtype=np.int32)
+            offs = np.ascontiguousarray(w.sub_offsets(), dtype=np.uintp)
+            sv = np.ascontiguousarray(w.subvectors(), dtype=np.float64)
+            cf = np.ascontiguousarray(w.class_factors, dtype=np.float64)
+            self._keep += [c, cls, offs, sv, cf]
+            sys[i] = System(w.na, w.nf, len(w.class_names), c.ctypes.data, cls.ctypes.data, w.nq,
+                            offs.ctypes.data, sv.ctypes.data, cf.ctypes.data)
+        self.shapes = [(w.nq, w.nf) for w in workloads]
+        h = _vp()
+        rc = self.lib.sass_batch_create(ctypes.byref(d), len(workloads), sys, ctypes.byref(h))
+        self._h = h
+        if rc != SASS_OK:
+            msg = self.error()
+            self.close()
+            raise SassError(rc, msg)
+
+    def error(self):
+        return self.lib.sass_batch_error(self._h).decode() if self._h else ""
+
+    def _check(self, rc):
+        if rc != SASS_OK:
+            raise SassError(rc, self.error())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.sass_batch_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def autotune(self, repeats=1):
+        out = [ctypes.c_int() for _ in range(4)]
+        ms = ctypes.c_double()
+        self._check(self.lib.sass_batch_autotune(self._h, repeats, *[ctypes.byref(o) for o in out],
+                                                 ctypes.byref(ms)))
+        r = dict(zip(("q_per_lane", "warps", "atoms", "split_atoms"), [o.value for o in out]))
+        r["ms"] = ms.value
+        return r
+
+    def run(self):
+        self._check(self.lib.sass_batch_run(self._h))
+
+    def sync(self):
+        self._check(self.lib.sass_batch_sync(self._h))
+
+    def results(self, i):
+        nq, nf = self.shapes[i]
+        fqt = np.zeros((nq, nf, 2))
+        fq = np.zeros((nq, 2))
+        fq2 = np.zeros((nq, 2))
+        self._check(self.lib.sass_batch_results(self._h, i, _ptr(fqt), _ptr(fq), _ptr(fq2)))
+        return (fqt[..., 0] + 1j * fqt[..., 1], fq[:, 0] + 1j * fq[:, 1], fq2[:, 0] + 1j * fq2[:, 1])
+
+    def timing(self):
+        t = Timing()
+        self._check(self.lib.sass_batch_timing(self._h, ctypes.byref(t)))
+        return t.as_dict()
+
+    def info(self):
+        terms = ctypes.c_double()
+        tiles = ctypes.c_uint64()
+        out = [ctypes.c_int() for _ in range(4)]
+        self._check(self.lib.sass_batch_info(self._h, ctypes.byref(terms), ctypes.byref(tiles),
+                                             *[ctypes.byref(o) for o in out]))
+        r = dict(zip(("q_per_lane", "warps", "atoms", "split_atoms"), [o.value for o in out]))
+        r.update(terms=terms.value, phase_tiles=tiles.value)
+        return r
 
 
 def probe_pipes(device=0):

@@ -17,7 +17,11 @@
 //   * ONE inverse FFT per shell (FP64 radix-2 DIT taking the bit-reversed spectrum,
 //     output natural order) gives sum_v C_v, normalised in FP64.
 // The padded length L is the next power of two >= 2NF; the linear correlation for
-// tau < NF is the same for any L >= 2NF-1, and the normalisation uses L.
+// tau < NF is the same for any L >= 2NF-1, and the normalisation uses L. Work items
+// carry their system, so one launch serves systems of different NF (twiddles come from
+// one table at the largest length of the launch, indexed with a per-system stride).
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -36,18 +40,17 @@ __device__ __forceinline__ double2 zero2<double2>() {
     return make_double2(0.0, 0.0);
 }
 
-__device__ __forceinline__ void conv(float2& d, double2 s) { d = make_float2((float)s.x, (float)s.y); }
-__device__ __forceinline__ void conv(double2& d, double2 s) { d = s; }
 __device__ __forceinline__ double2 to_d2(float2 a) { return make_double2(a.x, a.y); }
 __device__ __forceinline__ double2 to_d2(double2 a) { return a; }
 
-// Remaining DIF stages (half-size L/4 .. 1) after the folded first stage.
+// Remaining DIF stages (half-size L/4 .. 1) after the folded first stage; twiddles
+// of length L are tw[k << tws] of the table for the launch's largest length.
 template <class T2, int NT>
-__device__ void dif_tail(T2* buf, const T2* tw, int lg) {
+__device__ void dif_tail(T2* buf, const T2* tw, int lg, int tws) {
     const int half = 1 << (lg - 1);
     for (int lh = lg - 2; lh >= 0; --lh) {
         const int h = 1 << lh;
-        const int sh = lg - 1 - lh;
+        const int sh = lg - 1 - lh + tws;
         for (int b = threadIdx.x; b < half; b += NT) {
             const int p = b & (h - 1);
             const int i0 = ((b >> lh) << (lh + 1)) + p;
@@ -61,11 +64,11 @@ __device__ void dif_tail(T2* buf, const T2* tw, int lg) {
 
 // Unnormalised inverse DIT FFT: bit-reversed input, natural output, twiddles conj(tw).
 template <int NT>
-__device__ void dit_inverse(double2* buf, const double2* __restrict__ tw, int lg) {
+__device__ void dit_inverse(double2* buf, const double2* __restrict__ tw, int lg, int tws) {
     const int half = 1 << (lg - 1);
     for (int lh = 0; lh < lg; ++lh) {
         const int h = 1 << lh;
-        const int sh = lg - 1 - lh;
+        const int sh = lg - 1 - lh + tws;
         for (int b = threadIdx.x; b < half; b += NT) {
             const int p = b & (h - 1);
             const int i0 = ((b >> lh) << (lh + 1)) + p;
@@ -100,7 +103,7 @@ __device__ double2 block_sum(double2 v, double2* red) {
     return s;
 }
 
-// Per-thread power-spectrum accumulator: Kahan FP32 (FP32 path) or plain FP64.
+// Per-thread power-spectrum accumulator: Kahan FP32 (FP32 form) or plain FP64.
 template <class T, int MAXR>
 struct PowerAcc;
 
@@ -148,23 +151,35 @@ __device__ __forceinline__ float2 self_term(float b, float4 r, float qx, float q
     return make_float2(b * c, b * s);
 }
 
+template <class T>
+__device__ __forceinline__ void load_q(const double* q, T& qx, T& qy, T& qz) {
+    if (sizeof(T) == 4) {  // FP32 form: revolutions per Angstrom
+        const double inv2pi = 0.15915494309189533577;
+        qx = (T)(q[0] * inv2pi);
+        qy = (T)(q[1] * inv2pi);
+        qz = (T)(q[2] * inv2pi);
+    } else {
+        qx = (T)q[0];
+        qy = (T)q[1];
+        qz = (T)q[2];
+    }
+}
+
 // Shared memory of the FFT accumulate kernels:
 //   buf [L] T2 | tw [L/2] T2 (FP32 only; FP64 twiddles are read through L1) |
 //   red [NT/32] double2 | rj [nf] float4 (incoherent only)
 template <class T>
-struct FftSmem {
-    static size_t bytes(int lg, int nt, int nf, bool self) {
-        size_t L = (size_t)1 << lg;
-        size_t b = L * sizeof(typename cplx<T>::type);
-        if (sizeof(T) == 4) b += (L / 2) * sizeof(typename cplx<T>::type);
-        b += (nt / 32) * sizeof(double2);
-        if (self) b += (size_t)nf * sizeof(float4);
-        return b;
-    }
-};
+size_t fft_smem(int lg, int nt, int nf, bool self) {
+    size_t L = (size_t)1 << lg;
+    size_t b = L * sizeof(typename cplx<T>::type);
+    if (sizeof(T) == 4) b += (L / 2) * sizeof(typename cplx<T>::type);
+    b += (nt / 32) * sizeof(double2);
+    if (self) b += (size_t)nf * sizeof(float4);
+    return b;
+}
 
-// Power spectrum of the series in buf (bit-reversed order): accumulate P and
-// return this thread's part of sum_w P(w) K(w).
+// Power spectrum of the series in buf (bit-reversed order): accumulate P and return
+// this thread's part of sum_w P(w) K(w).
 template <class T, int NT, int MAXR>
 __device__ __forceinline__ double2 absorb_power(const typename cplx<T>::type* buf, int L,
                                                 const typename cplx<T>::type* __restrict__ kbr,
@@ -195,48 +210,47 @@ __device__ __forceinline__ void write_power(const PowerAcc<T, MAXR>& acc, int L,
     }
 }
 
-// ---------------------------------------------------------------------------
+// Shared twiddle table of the launch: FP32 copies into shared memory, FP64 reads L1.
+template <class T, int NT>
+__device__ __forceinline__ const typename cplx<T>::type* stage_twiddles(
+    typename cplx<T>::type* tws, const void* tw_, int lg_max) {
+    typedef typename cplx<T>::type T2;
+    const T2* twg = reinterpret_cast<const T2*>(tw_);
+    if (sizeof(T) != 4) return twg;
+    for (int i = threadIdx.x; i < (1 << (lg_max - 1)); i += NT) tws[i] = twg[i];
+    return tws;
+}
+
+// ---------------------------------------------------------------------------------------
 // Coherent autocorrelation: one CTA per chunk of series of one shell.
-// ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------------------
 template <class T, int NT, int MAXR>
-__global__ void __launch_bounds__(NT)
-    corr_fft_kernel(const void* __restrict__ A_, int nf, int lg, const void* tw_,
-                    const void* kbr_, const SeriesChunk* __restrict__ chunks,
-                    double* __restrict__ ppart, double2* __restrict__ apart,
-                    double* __restrict__ a2part) {
+__global__ void __launch_bounds__(NT) corr_fft_kernel(CorrLaunch a) {
     typedef typename cplx<T>::type T2;
     extern __shared__ __align__(16) unsigned char smem[];
-    const int L = 1 << lg, half = L >> 1;
-    const T2* twg = reinterpret_cast<const T2*>(tw_);
-    const T2* kbr = reinterpret_cast<const T2*>(kbr_);
+    const CorrChunk c = a.chunks[blockIdx.x];
+    const CorrSystem sys = a.systems[c.system];
+    const int lg = sys.lg, L = 1 << lg, half = L >> 1, tws = a.lg_max - lg;
     T2* buf = reinterpret_cast<T2*>(smem);
-    const T2* tw;
-    double2* red;
-    if (sizeof(T) == 4) {
-        T2* tws = buf + L;
-        for (int i = threadIdx.x; i < half; i += NT) tws[i] = twg[i];
-        tw = tws;
-        red = reinterpret_cast<double2*>(tws + half);
-    } else {
-        tw = twg;
-        red = reinterpret_cast<double2*>(buf + L);
-    }
-    const SeriesChunk c = chunks[blockIdx.x];
+    T2* twsm = buf + (1 << a.lg_max);
+    const T2* tw = stage_twiddles<T, NT>(twsm, a.tw, a.lg_max);
+    double2* red = reinterpret_cast<double2*>(sizeof(T) == 4 ? twsm + (1 << (a.lg_max - 1)) : twsm);
+    const T2* kbr = reinterpret_cast<const T2*>(sys.kbr);
     PowerAcc<T, MAXR> acc;
     acc.clear();
     double2 asum = make_double2(0.0, 0.0);
     double a2sum = 0.0;
     __syncthreads();
     for (int v = c.v_begin; v < c.v_end; ++v) {
-        const T2* src = reinterpret_cast<const T2*>(A_) + (size_t)v * nf;
+        const T2* src = reinterpret_cast<const T2*>(sys.A) + (size_t)v * sys.nf;
         for (int p = threadIdx.x; p < half; p += NT) {
             T2 x = zero2<T2>();
-            if (p < nf) x = src[p];
+            if (p < sys.nf) x = src[p];
             buf[p] = x;
-            buf[p + half] = cmul(x, tw[p]);
+            buf[p + half] = cmul(x, tw[p << tws]);
         }
         __syncthreads();
-        dif_tail<T2, NT>(buf, tw, lg);
+        dif_tail<T2, NT>(buf, tw, lg, tws);
         double2 av = block_sum<NT>(absorb_power<T, NT, MAXR>(buf, L, kbr, acc), red);
         if (threadIdx.x == 0) {
             asum.x += av.x;
@@ -244,74 +258,52 @@ __global__ void __launch_bounds__(NT)
             a2sum += av.x * av.x + av.y * av.y;
         }
     }
-    write_power<T, NT, MAXR>(acc, L, ppart + (size_t)c.slot * L);
+    write_power<T, NT, MAXR>(acc, L, a.ppart + c.part_off);
     if (threadIdx.x == 0) {
-        apart[c.slot] = asum;
-        a2part[c.slot] = a2sum;
+        a.apart[c.slot] = asum;
+        a.a2part[c.slot] = a2sum;
     }
 }
 
-// ---------------------------------------------------------------------------
-// Incoherent autocorrelation: one CTA per chunk of atoms of one shell; for each
-// atom its trajectory is staged once and reused for every direction of the shell.
-// ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------------------
+// Incoherent autocorrelation: one CTA per chunk of atoms of one shell; each atom's
+// trajectory is staged once and reused for every direction of the shell.
+// ---------------------------------------------------------------------------------------
 template <class T, int NT, int MAXR>
-__global__ void __launch_bounds__(NT)
-    self_fft_kernel(const float4* __restrict__ xyz, int na_pad, int nf, int lg,
-                    const double* __restrict__ qv, const T* __restrict__ bfac,
-                    const int* __restrict__ shell_v, const void* tw_, const void* kbr_,
-                    const AtomChunk* __restrict__ chunks, double* __restrict__ ppart,
-                    double2* __restrict__ apart, double* __restrict__ a2part) {
+__global__ void __launch_bounds__(NT) self_fft_kernel(CorrLaunch a) {
     typedef typename cplx<T>::type T2;
     extern __shared__ __align__(16) unsigned char smem[];
-    const int L = 1 << lg, half = L >> 1;
-    const T2* twg = reinterpret_cast<const T2*>(tw_);
-    const T2* kbr = reinterpret_cast<const T2*>(kbr_);
+    const CorrChunk c = a.chunks[blockIdx.x];
+    const CorrSystem sys = a.systems[c.system];
+    const int lg = sys.lg, L = 1 << lg, half = L >> 1, tws = a.lg_max - lg, nf = sys.nf;
     T2* buf = reinterpret_cast<T2*>(smem);
-    const T2* tw;
-    double2* red;
-    if (sizeof(T) == 4) {
-        T2* tws = buf + L;
-        for (int i = threadIdx.x; i < half; i += NT) tws[i] = twg[i];
-        tw = tws;
-        red = reinterpret_cast<double2*>(tws + half);
-    } else {
-        tw = twg;
-        red = reinterpret_cast<double2*>(buf + L);
-    }
+    T2* twsm = buf + (1 << a.lg_max);
+    const T2* tw = stage_twiddles<T, NT>(twsm, a.tw, a.lg_max);
+    double2* red = reinterpret_cast<double2*>(sizeof(T) == 4 ? twsm + (1 << (a.lg_max - 1)) : twsm);
     float4* rj = reinterpret_cast<float4*>(red + NT / 32);
-    const AtomChunk c = chunks[blockIdx.x];
-    const int v0 = shell_v[c.shell], v1 = shell_v[c.shell + 1];
+    const T2* kbr = reinterpret_cast<const T2*>(sys.kbr);
+    const T* bfac = reinterpret_cast<const T*>(sys.bfac);
+    const int v0 = sys.shell_v[c.shell], v1 = sys.shell_v[c.shell + 1];
     PowerAcc<T, MAXR> acc;
     acc.clear();
     double2 asum = make_double2(0.0, 0.0);
     double a2sum = 0.0;
-    const double inv2pi = 0.15915494309189533577;
-    for (int j = c.j_begin; j < c.j_end; ++j) {
+    for (int j = c.v_begin; j < c.v_end; ++j) {
         __syncthreads();  // previous atom's series fully consumed
-        for (int t = threadIdx.x; t < nf; t += NT) rj[t] = xyz[(size_t)t * na_pad + j];
-        const T b = bfac[(size_t)c.shell * na_pad + j];
+        for (int t = threadIdx.x; t < nf; t += NT) rj[t] = sys.xyz[(size_t)t * sys.na_pad + j];
+        const T b = bfac[(size_t)c.shell * sys.na_pad + j];
         __syncthreads();
         for (int v = v0; v < v1; ++v) {
-            const double* q = qv + 3 * (size_t)v;
             T qx, qy, qz;
-            if (sizeof(T) == 4) {
-                qx = (T)(q[0] * inv2pi);
-                qy = (T)(q[1] * inv2pi);
-                qz = (T)(q[2] * inv2pi);
-            } else {
-                qx = (T)q[0];
-                qy = (T)q[1];
-                qz = (T)q[2];
-            }
+            load_q(sys.qv + 3 * (size_t)v, qx, qy, qz);
             for (int p = threadIdx.x; p < half; p += NT) {
                 T2 x = zero2<T2>();
                 if (p < nf) x = self_term(b, rj[p], qx, qy, qz);
                 buf[p] = x;
-                buf[p + half] = cmul(x, tw[p]);
+                buf[p + half] = cmul(x, tw[p << tws]);
             }
             __syncthreads();
-            dif_tail<T2, NT>(buf, tw, lg);
+            dif_tail<T2, NT>(buf, tw, lg, tws);
             double2 av = block_sum<NT>(absorb_power<T, NT, MAXR>(buf, L, kbr, acc), red);
             if (threadIdx.x == 0) {
                 asum.x += av.x;
@@ -320,25 +312,25 @@ __global__ void __launch_bounds__(NT)
             }
         }
     }
-    write_power<T, NT, MAXR>(acc, L, ppart + (size_t)c.slot * L);
+    write_power<T, NT, MAXR>(acc, L, a.ppart + c.part_off);
     if (threadIdx.x == 0) {
-        apart[c.slot] = asum;
-        a2part[c.slot] = a2sum;
+        a.apart[c.slot] = asum;
+        a.a2part[c.slot] = a2sum;
     }
 }
 
-// ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------------------
 // dsp = square | plain (no transform): C_v(t) = |A_v(t)|^2 or A_v(t) * exp(i q_v.c).
-// Partials are complex per frame: ppart as double2 [slot][nf].
-// ---------------------------------------------------------------------------
+// Partials are complex per frame (double2 [nf] at part_off).
+// ---------------------------------------------------------------------------------------
 template <class AT, int NT, int MAXT>
-__global__ void __launch_bounds__(NT)
-    corr_direct_kernel(const AT* __restrict__ A, int nf, int square, const double* __restrict__ qv,
-                       double cx, double cy, double cz, int restore, const SeriesChunk* __restrict__ chunks,
-                       double2* __restrict__ ppart, double2* __restrict__ apart,
-                       double* __restrict__ a2part) {
+__global__ void __launch_bounds__(NT) corr_direct_kernel(CorrLaunch a) {
     __shared__ double2 red[NT / 32];
-    const SeriesChunk c = chunks[blockIdx.x];
+    const CorrChunk c = a.chunks[blockIdx.x];
+    const CorrSystem sys = a.systems[c.system];
+    const int nf = sys.nf;
+    const bool square = a.dsp == DSP_SQUARE;
+    const AT* A = reinterpret_cast<const AT*>(sys.A);
     double2 acc[MAXT];
 #pragma unroll
     for (int r = 0; r < MAXT; ++r) acc[r] = make_double2(0.0, 0.0);
@@ -346,17 +338,17 @@ __global__ void __launch_bounds__(NT)
     double a2sum = 0.0;
     for (int v = c.v_begin; v < c.v_end; ++v) {
         double2 ph = make_double2(1.0, 0.0);
-        if (!square && restore) {
-            const double* q = qv + 3 * (size_t)v;
-            sincos(q[0] * cx + q[1] * cy + q[2] * cz, &ph.y, &ph.x);
+        if (!square && a.restore_phase) {
+            const double* q = sys.qv + 3 * (size_t)v;
+            sincos(q[0] * sys.cx + q[1] * sys.cy + q[2] * sys.cz, &ph.y, &ph.x);
         }
         double2 part = make_double2(0.0, 0.0);
 #pragma unroll
         for (int r = 0; r < MAXT; ++r) {
             const int t = threadIdx.x + r * NT;
             if (t < nf) {
-                double2 a = to_d2(A[(size_t)v * nf + t]);
-                double2 cv = square ? make_double2(a.x * a.x + a.y * a.y, 0.0) : cmul(a, ph);
+                double2 x = to_d2(A[(size_t)v * nf + t]);
+                double2 cv = square ? make_double2(x.x * x.x + x.y * x.y, 0.0) : cmul(x, ph);
                 acc[r].x += cv.x;
                 acc[r].y += cv.y;
                 part.x += cv.x;
@@ -371,57 +363,47 @@ __global__ void __launch_bounds__(NT)
             a2sum += av.x * av.x + av.y * av.y;
         }
     }
+    double2* dst = reinterpret_cast<double2*>(a.ppart + c.part_off);
 #pragma unroll
     for (int r = 0; r < MAXT; ++r) {
         const int t = threadIdx.x + r * NT;
-        if (t < nf) ppart[(size_t)c.slot * nf + t] = acc[r];
+        if (t < nf) dst[t] = acc[r];
     }
     if (threadIdx.x == 0) {
-        apart[c.slot] = asum;
-        a2part[c.slot] = a2sum;
+        a.apart[c.slot] = asum;
+        a.a2part[c.slot] = a2sum;
     }
 }
 
 template <class T, int NT, int MAXT>
-__global__ void __launch_bounds__(NT)
-    self_direct_kernel(const float4* __restrict__ xyz, int na_pad, int nf, int square,
-                       const double* __restrict__ qv, const T* __restrict__ bfac,
-                       const int* __restrict__ shell_v, double cx, double cy, double cz,
-                       int restore, const AtomChunk* __restrict__ chunks,
-                       double2* __restrict__ ppart, double2* __restrict__ apart,
-                       double* __restrict__ a2part) {
+__global__ void __launch_bounds__(NT) self_direct_kernel(CorrLaunch a) {
     typedef typename cplx<T>::type T2;
     __shared__ double2 red[NT / 32];
-    const AtomChunk c = chunks[blockIdx.x];
-    const int v0 = shell_v[c.shell], v1 = shell_v[c.shell + 1];
-    const double inv2pi = 0.15915494309189533577;
+    const CorrChunk c = a.chunks[blockIdx.x];
+    const CorrSystem sys = a.systems[c.system];
+    const int nf = sys.nf;
+    const bool square = a.dsp == DSP_SQUARE;
+    const T* bfac = reinterpret_cast<const T*>(sys.bfac);
+    const int v0 = sys.shell_v[c.shell], v1 = sys.shell_v[c.shell + 1];
     double2 acc[MAXT];
 #pragma unroll
     for (int r = 0; r < MAXT; ++r) acc[r] = make_double2(0.0, 0.0);
     double2 asum = make_double2(0.0, 0.0);
     double a2sum = 0.0;
-    for (int j = c.j_begin; j < c.j_end; ++j) {
-        const T b = bfac[(size_t)c.shell * na_pad + j];
+    for (int j = c.v_begin; j < c.v_end; ++j) {
+        const T b = bfac[(size_t)c.shell * sys.na_pad + j];
         for (int v = v0; v < v1; ++v) {
-            const double* q = qv + 3 * (size_t)v;
+            const double* q = sys.qv + 3 * (size_t)v;
             double2 ph = make_double2(1.0, 0.0);
-            if (!square && restore) sincos(q[0] * cx + q[1] * cy + q[2] * cz, &ph.y, &ph.x);
+            if (!square && a.restore_phase) sincos(q[0] * sys.cx + q[1] * sys.cy + q[2] * sys.cz, &ph.y, &ph.x);
             T qx, qy, qz;
-            if (sizeof(T) == 4) {
-                qx = (T)(q[0] * inv2pi);
-                qy = (T)(q[1] * inv2pi);
-                qz = (T)(q[2] * inv2pi);
-            } else {
-                qx = (T)q[0];
-                qy = (T)q[1];
-                qz = (T)q[2];
-            }
+            load_q(q, qx, qy, qz);
             double2 part = make_double2(0.0, 0.0);
 #pragma unroll
             for (int r = 0; r < MAXT; ++r) {
                 const int t = threadIdx.x + r * NT;
                 if (t < nf) {
-                    T2 x = self_term(b, xyz[(size_t)t * na_pad + j], qx, qy, qz);
+                    T2 x = self_term(b, sys.xyz[(size_t)t * sys.na_pad + j], qx, qy, qz);
                     double2 xd = to_d2(x);
                     double2 cv = square ? make_double2(xd.x * xd.x + xd.y * xd.y, 0.0) : cmul(xd, ph);
                     acc[r].x += cv.x;
@@ -439,66 +421,98 @@ __global__ void __launch_bounds__(NT)
             }
         }
     }
+    double2* dst = reinterpret_cast<double2*>(a.ppart + c.part_off);
 #pragma unroll
     for (int r = 0; r < MAXT; ++r) {
         const int t = threadIdx.x + r * NT;
-        if (t < nf) ppart[(size_t)c.slot * nf + t] = acc[r];
+        if (t < nf) dst[t] = acc[r];
     }
     if (threadIdx.x == 0) {
-        apart[c.slot] = asum;
-        a2part[c.slot] = a2sum;
+        a.apart[c.slot] = asum;
+        a.a2part[c.slot] = a2sum;
     }
 }
 
-// ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------------------
 // Per-shell finalisation in FP64: sum partial slots, inverse FFT (autocorrelate),
 // normalise by 1/(L (NF - tau)) and 1/NM, conjugate for dsp.method = direct.
-// ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------------------
 template <int NT>
-__global__ void __launch_bounds__(NT) finalize_kernel(FinalizeArgs a) {
+__global__ void __launch_bounds__(NT) finalize_kernel(FinalLaunch a) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const int s = blockIdx.x;
-    const int sb = a.slot_begin[s], se = a.slot_begin[s + 1];
-    const int nf = a.nf;
-    const double inv_nm = a.inv_nm[s];
+    const FinalEntry e = a.entries[blockIdx.x];
+    const int nf = e.nf;
     const double sgn = a.conj_out ? -1.0 : 1.0;
-    double2* out = a.fqt + (size_t)s * nf;
     if (a.dsp == DSP_AUTOCORRELATE) {
-        const int L = 1 << a.lg;
+        const int L = 1 << e.lg;
         double2* buf = reinterpret_cast<double2*>(smem);
         for (int i = threadIdx.x; i < L; i += NT) {
             double p = 0.0;
-            for (int k = sb; k < se; ++k) p += a.ppart[(size_t)k * L + i];
+            for (int k = e.slot_begin; k < e.slot_end; ++k)
+                p += a.ppart[e.part_off + (size_t)(k - e.slot_begin) * e.part_len + i];
             buf[i] = make_double2(p, 0.0);
         }
         __syncthreads();
-        dit_inverse<NT>(buf, a.tw, a.lg);
+        dit_inverse<NT>(buf, a.tw, e.lg, a.lg_max - e.lg);
         for (int t = threadIdx.x; t < nf; t += NT) {
-            double f = (1.0 / ((double)L * (double)(nf - t))) * inv_nm;
-            out[t] = make_double2(buf[t].x * f, sgn * buf[t].y * f);
+            double f = (1.0 / ((double)L * (double)(nf - t))) * e.inv_nm;
+            e.fqt[t] = make_double2(buf[t].x * f, sgn * buf[t].y * f);
         }
     } else {
-        const double2* pp = reinterpret_cast<const double2*>(a.ppart);
         for (int t = threadIdx.x; t < nf; t += NT) {
             double2 v = make_double2(0.0, 0.0);
-            for (int k = sb; k < se; ++k) {
-                double2 x = pp[(size_t)k * nf + t];
-                v.x += x.x;
-                v.y += x.y;
+            for (int k = e.slot_begin; k < e.slot_end; ++k) {
+                const double* x = a.ppart + e.part_off + (size_t)(k - e.slot_begin) * e.part_len + 2 * t;
+                v.x += x[0];
+                v.y += x[1];
             }
-            out[t] = make_double2(v.x * inv_nm, sgn * v.y * inv_nm);
+            e.fqt[t] = make_double2(v.x * e.inv_nm, sgn * v.y * e.inv_nm);
         }
     }
     if (threadIdx.x == 0) {
         double2 as = make_double2(0.0, 0.0);
         double a2 = 0.0;
-        for (int k = sb; k < se; ++k) {
+        for (int k = e.slot_begin; k < e.slot_end; ++k) {
             as.x += a.apart[k].x;
             as.y += a.apart[k].y;
             a2 += a.a2part[k];
         }
-        a.fq[s] = make_double2(as.x * inv_nm, sgn * as.y * inv_nm);
-        a.fq2[s] = make_double2(a2 * inv_nm, 0.0);
+        *e.fq = make_double2(as.x * e.inv_nm, sgn * as.y * e.inv_nm);
+        *e.fq2 = make_double2(a2 * e.inv_nm, 0.0);
+    }
+}
+
+__global__ void twiddle_kernel(double2* tw64, float2* tw32, int L) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < L / 2; k += gridDim.x * blockDim.x) {
+        double s, c;
+        sincospi(-2.0 * (double)k / (double)L, &s, &c);
+        tw64[k] = make_double2(c, s);
+        tw32[k] = make_float2((float)c, (float)s);
+    }
+}
+
+// K(w) = sum_{tau<NF} exp(+2 pi i w tau / L) / (NF L (NF - tau)) at bit-reversed position
+// of w; exp(+2 pi i m / L) = conj(tw[m]) for m < L/2 and -conj(tw[m - L/2]) otherwise,
+// with tw the table of length 2^lg_tw >= L read at stride 2^(lg_tw - lg).
+__global__ void store_kernel_kernel(const double2* __restrict__ tw, int lg_tw, double2* k64,
+                                    float2* k32, int nf, int lg) {
+    const int L = 1 << lg, sh = lg_tw - lg;
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < L; w += gridDim.x * blockDim.x) {
+        double re = 0.0, im = 0.0;
+        long long m = 0;
+        for (int t = 0; t < nf; ++t) {
+            const double wt = 1.0 / ((double)nf * (double)L * (double)(nf - t));
+            const bool lo = m < L / 2;
+            double2 z = tw[(lo ? m : m - L / 2) << sh];
+            const double sg = lo ? 1.0 : -1.0;
+            re += wt * sg * z.x;
+            im -= wt * sg * z.y;
+            m += w;
+            if (m >= L) m -= L;
+        }
+        const int i = (int)(__brev((unsigned)w) >> (32 - lg));
+        k64[i] = make_double2(re, im);
+        k32[i] = make_float2((float)re, (float)im);
     }
 }
 
@@ -553,24 +567,31 @@ cudaError_t set_smem(K k, size_t bytes) {
 }
 
 template <class T, int NT, int MAXR>
-cudaError_t launch_corr_fft(const CorrArgs& a, cudaStream_t st) {
-    size_t sm = FftSmem<T>::bytes(a.lg, NT, a.nf, false);
-    auto k = corr_fft_kernel<T, NT, MAXR>;
+cudaError_t launch_fft(const CorrLaunch& a, bool self, cudaStream_t st) {
+    const size_t sm = fft_smem<T>(a.lg_max, NT, a.nf_max, self);
+    auto k = self ? self_fft_kernel<T, NT, MAXR> : corr_fft_kernel<T, NT, MAXR>;
     cudaError_t e = set_smem(k, sm);
     if (e != cudaSuccess) return e;
-    k<<<a.nchunks, NT, sm, st>>>(a.A, a.nf, a.lg, a.tw, a.kbr, a.chunks, a.ppart, a.apart,
-                                 a.a2part);
+    k<<<a.nchunks, NT, sm, st>>>(a);
     return cudaGetLastError();
 }
 
-template <class T, int NT, int MAXR>
-cudaError_t launch_self_fft(const CorrArgs& a, cudaStream_t st) {
-    size_t sm = FftSmem<T>::bytes(a.lg, NT, a.nf, true);
-    auto k = self_fft_kernel<T, NT, MAXR>;
-    cudaError_t e = set_smem(k, sm);
-    if (e != cudaSuccess) return e;
-    k<<<a.nchunks, NT, sm, st>>>(a.xyz, a.na_pad, a.nf, a.lg, a.qv, (const T*)a.bfac, a.shell_v,
-                                 a.tw, a.kbr, a.achunks, a.ppart, a.apart, a.a2part);
+cudaError_t launch_accumulate(const CorrLaunch& a, bool self, cudaStream_t st) {
+    if (a.nchunks == 0) return cudaSuccess;
+    if (a.dsp == DSP_AUTOCORRELATE) {
+        if (a.lg_max < 2 || a.lg_max > kMaxLg) return cudaErrorInvalidValue;
+        if (a.precision == PREC_FP32)
+            return a.lg_max <= 9 ? launch_fft<float, 64, 8>(a, self, st) : launch_fft<float, 256, 32>(a, self, st);
+        return a.lg_max <= 9 ? launch_fft<double, 64, 8>(a, self, st) : launch_fft<double, 256, 32>(a, self, st);
+    }
+    if (a.nf_max > 256 * 16) return cudaErrorInvalidValue;
+    if (self) {
+        if (a.precision == PREC_FP32) self_direct_kernel<float, 256, 16><<<a.nchunks, 256, 0, st>>>(a);
+        else self_direct_kernel<double, 256, 16><<<a.nchunks, 256, 0, st>>>(a);
+    } else {
+        if (a.precision == PREC_FP32) corr_direct_kernel<float2, 256, 16><<<a.nchunks, 256, 0, st>>>(a);
+        else corr_direct_kernel<double2, 256, 16><<<a.nchunks, 256, 0, st>>>(a);
+    }
     return cudaGetLastError();
 }
 
@@ -578,63 +599,33 @@ cudaError_t launch_self_fft(const CorrArgs& a, cudaStream_t st) {
 
 size_t fft_smem_bytes(int precision, int lg, int nf, bool self) {
     const int nt = lg <= 9 ? 64 : 256;
-    return precision == PREC_FP32 ? FftSmem<float>::bytes(lg, nt, nf, self)
-                                  : FftSmem<double>::bytes(lg, nt, nf, self);
+    return precision == PREC_FP32 ? fft_smem<float>(lg, nt, nf, self) : fft_smem<double>(lg, nt, nf, self);
 }
 
-cudaError_t launch_corr_accumulate(const CorrArgs& a, int dsp, cudaStream_t st) {
-    if (a.nchunks == 0) return cudaSuccess;
-    if (dsp == DSP_AUTOCORRELATE) {
-        if (a.lg < 2 || a.lg > 13) return cudaErrorInvalidValue;
-        if (a.precision == PREC_FP32)
-            return a.lg <= 9 ? launch_corr_fft<float, 64, 8>(a, st)
-                             : launch_corr_fft<float, 256, 32>(a, st);
-        return a.lg <= 9 ? launch_corr_fft<double, 64, 8>(a, st)
-                         : launch_corr_fft<double, 256, 32>(a, st);
-    }
-    if (a.nf > 256 * 16) return cudaErrorInvalidValue;
-    if (a.precision == PREC_FP32)
-        corr_direct_kernel<float2, 256, 16><<<a.nchunks, 256, 0, st>>>(
-            reinterpret_cast<const float2*>(a.A), a.nf, dsp == DSP_SQUARE, a.qv, a.cx, a.cy, a.cz,
-            a.restore_phase, a.chunks, reinterpret_cast<double2*>(a.ppart), a.apart, a.a2part);
-    else
-        corr_direct_kernel<double2, 256, 16><<<a.nchunks, 256, 0, st>>>(
-            reinterpret_cast<const double2*>(a.A), a.nf, dsp == DSP_SQUARE, a.qv, a.cx, a.cy, a.cz,
-            a.restore_phase, a.chunks, reinterpret_cast<double2*>(a.ppart), a.apart, a.a2part);
-    return cudaGetLastError();
-}
+cudaError_t launch_corr_accumulate(const CorrLaunch& a, cudaStream_t st) { return launch_accumulate(a, false, st); }
 
-cudaError_t launch_self_accumulate(const CorrArgs& a, int dsp, cudaStream_t st) {
-    if (a.nchunks == 0) return cudaSuccess;
-    if (dsp == DSP_AUTOCORRELATE) {
-        if (a.lg < 2 || a.lg > 13) return cudaErrorInvalidValue;
-        if (a.precision == PREC_FP32)
-            return a.lg <= 9 ? launch_self_fft<float, 64, 8>(a, st)
-                             : launch_self_fft<float, 256, 32>(a, st);
-        return a.lg <= 9 ? launch_self_fft<double, 64, 8>(a, st)
-                         : launch_self_fft<double, 256, 32>(a, st);
-    }
-    if (a.nf > 256 * 16) return cudaErrorInvalidValue;
-    if (a.precision == PREC_FP32)
-        self_direct_kernel<float, 256, 16><<<a.nchunks, 256, 0, st>>>(
-            a.xyz, a.na_pad, a.nf, dsp == DSP_SQUARE, a.qv, (const float*)a.bfac, a.shell_v, a.cx,
-            a.cy, a.cz, a.restore_phase, a.achunks, reinterpret_cast<double2*>(a.ppart), a.apart,
-            a.a2part);
-    else
-        self_direct_kernel<double, 256, 16><<<a.nchunks, 256, 0, st>>>(
-            a.xyz, a.na_pad, a.nf, dsp == DSP_SQUARE, a.qv, (const double*)a.bfac, a.shell_v, a.cx,
-            a.cy, a.cz, a.restore_phase, a.achunks, reinterpret_cast<double2*>(a.ppart), a.apart,
-            a.a2part);
-    return cudaGetLastError();
-}
+cudaError_t launch_self_accumulate(const CorrLaunch& a, cudaStream_t st) { return launch_accumulate(a, true, st); }
 
-cudaError_t launch_finalize(const FinalizeArgs& a, cudaStream_t st) {
-    if (a.nshell == 0) return cudaSuccess;
-    size_t sm = a.dsp == DSP_AUTOCORRELATE ? ((size_t)1 << a.lg) * sizeof(double2) : 0;
+cudaError_t launch_finalize(const FinalLaunch& a, cudaStream_t st) {
+    if (a.nentries == 0) return cudaSuccess;
+    const size_t sm = a.dsp == DSP_AUTOCORRELATE ? ((size_t)1 << a.lg_max) * sizeof(double2) : 0;
     auto k = finalize_kernel<256>;
     cudaError_t e = set_smem(k, sm);
     if (e != cudaSuccess) return e;
-    k<<<a.nshell, 256, sm, st>>>(a);
+    k<<<a.nentries, 256, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_twiddles(double2* tw64, float2* tw32, int lg, cudaStream_t st) {
+    const int L = 1 << lg;
+    twiddle_kernel<<<grid_for(L / 2, 256), 256, 0, st>>>(tw64, tw32, L);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_store_kernel(const double2* tw64, int lg_tw, double2* k64, float2* k32, int nf,
+                                int lg, cudaStream_t st) {
+    const int L = 1 << lg;
+    store_kernel_kernel<<<grid_for(L, 128), 128, 0, st>>>(tw64, lg_tw, k64, k32, nf, lg);
     return cudaGetLastError();
 }
 
@@ -651,11 +642,11 @@ cudaError_t launch_expand_factors(const double* class_factors, int nclass, int n
     size_t n = (size_t)nshell * na_pad;
     if (n == 0) return cudaSuccess;
     if (precision == PREC_FP32)
-        expand_factors_kernel<float><<<grid_for(n, 256), 256, 0, st>>>(
-            class_factors, nclass, nshell, cls, na_pad, (float*)b);
+        expand_factors_kernel<float><<<grid_for(n, 256), 256, 0, st>>>(class_factors, nclass, nshell, cls,
+                                                                       na_pad, (float*)b);
     else
-        expand_factors_kernel<double><<<grid_for(n, 256), 256, 0, st>>>(
-            class_factors, nclass, nshell, cls, na_pad, (double*)b);
+        expand_factors_kernel<double><<<grid_for(n, 256), 256, 0, st>>>(class_factors, nclass, nshell, cls,
+                                                                        na_pad, (double*)b);
     return cudaGetLastError();
 }
 

@@ -1,0 +1,488 @@
+#include "engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace sassgpu {
+
+cudaError_t DevBuf::ensure(size_t n) {
+    if (n <= bytes && p) return cudaSuccess;
+    release();
+    if (n == 0) n = 16;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    else p = nullptr;
+    return e;
+}
+
+void DevBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+cudaError_t HostPinned::ensure(size_t n) {
+    if (n <= bytes && p) return cudaSuccess;
+    release();
+    cudaError_t e = cudaHostAlloc(&p, n ? n : 16, cudaHostAllocDefault);
+    if (e == cudaSuccess) bytes = n ? n : 16;
+    else p = nullptr;
+    return e;
+}
+
+void HostPinned::release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+int sm_count(int device) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || n <= 0) n = 152;
+    return n;
+}
+
+namespace {
+
+// Status codes (mirror include/sassena_gb300.h).
+constexpr int kOk = 0, kErrArg = 1, kErrOom = 2, kErrUnsupported = 3, kErrCuda = 4;
+
+int fail_cuda(cudaError_t e, const char* what, std::string& err) {
+    cudaGetLastError();
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? kErrOom : kErrCuda;
+}
+
+#define ECK(expr)                                               \
+    do {                                                        \
+        cudaError_t e_ = (expr);                                \
+        if (e_ != cudaSuccess) return fail_cuda(e_, #expr, err); \
+    } while (0)
+
+template <class T>
+size_t push(std::vector<unsigned char>& blob, const std::vector<T>& v) {
+    size_t off = (blob.size() + 255) & ~(size_t)255;
+    blob.resize(off + v.size() * sizeof(T));
+    if (!v.empty()) memcpy(blob.data() + off, v.data(), v.size() * sizeof(T));
+    return off;
+}
+
+PhaseShape default_shape(int precision, size_t min_nm) {
+    if (precision == PREC_FP64) return PhaseShape{min_nm >= 64 ? 2 : 1, 4, 64};
+    int q = 1;
+    for (int cand : {8, 4, 2}) {  // the largest Q that wastes little of a shell's lanes
+        size_t per = 32 * (size_t)cand;
+        size_t groups = (min_nm + per - 1) / per;
+        double waste = 1.0 - (double)min_nm / (double)(groups * per);
+        if (waste <= 0.15) {
+            q = cand;
+            break;
+        }
+    }
+    return PhaseShape{q, 8, 128};
+}
+
+}  // namespace
+
+int build_system_tables(SystemState& s, cudaStream_t st, std::string& err) {
+    const size_t L = (size_t)1 << s.lg;
+    ECK(s.tw64.ensure(L / 2 * sizeof(double2)));
+    ECK(s.tw32.ensure(L / 2 * sizeof(float2)));
+    ECK(s.k64.ensure(L * sizeof(double2)));
+    ECK(s.k32.ensure(L * sizeof(float2)));
+    ECK(launch_twiddles(s.tw64.as<double2>(), s.tw32.as<float2>(), s.lg, st));
+    ECK(launch_store_kernel(s.tw64.as<double2>(), s.lg, s.k64.as<double2>(), s.k32.as<float2>(), (int)s.nf, s.lg,
+                            st));
+    ECK(cudaStreamSynchronize(st));
+    return kOk;
+}
+
+int stage_system(SystemState& s, const float* coords, bool on_device, int precision, cudaStream_t st,
+                 std::string& err) {
+    if (!coords) {
+        err = "coords is NULL";
+        return kErrArg;
+    }
+    const size_t n = s.nf * s.na * 3;
+    const float* src = coords;
+    std::vector<float> f0(s.na * 3);
+    if (!on_device) {
+        ECK(s.raw.ensure(n * sizeof(float)));
+        ECK(cudaMemcpyAsync(s.raw.p, coords, n * sizeof(float), cudaMemcpyHostToDevice, st));
+        src = s.raw.as<float>();
+        memcpy(f0.data(), coords, f0.size() * sizeof(float));
+    } else {
+        ECK(cudaMemcpyAsync(f0.data(), coords, f0.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+        ECK(cudaStreamSynchronize(st));
+    }
+    // FP32 form: fixed centre = midpoint of frame 0's bounding box (FP64)
+    double c[3] = {0, 0, 0};
+    if (precision == PREC_FP32) {
+        for (int k = 0; k < 3; ++k) {
+            double lo = f0[k], hi = f0[k];
+            for (size_t j = 1; j < s.na; ++j) {
+                lo = std::min(lo, (double)f0[3 * j + k]);
+                hi = std::max(hi, (double)f0[3 * j + k]);
+            }
+            c[k] = 0.5 * (lo + hi);
+        }
+        if (!std::isfinite(c[0]) || !std::isfinite(c[1]) || !std::isfinite(c[2])) {
+            err = "non-finite coordinates in frame 0";
+            return kErrArg;
+        }
+    }
+    memcpy(s.center, c, sizeof(c));
+    ECK(s.xyz.ensure(s.nf * s.na_pad * sizeof(float4)));
+    ECK(launch_stage(src, (int)s.nf, (int)s.na, (int)s.na_pad, c[0], c[1], c[2], precision == PREC_FP32,
+                     s.xyz.as<float4>(), st));
+    ECK(cudaStreamSynchronize(st));
+    s.staged = true;
+    return kOk;
+}
+
+int set_system_classes(SystemState& s, const int32_t* cls, bool on_device, cudaStream_t st, std::string& err) {
+    if (!cls) {
+        err = "atom_class is NULL";
+        return kErrArg;
+    }
+    std::vector<int32_t> h(s.na_pad, -1);
+    if (on_device) ECK(cudaMemcpy(h.data(), cls, s.na * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    else memcpy(h.data(), cls, s.na * sizeof(int32_t));
+    for (size_t j = 0; j < s.na; ++j)
+        if (h[j] < 0 || (size_t)h[j] >= s.nclass) {
+            err = "atom " + std::to_string(j) + " has class " + std::to_string(h[j]) + " outside [0," +
+                  std::to_string(s.nclass) + ")";
+            return kErrArg;
+        }
+    ECK(s.cls.ensure(s.na_pad * sizeof(int32_t)));
+    ECK(cudaMemcpyAsync(s.cls.p, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    ECK(cudaStreamSynchronize(st));
+    s.classes_set = true;
+    return kOk;
+}
+
+void Engine::release() {
+    DevBuf* bufs[] = {&blob_, &bfac_, &amp_, &part_, &ppart_, &apart_, &a2part_, &counter_, &err_, &tw64_, &tw32_};
+    for (DevBuf* b : bufs) b->release();
+    hblob_.release();
+}
+
+int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items, std::string& err) {
+    cfg_ = cfg;
+    stats_ = EngineStats();
+    const bool f32 = cfg.precision == PREC_FP32;
+    const bool coherent = cfg.scattering == 0;
+    const bool autoc = cfg.dsp == DSP_AUTOCORRELATE;
+    const size_t bsz = f32 ? 4 : 8;
+    nitems_ = (int)items.size();
+    if (items.empty()) {
+        err = "no work";
+        return kErrArg;
+    }
+    const int sms = sm_count(cfg.device);
+
+    // ---- shape and sizes ----------------------------------------------------------------
+    size_t min_nm = (size_t)-1, total_shells = 0;
+    lg_max_ = 2;
+    nf_max_ = 1;
+    for (const WorkItem& it : items) {
+        for (size_t s = 0; s + 1 < it.offs.size(); ++s) min_nm = std::min(min_nm, it.offs[s + 1] - it.offs[s]);
+        total_shells += it.offs.size() - 1;
+        lg_max_ = std::max(lg_max_, it.sys->lg);
+        nf_max_ = std::max(nf_max_, (int)it.sys->nf);
+    }
+    PhaseShape shape = cfg.shape.q_per_lane ? cfg.shape : default_shape(cfg.precision, min_nm);
+    if (coherent && !phase_shape_supported(cfg.precision, shape)) {
+        err = "phase tile shape not instantiated";
+        return kErrUnsupported;
+    }
+    stats_.shape = shape;
+
+    // atom splits: enough tiles for the persistent grid to balance
+    nsplit_.assign(items.size(), 1);
+    size_t base_tiles = 0;
+    for (const WorkItem& it : items) {
+        size_t groups = 0;
+        for (size_t s = 0; s + 1 < it.offs.size(); ++s)
+            groups += (it.offs[s + 1] - it.offs[s] + 32 * shape.q_per_lane - 1) / (32 * shape.q_per_lane);
+        base_tiles += groups * ((it.sys->nf + shape.warps - 1) / shape.warps);
+    }
+    const size_t target = (size_t)sms * 8;
+    for (size_t i = 0; i < items.size(); ++i) {
+        const int max_split = (int)(items[i].sys->na_pad / shape.atoms);
+        int ns = 1;
+        if (cfg.split_atoms > 0) ns = (int)((items[i].sys->na_pad + cfg.split_atoms - 1) / cfg.split_atoms);
+        else if (base_tiles < target) ns = (int)((target + base_tiles - 1) / std::max<size_t>(base_tiles, 1));
+        nsplit_[i] = std::max(1, std::min(ns, max_split));
+    }
+    stats_.split_atoms = cfg.split_atoms;
+
+    // ---- working buffers ---------------------------------------------------------------
+    bfac_off_.assign(items.size(), 0);
+    amp_off_.assign(items.size(), 0);
+    part_off_.assign(items.size(), 0);
+    size_t bfac_bytes = 0, amp_bytes = 0, part_bytes = 0;
+    for (size_t i = 0; i < items.size(); ++i) {
+        const WorkItem& it = items[i];
+        const size_t nq = it.offs.size() - 1, nv = it.offs.back(), nf = it.sys->nf;
+        bfac_off_[i] = bfac_bytes;
+        bfac_bytes += ((nq * it.sys->na_pad * bsz + 255) & ~(size_t)255);
+        if (coherent) {
+            amp_off_[i] = amp_bytes;
+            amp_bytes += ((nv * nf * (f32 ? 8 : 16) + 255) & ~(size_t)255);
+            if (nsplit_[i] > 1) {
+                part_off_[i] = part_bytes;
+                part_bytes += (size_t)nsplit_[i] * nv * nf * 16;
+            }
+        }
+        stats_.terms += (double)nv * (double)it.sys->na * (double)nf;
+    }
+    ECK(bfac_.ensure(bfac_bytes));
+    if (coherent) ECK(amp_.ensure(amp_bytes));
+    if (part_bytes) ECK(part_.ensure(part_bytes));
+
+    // ---- phase-sum descriptors -------------------------------------------------------------
+    std::vector<PhaseSystem> psys(items.size());
+    std::vector<PhaseTileDesc> tiles;
+    std::vector<CorrSystem> csys(items.size());
+    std::vector<std::vector<int>> shell_v(items.size());
+    item_nv_.assign(items.size(), 0);
+    item_nf_.assign(items.size(), 0);
+    split_part_.assign(items.size(), {nullptr, nullptr});
+    split_out32_.assign(items.size(), nullptr);
+    item_cf_.assign(items.size(), nullptr);
+    item_sys_.assign(items.size(), nullptr);
+    item_nq_.assign(items.size(), 0);
+    for (size_t i = 0; i < items.size(); ++i) {
+        const WorkItem& it = items[i];
+        SystemState& s = *it.sys;
+        const size_t nq = it.offs.size() - 1, nv = it.offs.back();
+        item_nv_[i] = nv;
+        item_nf_[i] = s.nf;
+        item_cf_[i] = it.d_cf;
+        item_sys_[i] = it.sys;
+        item_nq_[i] = nq;
+        for (size_t k = 0; k <= nq; ++k) shell_v[i].push_back((int)it.offs[k]);
+        void* bfac = bfac_.as<unsigned char>() + bfac_off_[i];
+        PhaseSystem& p = psys[i];
+        p.xyz = s.xyz.as<float4>();
+        p.bfac = bfac;
+        p.qv = it.d_qv;
+        p.na_pad = (int)s.na_pad;
+        p.nf = (int)s.nf;
+        p.split_stride = nv * s.nf;
+        void* amp = coherent ? (void*)(amp_.as<unsigned char>() + amp_off_[i]) : nullptr;
+        if (coherent) {
+            if (nsplit_[i] > 1) {
+                double2* part = reinterpret_cast<double2*>(part_.as<unsigned char>() + part_off_[i]);
+                p.out = part;
+                p.out_f32 = nullptr;
+                split_part_[i] = {part, f32 ? nullptr : reinterpret_cast<double2*>(amp)};
+                if (f32) split_out32_[i] = reinterpret_cast<float2*>(amp);
+            } else {
+                p.out = f32 ? nullptr : reinterpret_cast<double2*>(amp);
+                p.out_f32 = f32 ? reinterpret_cast<float2*>(amp) : nullptr;
+            }
+            const int per = 32 * shape.q_per_lane;
+            const int tiles_atoms = (int)(s.na_pad / shape.atoms);
+            const int split_len = ((tiles_atoms + nsplit_[i] - 1) / nsplit_[i]) * shape.atoms;
+            for (size_t sh = 0; sh < nq; ++sh)
+                for (size_t v = it.offs[sh]; v < it.offs[sh + 1]; v += per)
+                    for (size_t f0 = 0; f0 < s.nf; f0 += shape.warps)
+                        for (int sp = 0; sp < nsplit_[i]; ++sp) {
+                            PhaseTileDesc t;
+                            t.system = (int)i;
+                            t.shell = (int)sh;
+                            t.v0 = (int)v;
+                            t.nv = (int)std::min<size_t>(per, it.offs[sh + 1] - v);
+                            t.f0 = (int)f0;
+                            t.j_begin = sp * split_len;
+                            t.j_end = std::min((int)s.na_pad, (sp + 1) * split_len);
+                            t.split = sp;
+                            if (t.j_end > t.j_begin) tiles.push_back(t);
+                        }
+        }
+        CorrSystem& c = csys[i];
+        c.A = amp;
+        c.xyz = s.xyz.as<float4>();
+        c.bfac = bfac;
+        c.qv = it.d_qv;
+        c.shell_v = nullptr;  // patched after upload
+        c.kbr = f32 ? (const void*)s.k32.p : (const void*)s.k64.p;
+        c.cx = s.center[0];
+        c.cy = s.center[1];
+        c.cz = s.center[2];
+        c.nf = (int)s.nf;
+        c.lg = s.lg;
+        c.na_pad = (int)s.na_pad;
+    }
+    // longest tiles first (cost ~ atoms x active frames) for the persistent queue
+    std::stable_sort(tiles.begin(), tiles.end(), [&](const PhaseTileDesc& a, const PhaseTileDesc& b) {
+        auto cost = [&](const PhaseTileDesc& t) {
+            long long fr = std::min<long long>(shape.warps, (long long)psys[t.system].nf - t.f0);
+            return (long long)(t.j_end - t.j_begin) * fr;
+        };
+        return cost(a) > cost(b);
+    });
+    ntiles_ = (int)tiles.size();
+    nphase_systems_ = (int)items.size();
+
+    // ---- correlation chunks and finalisation entries ------------------------------------------
+    std::vector<CorrChunk> chunks;
+    std::vector<FinalEntry> entries;
+    const size_t per_shell = std::max<size_t>(1, ((size_t)sms * 4 + total_shells - 1) / total_shells);
+    size_t poff = 0;
+    int slot = 0;
+    for (size_t i = 0; i < items.size(); ++i) {
+        const WorkItem& it = items[i];
+        SystemState& s = *it.sys;
+        const size_t L = (size_t)1 << s.lg;
+        const size_t plen = autoc ? L : 2 * s.nf;
+        for (size_t sh = 0; sh + 1 < it.offs.size(); ++sh) {
+            FinalEntry e{};
+            e.slot_begin = slot;
+            e.part_off = poff;
+            e.part_len = plen;
+            e.nf = (int)s.nf;
+            e.lg = s.lg;
+            e.inv_nm = 1.0 / (double)(it.offs[sh + 1] - it.offs[sh]);
+            e.fqt = it.d_fqt + sh * s.nf;
+            e.fq = it.d_fq + sh;
+            e.fq2 = it.d_fq2 + sh;
+            const size_t units = coherent ? it.offs[sh + 1] - it.offs[sh] : s.na;
+            const size_t g = std::min(per_shell, units);
+            const size_t len = (units + g - 1) / g;
+            for (size_t u = 0; u < units; u += len) {
+                CorrChunk c{};
+                c.system = (int)i;
+                c.shell = (int)sh;
+                c.v_begin = (int)((coherent ? it.offs[sh] : 0) + u);
+                c.v_end = (int)((coherent ? it.offs[sh] : 0) + std::min(units, u + len));
+                c.part_off = poff;
+                c.slot = slot++;
+                poff += plen;
+                chunks.push_back(c);
+            }
+            e.slot_end = slot;
+            entries.push_back(e);
+        }
+    }
+    nchunks_ = (int)chunks.size();
+    nentries_ = (int)entries.size();
+    ECK(ppart_.ensure(poff * sizeof(double)));
+    ECK(apart_.ensure(slot * sizeof(double2)));
+    ECK(a2part_.ensure(slot * sizeof(double)));
+    ECK(counter_.ensure(sizeof(unsigned)));
+    ECK(err_.ensure(sizeof(unsigned)));
+
+    // shared twiddle table at the largest length
+    if (tw_lg_ != lg_max_ || !tw64_.p) {
+        const size_t Lm = (size_t)1 << lg_max_;
+        ECK(tw64_.ensure(Lm / 2 * sizeof(double2)));
+        ECK(tw32_.ensure(Lm / 2 * sizeof(float2)));
+        ECK(launch_twiddles(tw64_.as<double2>(), tw32_.as<float2>(), lg_max_, 0));
+        tw_lg_ = lg_max_;
+    }
+
+    // ---- upload all descriptors in one copy ------------------------------------------------------
+    std::vector<unsigned char> blob;
+    std::vector<size_t> shell_off(items.size());
+    for (size_t i = 0; i < items.size(); ++i) shell_off[i] = push(blob, shell_v[i]);
+    size_t o_psys = push(blob, psys), o_tiles = push(blob, tiles);
+    // CorrSystem.shell_v points into the blob: patch with the final device address
+    ECK(blob_.ensure(blob.size() + 4096 + csys.size() * sizeof(CorrSystem) + chunks.size() * sizeof(CorrChunk) +
+                     entries.size() * sizeof(FinalEntry) + 4096));
+    for (size_t i = 0; i < items.size(); ++i)
+        csys[i].shell_v = reinterpret_cast<const int*>(blob_.as<unsigned char>() + shell_off[i]);
+    size_t o_csys = push(blob, csys), o_chunks = push(blob, chunks), o_entries = push(blob, entries);
+    if (blob.size() > blob_.bytes) {
+        err = "descriptor blob sizing";
+        return kErrArg;
+    }
+    ECK(hblob_.ensure(blob.size()));
+    memcpy(hblob_.p, blob.data(), blob.size());
+    ECK(cudaMemcpy(blob_.p, hblob_.p, blob.size(), cudaMemcpyHostToDevice));
+    unsigned char* base = blob_.as<unsigned char>();
+    d_psys_ = reinterpret_cast<PhaseSystem*>(base + o_psys);
+    d_tiles_ = reinterpret_cast<PhaseTileDesc*>(base + o_tiles);
+    d_csys_ = reinterpret_cast<CorrSystem*>(base + o_csys);
+    d_chunks_ = reinterpret_cast<CorrChunk*>(base + o_chunks);
+    d_entries_ = reinterpret_cast<FinalEntry*>(base + o_entries);
+    ECK(cudaDeviceSynchronize());
+    stats_.phase_tiles = tiles.size();
+    stats_.corr_chunks = chunks.size();
+    stats_.final_entries = entries.size();
+    return kOk;
+}
+
+int Engine::enqueue(cudaStream_t st, std::string& err, cudaEvent_t* ev) {
+    const bool f32 = cfg_.precision == PREC_FP32;
+    const bool coherent = cfg_.scattering == 0;
+    size_t launches = 0, phase_launches = 0;
+    ECK(cudaMemsetAsync(err_.p, 0, sizeof(unsigned), st));
+    ECK(cudaMemsetAsync(counter_.p, 0, sizeof(unsigned), st));
+    for (int i = 0; i < nitems_; ++i) {
+        SystemState& s = *item_sys_[i];
+        ECK(launch_expand_factors(item_cf_[i], (int)s.nclass, (int)item_nq_[i], s.cls.as<int>(), (int)s.na_pad,
+                                  cfg_.precision, bfac_.as<unsigned char>() + bfac_off_[i], st));
+        ++launches;
+    }
+    if (ev) ECK(cudaEventRecord(ev[0], st));
+    if (coherent) {
+        PhaseLaunch pl{};
+        pl.precision = cfg_.precision;
+        pl.shape = stats_.shape;
+        pl.systems = d_psys_;
+        pl.tiles = d_tiles_;
+        pl.ntiles = ntiles_;
+        pl.counter = counter_.as<unsigned>();
+        pl.err = err_.as<unsigned>();
+        ECK(launch_phase_sum(pl, st));
+        ++launches;
+        ++phase_launches;
+        for (int i = 0; i < nitems_; ++i) {
+            if (nsplit_[i] <= 1) continue;
+            const size_t n = item_nv_[i] * item_nf_[i];
+            if (f32) ECK(launch_split_reduce_f32(split_part_[i].first, nsplit_[i], n, split_out32_[i], st));
+            else ECK(launch_split_reduce(split_part_[i].first, nsplit_[i], n, split_part_[i].second, st));
+            ++launches;
+        }
+    }
+    if (ev) ECK(cudaEventRecord(ev[1], st));
+    CorrLaunch cl{};
+    cl.precision = cfg_.precision;
+    cl.dsp = cfg_.dsp;
+    cl.systems = d_csys_;
+    cl.chunks = d_chunks_;
+    cl.nchunks = nchunks_;
+    cl.lg_max = lg_max_;
+    cl.nf_max = nf_max_;
+    cl.tw = f32 ? (const void*)tw32_.p : (const void*)tw64_.p;
+    cl.restore_phase = f32;
+    cl.ppart = ppart_.as<double>();
+    cl.apart = apart_.as<double2>();
+    cl.a2part = a2part_.as<double>();
+    cl.err = err_.as<unsigned>();
+    ECK(coherent ? launch_corr_accumulate(cl, st) : launch_self_accumulate(cl, st));
+    ++launches;
+    if (ev) ECK(cudaEventRecord(ev[2], st));
+    FinalLaunch fl{};
+    fl.dsp = cfg_.dsp;
+    fl.conj_out = cfg_.dsp == DSP_AUTOCORRELATE && cfg_.method == 1;
+    fl.entries = d_entries_;
+    fl.nentries = nentries_;
+    fl.lg_max = lg_max_;
+    fl.ppart = ppart_.as<double>();
+    fl.apart = apart_.as<double2>();
+    fl.a2part = a2part_.as<double>();
+    fl.tw = tw64_.as<double2>();
+    ECK(launch_finalize(fl, st));
+    ++launches;
+    if (ev) ECK(cudaEventRecord(ev[3], st));
+    stats_.launches = launches;
+    stats_.phase_launches = phase_launches;
+    return kOk;
+}
+
+}  // namespace sassgpu

@@ -1,0 +1,122 @@
+// Scheduling and launch engine shared by the single-plan path (sass_compute), the
+// batched path (sass_batch_*) and the autotuner: turns a list of systems with their
+// q-vectors into descriptor lists, working buffers and a launch sequence that contains
+// no host synchronisation (so it can be captured into a CUDA graph).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+
+namespace sassgpu {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t n);
+    void release();
+    template <class T>
+    T* as() const {
+        return reinterpret_cast<T*>(p);
+    }
+    ~DevBuf() { release(); }
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+};
+
+struct HostPinned {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t n);
+    void release();
+    ~HostPinned() { release(); }
+    HostPinned() = default;
+    HostPinned(const HostPinned&) = delete;
+    HostPinned& operator=(const HostPinned&) = delete;
+};
+
+// One staged trajectory on the device.
+struct SystemState {
+    size_t na = 0, nf = 0, na_pad = 0, nclass = 0;
+    int lg = 0;  // padded FFT length 2^lg >= 2 nf
+    double center[3] = {0, 0, 0};
+    DevBuf raw, xyz, cls, tw64, tw32, k64, k32;
+    bool staged = false, classes_set = false;
+};
+
+struct EngineConfig {
+    int scattering = 0, dsp = 0, method = 0, precision = 0;
+    PhaseShape shape{0, 0, 0};  // q_per_lane 0: automatic
+    int split_atoms = 0;        // atoms per phase-sum tile (0: automatic)
+    int device = 0;
+};
+
+// One system's q-vectors in a launch. All pointers are device pointers except `offs`.
+struct WorkItem {
+    SystemState* sys = nullptr;
+    std::vector<size_t> offs;  // [nq+1] sub-vector offsets, offs[0] == 0
+    const double* d_qv = nullptr;
+    const double* d_cf = nullptr;  // [nq][nclass]
+    double2* d_fqt = nullptr;      // [nq][nf]
+    double2* d_fq = nullptr;       // [nq]
+    double2* d_fq2 = nullptr;      // [nq]
+};
+
+struct EngineStats {
+    size_t phase_tiles = 0, corr_chunks = 0, final_entries = 0, launches = 0, phase_launches = 0;
+    PhaseShape shape{0, 0, 0};
+    int split_atoms = 0;
+    double terms = 0;
+};
+
+// Allocate the FFT tables of a system (device kernels); needs the stream only for order.
+int build_system_tables(SystemState& s, cudaStream_t st, std::string& err);
+// Stage frame-major float32 [nf][na][3] (host or device) into `s` (centred for FP32).
+int stage_system(SystemState& s, const float* coords, bool on_device, int precision, cudaStream_t st,
+                 std::string& err);
+int set_system_classes(SystemState& s, const int32_t* cls, bool on_device, cudaStream_t st, std::string& err);
+
+class Engine {
+public:
+    // Build descriptors and working buffers for `items`; uploads the descriptors
+    // (synchronously) so that enqueue() is free of host work.
+    int prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items, std::string& err);
+    // Enqueue the whole computation on `st`. With `events` non-null, records
+    // [phase start, phase end, corr end, finalize end] (not while capturing).
+    int enqueue(cudaStream_t st, std::string& err, cudaEvent_t* events = nullptr);
+    const EngineStats& stats() const { return stats_; }
+    unsigned int* err_word() const { return err_.as<unsigned int>(); }
+    // the amplitudes of item i after enqueue() (coherent): float2 (FP32) or double2 [nv][nf]
+    const void* amplitudes(int i) const { return amp_.as<unsigned char>() + amp_off_[i]; }
+    void release();
+
+private:
+    EngineConfig cfg_;
+    EngineStats stats_;
+    int lg_max_ = 2, nf_max_ = 1, nitems_ = 0;
+    std::vector<int> nsplit_;
+    std::vector<size_t> item_nv_, item_nf_;
+    std::vector<std::pair<double2*, double2*>> split_part_;  // (partials, FP64 out) per item
+    std::vector<float2*> split_out32_;
+    std::vector<const double*> item_cf_;
+    std::vector<SystemState*> item_sys_;
+    std::vector<size_t> item_nq_;
+    int nphase_systems_ = 0, ntiles_ = 0, nchunks_ = 0, nentries_ = 0;
+    DevBuf blob_, bfac_, amp_, part_, ppart_, apart_, a2part_, counter_, err_, tw64_, tw32_;
+    HostPinned hblob_;
+    std::vector<size_t> bfac_off_, amp_off_, part_off_;
+    PhaseSystem* d_psys_ = nullptr;
+    PhaseTileDesc* d_tiles_ = nullptr;
+    CorrSystem* d_csys_ = nullptr;
+    CorrChunk* d_chunks_ = nullptr;
+    FinalEntry* d_entries_ = nullptr;
+    int tw_lg_ = 0;
+};
+
+int sm_count(int device);
+
+}  // namespace sassgpu

@@ -1,9 +1,15 @@
-// Host-side launch interface of the sassena_gb300 kernels (internal, not the C-ABI).
+// Host-side launch interface of the sassena_gb300 kernels (internal, not the C ABI).
+//
+// Every launch works on lists of descriptors so that one launch can cover many
+// systems (trajectories) with different atom counts, frame counts, shells and
+// direction sets. A single scatter-device computation is a list with one system.
 #pragma once
 
 #include <cuda_runtime.h>
 #include <stddef.h>
 #include <stdint.h>
+
+#include <vector>
 
 namespace sassgpu {
 
@@ -19,105 +25,133 @@ enum DeviceError : unsigned int {
 // Atom padding granule: every device coordinate row holds a multiple of this many
 // atoms, so every staged tile is whole and 16-byte aligned.
 constexpr int kAtomGranule = 128;
+// Largest padded FFT length of the correlation kernels (NF <= 4096).
+constexpr int kMaxLg = 13;
 
-// One CTA-row of the phase sum: `nv` consecutive sub-vectors starting at `v0`,
-// all belonging to shell `shell` (so they share the per-atom factors b_j).
-struct VecGroup {
-    int shell, v0, nv, pad;
-};
-
-// Tile shape of the phase-sum kernel: q-vectors per lane, warps (= frames) per
-// CTA, atoms per pipeline stage. Only the instantiated shapes are accepted.
-struct PhaseTile {
+// ---------------------------------------------------------------------------------------
+// Phase sum
+// ---------------------------------------------------------------------------------------
+// Tile shape: q-vectors per lane, warps (= frames) per CTA, atoms per pipeline stage.
+struct PhaseShape {
     int q_per_lane;
     int warps;
     int atoms;
 };
 
-struct PhaseSumArgs {
-    int precision;
-    const float4* xyz;        // [nf][na_pad]
+struct PhaseSystem {
+    const float4* xyz;     // [nf][na_pad] staged coordinates
+    const void* bfac;      // [nshell][na_pad] factors: float (FP32) or double (FP64)
+    const double* qv;      // [nv][3] sub-vectors of this system
+    double2* out;          // FP64 amplitudes [nv][nf], or FP64 split partials [nsplit][nv][nf]
+    float2* out_f32;       // FP32 amplitudes [nv][nf] when the system has one atom split
+    size_t split_stride;   // nv * nf
     int na_pad, nf;
-    const void* bfac;         // [nshell][na_pad] float (FP32) or double (FP64)
-    const double* qv;         // [nv_total][3]
-    const VecGroup* groups;   // [ngroups]
-    int ngroups;
-    int nsplit;               // atom splits (grid z)
-    int atoms_per_split;      // multiple of the tile's atom count
-    double2* out;             // FP64: [nv_total][nf]; FP32 with nsplit > 1: [nsplit][nv_total][nf]
-    float2* out_f32;          // FP32 with nsplit == 1: [nv_total][nf]
-    size_t split_stride;      // elements between splits of `out`
-    unsigned int* err;
-    PhaseTile tile;
 };
 
-bool phase_tile_supported(int precision, PhaseTile t);
-cudaError_t launch_phase_sum(const PhaseSumArgs& a, cudaStream_t st);
-// out[v][f] = sum_s part[s][v][f] in split order (FP64), stored as double2 or float2.
+struct PhaseTileDesc {
+    int system, shell;     // shell index into the system's factor rows
+    int v0, nv;            // sub-vectors [v0, v0+nv) of the system, nv <= 32 * q_per_lane
+    int f0;                // first frame (one per warp)
+    int j_begin, j_end;    // atoms (multiples of the stage size)
+    int split;             // atom-split slice written by this tile
+};
+
+struct PhaseLaunch {
+    int precision;
+    PhaseShape shape;
+    const PhaseSystem* systems;
+    const PhaseTileDesc* tiles;
+    int ntiles;
+    unsigned int* counter;  // work-queue counter, zero before the launch
+    unsigned int* err;
+    int max_ctas;           // 0: SMs x resident CTAs per SM
+};
+
+bool phase_shape_supported(int precision, PhaseShape t);
+std::vector<PhaseShape> phase_shapes(int precision);
+cudaError_t launch_phase_sum(const PhaseLaunch& a, cudaStream_t st);
+// out[i] = sum_s part[s][i] in split order (FP64), stored as double2 or float2.
 cudaError_t launch_split_reduce(const double2* part, int nsplit, size_t n, double2* out,
                                 cudaStream_t st);
 cudaError_t launch_split_reduce_f32(const double2* part, int nsplit, size_t n, float2* out,
                                     cudaStream_t st);
 
-// Work unit of the correlation / store kernels: series [v_begin, v_end) of one
-// shell, reduced into partial slot `slot`.
-struct SeriesChunk {
-    int shell, v_begin, v_end, slot;
+// ---------------------------------------------------------------------------------------
+// Correlation, store and orientational average
+// ---------------------------------------------------------------------------------------
+enum DspType { DSP_AUTOCORRELATE = 0, DSP_SQUARE = 1, DSP_PLAIN = 2 };
+
+// Per-system data of the correlation kernels.
+struct CorrSystem {
+    const void* A;          // coherent amplitudes [nv][nf]: float2 (FP32) or double2 (FP64)
+    const float4* xyz;      // incoherent: staged coordinates [nf][na_pad]
+    const void* bfac;       // incoherent: factors [nshell][na_pad]
+    const double* qv;       // sub-vectors [nv][3]
+    const int* shell_v;     // [nshell+1] sub-vector offsets of each shell
+    const void* kbr;        // [L] bit-reversed store kernel: float2 (FP32) or double2 (FP64)
+    double cx, cy, cz;      // frame centre (FP32 form) for the plain-dsp phase restore
+    int nf, lg, na_pad;
 };
 
-// Work unit of the incoherent kernel: atoms [j_begin, j_end) of one shell.
-struct AtomChunk {
-    int shell, j_begin, j_end, slot;
+// Work unit: series [v_begin, v_end) (coherent) or atoms [v_begin, v_end) with all the
+// shell's directions (incoherent) of one shell of one system, into one partial slot.
+struct CorrChunk {
+    int system, shell, v_begin, v_end;
+    size_t part_off;        // offset (in doubles) of this slot's partial spectrum / series
+    int slot;               // index into apart / a2part
+    int pad;
 };
 
-struct CorrArgs {
-    int precision;
-    int nf, lg;                 // FFT length L = 1 << lg >= 2*nf
-    const void* A;              // [nv][nf] amplitudes: float2 (FP32) or double2 (FP64)
-    const void* tw;             // [L/2] exp(-2 pi i k / L), float2 (FP32) or double2 (FP64)
-    const void* kbr;            // [L] bit-reversed store kernel, same type as tw
-    const SeriesChunk* chunks;  // coherent chunks
-    const AtomChunk* achunks;   // incoherent chunks
+struct CorrLaunch {
+    int precision, dsp;
+    const CorrSystem* systems;
+    const CorrChunk* chunks;
     int nchunks;
-    // incoherent inputs
-    const float4* xyz;
-    int na_pad;
-    const double* qv;
-    const void* bfac;
-    const int* shell_v;         // [nshell+1] sub-vector offsets of each shell
-    // plain-dsp phase restore (frame-centred FP32 coordinates): exp(i q.c)
-    double cx, cy, cz;
-    int restore_phase;
-    // partials
-    double* ppart;              // [nslot][L] (autocorrelate) or double2 [nslot][nf] (square/plain)
-    double2* apart;             // [nslot]
-    double* a2part;             // [nslot]
+    int lg_max;             // largest padded length of the batch (shared memory sizing)
+    int nf_max;
+    const void* tw;         // [L_max/2] exp(-2 pi i k / L_max), float2 or double2
+    int restore_phase;      // FP32 form with dsp=plain: multiply by exp(i q.c)
+    double* ppart;          // partial spectra / series (see CorrChunk::part_off)
+    double2* apart;         // [nslot]
+    double* a2part;         // [nslot]
     unsigned int* err;
 };
 
-enum DspType { DSP_AUTOCORRELATE = 0, DSP_SQUARE = 1, DSP_PLAIN = 2 };
+cudaError_t launch_corr_accumulate(const CorrLaunch& a, cudaStream_t st);  // coherent
+cudaError_t launch_self_accumulate(const CorrLaunch& a, cudaStream_t st);  // incoherent
 
-// Coherent: per series FFT power spectrum / store reductions into partial slots.
-cudaError_t launch_corr_accumulate(const CorrArgs& a, int dsp, cudaStream_t st);
-// Incoherent: fused series generation + correlation into partial slots.
-cudaError_t launch_self_accumulate(const CorrArgs& a, int dsp, cudaStream_t st);
+// Per-shell finalisation entry.
+struct FinalEntry {
+    int slot_begin, slot_end;  // partial slots of this shell (consecutive)
+    size_t part_off;           // offset of slot_begin's partial; slots are `part_len` apart
+    size_t part_len;           // L (autocorrelate) or 2*nf (square/plain) doubles per slot
+    int nf, lg;
+    double inv_nm;
+    double2* fqt;              // [nf]
+    double2* fq;
+    double2* fq2;
+};
 
-struct FinalizeArgs {
-    int nf, lg, dsp, conj_out;
-    const double* ppart;        // as produced by the accumulate kernels
+struct FinalLaunch {
+    int dsp, conj_out;
+    const FinalEntry* entries;
+    int nentries;
+    int lg_max;
+    const double* ppart;
     const double2* apart;
     const double* a2part;
-    const int* slot_begin;      // [nshell+1] partial slots of each shell
-    const double* inv_nm;       // [nshell] 1/NM per shell
-    const double2* tw;          // [L/2]
-    double2* fqt;               // [nshell][nf]
-    double2* fq;                // [nshell]
-    double2* fq2;               // [nshell]
-    int nshell;
+    const double2* tw;         // [L_max/2] FP64
 };
-cudaError_t launch_finalize(const FinalizeArgs& a, cudaStream_t st);
+cudaError_t launch_finalize(const FinalLaunch& a, cudaStream_t st);
+
 // Shared memory of the FFT accumulate kernels for padded length 2^lg.
 size_t fft_smem_bytes(int precision, int lg, int nf, bool self);
+
+// FFT tables on the device: tw[k] = exp(-2 pi i k / L) (k < L/2) in FP64 and FP32, and
+// the store kernel K at bit-reversed positions for (nf, lg).
+cudaError_t launch_twiddles(double2* tw64, float2* tw32, int lg, cudaStream_t st);
+cudaError_t launch_store_kernel(const double2* tw64, int lg_tw, double2* k64, float2* k32, int nf,
+                                int lg, cudaStream_t st);
 
 // Staging: raw frame-major float [nf][na][3] -> float4 [nf][na_pad] (minus centre).
 cudaError_t launch_stage(const float* raw, int nf, int na, int na_pad, double cx, double cy,

@@ -11,7 +11,7 @@
 // which exists from the moment the library is loaded on a device.
 //
 // Limits: at most kMaxQ q-vectors per call and NF <= 4096 (padded FFT length 8192).
-// The array holds kScratchBytes (8,593,664 bytes, 8.2 MiB) on every GPU that loads the library,
+// The array holds kScratchBytes (8,601,856 bytes, 8.2 MiB) on every GPU that loads the library,
 // until the process exits.
 //
 // Sharing: every call uses the same array and the array keeps the previous call's
@@ -35,8 +35,8 @@ using namespace sassgpu;
 
 namespace {
 
-constexpr int kMaxLg = 13;                 // padded length 8192 => NF <= 4096
-constexpr int kMaxL = 1 << kMaxLg;
+constexpr int kNoAllocMaxLg = 13;          // padded length 8192 => NF <= 4096
+constexpr int kMaxL = 1 << kNoAllocMaxLg;
 constexpr int kMaxQ = 128;                 // q-vectors per call
 constexpr int kMaxSlots = 128;             // partial slots (chunks) per call
 constexpr int kMaxDevices = 64;
@@ -47,11 +47,13 @@ constexpr size_t kOffApart = kOffPart + (size_t)kMaxSlots * kMaxL * 8;     // do
 constexpr size_t kOffA2 = kOffApart + kMaxSlots * 16;                      // double [slots]
 constexpr size_t kOffTw = kOffA2 + kMaxSlots * 8 + 1024;                   // double2 [L/2]
 constexpr size_t kOffK = kOffTw + (size_t)(kMaxL / 2) * 16;                // double2 [L]
-constexpr size_t kOffChunks = kOffK + (size_t)kMaxL * 16;                  // SeriesChunk [slots]
-constexpr size_t kOffSlotBegin = kOffChunks + kMaxSlots * sizeof(SeriesChunk);  // int [Q+1]
-constexpr size_t kOffInvNm = kOffSlotBegin + 1024;                         // double [Q]
-constexpr size_t kScratchBytes = kOffInvNm + kMaxQ * 8 + 256;
-static_assert(kScratchBytes == 8593664, "documented scratch size");
+constexpr size_t kOffChunks = kOffK + (size_t)kMaxL * 16;                  // CorrChunk [slots]
+constexpr size_t kOffEntries = kOffChunks + kMaxSlots * 32;                // FinalEntry [Q]
+constexpr size_t kOffSystem = kOffEntries + kMaxQ * 64;                    // CorrSystem
+constexpr size_t kScratchBytes = kOffSystem + 256;
+static_assert(sizeof(CorrChunk) <= 32 && sizeof(FinalEntry) <= 64 && sizeof(CorrSystem) <= 256,
+              "descriptor sizes of the fixed layout");
+static_assert(kScratchBytes == 8601856, "documented scratch size");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -95,9 +97,12 @@ __global__ void noalloc_store_kernel_table(const double2* __restrict__ tw, doubl
     }
 }
 
-// Chunks of each q's sub-vectors (g per q, some possibly empty), slot offsets and 1/NM.
-__global__ void noalloc_schedule(const unsigned long long* __restrict__ offs, int nq, int g,
-                                 SeriesChunk* chunks, int* slot_begin, double* inv_nm) {
+// Descriptors of one call, written on the device from the device-side offsets: g chunks
+// per q (some possibly empty), one finalisation entry per q, the system record.
+__global__ void noalloc_schedule(const unsigned long long* __restrict__ offs, int nq, int g, int nf, int lg,
+                                 const double2* A, const double2* kbr, double2* fqt, double2* fq, double2* fq2,
+                                 CorrChunk* chunks, FinalEntry* entries, CorrSystem* sys) {
+    const size_t L = (size_t)1 << lg;
     for (int c = threadIdx.x; c < nq * g; c += blockDim.x) {
         const int s = c / g, k = c - s * g;
         const long long b = (long long)offs[s], e = (long long)offs[s + 1];
@@ -106,17 +111,44 @@ __global__ void noalloc_schedule(const unsigned long long* __restrict__ offs, in
         long long vb = b + k * len, ve = vb + len;
         if (vb > e) vb = e;
         if (ve > e) ve = e;
-        SeriesChunk ch;
+        CorrChunk ch;
+        ch.system = 0;
         ch.shell = s;
         ch.v_begin = (int)vb;
         ch.v_end = (int)ve;
+        ch.part_off = (size_t)c * L;
         ch.slot = c;
+        ch.pad = 0;
         chunks[c] = ch;
     }
-    for (int s = threadIdx.x; s <= nq; s += blockDim.x) slot_begin[s] = s * g;
     for (int s = threadIdx.x; s < nq; s += blockDim.x) {
         const long long nm = (long long)offs[s + 1] - (long long)offs[s];
-        inv_nm[s] = nm > 0 ? 1.0 / (double)nm : __longlong_as_double(0x7ff8000000000000LL);
+        FinalEntry e;
+        e.slot_begin = s * g;
+        e.slot_end = (s + 1) * g;
+        e.part_off = (size_t)s * g * L;
+        e.part_len = L;
+        e.nf = nf;
+        e.lg = lg;
+        e.inv_nm = nm > 0 ? 1.0 / (double)nm : __longlong_as_double(0x7ff8000000000000LL);
+        e.fqt = fqt + (size_t)s * nf;
+        e.fq = fq + s;
+        e.fq2 = fq2 + s;
+        entries[s] = e;
+    }
+    if (threadIdx.x == 0) {
+        CorrSystem y;
+        y.A = A;
+        y.xyz = nullptr;
+        y.bfac = nullptr;
+        y.qv = nullptr;
+        y.shell_v = nullptr;
+        y.kbr = kbr;
+        y.cx = y.cy = y.cz = 0.0;
+        y.nf = nf;
+        y.lg = lg;
+        y.na_pad = 0;
+        *sys = y;
     }
 }
 
@@ -131,7 +163,7 @@ extern "C" int sass_correlate_noalloc(int device, void* stream, const double* am
     if (device < 0 || device >= kMaxDevices) return SASS_ERR_ARG;
     int lg = 2;
     while (((size_t)1 << lg) < 2 * nf) ++lg;
-    if (lg > kMaxLg || nq > (size_t)kMaxQ) return SASS_ERR_UNSUPPORTED;  // beyond the fixed array
+    if (lg > kNoAllocMaxLg || nq > (size_t)kMaxQ) return SASS_ERR_UNSUPPORTED;  // beyond the fixed array
     cudaStream_t st = (cudaStream_t)stream;
 
     std::lock_guard<std::mutex> guard(g_lock);
@@ -158,42 +190,39 @@ extern "C" int sass_correlate_noalloc(int device, void* stream, const double* am
         ds.table_nf = (int)nf;
     }
     const int g = kMaxSlots / (int)nq;  // chunks per q (>= 1)
-    SeriesChunk* chunks = reinterpret_cast<SeriesChunk*>(b + kOffChunks);
-    int* slot_begin = reinterpret_cast<int*>(b + kOffSlotBegin);
-    double* inv_nm = reinterpret_cast<double*>(b + kOffInvNm);
-    noalloc_schedule<<<1, 256, 0, st>>>(reinterpret_cast<const unsigned long long*>(sub_offsets),
-                                        (int)nq, g, chunks, slot_begin, inv_nm);
+    CorrChunk* chunks = reinterpret_cast<CorrChunk*>(b + kOffChunks);
+    FinalEntry* entries = reinterpret_cast<FinalEntry*>(b + kOffEntries);
+    CorrSystem* sys = reinterpret_cast<CorrSystem*>(b + kOffSystem);
+    noalloc_schedule<<<1, 256, 0, st>>>(reinterpret_cast<const unsigned long long*>(sub_offsets), (int)nq, g,
+                                        (int)nf, lg, reinterpret_cast<const double2*>(amplitudes), kbr,
+                                        reinterpret_cast<double2*>(fqt), reinterpret_cast<double2*>(fq),
+                                        reinterpret_cast<double2*>(fq2), chunks, entries, sys);
     if (cudaGetLastError() != cudaSuccess) return SASS_ERR_CUDA;
 
-    CorrArgs ca{};
+    CorrLaunch ca{};
     ca.precision = PREC_FP64;
-    ca.nf = (int)nf;
-    ca.lg = lg;
-    ca.A = reinterpret_cast<const double2*>(amplitudes);
-    ca.tw = tw;
-    ca.kbr = kbr;
+    ca.dsp = DSP_AUTOCORRELATE;
+    ca.systems = sys;
     ca.chunks = chunks;
     ca.nchunks = (int)nq * g;
+    ca.lg_max = lg;
+    ca.nf_max = (int)nf;
+    ca.tw = tw;
     ca.ppart = reinterpret_cast<double*>(b + kOffPart);
     ca.apart = reinterpret_cast<double2*>(b + kOffApart);
     ca.a2part = reinterpret_cast<double*>(b + kOffA2);
-    if (launch_corr_accumulate(ca, DSP_AUTOCORRELATE, st) != cudaSuccess) return SASS_ERR_CUDA;
+    if (launch_corr_accumulate(ca, st) != cudaSuccess) return SASS_ERR_CUDA;
 
-    FinalizeArgs fa{};
-    fa.nf = (int)nf;
-    fa.lg = lg;
+    FinalLaunch fa{};
     fa.dsp = DSP_AUTOCORRELATE;
     fa.conj_out = dsp_method == SASS_METHOD_DIRECT;
+    fa.entries = entries;
+    fa.nentries = (int)nq;
+    fa.lg_max = lg;
     fa.ppart = ca.ppart;
     fa.apart = ca.apart;
     fa.a2part = ca.a2part;
-    fa.slot_begin = slot_begin;
-    fa.inv_nm = inv_nm;
     fa.tw = tw;
-    fa.fqt = reinterpret_cast<double2*>(fqt);
-    fa.fq = reinterpret_cast<double2*>(fq);
-    fa.fq2 = reinterpret_cast<double2*>(fq2);
-    fa.nshell = (int)nq;
     if (launch_finalize(fa, st) != cudaSuccess) return SASS_ERR_CUDA;
     return SASS_OK;
 }

@@ -4,15 +4,19 @@
 // all_vectors_scatter_device.cpp:388-439): the reference runs one host thread per
 // sub-vector and, for each frame, sums atoms sequentially in FP64 with libm cos/sin.
 //
-// GB300 layout: one CTA = one group of sub-vectors of a single shell (32*Q of
-// them, Q held in registers by every lane) x W consecutive frames (one warp per
-// frame). Each warp streams its own frame's atoms through a private S-stage
-// shared-memory ring filled by 1-D bulk copies (TMA engine, cp.async.bulk) of
-// T float4 coordinates plus T factors, completion tracked on mbarriers with
-// bounded waits. Every lane of a warp reads the same atom (shared-memory
-// broadcast) and evaluates its Q sub-vectors. Results are transposed through
-// shared memory so that each sub-vector's frames are written as one contiguous
-// row.
+// GB300 layout. The work is a list of tiles; a tile is one group of 32*Q sub-vectors of
+// one shell of one system (Q held in registers by every lane) x W consecutive frames
+// (one warp per frame) x a range of atoms. The kernel is persistent: every CTA takes
+// tiles from a global work counter (atomicAdd) until the list is exhausted, so one
+// launch covers many systems of uneven size (the batched form) as well as a single
+// system. Each warp streams its own frame's atoms through a private S-stage
+// shared-memory ring filled by 1-D bulk copies (TMA engine, cp.async.bulk) of T float4
+// coordinates plus T factors, completion tracked on mbarriers whose phases run on
+// across tiles; every wait is bounded. All lanes of a warp read the same atom (shared-
+// memory broadcast) and evaluate their Q sub-vectors. Results are transposed through
+// shared memory so each sub-vector's frames are written as one contiguous row. Tiles
+// never accumulate into each other (atom splits write separate FP64 partial slices), so
+// results do not depend on which CTA processed which tile.
 //
 // Two arithmetic forms:
 //   FP64 ("plain"): q.r and the atom sum in FP64 exactly as the reference writes
@@ -22,9 +26,11 @@
 //     exp(i q.c) cancels in |A|^2 and in the autocorrelation and is restored in
 //     FP64 for dsp=plain), q pre-scaled to revolutions (q/2pi), explicit range
 //     reduction u - rint(u) (magic-number rounding, exact subtraction), SFU
-//     sin/cos on the reduced angle, per-tile FP32 partial sums folded into a
-//     Kahan-compensated FP32 accumulator; the per-thread result is converted to
-//     FP64 for the cross-block (atom-split) reduction.
+//     sin/cos on the reduced angle, per-stage FP32 partial sums folded into a
+//     Kahan-compensated FP32 accumulator; atom-split partials are FP64 and reduced
+//     in FP64 (the cross-block reduction), single-split results are stored as FP32.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -37,275 +43,222 @@ struct PipeLayout {
     static constexpr int kCoordBytes = W * S * T * 16;
     static constexpr int kFactorBytes = W * S * T * BBYTES;
     static constexpr int kBarOffset = kCoordBytes + kFactorBytes;
-    static constexpr int kBytes = kBarOffset + W * S * 8;
+    static constexpr int kTileOffset = kBarOffset + W * S * 8;
+    static constexpr int kBytes = kTileOffset + 16;
 };
 
-// Issue the bulk copies of tile `t` of this warp's frame into ring stage `st`.
+// Issue the bulk copies of one stage (T coordinates + T factors) into a ring slot.
 template <int T, int BBYTES>
-__device__ __forceinline__ void issue_tile(float4* sx, void* sb, uint64_t* bar, const float4* src_x,
-                                           const unsigned char* src_b) {
+__device__ __forceinline__ void issue_stage(float4* sx, void* sb, uint64_t* bar, const float4* src_x,
+                                            const unsigned char* src_b) {
     fence_proxy_async_smem();
     mbar_arrive_expect_tx(bar, T * 16 + T * BBYTES);
     bulk_g2s(sx, src_x, T * 16, bar);
     bulk_g2s(sb, src_b, T * BBYTES, bar);
 }
 
-// Drain: after a timeout, wait (bounded) for any copy still in flight so that no
-// asynchronous write lands in shared memory after the CTA has moved on.
-template <int S>
-__device__ void drain(uint64_t* bars, int first_pending, int issued) {
-    for (int t = first_pending; t < issued; ++t) mbar_wait_parity(&bars[t % S], (t / S) & 1);
-}
-
-template <int Q, int W, int T, int S>
-__global__ void __launch_bounds__(W * 32)
-    phase_sum_fp32_kernel(const float4* __restrict__ xyz, int na_pad, int nf,
-                          const float* __restrict__ bfac, const double* __restrict__ qv,
-                          const VecGroup* __restrict__ groups, int atoms_per_split,
-                          double2* __restrict__ out, float2* __restrict__ out_f32,
-                          size_t split_stride, unsigned int* err) {
-    using L = PipeLayout<W, T, S, 4>;
-    static_assert(S * T >= 32 * Q, "output staging must fit in the coordinate ring");
-    extern __shared__ __align__(128) unsigned char smem[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int f = blockIdx.x * W + warp;
-    const VecGroup g = groups[blockIdx.y];
-    const int j_begin = blockIdx.z * atoms_per_split;
-    const int j_end = min(j_begin + atoms_per_split, na_pad);
-    const int ntiles = j_end > j_begin ? (j_end - j_begin) / T : 0;
-
-    float4* sx = reinterpret_cast<float4*>(smem) + warp * S * T;
-    float* sb = reinterpret_cast<float*>(smem + L::kCoordBytes) + warp * S * T;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L::kBarOffset) + warp * S;
-
-    // q in revolutions per Angstrom, rounded once from FP64.
-    const double inv2pi = 0.15915494309189533577;
-    float qx[Q], qy[Q], qz[Q];
+template <int Q>
+struct Fp32Acc {
+    float qx[Q], qy[Q], qz[Q], sr[Q], si[Q], cr[Q], ci[Q];
+    __device__ void load_q(const double* qv, int v0, int nv, int lane) {
+        const double inv2pi = 0.15915494309189533577;
 #pragma unroll
-    for (int k = 0; k < Q; ++k) {
-        int vl = lane + 32 * k;
-        if (vl < g.nv) {
-            const double* q = qv + 3 * (size_t)(g.v0 + vl);
-            qx[k] = (float)(q[0] * inv2pi);
-            qy[k] = (float)(q[1] * inv2pi);
-            qz[k] = (float)(q[2] * inv2pi);
-        } else {
-            qx[k] = qy[k] = qz[k] = 0.f;
+        for (int k = 0; k < Q; ++k) {
+            int vl = lane + 32 * k;
+            if (vl < nv) {
+                const double* q = qv + 3 * (size_t)(v0 + vl);
+                qx[k] = (float)(q[0] * inv2pi);
+                qy[k] = (float)(q[1] * inv2pi);
+                qz[k] = (float)(q[2] * inv2pi);
+            } else {
+                qx[k] = qy[k] = qz[k] = 0.f;
+            }
+            sr[k] = si[k] = cr[k] = ci[k] = 0.f;
         }
     }
-
-    float sr[Q], si[Q], cr[Q], ci[Q];
-#pragma unroll
-    for (int k = 0; k < Q; ++k) sr[k] = si[k] = cr[k] = ci[k] = 0.f;
-
-    if (f < nf && ntiles > 0) {
-        const float4* row = xyz + (size_t)f * na_pad;
-        const unsigned char* brow =
-            reinterpret_cast<const unsigned char*>(bfac + (size_t)g.shell * na_pad);
-        if (lane == 0) {
-#pragma unroll
-            for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
-            fence_mbar_init();
-        }
-        __syncwarp();
-        int issued = 0;
-        if (lane == 0)
-            for (; issued < S && issued < ntiles; ++issued)
-                issue_tile<T, 4>(sx + issued * T, sb + issued * T, &bars[issued],
-                                 row + j_begin + issued * T,
-                                 brow + (size_t)(j_begin + issued * T) * 4);
-        issued = __shfl_sync(0xffffffffu, issued, 0);
-
-        const float kMagic = 12582912.0f;  // 1.5 * 2^23: adds round to nearest integer
+    template <int T>
+    __device__ __forceinline__ void stage(const float4* cx, const float* cb) {
+        const float kMagic = 12582912.0f;  // 1.5 * 2^23: adds round to the nearest integer
         const float kTwoPi = 6.28318530717958647692f;
-        int t = 0;
-        for (; t < ntiles; ++t) {
-            const int st = t % S;
-            bool ok = mbar_wait_parity(&bars[st], (t / S) & 1);
-            if (!__all_sync(0xffffffffu, ok)) break;
-            const float4* cx = sx + st * T;
-            const float* cb = sb + st * T;
-            float tr[Q], ti[Q];
+        float tr[Q], ti[Q];
 #pragma unroll
-            for (int k = 0; k < Q; ++k) tr[k] = ti[k] = 0.f;
+        for (int k = 0; k < Q; ++k) tr[k] = ti[k] = 0.f;
 #pragma unroll 2
-            for (int jj = 0; jj < T; ++jj) {
-                const float4 r = cx[jj];
-                const float b = cb[jj];
+        for (int jj = 0; jj < T; ++jj) {
+            const float4 r = cx[jj];
+            const float b = cb[jj];
 #pragma unroll
-                for (int k = 0; k < Q; ++k) {
-                    float u = fmaf(r.z, qz[k], fmaf(r.y, qy[k], r.x * qx[k]));
-                    float n = __fsub_rn(__fadd_rn(u, kMagic), kMagic);
-                    float fr = __fsub_rn(u, n);  // in [-1/2, 1/2], exact
-                    float s, c;
-                    __sincosf(fr * kTwoPi, &s, &c);
-                    tr[k] = fmaf(b, c, tr[k]);
-                    ti[k] = fmaf(b, s, ti[k]);
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < Q; ++k) {  // Kahan: fold the tile sum into (s, c)
-                float y = __fsub_rn(tr[k], cr[k]);
-                float tt = __fadd_rn(sr[k], y);
-                cr[k] = __fsub_rn(__fsub_rn(tt, sr[k]), y);
-                sr[k] = tt;
-                y = __fsub_rn(ti[k], ci[k]);
-                tt = __fadd_rn(si[k], y);
-                ci[k] = __fsub_rn(__fsub_rn(tt, si[k]), y);
-                si[k] = tt;
-            }
-            __syncwarp();  // every lane is done with stage st: refill it with tile t+S
-            if (t + S < ntiles) {
-                if (lane == 0)
-                    issue_tile<T, 4>(sx + st * T, sb + st * T, &bars[st],
-                                     row + j_begin + (t + S) * T,
-                                     brow + (size_t)(j_begin + (t + S) * T) * 4);
-                ++issued;
+            for (int k = 0; k < Q; ++k) {
+                float u = fmaf(r.z, qz[k], fmaf(r.y, qy[k], r.x * qx[k]));
+                float n = __fsub_rn(__fadd_rn(u, kMagic), kMagic);
+                float fr = __fsub_rn(u, n);  // in [-1/2, 1/2], exact
+                float s, c;
+                __sincosf(fr * kTwoPi, &s, &c);
+                tr[k] = fmaf(b, c, tr[k]);
+                ti[k] = fmaf(b, s, ti[k]);
             }
         }
-        if (t < ntiles) {  // timed out: record, let in-flight copies land, stop
-            if (lane == 0) {
-                set_error(err, DEV_MBAR_TIMEOUT);
-                drain<S>(bars, t, issued);
-            }
-            __syncwarp();
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {  // Kahan: fold the stage sum into (s, c)
+            float y = __fsub_rn(tr[k], cr[k]);
+            float t = __fadd_rn(sr[k], y);
+            cr[k] = __fsub_rn(__fsub_rn(t, sr[k]), y);
+            sr[k] = t;
+            y = __fsub_rn(ti[k], ci[k]);
+            t = __fadd_rn(si[k], y);
+            ci[k] = __fsub_rn(__fsub_rn(t, si[k]), y);
+            si[k] = t;
         }
     }
+    __device__ double2 result(int k) const {
+        return make_double2((double)sr[k] - (double)cr[k], (double)si[k] - (double)ci[k]);
+    }
+};
 
-    // Transpose through shared memory: so[vl][w], then rows of W frames per v.
-    __syncthreads();
-    double2* so = reinterpret_cast<double2*>(smem);
+template <int Q>
+struct Fp64Acc {
+    double qx[Q], qy[Q], qz[Q], ar[Q], ai[Q];
+    __device__ void load_q(const double* qv, int v0, int nv, int lane) {
 #pragma unroll
-    for (int k = 0; k < Q; ++k) {
-        int vl = lane + 32 * k;
-        so[vl * W + warp] =
-            make_double2((double)sr[k] - (double)cr[k], (double)si[k] - (double)ci[k]);
+        for (int k = 0; k < Q; ++k) {
+            int vl = lane + 32 * k;
+            if (vl < nv) {
+                const double* q = qv + 3 * (size_t)(v0 + vl);
+                qx[k] = q[0];
+                qy[k] = q[1];
+                qz[k] = q[2];
+            } else {
+                qx[k] = qy[k] = qz[k] = 0.0;
+            }
+            ar[k] = ai[k] = 0.0;
+        }
     }
-    __syncthreads();
-    if (out_f32) {  // single atom split: the result goes straight to FP32 amplitudes
-        for (int idx = threadIdx.x; idx < g.nv * W; idx += W * 32) {
-            int vl = idx / W, w = idx - vl * W;
-            int ff = blockIdx.x * W + w;
-            if (ff < nf) {
-                double2 v = so[vl * W + w];
-                out_f32[(size_t)(g.v0 + vl) * nf + ff] = make_float2((float)v.x, (float)v.y);
+    template <int T>
+    __device__ __forceinline__ void stage(const float4* cx, const double* cb) {
+        for (int jj = 0; jj < T; ++jj) {
+            const float4 r = cx[jj];
+            const double b = cb[jj];
+#pragma unroll
+            for (int k = 0; k < Q; ++k) {
+                // p = x*qx + y*qy + z*qz, rounded as the reference writes it
+                double p = __dadd_rn(__dadd_rn(__dmul_rn((double)r.x, qx[k]), __dmul_rn((double)r.y, qy[k])),
+                                     __dmul_rn((double)r.z, qz[k]));
+                double s, c;
+                sincos(p, &s, &c);
+                ar[k] = __dadd_rn(ar[k], __dmul_rn(b, c));
+                ai[k] = __dadd_rn(ai[k], __dmul_rn(b, s));
             }
         }
-        return;
     }
-    double2* dst = out + (size_t)blockIdx.z * split_stride;  // FP64 partial of this atom split
-    for (int idx = threadIdx.x; idx < g.nv * W; idx += W * 32) {
-        int vl = idx / W, w = idx - vl * W;
-        int ff = blockIdx.x * W + w;
-        if (ff < nf) dst[(size_t)(g.v0 + vl) * nf + ff] = so[vl * W + w];
-    }
-}
+    __device__ double2 result(int k) const { return make_double2(ar[k], ai[k]); }
+};
 
-template <int Q, int W, int T, int S>
+template <bool F32, int Q>
+struct AccSel;
+template <int Q>
+struct AccSel<true, Q> {
+    typedef Fp32Acc<Q> type;
+    typedef float B;
+};
+template <int Q>
+struct AccSel<false, Q> {
+    typedef Fp64Acc<Q> type;
+    typedef double B;
+};
+
+template <bool F32, int Q, int W, int T, int S>
 __global__ void __launch_bounds__(W * 32)
-    phase_sum_fp64_kernel(const float4* __restrict__ xyz, int na_pad, int nf,
-                          const double* __restrict__ bfac, const double* __restrict__ qv,
-                          const VecGroup* __restrict__ groups, int atoms_per_split,
-                          double2* __restrict__ out, float2* __restrict__ out_f32,
-                          size_t split_stride, unsigned int* err) {
-    using L = PipeLayout<W, T, S, 8>;
-    (void)out_f32;
+    phase_sum_kernel(const PhaseSystem* __restrict__ systems, const PhaseTileDesc* __restrict__ tiles,
+                     int ntiles, unsigned int* __restrict__ counter, unsigned int* err) {
+    typedef typename AccSel<F32, Q>::type Acc;
+    typedef typename AccSel<F32, Q>::B B;
+    constexpr int BB = sizeof(B);
+    using L = PipeLayout<W, T, S, BB>;
     static_assert(S * T >= 32 * Q, "output staging must fit in the coordinate ring");
     extern __shared__ __align__(128) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int f = blockIdx.x * W + warp;
-    const VecGroup g = groups[blockIdx.y];
-    const int j_begin = blockIdx.z * atoms_per_split;
-    const int j_end = min(j_begin + atoms_per_split, na_pad);
-    const int ntiles = j_end > j_begin ? (j_end - j_begin) / T : 0;
-
     float4* sx = reinterpret_cast<float4*>(smem) + warp * S * T;
-    double* sb = reinterpret_cast<double*>(smem + L::kCoordBytes) + warp * S * T;
+    B* sb = reinterpret_cast<B*>(smem + L::kCoordBytes) + warp * S * T;
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L::kBarOffset) + warp * S;
+    volatile int* s_tile = reinterpret_cast<volatile int*>(smem + L::kTileOffset);
+    double2* so = reinterpret_cast<double2*>(smem);
 
-    double qx[Q], qy[Q], qz[Q], ar[Q], ai[Q];
+    if (lane == 0) {
 #pragma unroll
-    for (int k = 0; k < Q; ++k) {
-        int vl = lane + 32 * k;
-        if (vl < g.nv) {
-            const double* q = qv + 3 * (size_t)(g.v0 + vl);
-            qx[k] = q[0];
-            qy[k] = q[1];
-            qz[k] = q[2];
-        } else {
-            qx[k] = qy[k] = qz[k] = 0.0;
-        }
-        ar[k] = ai[k] = 0.0;
+        for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
     }
+    __syncwarp();
+    unsigned used = 0;    // stages this warp has consumed: ring slot and phase parity run on
+    bool failed = false;  // a bounded wait gave up: this warp does no further work
 
-    if (f < nf && ntiles > 0) {
-        const float4* row = xyz + (size_t)f * na_pad;
-        const unsigned char* brow =
-            reinterpret_cast<const unsigned char*>(bfac + (size_t)g.shell * na_pad);
-        if (lane == 0) {
-#pragma unroll
-            for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
-            fence_mbar_init();
+    for (;;) {
+        __syncthreads();  // the previous tile's output staging has been read by everyone
+        if (threadIdx.x == 0) *s_tile = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int ti = *s_tile;
+        if (ti >= ntiles) break;
+        const PhaseTileDesc td = tiles[ti];
+        const PhaseSystem sys = systems[td.system];
+        const int f = td.f0 + warp;
+        const int nst = (td.j_end - td.j_begin) / T;
+        Acc acc;
+        acc.load_q(sys.qv, td.v0, td.nv, lane);
+
+        if (f < sys.nf && nst > 0 && !failed) {
+            const float4* row = sys.xyz + (size_t)f * sys.na_pad + td.j_begin;
+            const unsigned char* brow = reinterpret_cast<const unsigned char*>(sys.bfac) +
+                                        ((size_t)td.shell * sys.na_pad + td.j_begin) * BB;
+            if (lane == 0)
+                for (int k = 0; k < S && k < nst; ++k) {
+                    const unsigned slot = (used + k) % S;
+                    issue_stage<T, BB>(sx + slot * T, sb + slot * T, &bars[slot], row + k * T,
+                                       brow + (size_t)k * T * BB);
+                }
+            int t = 0;
+            for (; t < nst; ++t) {
+                const unsigned slot = (used + t) % S;
+                const unsigned parity = ((used + t) / S) & 1u;
+                bool ok = mbar_wait_parity(&bars[slot], parity);
+                if (!__all_sync(0xffffffffu, ok)) break;
+                acc.template stage<T>(sx + slot * T, sb + slot * T);
+                __syncwarp();  // every lane is done with this slot: refill it with stage t+S
+                if (lane == 0 && t + S < nst)
+                    issue_stage<T, BB>(sx + slot * T, sb + slot * T, &bars[slot], row + (t + S) * T,
+                                       brow + (size_t)(t + S) * T * BB);
+            }
+            if (t < nst) {  // timed out: record, let issued copies land (bounded), stop
+                if (lane == 0) {
+                    set_error(err, DEV_MBAR_TIMEOUT);
+                    for (int k = t; k < nst && k < t + S; ++k)
+                        mbar_wait_parity(&bars[(used + k) % S], ((used + k) / S) & 1u);
+                }
+                failed = true;
+                __syncwarp();
+            }
+            used += nst;
         }
-        __syncwarp();
-        int issued = 0;
-        if (lane == 0)
-            for (; issued < S && issued < ntiles; ++issued)
-                issue_tile<T, 8>(sx + issued * T, sb + issued * T, &bars[issued],
-                                 row + j_begin + issued * T,
-                                 brow + (size_t)(j_begin + issued * T) * 8);
-        issued = __shfl_sync(0xffffffffu, issued, 0);
 
-        int t = 0;
-        for (; t < ntiles; ++t) {
-            const int st = t % S;
-            bool ok = mbar_wait_parity(&bars[st], (t / S) & 1);
-            if (!__all_sync(0xffffffffu, ok)) break;
-            const float4* cx = sx + st * T;
-            const double* cb = sb + st * T;
-            for (int jj = 0; jj < T; ++jj) {
-                const float4 r = cx[jj];
-                const double b = cb[jj];
+        __syncthreads();  // every pipeline of this tile is drained: the ring becomes staging
 #pragma unroll
-                for (int k = 0; k < Q; ++k) {
-                    // p = x*qx + y*qy + z*qz, rounded as the reference writes it
-                    double p = __dadd_rn(__dadd_rn(__dmul_rn((double)r.x, qx[k]),
-                                                   __dmul_rn((double)r.y, qy[k])),
-                                         __dmul_rn((double)r.z, qz[k]));
-                    double s, c;
-                    sincos(p, &s, &c);
-                    ar[k] = __dadd_rn(ar[k], __dmul_rn(b, c));
-                    ai[k] = __dadd_rn(ai[k], __dmul_rn(b, s));
+        for (int k = 0; k < Q; ++k) so[(lane + 32 * k) * W + warp] = acc.result(k);
+        __syncthreads();
+        if (F32 && sys.out_f32) {
+            float2* dst = sys.out_f32;
+            for (int idx = threadIdx.x; idx < td.nv * W; idx += W * 32) {
+                int vl = idx / W, w = idx - vl * W, ff = td.f0 + w;
+                if (ff < sys.nf) {
+                    double2 v = so[vl * W + w];
+                    dst[(size_t)(td.v0 + vl) * sys.nf + ff] = make_float2((float)v.x, (float)v.y);
                 }
             }
-            __syncwarp();  // every lane is done with stage st: refill it with tile t+S
-            if (t + S < ntiles) {
-                if (lane == 0)
-                    issue_tile<T, 8>(sx + st * T, sb + st * T, &bars[st],
-                                     row + j_begin + (t + S) * T,
-                                     brow + (size_t)(j_begin + (t + S) * T) * 8);
-                ++issued;
+        } else {
+            double2* dst = sys.out + (size_t)td.split * sys.split_stride;
+            for (int idx = threadIdx.x; idx < td.nv * W; idx += W * 32) {
+                int vl = idx / W, w = idx - vl * W, ff = td.f0 + w;
+                if (ff < sys.nf) dst[(size_t)(td.v0 + vl) * sys.nf + ff] = so[vl * W + w];
             }
         }
-        if (t < ntiles) {
-            if (lane == 0) {
-                set_error(err, DEV_MBAR_TIMEOUT);
-                drain<S>(bars, t, issued);
-            }
-            __syncwarp();
-        }
-    }
-
-    __syncthreads();
-    double2* so = reinterpret_cast<double2*>(smem);
-#pragma unroll
-    for (int k = 0; k < Q; ++k) so[(lane + 32 * k) * W + warp] = make_double2(ar[k], ai[k]);
-    __syncthreads();
-    double2* dst = out + (size_t)blockIdx.z * split_stride;
-    for (int idx = threadIdx.x; idx < g.nv * W; idx += W * 32) {
-        int vl = idx / W, w = idx - vl * W;
-        int ff = blockIdx.x * W + w;
-        if (ff < nf) dst[(size_t)(g.v0 + vl) * nf + ff] = so[vl * W + w];
     }
 }
 
@@ -335,70 +288,78 @@ __global__ void split_reduce_kernel(const double2* __restrict__ part, int nsplit
     }
 }
 
+template <bool F32, int Q, int W, int T, int S>
+cudaError_t launch_tiles(const PhaseLaunch& a, cudaStream_t st) {
+    auto k = phase_sum_kernel<F32, Q, W, T, S>;
+    const int smem = PipeLayout<W, T, S, F32 ? 4 : 8>::kBytes;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, W * 32, smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long long grid = (long long)std::max(per_sm, 1) * std::max(sms, 1);
+    if (a.max_ctas > 0 && grid > a.max_ctas) grid = a.max_ctas;
+    if (grid > a.ntiles) grid = a.ntiles;
+    if (grid < 1) return cudaSuccess;
+    k<<<(unsigned)grid, W * 32, smem, st>>>(a.systems, a.tiles, a.ntiles, a.counter, a.err);
+    return cudaGetLastError();
+}
+
 }  // namespace
 
-#define SASS_FP32_TILES(X) X(1, 8, 128, 2) X(2, 8, 128, 2) X(4, 8, 128, 2) X(8, 8, 128, 2)
-#define SASS_FP64_TILES(X) X(1, 4, 64, 2) X(2, 4, 64, 2)
+// Instantiated tile shapes (q per lane, warps = frames per CTA, atoms per stage).
+#define SASS_FP32_SHAPES(X) \
+    X(1, 8, 128) X(2, 8, 128) X(4, 8, 128) X(8, 8, 128) X(4, 4, 128) X(8, 4, 128) X(2, 8, 64) X(4, 8, 64)
+#define SASS_FP64_SHAPES(X) X(1, 4, 64) X(2, 4, 64) X(2, 8, 64)
 
-bool phase_tile_supported(int precision, PhaseTile t) {
-#define CHECK(Q, W, T, S) \
+bool phase_shape_supported(int precision, PhaseShape t) {
+#define CHECK(Q, W, T) \
     if (t.q_per_lane == Q && t.warps == W && t.atoms == T) return true;
     if (precision == PREC_FP32) {
-        SASS_FP32_TILES(CHECK)
+        SASS_FP32_SHAPES(CHECK)
     } else {
-        SASS_FP64_TILES(CHECK)
+        SASS_FP64_SHAPES(CHECK)
     }
 #undef CHECK
     return false;
 }
 
-cudaError_t launch_phase_sum(const PhaseSumArgs& a, cudaStream_t st) {
-    if (a.ngroups == 0 || a.nf == 0) return cudaSuccess;
-#define LAUNCH32(Q, W, T, S)                                                                    \
-    if (a.tile.q_per_lane == Q && a.tile.warps == W && a.tile.atoms == T) {                     \
-        constexpr int smem = PipeLayout<W, T, S, 4>::kBytes;                                    \
-        auto k = phase_sum_fp32_kernel<Q, W, T, S>;                                             \
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem); \
-        if (e != cudaSuccess) return e;                                                         \
-        for (int g0 = 0; g0 < a.ngroups; g0 += 65535) {                                         \
-        dim3 grid((a.nf + W - 1) / W, min(65535, a.ngroups - g0), a.nsplit);                    \
-        k<<<grid, W * 32, smem, st>>>(a.xyz, a.na_pad, a.nf, (const float*)a.bfac, a.qv,        \
-                                      a.groups + g0, a.atoms_per_split, a.out, a.out_f32,       \
-                                      a.split_stride,                                           \
-                                      a.err);                                                   \
-        }                                                                                       \
-        return cudaGetLastError();                                                              \
-    }
-#define LAUNCH64(Q, W, T, S)                                                                    \
-    if (a.tile.q_per_lane == Q && a.tile.warps == W && a.tile.atoms == T) {                     \
-        constexpr int smem = PipeLayout<W, T, S, 8>::kBytes;                                    \
-        auto k = phase_sum_fp64_kernel<Q, W, T, S>;                                             \
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem); \
-        if (e != cudaSuccess) return e;                                                         \
-        for (int g0 = 0; g0 < a.ngroups; g0 += 65535) {                                         \
-        dim3 grid((a.nf + W - 1) / W, min(65535, a.ngroups - g0), a.nsplit);                    \
-        k<<<grid, W * 32, smem, st>>>(a.xyz, a.na_pad, a.nf, (const double*)a.bfac, a.qv,       \
-                                      a.groups + g0, a.atoms_per_split, a.out, a.out_f32,       \
-                                      a.split_stride,                                           \
-                                      a.err);                                                   \
-        }                                                                                       \
-        return cudaGetLastError();                                                              \
-    }
-    if (a.precision == PREC_FP32) {
-        SASS_FP32_TILES(LAUNCH32)
+std::vector<PhaseShape> phase_shapes(int precision) {
+    std::vector<PhaseShape> v;
+#define ADD(Q, W, T) v.push_back(PhaseShape{Q, W, T});
+    if (precision == PREC_FP32) {
+        SASS_FP32_SHAPES(ADD)
     } else {
-        SASS_FP64_TILES(LAUNCH64)
+        SASS_FP64_SHAPES(ADD)
     }
-#undef LAUNCH32
-#undef LAUNCH64
+#undef ADD
+    return v;
+}
+
+cudaError_t launch_phase_sum(const PhaseLaunch& a, cudaStream_t st) {
+    if (a.ntiles <= 0) return cudaSuccess;
+    const PhaseShape& t = a.shape;
+#define L32(Q, W, T) \
+    if (t.q_per_lane == Q && t.warps == W && t.atoms == T) return launch_tiles<true, Q, W, T, 2>(a, st);
+#define L64(Q, W, T) \
+    if (t.q_per_lane == Q && t.warps == W && t.atoms == T) return launch_tiles<false, Q, W, T, 2>(a, st);
+    if (a.precision == PREC_FP32) {
+        SASS_FP32_SHAPES(L32)
+    } else {
+        SASS_FP64_SHAPES(L64)
+    }
+#undef L32
+#undef L64
     return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_split_reduce(const double2* part, int nsplit, size_t n, double2* out,
                                 cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    int blocks = (int)((n + 255) / 256);
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
     split_reduce_kernel<double2><<<blocks, 256, 0, st>>>(part, nsplit, n, out);
     return cudaGetLastError();
 }
@@ -406,8 +367,7 @@ cudaError_t launch_split_reduce(const double2* part, int nsplit, size_t n, doubl
 cudaError_t launch_split_reduce_f32(const double2* part, int nsplit, size_t n, float2* out,
                                     cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    int blocks = (int)((n + 255) / 256);
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
     split_reduce_kernel<float2><<<blocks, 256, 0, st>>>(part, nsplit, n, out);
     return cudaGetLastError();
 }

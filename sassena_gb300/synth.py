@@ -333,3 +333,33 @@ def write_files(directory, w, precision="fp64", method="fftw", qvectors_file=Tru
     with open(path, "w") as f:
         f.write(xml)
     return path
+
+
+def batched_uneven(seed=4, nsys=64, na_range=(500, 50000), nf_range=(256, 4096), nq_range=(5, 40),
+                   nm_range=(100, 1000), qrange=(0.1, 2.5), density=0.1, sigma=0.1,
+                   scattering="all"):
+    """Many independent systems of uneven size for the batched launch.
+
+    Atom and frame counts are log-uniform in their ranges, each system is built as the
+    1,000-atom workload (uniform positions at `density` atoms/A^3, Gaussian random walk,
+    H/C/N/O 50/30/10/10) with its own shells (uniform in `qrange`, sorted) and its own
+    direction set (size uniform in `nm_range`)."""
+    rng = np.random.default_rng(np.random.PCG64(seed))
+    names = ["H", "C", "N", "O"]
+    table = COHERENT_FM if scattering == "all" else INCOHERENT_FM
+    b = np.array([table[n] for n in names])
+    out = []
+    for i in range(nsys):
+        na = int(round(math.exp(rng.uniform(math.log(na_range[0]), math.log(na_range[1])))))
+        nf = int(round(math.exp(rng.uniform(math.log(nf_range[0]), math.log(nf_range[1])))))
+        nq = int(rng.integers(nq_range[0], nq_range[1] + 1))
+        nm = int(rng.integers(nm_range[0], nm_range[1] + 1))
+        box = (na / density) ** (1.0 / 3.0)
+        cls = _types(rng, na, names, [50, 30, 10, 10])
+        r0 = rng.uniform(0.0, box, (na, 3))
+        coords = random_walk(rng, r0, nf, sigma)
+        shells = np.sort(rng.uniform(qrange[0], qrange[1], nq))
+        out.append(Workload("batched_%d" % i, coords, cls, names, np.tile(b, (nq, 1)), shells,
+                            sphere_directions(nm, seed * 1000 + i), scattering=scattering,
+                            meta=dict(box=box, seed=seed)))
+    return out
