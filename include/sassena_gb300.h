@@ -171,6 +171,9 @@ int sass_batch_create(const sass_plan_desc* desc, size_t nsystems, const sass_sy
 /* Autotune tile shape and atom-split size over the whole batch (coherent). */
 int sass_batch_autotune(sass_batch* batch, int repeats, int* q_per_lane, int* warps, int* atoms,
                         int* split_atoms, double* best_ms);
+/* Set the tile shape and atom-split size (atoms per tile, a multiple of 128; 0 =
+ * automatic), e.g. from sass_batch_autotune on a representative smaller batch. */
+int sass_batch_set_tile(sass_batch* batch, int q_per_lane, int warps, int atoms, int split_atoms);
 /* Enqueue one replay of the batch's graph (asynchronous on the batch stream). */
 int sass_batch_run(sass_batch* batch);
 /* Wait for the last run and check the device error word. */

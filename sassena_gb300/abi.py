@@ -31,7 +31,7 @@ EXPORTS = [
     "sass_host_free", "sass_probe_pipes", "sass_correlate_noalloc", "sass_version",
     "sass_autotune", "sass_batch_create", "sass_batch_autotune", "sass_batch_run",
     "sass_batch_sync", "sass_batch_results", "sass_batch_timing", "sass_batch_info",
-    "sass_batch_error", "sass_batch_destroy",
+    "sass_batch_error", "sass_batch_destroy", "sass_batch_set_tile",
 ]
 
 
@@ -108,6 +108,7 @@ def load(path=LIB_PATH):
                                     ctypes.POINTER(_vp)]
     L.sass_batch_autotune.argtypes = [_vp, ctypes.c_int, _ip, _ip, _ip, _ip, _dp]
     L.sass_batch_run.argtypes = [_vp]
+    L.sass_batch_set_tile.argtypes = [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.sass_batch_sync.argtypes = [_vp]
     L.sass_batch_results.argtypes = [_vp, _sz, _vp, _vp, _vp]
     L.sass_batch_timing.argtypes = [_vp, ctypes.POINTER(Timing)]
@@ -299,6 +300,9 @@ class Batch:
         r = dict(zip(("q_per_lane", "warps", "atoms", "split_atoms"), [o.value for o in out]))
         r["ms"] = ms.value
         return r
+
+    def set_tile(self, q_per_lane=0, warps=0, atoms=0, split_atoms=0):
+        self._check(self.lib.sass_batch_set_tile(self._h, q_per_lane, warps, atoms, split_atoms))
 
     def run(self):
         self._check(self.lib.sass_batch_run(self._h))

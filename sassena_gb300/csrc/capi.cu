@@ -701,6 +701,21 @@ int sass_batch_autotune(sass_batch* b, int repeats, int* q_per_lane, int* warps,
     return SASS_OK;
 }
 
+int sass_batch_set_tile(sass_batch* b, int q_per_lane, int warps, int atoms, int split_atoms) {
+    if (!b) return SASS_ERR_ARG;
+    PhaseShape t{q_per_lane, warps, atoms};
+    if (q_per_lane != 0 && !phase_shape_supported(b->d.precision, t))
+        return set_msg(b->msg, SASS_ERR_UNSUPPORTED, "phase tile Q=%d W=%d T=%d not instantiated", q_per_lane, warps,
+                       atoms);
+    if (split_atoms < 0 || split_atoms % kAtomGranule)
+        return set_msg(b->msg, SASS_ERR_ARG, "split_atoms must be a non-negative multiple of %d", kAtomGranule);
+    b->shape = q_per_lane ? t : PhaseShape{0, 0, 0};
+    b->split_atoms = split_atoms;
+    b->prepared = false;
+    drop_graph(b);
+    return SASS_OK;
+}
+
 int sass_batch_run(sass_batch* b) {
     if (!b) return SASS_ERR_ARG;
     CK(b->msg, cudaSetDevice(b->d.device));
