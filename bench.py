@@ -209,7 +209,9 @@ def run_ours(args, dist):
     dev = dist.local
     torch.cuda.set_device(dev)
     w = make_workload(args.workload, args.nq, args.nf)
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the library's work and the timing events share it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     nclass = len(w.class_names)
     terms = w.terms()
     plan = abi.Plan(w.na, w.nf, nclass, w.scattering, w.dsp, "fftw", "fp32", device=dev,
@@ -347,7 +349,8 @@ def run_batched(args, dist):
     nsys = args.nsys or 64
     ws = synth.batched_uneven(seed=4, nsys=nsys)
     terms = sum(w.terms() for w in ws)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     # autotune on a representative subset (every 8th system), apply to the full batch
     t0 = time.perf_counter()
     with abi.Batch(ws[::8], precision="fp32", device=dev, stream=stream.cuda_stream) as sub:

@@ -187,6 +187,38 @@ int sass_batch_info(const sass_batch* batch, double* terms, uint64_t* phase_tile
 const char* sass_batch_error(const sass_batch* batch);
 void sass_batch_destroy(sass_batch* batch);
 
+/* ---- Learned control variate for the orientational average ----
+ * A 4 -> 128 -> 128 -> 1 tanh network g(u, |q|) with BF16 weights and FP32
+ * accumulation, trained on the GPU by this library's own kernels on exact intensities
+ * (inputs x = (ux, uy, uz, (|q| - q_mid)/q_half), target the normalised log intensity,
+ * g = exp(y * y_std + y_mean)). No counterpart in the reference, whose orientational
+ * average is the plain mean over random orientations (all_vectors_scatter_device.cpp:355-360). */
+typedef struct sass_mlp sass_mlp;
+int sass_mlp_create(int device, uint64_t seed, sass_mlp** net);
+void sass_mlp_destroy(sass_mlp* net);
+const char* sass_mlp_error(const sass_mlp* net);
+int sass_mlp_param_count(void);
+int sass_mlp_set_scaling(sass_mlp* net, double q_mid, double q_half, double y_mean, double y_std);
+/* FP32 master weights and their BF16 copy (either pointer may be NULL). Layout:
+ * W1 [128][4], b1 [128], W2 [128][128], b2 [128], W3 [128], b3. */
+int sass_mlp_get_params(const sass_mlp* net, float* master, uint16_t* bf16);
+int sass_mlp_set_params(sass_mlp* net, const float* master);
+/* Gradient of mean (y - t)^2 over the n samples x [n][4], t [n] (no update). */
+int sass_mlp_gradient(sass_mlp* net, const float* x, const float* t, size_t n, float* grad, double* loss);
+/* Adam steps on consecutive mini-batches of the (caller-shuffled) samples. */
+int sass_mlp_train(sass_mlp* net, const float* x, const float* t, size_t n, int steps, int batch, double lr,
+                   double* last_loss);
+int sass_mlp_predict(sass_mlp* net, const float* x, size_t n, float* y);
+/* Mean of g over the sphere at each |q| (spherical-Fibonacci quadrature, FP64 sums). */
+int sass_mlp_sphere_mean(sass_mlp* net, const double* qlen, size_t nshell, size_t npoints, double* gbar);
+/* Control-variate estimate of S(q,t) and fq for a coherent plan (dsp autocorrelate or
+ * square) from m directions shared by all shells, with the plain Monte Carlo estimate on
+ * the same directions beside it. fqt_* [nq][nf][2], fq_* [nq][2], diag [nq][3] (optional:
+ * quadrature mean of g, mean of g over the directions, variance of g). */
+int sass_compute_cv(sass_plan* plan, sass_mlp* net, size_t nq, const double* qlen, size_t m,
+                    const double* dirs, const double* class_factors, size_t nquad, double* fqt_cv,
+                    double* fqt_mc, double* fq_cv, double* fq_mc, double* diag);
+
 /* Pinned host memory for faster staging (cudaHostAlloc / cudaFreeHost). */
 void* sass_host_alloc(size_t bytes);
 void sass_host_free(void* p);

@@ -32,6 +32,9 @@ EXPORTS = [
     "sass_autotune", "sass_batch_create", "sass_batch_autotune", "sass_batch_run",
     "sass_batch_sync", "sass_batch_results", "sass_batch_timing", "sass_batch_info",
     "sass_batch_error", "sass_batch_destroy", "sass_batch_set_tile",
+    "sass_mlp_create", "sass_mlp_destroy", "sass_mlp_error", "sass_mlp_param_count",
+    "sass_mlp_set_scaling", "sass_mlp_get_params", "sass_mlp_set_params", "sass_mlp_gradient",
+    "sass_mlp_train", "sass_mlp_predict", "sass_mlp_sphere_mean", "sass_compute_cv",
 ]
 
 
@@ -117,6 +120,21 @@ def load(path=LIB_PATH):
     L.sass_batch_error.restype = ctypes.c_char_p
     L.sass_batch_destroy.argtypes = [_vp]
     L.sass_batch_destroy.restype = None
+    L.sass_mlp_create.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(_vp)]
+    L.sass_mlp_destroy.argtypes = [_vp]
+    L.sass_mlp_destroy.restype = None
+    L.sass_mlp_error.argtypes = [_vp]
+    L.sass_mlp_error.restype = ctypes.c_char_p
+    L.sass_mlp_set_scaling.argtypes = [_vp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_double]
+    L.sass_mlp_get_params.argtypes = [_vp, _vp, _vp]
+    L.sass_mlp_set_params.argtypes = [_vp, _vp]
+    L.sass_mlp_gradient.argtypes = [_vp, _vp, _vp, _sz, _vp, _dp]
+    L.sass_mlp_train.argtypes = [_vp, _vp, _vp, _sz, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                 _dp]
+    L.sass_mlp_predict.argtypes = [_vp, _vp, _sz, _vp]
+    L.sass_mlp_sphere_mean.argtypes = [_vp, _vp, _sz, _sz, _vp]
+    L.sass_compute_cv.argtypes = [_vp, _vp, _sz, _vp, _sz, _vp, _vp, _sz, _vp, _vp, _vp, _vp, _vp]
     L.sass_correlate_noalloc.argtypes = [ctypes.c_int, _vp, _vp, _sz, _sz, _vp, ctypes.c_int, _vp,
                                          _vp, _vp]
     _lib = L
@@ -332,6 +350,95 @@ class Batch:
         r = dict(zip(("q_per_lane", "warps", "atoms", "split_atoms"), [o.value for o in out]))
         r.update(terms=terms.value, phase_tiles=tiles.value)
         return r
+
+
+class MLP:
+    """The control-variate network (sass_mlp_*)."""
+
+    def __init__(self, device=0, seed=0):
+        self.lib = load()
+        self.nparams = self.lib.sass_mlp_param_count()
+        h = _vp()
+        rc = self.lib.sass_mlp_create(device, seed, ctypes.byref(h))
+        self._h = h
+        if rc != SASS_OK:
+            raise SassError(rc, self.error())
+
+    def error(self):
+        return self.lib.sass_mlp_error(self._h).decode() if self._h else ""
+
+    def _check(self, rc):
+        if rc != SASS_OK:
+            raise SassError(rc, self.error())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.sass_mlp_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_scaling(self, q_mid, q_half, y_mean, y_std):
+        self._check(self.lib.sass_mlp_set_scaling(self._h, q_mid, q_half, y_mean, y_std))
+
+    def params(self):
+        m = np.zeros(self.nparams, np.float32)
+        b = np.zeros(self.nparams, np.uint16)
+        self._check(self.lib.sass_mlp_get_params(self._h, _ptr(m), _ptr(b)))
+        bf = (b.astype(np.uint32) << 16).view(np.float32)
+        return m, bf
+
+    def set_params(self, master):
+        m = np.ascontiguousarray(master, np.float32)
+        self._check(self.lib.sass_mlp_set_params(self._h, _ptr(m)))
+
+    def gradient(self, x, t):
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        g = np.zeros(self.nparams, np.float32)
+        loss = ctypes.c_double()
+        self._check(self.lib.sass_mlp_gradient(self._h, _ptr(x), _ptr(t), len(t), _ptr(g),
+                                               ctypes.byref(loss)))
+        return g, loss.value
+
+    def train(self, x, t, steps, batch=4096, lr=1e-3):
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        loss = ctypes.c_double()
+        self._check(self.lib.sass_mlp_train(self._h, _ptr(x), _ptr(t), len(t), steps, batch, lr,
+                                            ctypes.byref(loss)))
+        return loss.value
+
+    def predict(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.zeros(len(x), np.float32)
+        self._check(self.lib.sass_mlp_predict(self._h, _ptr(x), len(x), _ptr(y)))
+        return y
+
+    def sphere_mean(self, qlen, npoints=32768):
+        q = np.ascontiguousarray(qlen, np.float64)
+        out = np.zeros(len(q))
+        self._check(self.lib.sass_mlp_sphere_mean(self._h, _ptr(q), len(q), npoints, _ptr(out)))
+        return out
+
+
+def compute_cv(plan, net, qlen, dirs, class_factors, nquad=32768):
+    """Control-variate and plain MC estimates on the same directions (see sass_compute_cv)."""
+    q = np.ascontiguousarray(qlen, np.float64)
+    d = np.ascontiguousarray(dirs, np.float64).reshape(-1, 3)
+    cf = np.ascontiguousarray(class_factors, np.float64).reshape(len(q), plan.nclass)
+    nq, nf = len(q), plan.nf
+    a, b = np.zeros((nq, nf, 2)), np.zeros((nq, nf, 2))
+    c, e = np.zeros((nq, 2)), np.zeros((nq, 2))
+    diag = np.zeros((nq, 3))
+    plan._check(plan.lib.sass_compute_cv(plan._h, net._h, nq, _ptr(q), len(d), _ptr(d), _ptr(cf),
+                                         nquad, _ptr(a), _ptr(b), _ptr(c), _ptr(e), _ptr(diag)))
+    z = lambda v: v[..., 0] + 1j * v[..., 1]  # noqa: E731
+    return z(a), z(b), z(c), z(e), diag
 
 
 def probe_pipes(device=0):

@@ -18,12 +18,11 @@
 #include "../../include/sassena_gb300.h"
 #include "engine.h"
 #include "kernels.h"
+#include "plan.h"
 
 using namespace sassgpu;
 
 namespace {
-
-constexpr int kEvents = 12;
 
 int ceil_log2(size_t n) {
     int lg = 0;
@@ -72,20 +71,6 @@ std::mutex g_tune_lock;
 std::map<std::string, std::pair<PhaseShape, int>> g_tune_cache;
 
 }  // namespace
-
-struct sass_plan {
-    sass_plan_desc d{};
-    SystemState sys;
-    Engine eng;
-    cudaStream_t st = nullptr;
-    bool own_stream = false;
-    std::string msg;
-    sass_timing timing{};
-    cudaEvent_t ev[kEvents] = {};
-    PhaseShape shape{0, 0, 0};
-    int split_atoms = 0;
-    DevBuf qv, cf, fqt, fq, fq2, amp_tmp;
-};
 
 struct sass_batch {
     sass_plan_desc d{};

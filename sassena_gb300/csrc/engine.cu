@@ -1,4 +1,5 @@
 #include "engine.h"
+#include "mlp.h"
 
 #include <algorithm>
 #include <cmath>
@@ -330,7 +331,18 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
 
     // ---- correlation chunks and finalisation entries ------------------------------------------
     std::vector<CorrChunk> chunks;
-    std::vector<FinalEntry> entries;
+    std::vector<FinalEntry> entries, entries_w;
+    weighted_ = false;
+    item_wsqrt_.assign(items.size(), nullptr);
+    for (size_t i = 0; i < items.size(); ++i)
+        if (items[i].d_wsqrt) {
+            if (!coherent) {
+                err = "weighted averages need the coherent path";
+                return kErrArg;
+            }
+            weighted_ = true;
+            item_wsqrt_[i] = items[i].d_wsqrt;
+        }
     const size_t per_shell = std::max<size_t>(1, ((size_t)sms * 4 + total_shells - 1) / total_shells);
     size_t poff = 0;
     int slot = 0;
@@ -366,6 +378,13 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
             }
             e.slot_end = slot;
             entries.push_back(e);
+            if (it.d_wsqrt) {
+                FinalEntry ew = e;
+                ew.fqt = it.d_fqt_w + sh * s.nf;
+                ew.fq = it.d_fq_w + sh;
+                ew.fq2 = it.d_fq2_w + sh;
+                entries_w.push_back(ew);
+            }
         }
     }
     nchunks_ = (int)chunks.size();
@@ -392,10 +411,11 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
     size_t o_psys = push(blob, psys), o_tiles = push(blob, tiles);
     // CorrSystem.shell_v points into the blob: patch with the final device address
     ECK(blob_.ensure(blob.size() + 4096 + csys.size() * sizeof(CorrSystem) + chunks.size() * sizeof(CorrChunk) +
-                     entries.size() * sizeof(FinalEntry) + 4096));
+                     (entries.size() + entries_w.size()) * sizeof(FinalEntry) + 4096));
     for (size_t i = 0; i < items.size(); ++i)
         csys[i].shell_v = reinterpret_cast<const int*>(blob_.as<unsigned char>() + shell_off[i]);
     size_t o_csys = push(blob, csys), o_chunks = push(blob, chunks), o_entries = push(blob, entries);
+    size_t o_entries_w = push(blob, entries_w);
     if (blob.size() > blob_.bytes) {
         err = "descriptor blob sizing";
         return kErrArg;
@@ -409,6 +429,7 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
     d_csys_ = reinterpret_cast<CorrSystem*>(base + o_csys);
     d_chunks_ = reinterpret_cast<CorrChunk*>(base + o_chunks);
     d_entries_ = reinterpret_cast<FinalEntry*>(base + o_entries);
+    d_entries_w_ = reinterpret_cast<FinalEntry*>(base + o_entries_w);
     ECK(cudaDeviceSynchronize());
     stats_.phase_tiles = tiles.size();
     stats_.corr_chunks = chunks.size();
@@ -479,6 +500,25 @@ int Engine::enqueue(cudaStream_t st, std::string& err, cudaEvent_t* ev) {
     fl.tw = tw64_.as<double2>();
     ECK(launch_finalize(fl, st));
     ++launches;
+    if (weighted_) {
+        // the autocorrelation is quadratic in A: scaling A_v by sqrt(w_v) turns the same
+        // correlation pass into (1/NM) sum_v w_v C_v(t)
+        for (int i = 0; i < nitems_; ++i) {
+            if (!item_wsqrt_[i]) continue;
+            ECK(launch_scale_series(const_cast<void*>(amplitudes(i)), f32, item_wsqrt_[i], item_nv_[i],
+                                    (int)item_nf_[i], st));
+            ++launches;
+        }
+        ECK(launch_corr_accumulate(cl, st));
+        FinalLaunch fw = fl;
+        fw.entries = d_entries_w_;
+        int nw = 0;
+        for (int i = 0; i < nitems_; ++i)
+            if (item_wsqrt_[i]) nw += (int)item_nq_[i];
+        fw.nentries = nw;
+        ECK(launch_finalize(fw, st));
+        launches += 2;
+    }
     if (ev) ECK(cudaEventRecord(ev[3], st));
     stats_.launches = launches;
     stats_.phase_launches = phase_launches;

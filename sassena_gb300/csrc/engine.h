@@ -64,6 +64,12 @@ struct WorkItem {
     double2* d_fqt = nullptr;      // [nq][nf]
     double2* d_fq = nullptr;       // [nq]
     double2* d_fq2 = nullptr;      // [nq]
+    // optional (coherent): sqrt of a positive weight per sub-vector; the engine then also
+    // writes the weighted averages (1/NM) sum_v w_v C_v(t) into the *_w outputs
+    const double* d_wsqrt = nullptr;  // [nv]
+    double2* d_fqt_w = nullptr;
+    double2* d_fq_w = nullptr;
+    double2* d_fq2_w = nullptr;
 };
 
 struct EngineStats {
@@ -114,6 +120,9 @@ private:
     CorrSystem* d_csys_ = nullptr;
     CorrChunk* d_chunks_ = nullptr;
     FinalEntry* d_entries_ = nullptr;
+    FinalEntry* d_entries_w_ = nullptr;  // weighted outputs (same slots)
+    std::vector<const double*> item_wsqrt_;
+    bool weighted_ = false;
     int tw_lg_ = 0;
 };
 

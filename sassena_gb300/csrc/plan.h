@@ -1,0 +1,25 @@
+// Internal definition of the plan object, shared by the C ABI translation units.
+#pragma once
+
+#include <string>
+
+#include "../../include/sassena_gb300.h"
+#include "engine.h"
+
+namespace sassgpu {
+constexpr int kEvents = 12;
+}
+
+struct sass_plan {
+    sass_plan_desc d{};
+    sassgpu::SystemState sys;
+    sassgpu::Engine eng;
+    cudaStream_t st = nullptr;
+    bool own_stream = false;
+    std::string msg;
+    sass_timing timing{};
+    cudaEvent_t ev[sassgpu::kEvents] = {};
+    sassgpu::PhaseShape shape{0, 0, 0};
+    int split_atoms = 0;
+    sassgpu::DevBuf qv, cf, fqt, fq, fq2, amp_tmp;
+};

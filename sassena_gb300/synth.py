@@ -363,3 +363,24 @@ def batched_uneven(seed=4, nsys=64, na_range=(500, 50000), nf_range=(256, 4096),
                             sphere_directions(nm, seed * 1000 + i), scattering=scattering,
                             meta=dict(box=box, seed=seed)))
     return out
+
+
+def layered(seed=5, na=50000, nf=2048, box=80.0, period=8.0, amplitude=0.3, sigma=0.05, nq=100,
+            qmin=0.1, qmax=1.5, nm=64):
+    """Anisotropic layered system: density along z modulated as 1 + amplitude*cos(2 pi z/period)
+    (rejection sampling), uniform in x and y, Gaussian random walk; coherent H/C/N/O lengths."""
+    rng = np.random.default_rng(np.random.PCG64(seed))
+    z = np.empty(0)
+    while len(z) < na:
+        c = rng.uniform(0.0, box, 2 * na)
+        keep = rng.uniform(0.0, 1.0 + amplitude, 2 * na) < 1.0 + amplitude * np.cos(2 * math.pi * c / period)
+        z = np.concatenate([z, c[keep]])
+    r0 = np.stack([rng.uniform(0.0, box, na), rng.uniform(0.0, box, na), z[:na]], axis=1)
+    names = ["H", "C", "N", "O"]
+    cls = _types(rng, na, names, [50, 30, 10, 10])
+    coords = random_walk(rng, r0, nf, sigma)
+    shells = np.linspace(qmin, qmax, nq)
+    b = np.array([COHERENT_FM[n] for n in names])
+    return Workload("layered", coords, cls, names, np.tile(b, (nq, 1)), shells,
+                    sphere_directions(nm, seed + 1000), scattering="all",
+                    meta=dict(box=box, period=period, amplitude=amplitude, seed=seed))

@@ -1,0 +1,89 @@
+"""The learned control variate: network gradients against the FP64 oracle, GPU training,
+sphere quadrature, and what the trained network gains over plain Monte Carlo at an equal
+direction budget on an anisotropic (layered) sample, with the estimate staying unbiased."""
+import numpy as np
+import pytest
+
+import oracle.mlp_oracle as mo
+from sassena_gb300 import abi, cv, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def test_mlp_gradient_matches_oracle(native_lib):
+    net = abi.MLP(seed=3)
+    rng = np.random.default_rng(0)
+    x = rng.normal(size=(777, 4)).astype(np.float32)
+    t = rng.normal(size=777).astype(np.float32)
+    master, bf = net.params()
+    g, loss = net.gradient(x, t)
+    gref, lref = mo.gradient(bf, x, t)  # the GPU computes with the BF16 weights
+    assert abs(loss - lref) <= 1e-5 * abs(lref)
+    err = np.abs(g - gref).max() / np.abs(gref).max()
+    assert err <= 2e-5, err
+    # and the forward pass
+    y = net.predict(x)
+    yref, _ = mo.forward(bf, x)
+    assert np.abs(y - yref).max() <= 1e-5 * max(1.0, np.abs(yref).max())
+
+
+def test_mlp_training_fits_a_smooth_function(native_lib):
+    rng = np.random.default_rng(1)
+    u = synth.sphere_directions(20000, 5)
+    s = rng.uniform(-1, 1, 20000)
+    x = np.concatenate([u, s[:, None]], axis=1).astype(np.float32)
+    t = (np.sin(3 * u[:, 0]) + u[:, 2] ** 2 * (1 + s)).astype(np.float32)
+    net = abi.MLP(seed=2)
+    _, loss0 = net.gradient(x, t)
+    net.train(x, t, steps=1500, batch=2048, lr=3e-3)
+    _, loss1 = net.gradient(x, t)
+    assert loss1 < 0.02 * loss0, (loss0, loss1)
+
+
+def test_sphere_mean_matches_quadrature_in_numpy(native_lib):
+    net = abi.MLP(seed=4)
+    net.set_scaling(1.0, 0.5, 0.2, 0.7)
+    q = np.array([0.6, 1.0, 1.4])
+    got = net.sphere_mean(q, 4096)
+    _, bf = net.params()
+    P = 4096
+    i = np.arange(P) + 0.5
+    z = 1 - 2 * i / P
+    r = np.sqrt(1 - z * z)
+    phi = np.pi * (3 - np.sqrt(5)) * i
+    u = np.stack([r * np.cos(phi), r * np.sin(phi), z], 1)
+    for k, qq in enumerate(q):
+        x = np.concatenate([u, np.full((P, 1), (qq - 1.0) / 0.5)], 1)
+        y, _ = mo.forward(bf, x)
+        ref = np.mean(np.exp(y * 0.7 + 0.2))
+        assert abs(got[k] - ref) <= 1e-5 * ref
+
+
+def test_control_variate_gain_and_unbiased(native_lib):
+    # layered sample: strong anisotropy at q ~ 2 pi / period along z
+    w = synth.layered(seed=8, na=3000, nf=16, box=24.0, period=6.0, amplitude=0.6, nq=3,
+                      qmin=0.8, qmax=1.3, nm=8)
+    with abi.Plan(w.na, w.nf, len(w.class_names), "all", "autocorrelate", "fftw", "fp32") as p:
+        p.stage(w.coords)
+        p.set_classes(w.atom_class)
+        x, t, sc = cv.training_set(p, w, 12000, seed=1)
+        net, _ = cv.fit(x, t, sc, steps=1500, batch=2048, lr=2e-3)
+        # truth: dense quasi-uniform direction set
+        dense = synth.fibonacci_sphere(8192)
+        offs = np.array([0, 8192, 16384, 24576], np.uintp)
+        sv = (w.shells[:, None, None] * dense[None]).reshape(-1, 3)
+        truth, truth_fq, _ = p.compute(offs, sv, w.class_factors)
+        m = 32
+        e_cv, e_mc = [], []
+        for seed in range(24):
+            dirs = synth.sphere_directions(m, 100 + seed)
+            fqt_cv, fqt_mc, fq_cv, fq_mc, diag = abi.compute_cv(p, net, w.shells, dirs,
+                                                                w.class_factors, nquad=65536)
+            e_cv.append((fqt_cv[:, 0] - truth[:, 0]).real / truth[:, 0].real)
+            e_mc.append((fqt_mc[:, 0] - truth[:, 0]).real / truth[:, 0].real)
+    e_cv, e_mc = np.array(e_cv), np.array(e_mc)
+    rms_cv, rms_mc = np.sqrt(np.mean(e_cv ** 2)), np.sqrt(np.mean(e_mc ** 2))
+    assert rms_cv < rms_mc / 2.0, (rms_cv, rms_mc)
+    # unbiased: the mean error over seeds is within its standard error (3 sigma)
+    se = e_cv.std(axis=0) / np.sqrt(len(e_cv))
+    assert np.all(np.abs(e_cv.mean(axis=0)) <= 3 * se + 1e-4), (e_cv.mean(axis=0), se)
