@@ -384,3 +384,27 @@ def layered(seed=5, na=50000, nf=2048, box=80.0, period=8.0, amplitude=0.3, sigm
     return Workload("layered", coords, cls, names, np.tile(b, (nq, 1)), shells,
                     sphere_directions(nm, seed + 1000), scattering="all",
                     meta=dict(box=box, period=period, amplitude=amplitude, seed=seed))
+
+
+def aligned_rods(seed=6, nmol=300, per_mol=8, spacing=1.5, box=40.0, nf=32, sigma=2.0, nq=3,
+                 qmin=0.5, qmax=1.5, nm=32):
+    """Rigid rod-like molecules aligned along z (per_mol atoms, `spacing` apart) whose centres
+    diffuse fast (Gaussian steps sigma per frame): intermolecular interference averages out over
+    the frames while the intramolecular form factor |sum_k exp(i q_z k d)|^2 leaves a smooth,
+    strongly anisotropic orientational dependence."""
+    rng = np.random.default_rng(np.random.PCG64(seed))
+    centres = rng.uniform(0.0, box, (nmol, 3))
+    offs = np.zeros((per_mol, 3))
+    offs[:, 2] = (np.arange(per_mol) - 0.5 * (per_mol - 1)) * spacing
+    coords = np.empty((nf, nmol * per_mol, 3), dtype=np.float32)
+    c = centres.copy()
+    for t in range(nf):
+        coords[t] = (c[:, None, :] + offs[None, :, :]).reshape(-1, 3)
+        c += rng.standard_normal(c.shape) * sigma
+    na = nmol * per_mol
+    names = ["C"]
+    cls = np.zeros(na, np.int32)
+    shells = np.linspace(qmin, qmax, nq)
+    return Workload("aligned_rods", coords, cls, names, np.full((nq, 1), COHERENT_FM["C"]), shells,
+                    sphere_directions(nm, seed + 1000), scattering="all",
+                    meta=dict(box=box, spacing=spacing, per_mol=per_mol, seed=seed))
