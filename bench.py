@@ -275,21 +275,31 @@ def run_ours(args, dist):
     d2h = w.nq * (w.nf + 2) * 16
 
     # ---- roofline of the dominant kernel (phase sum) ------------------------------------
+    sch = plan.schedule()
     sfu, fma = abi.probe_pipes(dev)
     ph = statistics.median(phase_ms)
     achieved = terms / (ph * 1e-3)
-    peak_terms = sfu / 2.0
+    rec_only = sch["rec_tiles"] > 0 and sch["direct_tiles"] == 0
+    kernel = "phase_rec_kernel" if rec_only else "phase_sum_kernel"
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "phase_sum_coherent_sqt.json")
+    prof = os.path.join(ROOT, "profiles", "%s_%s.json" % (kernel, w.name))
     if os.path.exists(prof):
         with open(prof) as f:
             traffic = json.load(f).get("dram_bytes_per_launch")
-    roof = {"bound": "sfu", "achieved": achieved, "peak": peak_terms, "unit": "terms/s",
-            "frac": achieved / peak_terms, "traffic": traffic,
-            "kernel": "phase_sum_fp32_kernel", "kernel_ms": ph,
-            "peak_source": "measured live: sass_probe_pipes SFU %.4g results/s / 2 per term"
-                           % sfu,
-            "fp32_fma_per_s": fma, "fp32_frac": (achieved * 6) / fma}
+    if rec_only:
+        # per term at least one FMA per component (recurrence) and one FADD per component
+        # (accumulation) on the FP32 pipe: 4 lane operations
+        peak_terms = fma / 4.0
+        roof = {"bound": "fp32", "peak_source": "measured live: sass_probe_pipes FP32 %.4g "
+                "lane-ops/s / 4 per term (2 FMA recurrence + 2 FADD accumulate)" % fma,
+                "sfu_results_per_s": sfu}
+    else:
+        peak_terms = sfu / 2.0
+        roof = {"bound": "sfu", "peak_source": "measured live: sass_probe_pipes SFU %.4g "
+                "results/s / 2 per term" % sfu, "fp32_fma_per_s": fma}
+    roof.update({"achieved": achieved, "peak": peak_terms, "unit": "terms/s",
+                 "frac": achieved / peak_terms, "traffic": traffic, "kernel": kernel,
+                 "kernel_ms": ph, "schedule": sch})
     corr = statistics.median(corr_ms)
     corr_bytes = (w.nq * w.nm * w.nf * 16) + (w.nq * w.nf * 16)
     roof_corr = {"bound": "hbm", "kernel": "corr_fft_kernel+finalize", "ms": corr,
@@ -320,9 +330,11 @@ def run_ours(args, dist):
             p64.set_classes(w.atom_class)
             ref = p64.compute(sub_offs, sub_sv, sub_cf)
             t64 = p64.timing()
-        fp32_sub = plan.compute(sub_offs, sub_sv, sub_cf)
+        # error of the measured FP32 path itself: its full-workload output at those shells
+        full = plan.compute(offs, w.subvectors(), np.ascontiguousarray(w.class_factors))
+        err = (np.abs(full[0][idx] - ref[0]).max(axis=1) / np.abs(ref[0][:, 0])).max()
+        plan.compute(sub_offs, sub_sv, sub_cf)
         t32 = plan.timing()
-        err = (np.abs(fp32_sub[0] - ref[0]).max(axis=1) / np.abs(ref[0][:, 0])).max()
         sub_terms = w.na * w.nf * w.nm * ns
         plain_tps = sub_terms / (t64["total_ms"] * 1e-3)
         out["plain_fp64"] = {"value": plain_tps, "unit": UNIT, "shells_run": ns,
@@ -357,8 +369,10 @@ def run_batched(args, dist):
         tuned = sub.autotune(repeats=1)
     tune_s = time.perf_counter() - t0
     t0 = time.perf_counter()
+    rec = tuned["rec_shells_per_lane"] or -1  # the subset's choice: a width, or off
     b = abi.Batch(ws, precision="fp32", device=dev, stream=stream.cuda_stream)
     b.set_tile(tuned["q_per_lane"], tuned["warps"], tuned["atoms"], tuned["split_atoms"])
+    b.set_recurrence(rec)
     create_s = time.perf_counter() - t0
     for _ in range(max(3, args.warmup)):
         b.run()
@@ -377,6 +391,7 @@ def run_batched(args, dist):
     b.sync()
     ms = dist.max(e0.elapsed_time(e1) / args.steps)
     info = b.info()
+    sched = b.schedule()
     launches = b.timing()["kernel_launches"] * args.steps
     # end to end: stage every system from host memory, one run, copy all results back
     e2e = []
@@ -385,6 +400,7 @@ def run_batched(args, dist):
         t0 = time.perf_counter()
         with abi.Batch(ws, precision="fp32", device=dev, stream=stream.cuda_stream) as bb:
             bb.set_tile(tuned["q_per_lane"], tuned["warps"], tuned["atoms"], tuned["split_atoms"])
+            bb.set_recurrence(rec)
             bb.run()
             for k in range(len(ws)):
                 bb.results(k)
@@ -400,6 +416,7 @@ def run_batched(args, dist):
                       "na_range": [min(w.na for w in ws), max(w.na for w in ws)],
                       "nf_range": [min(w.nf for w in ws), max(w.nf for w in ws)],
                       "terms_per_step": terms, "phase_tiles": info["phase_tiles"],
+                      "schedule": sched,
                       "tile": tuned, "autotune_s": tune_s, "create_s": create_s,
                       "l2": "inputs larger than L2"},
            "e2e": {"value": terms / (min(e2e) * 1e-3) if e2e else None, "unit": UNIT,

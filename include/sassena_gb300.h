@@ -129,8 +129,9 @@ int sass_amplitudes(sass_plan* plan, size_t nsub, const double* subvectors,
 
 /* Time every instantiated phase-sum tile shape and atom-split size on this
  * workload (the arguments of sass_compute, host arrays) and keep the fastest for the
- * plan's later calls; the choice is cached per process by problem signature. The
- * chosen shape is returned through the (optional) out-pointers. */
+ * plan's later calls; the choice is cached per process by problem signature. FP32
+ * plans whose q-vectors share one direction set also try every shell-recurrence width
+ * (and none). The chosen shape is returned through the (optional) out-pointers. */
 int sass_autotune(sass_plan* plan, size_t nq, const size_t* sub_offsets, const double* subvectors,
                   const double* class_factors, int repeats, int* q_per_lane, int* warps, int* atoms,
                   int* split_atoms);
@@ -145,6 +146,27 @@ int sass_set_phase_tile(sass_plan* plan, int q_per_lane, int warps, int atoms, i
 
 /* Frame centre used by the FP32 form (frame-0 bounding-box midpoint). */
 int sass_frame_center(const sass_plan* plan, double* center3);
+
+/* Shell recurrence of the FP32 form. When every q-vector's sub-vectors are multiples of
+ * one direction set (the reference's "file" and "sphere" orientation types,
+ * abstract_vectors_scatter_device.cpp:112-130) and consecutive |q| lie on a line (linear
+ * scans), runs of at least 3 such shells are evaluated by a kernel that carries
+ * exp(i q_k u.r) from shell to shell with a three-term recurrence: two reduced sin/cos
+ * pairs per atom for up to `shells_per_lane` shells. 0 = automatic (default), -1 = off,
+ * else one of 4, 6, 8, 10, 12, 16. FP64 plans ignore it. */
+int sass_set_shell_recurrence(sass_plan* plan, int shells_per_lane);
+
+/* How the last sass_compute (or batch run) scheduled the phase sum. */
+typedef struct sass_schedule {
+    double terms;                  /* atom x sub-vector x frame terms */
+    uint64_t direct_tiles;         /* tiles of the direct phase-sum kernel */
+    uint64_t rec_tiles;            /* tiles of the shell-recurrence kernel */
+    uint64_t rec_shells;           /* q-vectors evaluated by the recurrence */
+    int rec_shells_per_lane;       /* 0: recurrence not used */
+    int q_per_lane, warps, atoms;  /* direct kernel tile shape */
+    int atom_splits;               /* largest atom-split count */
+} sass_schedule;
+int sass_plan_schedule(const sass_plan* plan, sass_schedule* out);
 
 /* ---- Batches: many independent systems in one graph-captured launch sequence ----
  * Each system has its own trajectory, atom classes, q-vectors and sub-vector sets of
@@ -184,6 +206,9 @@ int sass_batch_timing(const sass_batch* batch, sass_timing* out);
 /* Total atom.q.frame terms, phase-sum tiles and the tile shape of the batch. */
 int sass_batch_info(const sass_batch* batch, double* terms, uint64_t* phase_tiles, int* q_per_lane,
                     int* warps, int* atoms, int* split_atoms);
+/* Shell recurrence for the batch (as sass_set_shell_recurrence) and its schedule. */
+int sass_batch_set_shell_recurrence(sass_batch* batch, int shells_per_lane);
+int sass_batch_schedule(const sass_batch* batch, sass_schedule* out);
 const char* sass_batch_error(const sass_batch* batch);
 void sass_batch_destroy(sass_batch* batch);
 

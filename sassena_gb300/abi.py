@@ -35,6 +35,8 @@ EXPORTS = [
     "sass_mlp_create", "sass_mlp_destroy", "sass_mlp_error", "sass_mlp_param_count",
     "sass_mlp_set_scaling", "sass_mlp_get_params", "sass_mlp_set_params", "sass_mlp_gradient",
     "sass_mlp_train", "sass_mlp_predict", "sass_mlp_sphere_mean", "sass_compute_cv",
+    "sass_set_shell_recurrence", "sass_plan_schedule", "sass_batch_set_shell_recurrence",
+    "sass_batch_schedule",
 ]
 
 
@@ -65,6 +67,16 @@ class Timing(ctypes.Structure):
                 ("d2h_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
                 ("kernel_launches", ctypes.c_uint64), ("phase_launches", ctypes.c_uint64),
                 ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Schedule(ctypes.Structure):
+    _fields_ = [("terms", ctypes.c_double), ("direct_tiles", ctypes.c_uint64),
+                ("rec_tiles", ctypes.c_uint64), ("rec_shells", ctypes.c_uint64),
+                ("rec_shells_per_lane", ctypes.c_int), ("q_per_lane", ctypes.c_int),
+                ("warps", ctypes.c_int), ("atoms", ctypes.c_int), ("atom_splits", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -137,6 +149,10 @@ def load(path=LIB_PATH):
     L.sass_compute_cv.argtypes = [_vp, _vp, _sz, _vp, _sz, _vp, _vp, _sz, _vp, _vp, _vp, _vp, _vp]
     L.sass_correlate_noalloc.argtypes = [ctypes.c_int, _vp, _vp, _sz, _sz, _vp, ctypes.c_int, _vp,
                                          _vp, _vp]
+    L.sass_set_shell_recurrence.argtypes = [_vp, ctypes.c_int]
+    L.sass_plan_schedule.argtypes = [_vp, ctypes.POINTER(Schedule)]
+    L.sass_batch_set_shell_recurrence.argtypes = [_vp, ctypes.c_int]
+    L.sass_batch_schedule.argtypes = [_vp, ctypes.POINTER(Schedule)]
     _lib = L
     return L
 
@@ -206,6 +222,15 @@ class Plan:
     def set_tile(self, q_per_lane=0, warps=0, atoms=0, atom_splits=0):
         self._check(self.lib.sass_set_phase_tile(self._h, q_per_lane, warps, atoms, atom_splits))
 
+    def set_recurrence(self, shells_per_lane=0):
+        """Shell recurrence of the FP32 form: 0 automatic, -1 off, else 4/6/8/10/12/16."""
+        self._check(self.lib.sass_set_shell_recurrence(self._h, shells_per_lane))
+
+    def schedule(self):
+        s = Schedule()
+        self._check(self.lib.sass_plan_schedule(self._h, ctypes.byref(s)))
+        return s.as_dict()
+
     def compute(self, sub_offsets, subvectors, class_factors):
         """Host in/out: returns (fqt [nq, nf] complex, fq [nq] complex, fq2 [nq] complex)."""
         offs = np.ascontiguousarray(sub_offsets, dtype=np.uintp)
@@ -250,7 +275,9 @@ class Plan:
         out = [ctypes.c_int() for _ in range(4)]
         self._check(self.lib.sass_autotune(self._h, nq, _ptr(offs), _ptr(sv), _ptr(cf), repeats,
                                            *[ctypes.byref(o) for o in out]))
-        return dict(zip(("q_per_lane", "warps", "atoms", "split_atoms"), [o.value for o in out]))
+        r = dict(zip(("q_per_lane", "warps", "atoms", "split_atoms"), [o.value for o in out]))
+        r["rec_shells_per_lane"] = self.schedule()["rec_shells_per_lane"]
+        return r
 
     def center(self):
         c = np.zeros(3)
@@ -317,10 +344,19 @@ class Batch:
                                                  ctypes.byref(ms)))
         r = dict(zip(("q_per_lane", "warps", "atoms", "split_atoms"), [o.value for o in out]))
         r["ms"] = ms.value
+        r["rec_shells_per_lane"] = self.schedule()["rec_shells_per_lane"]
         return r
 
     def set_tile(self, q_per_lane=0, warps=0, atoms=0, split_atoms=0):
         self._check(self.lib.sass_batch_set_tile(self._h, q_per_lane, warps, atoms, split_atoms))
+
+    def set_recurrence(self, shells_per_lane=0):
+        self._check(self.lib.sass_batch_set_shell_recurrence(self._h, shells_per_lane))
+
+    def schedule(self):
+        s = Schedule()
+        self._check(self.lib.sass_batch_schedule(self._h, ctypes.byref(s)))
+        return s.as_dict()
 
     def run(self):
         self._check(self.lib.sass_batch_run(self._h))
@@ -451,15 +487,24 @@ def probe_pipes(device=0):
     return a.value, b.value
 
 
-def compute_workload(w, precision="fp64", method="fftw", device=0, tile=None):
-    """Run a synth.Workload through the C ABI; returns (fqt, fq, fq2)."""
+def compute_workload(w, precision="fp64", method="fftw", device=0, tile=None, recurrence=None,
+                     schedule=None):
+    """Run a synth.Workload through the C ABI; returns (fqt, fq, fq2).
+
+    recurrence: shells per lane of the FP32 shell recurrence (None: automatic, -1: off);
+    schedule: a dict that receives the plan's schedule of the call."""
     with Plan(w.na, w.nf, len(w.class_names), w.scattering, w.dsp, method, precision,
               device) as p:
         p.stage(w.coords)
         p.set_classes(w.atom_class)
         if tile:
             p.set_tile(*tile)
-        return p.compute(w.sub_offsets(), w.subvectors(), w.class_factors)
+        if recurrence is not None:
+            p.set_recurrence(recurrence)
+        out = p.compute(w.sub_offsets(), w.subvectors(), w.class_factors)
+        if schedule is not None:
+            schedule.update(p.schedule())
+        return out
 
 
 # ----------------------------------------------------------------------------------------

@@ -29,7 +29,10 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-
 CXX = os.environ.get("CXX", "g++")
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + INCLUDE, "-I" + HOST]
 
-CUDA_SOURCES = ["capi.cu", "engine.cu", "phase_sum.cu", "correlate.cu", "peaks.cu", "noalloc.cu", "mlp.cu", "cv.cu"]
+CUDA_SOURCES = [
+    "capi.cu", "engine.cu", "phase_sum.cu", "phase_rec.cu", "correlate.cu", "peaks.cu", "noalloc.cu", "mlp.cu",
+    "cv.cu",
+]
 HOST_SOURCES = []  # filled when the host layer exists (see host_sources())
 
 LIB = os.path.join(OUT, "libsassena_gb300.so")

@@ -66,9 +66,17 @@ EngineConfig engine_config(const sass_plan_desc& d) {
     return c;
 }
 
-// Process-wide autotuning cache: problem signature -> best (shape, split_atoms).
+// Process-wide autotuning cache: problem signature -> best configuration.
+struct TuneChoice {
+    PhaseShape shape{0, 0, 0};
+    int split_atoms = 0, rec_k = 0;
+};
 std::mutex g_tune_lock;
-std::map<std::string, std::pair<PhaseShape, int>> g_tune_cache;
+std::map<std::string, TuneChoice> g_tune_cache;
+
+// Product-set detection on host sub-vectors (copied from the device when needed).
+int product_of(std::string& m, const double* qv, bool on_device, const std::vector<size_t>& offs,
+               std::vector<double>& lam, int& base);
 
 }  // namespace
 
@@ -86,7 +94,9 @@ struct sass_batch {
     cudaGraphExec_t exec = nullptr;
     bool prepared = false;
     PhaseShape shape{0, 0, 0};
-    int split_atoms = 0;
+    int split_atoms = 0, rec_k = 0;
+    std::vector<std::vector<double>> lam;  // product structure per system (empty: none)
+    std::vector<int> lam_base;
     std::string msg;
     sass_timing timing{};
     cudaEvent_t ev[kEvents] = {};
@@ -158,39 +168,112 @@ int init_system(std::string& m, SystemState& s, const sass_plan_desc& d, int lg,
     return build_system_tables(s, st, m);
 }
 
-// Time the engine over candidate phase shapes and atom-split sizes; keep the best.
+int time_config(std::string& m, Engine& eng, const EngineConfig& c, const std::vector<WorkItem>& items,
+                cudaStream_t st, cudaEvent_t* ev, int repeats, double& ms) {
+    std::string err;
+    ms = -1;
+    if (eng.prepare(c, items, err) != SASS_OK) return SASS_OK;  // configuration not applicable
+    if (eng.enqueue(st, err) != SASS_OK) return SASS_OK;         // warm-up
+    CK(m, cudaEventRecord(ev[10], st));
+    for (int r = 0; r < repeats; ++r)
+        if (eng.enqueue(st, err) != SASS_OK) return set_msg(m, SASS_ERR_CUDA, "%s", err.c_str());
+    CK(m, cudaEventRecord(ev[11], st));
+    CK(m, cudaEventSynchronize(ev[11]));
+    int rc = read_err_word(m, eng.err_word(), st);
+    if (rc) return rc;
+    ms = ev_ms(ev[10], ev[11]) / std::max(repeats, 1);
+    return SASS_OK;
+}
+
+// Time the engine over candidate configurations and keep the best: first the shell
+// recurrence width (FP32 product sets: off and every instantiated width, automatic tile),
+// then the direct kernel's tile shapes x atom-split sizes with that width (only split
+// sizes when the recurrence covers every shell).
 int autotune_engine(std::string& m, Engine& eng, const EngineConfig& base, const std::vector<WorkItem>& items,
-                    cudaStream_t st, cudaEvent_t* ev, int repeats, PhaseShape& best_shape, int& best_split,
-                    double& best_ms) {
-    std::vector<PhaseShape> shapes = phase_shapes(base.precision);
-    std::vector<int> splits = {0, 2048, 8192};
+                    cudaStream_t st, cudaEvent_t* ev, int repeats, TuneChoice& best, double& best_ms) {
     best_ms = 1e300;
     bool any = false;
+    auto consider = [&](const EngineConfig& c) -> int {
+        double ms = 0;
+        int rc = time_config(m, eng, c, items, st, ev, repeats, ms);
+        if (rc) return rc;
+        if (ms >= 0 && ms < best_ms) {
+            best_ms = ms;
+            best.shape = c.shape;
+            best.split_atoms = c.split_atoms;
+            best.rec_k = c.rec_k;
+            any = true;
+        }
+        return SASS_OK;
+    };
+    bool product = false;
+    for (const WorkItem& it : items) product = product || !it.lam.empty();
+    int rec_k = -1;
+    bool all_rec = false;
+    if (base.precision == PREC_FP32 && product) {
+        std::vector<int> ks = {-1};
+        for (int k : rec_shell_counts()) ks.push_back(k);
+        for (int k : ks) {
+            EngineConfig c = base;
+            c.rec_k = k;
+            int rc = consider(c);
+            if (rc) return rc;
+        }
+        rec_k = best.rec_k;
+        if (rec_k > 0) {
+            EngineConfig c = base;
+            c.rec_k = rec_k;
+            std::string err;
+            if (eng.prepare(c, items, err) == SASS_OK) all_rec = eng.stats().phase_tiles == 0;
+        }
+    }
+    std::vector<PhaseShape> shapes = all_rec ? std::vector<PhaseShape>{PhaseShape{0, 0, 0}} : phase_shapes(base.precision);
     for (const PhaseShape& sh : shapes)
-        for (int sp : splits) {
+        for (int sp : {0, 2048, 8192}) {
             EngineConfig c = base;
             c.shape = sh;
             c.split_atoms = sp;
-            std::string err;
-            if (eng.prepare(c, items, err) != SASS_OK) continue;
-            if (eng.enqueue(st, err) != SASS_OK) continue;  // warm-up
-            CK(m, cudaEventRecord(ev[10], st));
-            for (int r = 0; r < repeats; ++r)
-                if (eng.enqueue(st, err) != SASS_OK) return set_msg(m, SASS_ERR_CUDA, "%s", err.c_str());
-            CK(m, cudaEventRecord(ev[11], st));
-            CK(m, cudaEventSynchronize(ev[11]));
-            int rc = read_err_word(m, eng.err_word(), st);
+            c.rec_k = rec_k;
+            int rc = consider(c);
             if (rc) return rc;
-            double ms = ev_ms(ev[10], ev[11]) / std::max(repeats, 1);
-            if (ms < best_ms) {
-                best_ms = ms;
-                best_shape = sh;
-                best_split = sp;
-                any = true;
-            }
         }
     if (!any) return set_msg(m, SASS_ERR_UNSUPPORTED, "no tile shape could be prepared");
+    // leave the engine prepared with the choice, so that its schedule describes it
+    EngineConfig c = base;
+    c.shape = best.shape;
+    c.split_atoms = best.split_atoms;
+    c.rec_k = best.rec_k;
+    std::string err;
+    if (eng.prepare(c, items, err) != SASS_OK) return set_msg(m, SASS_ERR_CUDA, "%s", err.c_str());
     return SASS_OK;
+}
+
+int product_of(std::string& m, const double* qv, bool on_device, const std::vector<size_t>& offs,
+               std::vector<double>& lam, int& base) {
+    lam.clear();
+    base = -1;
+    const double* h = qv;
+    std::vector<double> copy;
+    if (on_device) {
+        copy.resize(offs.back() * 3);
+        CK(m, cudaMemcpy(copy.data(), qv, copy.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        h = copy.data();
+    }
+    detect_product(h, offs, lam, base);
+    return SASS_OK;
+}
+
+void fill_schedule(const EngineStats& s, sass_schedule* out) {
+    memset(out, 0, sizeof(*out));
+    out->terms = s.terms;
+    out->direct_tiles = s.phase_tiles;
+    out->rec_tiles = s.rec_tiles;
+    out->rec_shells = s.rec_shells;
+    out->rec_shells_per_lane = s.rec_tiles ? s.rec_k : 0;
+    out->q_per_lane = s.shape.q_per_lane;
+    out->warps = s.shape.warps;
+    out->atoms = s.shape.atoms;
+    out->atom_splits = s.max_split;
 }
 
 std::string signature(const sass_plan_desc& d, const std::vector<WorkItem>& items) {
@@ -300,6 +383,22 @@ int sass_frame_center(const sass_plan* p, double* c) {
     return SASS_OK;
 }
 
+static bool rec_width_ok(int k) { return k == 0 || k == -1 || rec_shells_supported(k); }
+
+int sass_set_shell_recurrence(sass_plan* p, int shells_per_lane) {
+    if (!p) return SASS_ERR_ARG;
+    if (!rec_width_ok(shells_per_lane))
+        return set_msg(p->msg, SASS_ERR_UNSUPPORTED, "shell recurrence width %d not instantiated", shells_per_lane);
+    p->rec_k = shells_per_lane;
+    return SASS_OK;
+}
+
+int sass_plan_schedule(const sass_plan* p, sass_schedule* out) {
+    if (!p || !out) return SASS_ERR_ARG;
+    fill_schedule(p->eng.stats(), out);
+    return SASS_OK;
+}
+
 static int check_ready(sass_plan* p) {
     if (!p->sys.staged) return set_msg(p->msg, SASS_ERR_STATE, "sass_stage_frames has not been called");
     if (!p->sys.classes_set) return set_msg(p->msg, SASS_ERR_STATE, "sass_set_atom_classes has not been called");
@@ -368,6 +467,9 @@ int sass_compute(sass_plan* p, size_t nq, const size_t* offs, const double* subv
     EngineConfig cfg = engine_config(p->d);
     cfg.shape = p->shape;
     cfg.split_atoms = p->split_atoms;
+    cfg.rec_k = p->rec_k;
+    const bool want_rec = p->d.precision == SASS_PRECISION_FP32 && p->d.scattering == SASS_SCATTERING_ALL &&
+                          p->rec_k >= 0;
     size_t i = 0;
     while (i < nq) {
         size_t j = i + 1;
@@ -381,6 +483,11 @@ int sass_compute(sass_plan* p, size_t nq, const size_t* offs, const double* subv
         it.sys = &p->sys;
         for (size_t k = i; k <= j; ++k) it.offs.push_back(offs[k] - offs[i]);
         it.d_qv = d_qv + 3 * offs[i];
+        if (want_rec) {
+            rc = product_of(p->msg, io_on_device ? d_qv + 3 * offs[i] : subvectors + 3 * offs[i], io_on_device != 0,
+                            it.offs, it.lam, it.lam_base);
+            if (rc) return rc;
+        }
         it.d_cf = d_cf + nclass * i;
         it.d_fqt = d_fqt + i * nf;
         it.d_fq = d_fq + i;
@@ -444,32 +551,35 @@ int sass_autotune(sass_plan* p, size_t nq, const size_t* offs, const double* sub
     items[0].d_fqt = p->fqt.as<double2>();
     items[0].d_fq = p->fq.as<double2>();
     items[0].d_fq2 = p->fq2.as<double2>();
-    PhaseShape best;
-    int split = 0;
+    if (p->d.precision == SASS_PRECISION_FP32) {
+        rc = product_of(p->msg, subvectors, false, items[0].offs, items[0].lam, items[0].lam_base);
+        if (rc) return rc;
+    }
+    TuneChoice best;
     double ms = 0;
-    const std::string key = signature(p->d, items);
+    std::string key = signature(p->d, items);
+    key += items[0].lam.empty() ? "|general" : "|product";
     {
         std::lock_guard<std::mutex> g(g_tune_lock);
         auto it = g_tune_cache.find(key);
         if (it != g_tune_cache.end()) {
-            best = it->second.first;
-            split = it->second.second;
+            best = it->second;
             ms = -1;
         }
     }
     if (ms == 0) {
-        rc = autotune_engine(p->msg, p->eng, engine_config(p->d), items, p->st, p->ev, std::max(1, repeats), best,
-                             split, ms);
+        rc = autotune_engine(p->msg, p->eng, engine_config(p->d), items, p->st, p->ev, std::max(1, repeats), best, ms);
         if (rc) return rc;
         std::lock_guard<std::mutex> g(g_tune_lock);
-        g_tune_cache[key] = {best, split};
+        g_tune_cache[key] = best;
     }
-    p->shape = best;
-    p->split_atoms = split;
-    if (q_per_lane) *q_per_lane = best.q_per_lane;
-    if (warps) *warps = best.warps;
-    if (atoms) *atoms = best.atoms;
-    if (split_atoms) *split_atoms = split;
+    p->shape = best.shape;
+    p->split_atoms = best.split_atoms;
+    p->rec_k = best.rec_k;
+    if (q_per_lane) *q_per_lane = best.shape.q_per_lane;
+    if (warps) *warps = best.shape.warps;
+    if (atoms) *atoms = best.shape.atoms;
+    if (split_atoms) *split_atoms = best.split_atoms;
     p->msg.clear();
     return SASS_OK;
 }
@@ -519,6 +629,7 @@ int sass_amplitudes(sass_plan* p, size_t nsub, const double* subvectors, const i
     cfg.dsp = SASS_DSP_PLAIN;  // the amplitudes are read before the store
     cfg.shape = p->shape;
     cfg.split_atoms = p->split_atoms;
+    cfg.rec_k = -1;
     rc = p->eng.prepare(cfg, items, p->msg);
     if (rc) return rc;
     rc = p->eng.enqueue(p->st, p->msg, p->ev);
@@ -603,6 +714,10 @@ int sass_batch_create(const sass_plan_desc* desc, size_t nsystems, const sass_sy
         rc = check_offsets(b->msg, s.nq, s.sub_offsets);
         if (rc) return rc;
         b->offs.emplace_back(s.sub_offsets, s.sub_offsets + s.nq + 1);
+        b->lam.emplace_back();
+        b->lam_base.push_back(-1);
+        if (b->d.precision == SASS_PRECISION_FP32 && b->d.scattering == SASS_SCATTERING_ALL)
+            detect_product(s.subvectors, b->offs.back(), b->lam.back(), b->lam_base.back());
         b->nq.push_back(s.nq);
         b->nv.push_back(s.sub_offsets[s.nq]);
         b->qv_off.push_back(qv_n);
@@ -645,6 +760,8 @@ static std::vector<WorkItem> batch_items(sass_batch* b) {
         it.sys = b->systems[i];
         it.offs = b->offs[i];
         it.d_qv = b->qv.as<double>() + b->qv_off[i];
+        it.lam = b->lam[i];
+        it.lam_base = b->lam_base[i];
         it.d_cf = b->cf.as<double>() + b->cf_off[i];
         it.d_fqt = reinterpret_cast<double2*>(b->out.as<double>() + b->fqt_off[i]);
         it.d_fq = reinterpret_cast<double2*>(b->out.as<double>() + b->fq_off[i]);
@@ -667,20 +784,19 @@ int sass_batch_autotune(sass_batch* b, int repeats, int* q_per_lane, int* warps,
         return set_msg(b->msg, SASS_ERR_STATE, "autotuning applies to the coherent phase sum");
     CK(b->msg, cudaSetDevice(b->d.device));
     std::vector<WorkItem> items = batch_items(b);
-    PhaseShape best;
-    int split = 0;
+    TuneChoice best;
     double ms = 0;
-    int rc = autotune_engine(b->msg, b->eng, engine_config(b->d), items, b->st, b->ev, std::max(1, repeats), best,
-                             split, ms);
+    int rc = autotune_engine(b->msg, b->eng, engine_config(b->d), items, b->st, b->ev, std::max(1, repeats), best, ms);
     if (rc) return rc;
-    b->shape = best;
-    b->split_atoms = split;
+    b->shape = best.shape;
+    b->split_atoms = best.split_atoms;
+    b->rec_k = best.rec_k;
     b->prepared = false;
     drop_graph(b);
-    if (q_per_lane) *q_per_lane = best.q_per_lane;
-    if (warps) *warps = best.warps;
-    if (atoms) *atoms = best.atoms;
-    if (split_atoms) *split_atoms = split;
+    if (q_per_lane) *q_per_lane = best.shape.q_per_lane;
+    if (warps) *warps = best.shape.warps;
+    if (atoms) *atoms = best.shape.atoms;
+    if (split_atoms) *split_atoms = best.split_atoms;
     if (best_ms) *best_ms = ms;
     b->msg.clear();
     return SASS_OK;
@@ -708,6 +824,7 @@ int sass_batch_run(sass_batch* b) {
         EngineConfig cfg = engine_config(b->d);
         cfg.shape = b->shape;
         cfg.split_atoms = b->split_atoms;
+        cfg.rec_k = b->rec_k;
         std::vector<WorkItem> items = batch_items(b);
         int rc = b->eng.prepare(cfg, items, b->msg);
         if (rc) return rc;
@@ -770,6 +887,22 @@ int sass_batch_info(const sass_batch* b, double* terms, uint64_t* phase_tiles, i
     if (warps) *warps = s.shape.warps;
     if (atoms) *atoms = s.shape.atoms;
     if (split_atoms) *split_atoms = s.split_atoms;
+    return SASS_OK;
+}
+
+int sass_batch_set_shell_recurrence(sass_batch* b, int shells_per_lane) {
+    if (!b) return SASS_ERR_ARG;
+    if (!rec_width_ok(shells_per_lane))
+        return set_msg(b->msg, SASS_ERR_UNSUPPORTED, "shell recurrence width %d not instantiated", shells_per_lane);
+    b->rec_k = shells_per_lane;
+    b->prepared = false;
+    drop_graph(b);
+    return SASS_OK;
+}
+
+int sass_batch_schedule(const sass_batch* b, sass_schedule* out) {
+    if (!b || !out) return SASS_ERR_ARG;
+    fill_schedule(b->eng.stats(), out);
     return SASS_OK;
 }
 

@@ -139,6 +139,7 @@ int stage_system(SystemState& s, const float* coords, bool on_device, int precis
                      s.xyz.as<float4>(), st));
     ECK(cudaStreamSynchronize(st));
     s.staged = true;
+    s.rec_valid = false;
     return kOk;
 }
 
@@ -159,12 +160,139 @@ int set_system_classes(SystemState& s, const int32_t* cls, bool on_device, cudaS
     ECK(s.cls.ensure(s.na_pad * sizeof(int32_t)));
     ECK(cudaMemcpyAsync(s.cls.p, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     ECK(cudaStreamSynchronize(st));
+    s.h_cls.assign(h.begin(), h.begin() + s.na);
     s.classes_set = true;
+    s.rec_valid = false;
     return kOk;
 }
 
+bool detect_product(const double* qv, const std::vector<size_t>& offs, std::vector<double>& lam, int& base) {
+    lam.clear();
+    base = -1;
+    const size_t nq = offs.size() - 1;
+    if (nq == 0 || !qv) return false;
+    const size_t nd = offs[1] - offs[0];
+    for (size_t s = 0; s < nq; ++s)
+        if (offs[s + 1] - offs[s] != nd) return false;
+    // base: the shell with the largest sub-vector (least relative rounding)
+    double best = 0;
+    for (size_t s = 0; s < nq; ++s)
+        for (size_t d = 0; d < nd; ++d) {
+            const double* v = qv + 3 * (offs[s] + d);
+            const double n2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+            if (n2 > best) {
+                best = n2;
+                base = (int)s;
+            }
+        }
+    if (base < 0 || !(best > 0) || !std::isfinite(best)) return false;
+    const double* u = qv + 3 * offs[base];
+    double uu = 0;
+    for (size_t d = 0; d < nd; ++d) uu += u[3 * d] * u[3 * d] + u[3 * d + 1] * u[3 * d + 1] + u[3 * d + 2] * u[3 * d + 2];
+    lam.assign(nq, 0.0);
+    for (size_t s = 0; s < nq; ++s) {
+        const double* v = qv + 3 * offs[s];
+        double uv = 0, vmax = 0;
+        for (size_t d = 0; d < 3 * nd; ++d) uv += u[d] * v[d];
+        const double l = (int)s == base ? 1.0 : uv / uu;
+        for (size_t d = 0; d < nd; ++d) {
+            const double* w = v + 3 * d;
+            vmax = std::max(vmax, std::sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]));
+        }
+        const double tol = 1e-12 * std::max(vmax, std::fabs(l) * std::sqrt(best));
+        for (size_t d = 0; d < 3 * nd; ++d)
+            if (!(std::fabs(v[d] - l * u[d]) <= tol)) {
+                lam.clear();
+                base = -1;
+                return false;
+            }
+        lam[s] = l;
+    }
+    return true;
+}
+
+std::vector<std::pair<int, int>> arithmetic_runs(const std::vector<double>& lam, int min_len) {
+    std::vector<std::pair<int, int>> out;
+    const int n = (int)lam.size();
+    auto on_line = [&](int a, int e) {  // shells [a, e] on the line through a and e
+        const double step = (lam[e] - lam[a]) / (double)(e - a);
+        double scale = 0;
+        for (int k = a; k <= e; ++k) scale = std::max(scale, std::fabs(lam[k]));
+        for (int k = a + 1; k < e; ++k)
+            if (!(std::fabs(lam[k] - (lam[a] + (double)(k - a) * step)) <= 2.5e-7 * scale)) return false;
+        return std::isfinite(step);
+    };
+    int a = 0;
+    while (a < n) {
+        int e = a + 1;
+        while (e < n && on_line(a, e)) ++e;
+        if (e - a >= min_len) out.emplace_back(a, e);
+        a = (e - a >= min_len) ? e : a + 1;
+    }
+    return out;
+}
+
+namespace {
+
+// Per-lane cost of a group of K shells, in units of one recurrence step (2 FMA + 2 FADD):
+// K steps plus the per-atom dot product, two reduced sin/cos pairs and the seed rotation.
+double rec_group_cost(int K) { return K + 7.0; }
+
+int choose_rec_k(const std::vector<std::vector<std::pair<int, int>>>& runs) {
+    int best = 0;
+    double best_cost = 1e300;
+    for (int K : rec_shell_counts()) {
+        double c = 0;
+        for (const auto& r : runs)
+            for (const auto& ae : r) c += std::ceil((double)(ae.second - ae.first) / K) * rec_group_cost(K);
+        if (c < best_cost) {
+            best_cost = c;
+            best = K;
+        }
+    }
+    return best;
+}
+
+// Class-sorted coordinates for the recurrence kernel: class segments padded to 32 atoms,
+// w = 1 / 0 in float4.w, rows padded to the 128-atom stage.
+int ensure_rec_layout(SystemState& s, std::string& err) {
+    if (s.rec_valid) return kOk;
+    if (s.h_cls.size() != s.na) {
+        err = "atom classes missing";
+        return kErrArg;
+    }
+    std::vector<std::vector<int>> members(s.nclass);
+    for (size_t j = 0; j < s.na; ++j) members[s.h_cls[j]].push_back((int)j);
+    std::vector<int> map, bcls;
+    int last = 0;
+    for (size_t c = 0; c < s.nclass; ++c) {
+        if (members[c].empty()) continue;
+        for (int j : members[c]) map.push_back(j);
+        while (map.size() % 32) map.push_back(-1);
+        bcls.resize(map.size() / 32, (int)c);
+        last = (int)c;
+    }
+    while (map.size() % 128 || map.empty()) map.push_back(-1);
+    bcls.resize(map.size() / 32, last);
+    s.na_rec = map.size();
+    DevBuf d_map;
+    ECK(d_map.ensure(map.size() * sizeof(int)));
+    ECK(cudaMemcpy(d_map.p, map.data(), map.size() * sizeof(int), cudaMemcpyHostToDevice));
+    ECK(s.block_class.ensure(bcls.size() * sizeof(int)));
+    ECK(cudaMemcpy(s.block_class.p, bcls.data(), bcls.size() * sizeof(int), cudaMemcpyHostToDevice));
+    ECK(s.xyz_rec.ensure(s.nf * s.na_rec * sizeof(float4)));
+    ECK(launch_permute_stage(s.xyz.as<float4>(), (int)s.na_pad, d_map.as<int>(), (int)s.na_rec, (int)s.nf,
+                             s.xyz_rec.as<float4>(), 0));
+    ECK(cudaDeviceSynchronize());
+    s.rec_valid = true;
+    return kOk;
+}
+
+}  // namespace
+
 void Engine::release() {
-    DevBuf* bufs[] = {&blob_, &bfac_, &amp_, &part_, &ppart_, &apart_, &a2part_, &counter_, &err_, &tw64_, &tw32_};
+    DevBuf* bufs[] = {&blob_,    &bfac_, &amp_, &part_,  &ppart_, &apart_,
+                      &a2part_, &counter_, &err_, &tw64_, &tw32_, &rec_bfac_};
     for (DevBuf* b : bufs) b->release();
     hblob_.release();
 }
@@ -200,22 +328,81 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
     }
     stats_.shape = shape;
 
+    // ---- shell-recurrence groups (FP32 form; shells along one direction set) ---------------------
+    std::vector<std::vector<char>> rec_on(items.size());
+    std::vector<RecGroup> rgroups;
+    std::vector<int> item_g0(items.size(), 0), item_ng(items.size(), 0), item_nd(items.size(), 0);
+    rec_k_ = 0;
+    if (f32 && coherent && cfg.rec_k >= 0) {
+        std::vector<std::vector<std::pair<int, int>>> runs(items.size());
+        bool any = false;
+        for (size_t i = 0; i < items.size(); ++i) {
+            const WorkItem& it = items[i];
+            if (it.lam.size() + 1 != it.offs.size() || it.lam_base < 0 || it.sys->nclass > (size_t)kRecMaxClass)
+                continue;
+            runs[i] = arithmetic_runs(it.lam, 3);
+            any = any || !runs[i].empty();
+        }
+        if (any) {
+            rec_k_ = cfg.rec_k > 0 ? cfg.rec_k : choose_rec_k(runs);
+            if (!rec_shells_supported(rec_k_)) {
+                err = "recurrence shell count " + std::to_string(rec_k_) + " not instantiated";
+                return kErrUnsupported;
+            }
+        }
+        for (size_t i = 0; rec_k_ && i < items.size(); ++i) {
+            if (runs[i].empty()) continue;
+            const WorkItem& it = items[i];
+            int rc = ensure_rec_layout(*it.sys, err);
+            if (rc) return rc;
+            rec_on[i].assign(it.offs.size() - 1, 0);
+            item_g0[i] = (int)rgroups.size();
+            item_nd[i] = (int)(it.offs[1] - it.offs[0]);
+            for (const auto& ae : runs[i]) {
+                const int n = ae.second - ae.first, ng = (n + rec_k_ - 1) / rec_k_;
+                int s0 = ae.first;
+                for (int g = 0; g < ng; ++g) {  // near-equal groups of at most K shells
+                    const int ks = n / ng + (g < n % ng ? 1 : 0);
+                    RecGroup rg{};
+                    rg.system = (int)i;
+                    rg.s0 = s0;
+                    rg.ks = ks;
+                    rg.lam0 = it.lam[s0];
+                    rg.dlam = ks > 1 ? (it.lam[s0 + ks - 1] - it.lam[s0]) / (double)(ks - 1) : 0.0;
+                    rgroups.push_back(rg);
+                    for (int k = 0; k < ks; ++k) rec_on[i][s0 + k] = 1;
+                    s0 += ks;
+                    stats_.rec_shells += ks;
+                }
+            }
+            item_ng[i] = (int)rgroups.size() - item_g0[i];
+        }
+    }
+    auto is_rec = [&](size_t i, size_t sh) { return !rec_on[i].empty() && rec_on[i][sh]; };
+    stats_.rec_k = rec_k_;
+    stats_.rec_groups = rgroups.size();
+
     // atom splits: enough tiles for the persistent grid to balance
     nsplit_.assign(items.size(), 1);
     size_t base_tiles = 0;
-    for (const WorkItem& it : items) {
+    for (size_t i = 0; i < items.size(); ++i) {
+        const WorkItem& it = items[i];
         size_t groups = 0;
         for (size_t s = 0; s + 1 < it.offs.size(); ++s)
-            groups += (it.offs[s + 1] - it.offs[s] + 32 * shape.q_per_lane - 1) / (32 * shape.q_per_lane);
+            if (!is_rec(i, s))
+                groups += (it.offs[s + 1] - it.offs[s] + 32 * shape.q_per_lane - 1) / (32 * shape.q_per_lane);
         base_tiles += groups * ((it.sys->nf + shape.warps - 1) / shape.warps);
+        if (item_ng[i]) base_tiles += ((size_t)item_ng[i] * item_nd[i] + 31) / 32 * ((it.sys->nf + 7) / 8);
     }
     const size_t target = (size_t)sms * 8;
     for (size_t i = 0; i < items.size(); ++i) {
-        const int max_split = (int)(items[i].sys->na_pad / shape.atoms);
+        int max_split = (int)(items[i].sys->na_pad / shape.atoms);
+        if (item_ng[i]) max_split = std::min(max_split, (int)(items[i].sys->na_rec / 128));
         int ns = 1;
         if (cfg.split_atoms > 0) ns = (int)((items[i].sys->na_pad + cfg.split_atoms - 1) / cfg.split_atoms);
         else if (base_tiles < target) ns = (int)((target + base_tiles - 1) / std::max<size_t>(base_tiles, 1));
         nsplit_[i] = std::max(1, std::min(ns, max_split));
+        stats_.max_split = std::max(stats_.max_split, nsplit_[i]);
     }
     stats_.split_atoms = cfg.split_atoms;
 
@@ -286,9 +473,10 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
                 p.out_f32 = f32 ? reinterpret_cast<float2*>(amp) : nullptr;
             }
             const int per = 32 * shape.q_per_lane;
-            const int tiles_atoms = (int)(s.na_pad / shape.atoms);
-            const int split_len = ((tiles_atoms + nsplit_[i] - 1) / nsplit_[i]) * shape.atoms;
-            for (size_t sh = 0; sh < nq; ++sh)
+            // balanced split of the stages: no slice is empty since nsplit <= stages
+            const long long nst = (long long)(s.na_pad / shape.atoms), ns = nsplit_[i];
+            for (size_t sh = 0; sh < nq; ++sh) {
+                if (is_rec(i, sh)) continue;
                 for (size_t v = it.offs[sh]; v < it.offs[sh + 1]; v += per)
                     for (size_t f0 = 0; f0 < s.nf; f0 += shape.warps)
                         for (int sp = 0; sp < nsplit_[i]; ++sp) {
@@ -298,11 +486,12 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
                             t.v0 = (int)v;
                             t.nv = (int)std::min<size_t>(per, it.offs[sh + 1] - v);
                             t.f0 = (int)f0;
-                            t.j_begin = sp * split_len;
-                            t.j_end = std::min((int)s.na_pad, (sp + 1) * split_len);
+                            t.j_begin = (int)(sp * nst / ns) * shape.atoms;
+                            t.j_end = (int)((sp + 1) * nst / ns) * shape.atoms;
                             t.split = sp;
-                            if (t.j_end > t.j_begin) tiles.push_back(t);
+                            tiles.push_back(t);
                         }
+            }
         }
         CorrSystem& c = csys[i];
         c.A = amp;
@@ -328,6 +517,53 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
     });
     ntiles_ = (int)tiles.size();
     nphase_systems_ = (int)items.size();
+
+    // recurrence tiles: 32 (group, direction) pairs x 8 frames x atom slice
+    std::vector<RecSystem> rsys(items.size());
+    std::vector<RecTileDesc> rtiles;
+    for (size_t i = 0; i < items.size(); ++i) {
+        if (!item_ng[i]) continue;
+        const WorkItem& it = items[i];
+        SystemState& s = *it.sys;
+        RecSystem& r = rsys[i];
+        r.xyzw = s.xyz_rec.as<float4>();
+        r.block_class = s.block_class.as<int>();
+        r.cf = it.d_cf;
+        r.dirs = it.d_qv + 3 * it.offs[it.lam_base];
+        r.out = psys[i].out;
+        r.out_f32 = psys[i].out_f32;
+        r.split_stride = psys[i].split_stride;
+        r.na_rec = (int)s.na_rec;
+        r.nf = (int)s.nf;
+        r.nd = item_nd[i];
+        r.nclass = (int)s.nclass;
+        r.g_begin = item_g0[i];
+        const int pairs = item_ng[i] * item_nd[i];
+        const long long nst = (long long)(s.na_rec / 128), ns = nsplit_[i];
+        for (int p0 = 0; p0 < pairs; p0 += 32)
+            for (size_t f0 = 0; f0 < s.nf; f0 += 8)
+                for (int sp = 0; sp < nsplit_[i]; ++sp) {
+                    RecTileDesc t{};
+                    t.system = (int)i;
+                    t.p0 = p0;
+                    t.np = std::min(32, pairs - p0);
+                    t.f0 = (int)f0;
+                    t.j_begin = (int)(sp * nst / ns) * 128;
+                    t.j_end = (int)((sp + 1) * nst / ns) * 128;
+                    t.split = sp;
+                    rtiles.push_back(t);
+                }
+    }
+    std::stable_sort(rtiles.begin(), rtiles.end(), [&](const RecTileDesc& a, const RecTileDesc& b) {
+        auto cost = [&](const RecTileDesc& t) {
+            long long fr = std::min<long long>(8, (long long)rsys[t.system].nf - t.f0);
+            return (long long)(t.j_end - t.j_begin) * fr;
+        };
+        return cost(a) > cost(b);
+    });
+    nrec_tiles_ = (int)rtiles.size();
+    nrec_groups_ = (int)rgroups.size();
+    if (nrec_groups_) ECK(rec_bfac_.ensure((size_t)nrec_groups_ * kRecMaxClass * rec_k_ * sizeof(float)));
 
     // ---- correlation chunks and finalisation entries ------------------------------------------
     std::vector<CorrChunk> chunks;
@@ -392,7 +628,7 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
     ECK(ppart_.ensure(poff * sizeof(double)));
     ECK(apart_.ensure(slot * sizeof(double2)));
     ECK(a2part_.ensure(slot * sizeof(double)));
-    ECK(counter_.ensure(sizeof(unsigned)));
+    ECK(counter_.ensure(2 * sizeof(unsigned)));
     ECK(err_.ensure(sizeof(unsigned)));
 
     // shared twiddle table at the largest length
@@ -409,6 +645,7 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
     std::vector<size_t> shell_off(items.size());
     for (size_t i = 0; i < items.size(); ++i) shell_off[i] = push(blob, shell_v[i]);
     size_t o_psys = push(blob, psys), o_tiles = push(blob, tiles);
+    size_t o_rsys = push(blob, rsys), o_rgroups = push(blob, rgroups), o_rtiles = push(blob, rtiles);
     // CorrSystem.shell_v points into the blob: patch with the final device address
     ECK(blob_.ensure(blob.size() + 4096 + csys.size() * sizeof(CorrSystem) + chunks.size() * sizeof(CorrChunk) +
                      (entries.size() + entries_w.size()) * sizeof(FinalEntry) + 4096));
@@ -426,12 +663,16 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
     unsigned char* base = blob_.as<unsigned char>();
     d_psys_ = reinterpret_cast<PhaseSystem*>(base + o_psys);
     d_tiles_ = reinterpret_cast<PhaseTileDesc*>(base + o_tiles);
+    d_rsys_ = reinterpret_cast<RecSystem*>(base + o_rsys);
+    d_rgroups_ = reinterpret_cast<RecGroup*>(base + o_rgroups);
+    d_rtiles_ = reinterpret_cast<RecTileDesc*>(base + o_rtiles);
     d_csys_ = reinterpret_cast<CorrSystem*>(base + o_csys);
     d_chunks_ = reinterpret_cast<CorrChunk*>(base + o_chunks);
     d_entries_ = reinterpret_cast<FinalEntry*>(base + o_entries);
     d_entries_w_ = reinterpret_cast<FinalEntry*>(base + o_entries_w);
     ECK(cudaDeviceSynchronize());
     stats_.phase_tiles = tiles.size();
+    stats_.rec_tiles = rtiles.size();
     stats_.corr_chunks = chunks.size();
     stats_.final_entries = entries.size();
     return kOk;
@@ -442,7 +683,7 @@ int Engine::enqueue(cudaStream_t st, std::string& err, cudaEvent_t* ev) {
     const bool coherent = cfg_.scattering == 0;
     size_t launches = 0, phase_launches = 0;
     ECK(cudaMemsetAsync(err_.p, 0, sizeof(unsigned), st));
-    ECK(cudaMemsetAsync(counter_.p, 0, sizeof(unsigned), st));
+    ECK(cudaMemsetAsync(counter_.p, 0, 2 * sizeof(unsigned), st));
     for (int i = 0; i < nitems_; ++i) {
         SystemState& s = *item_sys_[i];
         ECK(launch_expand_factors(item_cf_[i], (int)s.nclass, (int)item_nq_[i], s.cls.as<int>(), (int)s.na_pad,
@@ -450,6 +691,21 @@ int Engine::enqueue(cudaStream_t st, std::string& err, cudaEvent_t* ev) {
         ++launches;
     }
     if (ev) ECK(cudaEventRecord(ev[0], st));
+    if (coherent && nrec_tiles_) {
+        RecLaunch rl{};
+        rl.K = rec_k_;
+        rl.systems = d_rsys_;
+        rl.groups = d_rgroups_;
+        rl.tiles = d_rtiles_;
+        rl.ntiles = nrec_tiles_;
+        rl.bfac = rec_bfac_.as<float>();
+        rl.counter = counter_.as<unsigned>() + 1;
+        rl.err = err_.as<unsigned>();
+        ECK(launch_rec_factors(rl, nrec_groups_, st));
+        ECK(launch_phase_rec(rl, st));
+        launches += 2;
+        ++phase_launches;
+    }
     if (coherent) {
         PhaseLaunch pl{};
         pl.precision = cfg_.precision;
@@ -459,9 +715,11 @@ int Engine::enqueue(cudaStream_t st, std::string& err, cudaEvent_t* ev) {
         pl.ntiles = ntiles_;
         pl.counter = counter_.as<unsigned>();
         pl.err = err_.as<unsigned>();
-        ECK(launch_phase_sum(pl, st));
-        ++launches;
-        ++phase_launches;
+        if (ntiles_) {
+            ECK(launch_phase_sum(pl, st));
+            ++launches;
+            ++phase_launches;
+        }
         for (int i = 0; i < nitems_; ++i) {
             if (nsplit_[i] <= 1) continue;
             const size_t n = item_nv_[i] * item_nf_[i];

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "kernels.h"
@@ -46,12 +47,18 @@ struct SystemState {
     double center[3] = {0, 0, 0};
     DevBuf raw, xyz, cls, tw64, tw32, k64, k32;
     bool staged = false, classes_set = false;
+    // class-sorted copy for the shell-recurrence kernel (built on first use)
+    std::vector<int32_t> h_cls;   // [na] classes (host copy)
+    DevBuf xyz_rec, block_class;  // [nf][na_rec] float4 with w; [na_rec / 32] int
+    size_t na_rec = 0;
+    bool rec_valid = false;
 };
 
 struct EngineConfig {
     int scattering = 0, dsp = 0, method = 0, precision = 0;
     PhaseShape shape{0, 0, 0};  // q_per_lane 0: automatic
     int split_atoms = 0;        // atoms per phase-sum tile (0: automatic)
+    int rec_k = 0;              // shells per lane of the recurrence kernel: 0 automatic, -1 off
     int device = 0;
 };
 
@@ -60,6 +67,10 @@ struct WorkItem {
     SystemState* sys = nullptr;
     std::vector<size_t> offs;  // [nq+1] sub-vector offsets, offs[0] == 0
     const double* d_qv = nullptr;
+    // optional product structure: qv[offs[s] + d] = lam[s] * qv[offs[base] + d] for every
+    // shell s (see detect_product); empty: general sub-vectors
+    std::vector<double> lam;
+    int lam_base = -1;
     const double* d_cf = nullptr;  // [nq][nclass]
     double2* d_fqt = nullptr;      // [nq][nf]
     double2* d_fq = nullptr;       // [nq]
@@ -74,6 +85,8 @@ struct WorkItem {
 
 struct EngineStats {
     size_t phase_tiles = 0, corr_chunks = 0, final_entries = 0, launches = 0, phase_launches = 0;
+    size_t rec_tiles = 0, rec_shells = 0, rec_groups = 0;
+    int rec_k = 0, max_split = 1;
     PhaseShape shape{0, 0, 0};
     int split_atoms = 0;
     double terms = 0;
@@ -85,6 +98,14 @@ int build_system_tables(SystemState& s, cudaStream_t st, std::string& err);
 int stage_system(SystemState& s, const float* coords, bool on_device, int precision, cudaStream_t st,
                  std::string& err);
 int set_system_classes(SystemState& s, const int32_t* cls, bool on_device, cudaStream_t st, std::string& err);
+
+// Whether shells [0, nq) of host sub-vectors qv (offsets offs) are multiples of one base
+// set: equal counts per shell and qv[offs[s] + d] = lam[s] * qv[offs[base] + d] within
+// 1e-12 of the shell's largest sub-vector. Fills lam and base on success.
+bool detect_product(const double* qv, const std::vector<size_t>& offs, std::vector<double>& lam, int& base);
+// Maximal runs [a, e) of at least min_len shells whose lam lies on a line within
+// 2.5e-7 of the run's largest |lam| (float-rounded linear scans qualify).
+std::vector<std::pair<int, int>> arithmetic_runs(const std::vector<double>& lam, int min_len);
 
 class Engine {
 public:
@@ -112,7 +133,11 @@ private:
     std::vector<SystemState*> item_sys_;
     std::vector<size_t> item_nq_;
     int nphase_systems_ = 0, ntiles_ = 0, nchunks_ = 0, nentries_ = 0;
-    DevBuf blob_, bfac_, amp_, part_, ppart_, apart_, a2part_, counter_, err_, tw64_, tw32_;
+    int nrec_tiles_ = 0, nrec_groups_ = 0, rec_k_ = 0;
+    RecSystem* d_rsys_ = nullptr;
+    RecGroup* d_rgroups_ = nullptr;
+    RecTileDesc* d_rtiles_ = nullptr;
+    DevBuf blob_, bfac_, amp_, part_, ppart_, apart_, a2part_, counter_, err_, tw64_, tw32_, rec_bfac_;
     HostPinned hblob_;
     std::vector<size_t> bfac_off_, amp_off_, part_off_;
     PhaseSystem* d_psys_ = nullptr;

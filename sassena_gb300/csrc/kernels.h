@@ -77,6 +77,61 @@ cudaError_t launch_split_reduce_f32(const double2* part, int nsplit, size_t n, f
                                     cudaStream_t st);
 
 // ---------------------------------------------------------------------------------------
+// Shell-recurrence phase sum (FP32 form): runs of shells lam_k = lam0 + k dlam along
+// shared base vectors, evaluated with a three-term recurrence over k.
+// ---------------------------------------------------------------------------------------
+constexpr int kRecMaxClass = 32;  // scattering classes the recurrence kernel handles
+
+struct RecGroup {
+    int system;            // owning system
+    int s0, ks;            // shells [s0, s0+ks) of the system, ks <= K
+    int pad;
+    double lam0, dlam;     // shell s0+k has sub-vectors (lam0 + k dlam) * dirs[d]
+};
+
+struct RecSystem {
+    const float4* xyzw;       // class-sorted coordinates [nf][na_rec], w = 1 atom / 0 padding
+    const int* block_class;   // [na_rec / 32] class of every 32-atom block
+    const double* cf;         // [nq][nclass] class factors
+    const double* dirs;       // [nd][3] base vectors (FP64)
+    double2* out;             // FP64 split partials [nsplit][nv][nf] (when split)
+    float2* out_f32;          // FP32 amplitudes [nv][nf] (one split)
+    size_t split_stride;      // nv * nf
+    int na_rec, nf, nd, nclass;
+    int g_begin;              // first group of this system in the launch's group list
+    int pad;
+};
+
+struct RecTileDesc {
+    int system;
+    int p0, np;            // (group, direction) pairs [p0, p0+np) of the system, np <= 32
+    int f0;                // first frame (one per warp)
+    int j_begin, j_end;    // atoms of the class-sorted rows (multiples of 128; may be empty)
+    int split;
+    int pad;
+};
+
+struct RecLaunch {
+    int K;                     // shells per lane (a value of rec_shell_counts())
+    const RecSystem* systems;
+    const RecGroup* groups;
+    const RecTileDesc* tiles;
+    int ntiles;
+    float* bfac;               // [ngroups][kRecMaxClass][K] filled by launch_rec_factors
+    unsigned int* counter;     // work-queue counter, zero before the launch
+    unsigned int* err;
+    int max_ctas;
+};
+
+std::vector<int> rec_shell_counts();
+bool rec_shells_supported(int K);
+cudaError_t launch_rec_factors(const RecLaunch& a, int ngroups, cudaStream_t st);
+cudaError_t launch_phase_rec(const RecLaunch& a, cudaStream_t st);
+// dst[f][j] = src[f][map[j]] with w = 1, or a zero row entry with w = 0 where map[j] < 0
+cudaError_t launch_permute_stage(const float4* src, int na_pad_src, const int* map, int na_dst, int nf,
+                                 float4* dst, cudaStream_t st);
+
+// ---------------------------------------------------------------------------------------
 // Correlation, store and orientational average
 // ---------------------------------------------------------------------------------------
 enum DspType { DSP_AUTOCORRELATE = 0, DSP_SQUARE = 1, DSP_PLAIN = 2 };

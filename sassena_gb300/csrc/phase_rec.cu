@@ -1,0 +1,293 @@
+// Shell-recurrence phase sum (FP32 form) for shells that share one direction set.
+//
+// The reference builds the sub-vectors of every |q| from the same orientation set
+// (init_subvectors, src/scatter_devices/abstract_vectors_scatter_device.cpp:112-130:
+// ql * vectors[i] for the "file" and "sphere" types), and its q-vector scans are linear
+// in the usual case (Params::create_from_scans, src/control/parameters.cpp). For a run of
+// shells lam_k = lam_0 + k dlam along the base vectors u_d, the phase of shell k is
+// phi_0 + k theta with phi_0 = lam_0 u.r and theta = dlam u.r, so
+//     z_k = exp(i (phi_0 + k theta)),  z_{k+1} = 2 cos(theta) z_k - z_{k-1},
+// a three-term (Chebyshev) recurrence with one FMA per component. One lane evaluates K
+// shells of one direction with two SFU sin/cos pairs per atom instead of K; the
+// recurrence restarts for every group of at most K shells, which bounds its rounding
+// growth (O(K^2) ulp for theta near 0 or pi).
+//
+// Layout: atoms are sorted by scattering class into segments padded to 32 atoms, with
+// w = 1 for atoms and 0 for padding in float4.w, so every 32-atom block has one class.
+// The lane keeps plain FP32 block sums per shell and, where the class changes or a
+// pipeline stage ends, folds them times the class factor into Kahan-compensated FP32
+// running sums. Lanes run over (group, direction) pairs of a system, so ragged direction
+// counts leave no idle lanes except in the last tile. Staging, the per-warp bulk-copy
+// ring, bounded mbarrier waits and the persistent work queue follow the direct kernel.
+#include <algorithm>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace sassgpu {
+
+namespace {
+
+constexpr int kRecWarps = 8, kRecAtoms = 128, kRecStages = 2, kRecBlock = 32;
+
+struct RecLayout {
+    static constexpr int kCoordBytes = kRecWarps * kRecStages * kRecAtoms * 16;
+    static constexpr int kBarOffset = kCoordBytes;
+    static constexpr int kTileOffset = kBarOffset + kRecWarps * kRecStages * 8;
+    static constexpr int kBytes = kTileOffset + 16;
+};
+
+__device__ __forceinline__ void issue_coords(float4* sx, uint64_t* bar, const float4* src) {
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(bar, kRecAtoms * 16);
+    bulk_g2s(sx, src, kRecAtoms * 16, bar);
+}
+
+// sin and cos of 2 pi u: explicit reduction of u (revolutions) to [-1/2, 1/2] with the
+// round-to-nearest magic constant 1.5 * 2^23, then the SFU approximation
+__device__ __forceinline__ void sincos_rev(float u, float& s, float& c) {
+    const float n = __fsub_rn(__fadd_rn(u, 12582912.0f), 12582912.0f);
+    __sincosf(__fmul_rn(__fsub_rn(u, n), 6.28318530717958647692f), &s, &c);
+}
+
+template <int K>
+__device__ __forceinline__ void kahan_fold(float (&sr)[K], float (&si)[K], float (&cr)[K], float (&ci)[K],
+                                           float (&tr)[K], float (&ti)[K], const float* __restrict__ bf) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const float b = __ldg(bf + k);
+        float y = __fsub_rn(__fmul_rn(b, tr[k]), cr[k]);
+        float t = __fadd_rn(sr[k], y);
+        cr[k] = __fsub_rn(__fsub_rn(t, sr[k]), y);
+        sr[k] = t;
+        y = __fsub_rn(__fmul_rn(b, ti[k]), ci[k]);
+        t = __fadd_rn(si[k], y);
+        ci[k] = __fsub_rn(__fsub_rn(t, si[k]), y);
+        si[k] = t;
+        tr[k] = 0.f;
+        ti[k] = 0.f;
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(kRecWarps * 32, K <= 10 ? 2 : 1)
+    phase_rec_kernel(const RecLaunch a) {
+    using L = RecLayout;
+    constexpr int T = kRecAtoms, S = kRecStages, NB = kRecAtoms / kRecBlock;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float4* sx = reinterpret_cast<float4*>(smem) + warp * S * T;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L::kBarOffset) + warp * S;
+    volatile int* s_tile = reinterpret_cast<volatile int*>(smem + L::kTileOffset);
+
+    if (lane == 0) {
+#pragma unroll
+        for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    unsigned used = 0;
+    bool failed = false;
+    const double inv2pi = 0.15915494309189533577;
+
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) *s_tile = (int)atomicAdd(a.counter, 1u);
+        __syncthreads();
+        const int ti_ = *s_tile;
+        if (ti_ >= a.ntiles) break;
+        const RecTileDesc td = a.tiles[ti_];
+        const RecSystem& sys = a.systems[td.system];
+        const int nf = sys.nf;
+        // this lane's (group, direction) pair
+        const bool act = lane < td.np;
+        const int p = td.p0 + (act ? lane : 0);
+        const int gl = p / sys.nd, d = p - gl * sys.nd;
+        const RecGroup g = a.groups[sys.g_begin + gl];
+        const float* bf = a.bfac + (size_t)(sys.g_begin + gl) * kRecMaxClass * K;
+        const double* u = sys.dirs + 3 * (size_t)d;
+        const float ux = (float)(u[0] * inv2pi), uy = (float)(u[1] * inv2pi), uz = (float)(u[2] * inv2pi);
+        const float q0 = (float)g.lam0, dq = (float)g.dlam;
+
+        float sr[K], si[K], cr[K], ci[K], tr[K], tim[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) sr[k] = si[k] = cr[k] = ci[k] = tr[k] = tim[k] = 0.f;
+        const int f = td.f0 + warp;
+        const int nst = (td.j_end - td.j_begin) / T;
+
+        if (f < nf && nst > 0 && !failed) {
+            const float4* row = sys.xyzw + (size_t)f * sys.na_rec + td.j_begin;
+            const int* bcls = sys.block_class + td.j_begin / kRecBlock;
+            if (lane == 0)
+                for (int k = 0; k < S && k < nst; ++k) {
+                    const unsigned slot = (used + k) % S;
+                    issue_coords(sx + slot * T, &bars[slot], row + k * T);
+                }
+            int t = 0;
+            for (; t < nst; ++t) {
+                const unsigned slot = (used + t) % S;
+                const bool ok = mbar_wait_parity(&bars[slot], ((used + t) / S) & 1u);
+                if (!__all_sync(0xffffffffu, ok)) break;
+                const float4* cx = sx + slot * T;
+                int cls = __ldg(bcls + t * NB);
+#pragma unroll 1
+                for (int b = 0; b < NB; ++b) {
+#pragma unroll 2
+                    for (int jj = 0; jj < kRecBlock; ++jj) {
+                        const float4 r = cx[b * kRecBlock + jj];
+                        const float du = fmaf(r.z, uz, fmaf(r.y, uy, __fmul_rn(r.x, ux)));
+                        float s0, c0, s1, c1;
+                        sincos_rev(__fmul_rn(q0, du), s0, c0);
+                        sincos_rev(__fmul_rn(dq, du), s1, c1);
+                        float zr0 = __fmul_rn(r.w, c0), zi0 = __fmul_rn(r.w, s0);
+                        tr[0] = __fadd_rn(tr[0], zr0);
+                        tim[0] = __fadd_rn(tim[0], zi0);
+                        if (K > 1) {
+                            float zr1 = fmaf(zr0, c1, -__fmul_rn(zi0, s1));
+                            float zi1 = fmaf(zr0, s1, __fmul_rn(zi0, c1));
+                            const float c2 = __fadd_rn(c1, c1);
+                            tr[1] = __fadd_rn(tr[1], zr1);
+                            tim[1] = __fadd_rn(tim[1], zi1);
+#pragma unroll
+                            for (int k = 2; k < K; ++k) {
+                                const float zr2 = fmaf(c2, zr1, -zr0), zi2 = fmaf(c2, zi1, -zi0);
+                                tr[k] = __fadd_rn(tr[k], zr2);
+                                tim[k] = __fadd_rn(tim[k], zi2);
+                                zr0 = zr1;
+                                zi0 = zi1;
+                                zr1 = zr2;
+                                zi1 = zi2;
+                            }
+                        }
+                    }
+                    const int next = (b + 1 < NB) ? __ldg(bcls + t * NB + b + 1) : -1;
+                    if (next != cls) {  // warp-uniform: every lane reads the same block classes
+                        kahan_fold<K>(sr, si, cr, ci, tr, tim, bf + cls * K);
+                        cls = next;
+                    }
+                }
+                __syncwarp();
+                if (lane == 0 && t + S < nst) issue_coords(sx + slot * T, &bars[slot], row + (t + S) * T);
+            }
+            if (t < nst) {
+                if (lane == 0) {
+                    set_error(a.err, DEV_MBAR_TIMEOUT);
+                    for (int k = t; k < nst && k < t + S; ++k)
+                        mbar_wait_parity(&bars[(used + k) % S], ((used + k) / S) & 1u);
+                }
+                failed = true;
+                __syncwarp();
+            }
+            used += nst;
+        }
+        // every (split, shell, direction, frame) slot is written, also for empty atom ranges
+        if (f < nf && act) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                if (k < g.ks) {
+                    const size_t v = (size_t)(g.s0 + k) * sys.nd + d;
+                    const double re = (double)sr[k] - (double)cr[k], im = (double)si[k] - (double)ci[k];
+                    if (sys.out_f32) sys.out_f32[v * nf + f] = make_float2((float)re, (float)im);
+                    else sys.out[(size_t)td.split * sys.split_stride + v * nf + f] = make_double2(re, im);
+                }
+            }
+        }
+    }
+}
+
+template <int K>
+cudaError_t launch_rec(const RecLaunch& a, cudaStream_t st) {
+    auto k = phase_rec_kernel<K>;
+    const int smem = RecLayout::kBytes;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kRecWarps * 32, smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    long long grid = (long long)std::max(per_sm, 1) * std::max(sms, 1);
+    if (a.max_ctas > 0) grid = std::min<long long>(grid, a.max_ctas);
+    if (grid > a.ntiles) grid = a.ntiles;
+    if (grid < 1) return cudaSuccess;
+    k<<<(unsigned)grid, kRecWarps * 32, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+// bfac[g][c][k] = class_factors[s0 + k][c] (float) for k < ks, else 0
+__global__ void rec_factors_kernel(const RecSystem* __restrict__ systems, const RecGroup* __restrict__ groups,
+                                   int ngroups, int K, float* __restrict__ bfac) {
+    const size_t n = (size_t)ngroups * kRecMaxClass * K;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int g = (int)(i / ((size_t)kRecMaxClass * K));
+        const int r = (int)(i - (size_t)g * kRecMaxClass * K);
+        const int c = r / K, k = r - c * K;
+        const RecGroup gr = groups[g];
+        const RecSystem& s = systems[gr.system];
+        float v = 0.f;
+        if (k < gr.ks && c < s.nclass) v = (float)s.cf[(size_t)(gr.s0 + k) * s.nclass + c];
+        bfac[i] = v;
+    }
+}
+
+}  // namespace
+
+std::vector<int> rec_shell_counts() { return {4, 6, 8, 10, 12, 16}; }
+
+bool rec_shells_supported(int K) {
+    for (int k : rec_shell_counts())
+        if (k == K) return true;
+    return false;
+}
+
+cudaError_t launch_rec_factors(const RecLaunch& a, int ngroups, cudaStream_t st) {
+    if (ngroups <= 0) return cudaSuccess;
+    const size_t n = (size_t)ngroups * kRecMaxClass * a.K;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 1024);
+    rec_factors_kernel<<<blocks, 256, 0, st>>>(a.systems, a.groups, ngroups, a.K, a.bfac);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_phase_rec(const RecLaunch& a, cudaStream_t st) {
+    if (a.ntiles <= 0) return cudaSuccess;
+    switch (a.K) {
+        case 4: return launch_rec<4>(a, st);
+        case 6: return launch_rec<6>(a, st);
+        case 8: return launch_rec<8>(a, st);
+        case 10: return launch_rec<10>(a, st);
+        case 12: return launch_rec<12>(a, st);
+        case 16: return launch_rec<16>(a, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
+// Class-sorted copy of the staged coordinates: dst[f][j] = src[f][map[j]] with w = 1,
+// or zero with w = 0 where map[j] < 0 (segment padding).
+__global__ void permute_stage_kernel(const float4* __restrict__ src, int na_pad_src, const int* __restrict__ map,
+                                     int na_dst, int nf, float4* __restrict__ dst) {
+    const size_t n = (size_t)nf * na_dst;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t f = i / na_dst;
+        const int j = (int)(i - f * na_dst);
+        const int s = map[j];
+        float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (s >= 0) {
+            r = src[f * na_pad_src + s];
+            r.w = 1.f;
+        }
+        dst[i] = r;
+    }
+}
+
+cudaError_t launch_permute_stage(const float4* src, int na_pad_src, const int* map, int na_dst, int nf, float4* dst,
+                                 cudaStream_t st) {
+    const size_t n = (size_t)nf * na_dst;
+    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 32);
+    permute_stage_kernel<<<std::max(blocks, 1), 256, 0, st>>>(src, na_pad_src, map, na_dst, nf, dst);
+    return cudaGetLastError();
+}
+
+}  // namespace sassgpu

@@ -21,5 +21,6 @@ struct sass_plan {
     cudaEvent_t ev[sassgpu::kEvents] = {};
     sassgpu::PhaseShape shape{0, 0, 0};
     int split_atoms = 0;
+    int rec_k = 0;  // shell recurrence: 0 automatic, -1 off, else shells per lane
     sassgpu::DevBuf qv, cf, fqt, fq, fq2, amp_tmp;
 };

@@ -47,7 +47,7 @@ def test_batch_autotune_keeps_results(native_lib):
     refs = [ref(w) for w in ws]
     with abi.Batch(ws, precision="fp32") as b:
         best = b.autotune(repeats=1)
-        assert best["q_per_lane"] in (1, 2, 4, 8) and best["ms"] > 0
+        assert best["q_per_lane"] in (0, 1, 2, 4, 8) and best["ms"] > 0
         b.run()
         b.sync()
         for i, r in enumerate(refs):
@@ -61,6 +61,7 @@ def test_plan_autotune(native_lib):
         p.stage(w.coords)
         p.set_classes(w.atom_class)
         shape = p.autotune(w.sub_offsets(), w.subvectors(), w.class_factors, repeats=1)
-        assert shape["q_per_lane"] in (1, 2, 4, 8)
         fqt, _, _ = p.compute(w.sub_offsets(), w.subvectors(), w.class_factors)
+        # q_per_lane 0: the automatic tile shape won (or the recurrence covers every shell)
+        assert shape["q_per_lane"] in (0, 1, 2, 4, 8)
     assert rel_err_sqt(fqt, r[0]).max() <= 1e-3
