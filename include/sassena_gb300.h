@@ -153,7 +153,7 @@ int sass_frame_center(const sass_plan* plan, double* center3);
  * scans), runs of at least 3 such shells are evaluated by a kernel that carries
  * exp(i q_k u.r) from shell to shell with a three-term recurrence: two reduced sin/cos
  * pairs per atom for up to `shells_per_lane` shells. 0 = automatic (default), -1 = off,
- * else one of 4, 6, 8, 10, 12, 16. FP64 plans ignore it. */
+ * else one of 4, 8, 12, 16, 20, 24, 32. FP64 plans ignore it. */
 int sass_set_shell_recurrence(sass_plan* plan, int shells_per_lane);
 
 /* How the last sass_compute (or batch run) scheduled the phase sum. */

@@ -223,7 +223,7 @@ class Plan:
         self._check(self.lib.sass_set_phase_tile(self._h, q_per_lane, warps, atoms, atom_splits))
 
     def set_recurrence(self, shells_per_lane=0):
-        """Shell recurrence of the FP32 form: 0 automatic, -1 off, else 4/6/8/10/12/16."""
+        """Shell recurrence of the FP32 form: 0 automatic, -1 off, else 4/8/12/16/20/24/32."""
         self._check(self.lib.sass_set_shell_recurrence(self._h, shells_per_lane))
 
     def schedule(self):

@@ -235,8 +235,9 @@ std::vector<std::pair<int, int>> arithmetic_runs(const std::vector<double>& lam,
 namespace {
 
 // Per-lane cost of a group of K shells, in units of one recurrence step (2 FMA + 2 FADD):
-// K steps plus the per-atom dot product, two reduced sin/cos pairs and the seed rotation.
-double rec_group_cost(int K) { return K + 7.0; }
+// K steps plus the per-atom dot product, two reduced sin/cos pairs and the seed rotation
+// (about 22 FP32 operations).
+double rec_group_cost(int K) { return K + 5.5; }
 
 int choose_rec_k(const std::vector<std::vector<std::pair<int, int>>>& runs) {
     int best = 0;
@@ -274,6 +275,12 @@ int ensure_rec_layout(SystemState& s, std::string& err) {
     }
     while (map.size() % 128 || map.empty()) map.push_back(-1);
     bcls.resize(map.size() / 32, last);
+    // block information: class in the low 16 bits, padding atoms of the block above
+    for (size_t b = 0; b < bcls.size(); ++b) {
+        int npad = 0;
+        for (int j = 0; j < 32; ++j) npad += map[32 * b + j] < 0;
+        bcls[b] |= npad << 16;
+    }
     s.na_rec = map.size();
     DevBuf d_map;
     ECK(d_map.ensure(map.size() * sizeof(int)));

@@ -90,8 +90,8 @@ struct RecGroup {
 };
 
 struct RecSystem {
-    const float4* xyzw;       // class-sorted coordinates [nf][na_rec], w = 1 atom / 0 padding
-    const int* block_class;   // [na_rec / 32] class of every 32-atom block
+    const float4* xyzw;       // class-sorted coordinates [nf][na_rec]; padding atoms at the origin
+    const int* block_class;   // [na_rec / 32] class (low 16 bits) | padding atoms << 16 of every 32-atom block
     const double* cf;         // [nq][nclass] class factors
     const double* dirs;       // [nd][3] base vectors (FP64)
     double2* out;             // FP64 split partials [nsplit][nv][nf] (when split)

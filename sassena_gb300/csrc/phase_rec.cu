@@ -12,13 +12,15 @@
 // recurrence restarts for every group of at most K shells, which bounds its rounding
 // growth (O(K^2) ulp for theta near 0 or pi).
 //
-// Layout: atoms are sorted by scattering class into segments padded to 32 atoms, with
-// w = 1 for atoms and 0 for padding in float4.w, so every 32-atom block has one class.
-// The lane keeps plain FP32 block sums per shell and, where the class changes or a
-// pipeline stage ends, folds them times the class factor into Kahan-compensated FP32
-// running sums. Lanes run over (group, direction) pairs of a system, so ragged direction
-// counts leave no idle lanes except in the last tile. Staging, the per-warp bulk-copy
-// ring, bounded mbarrier waits and the persistent work queue follow the direct kernel.
+// Layout: atoms are sorted by scattering class into segments padded to 32 atoms, so every
+// 32-atom block has one class; padding atoms sit at the origin, where every shell's term
+// is exactly 1, and are subtracted by count. The lane keeps plain FP32 block sums per
+// shell in registers and, where the class changes or a pipeline stage ends, folds them
+// times the class factor into Kahan-compensated FP32 running sums held in shared memory
+// (so registers grow by 2 per shell, allowing groups of up to 32 shells). Lanes run over
+// (group, direction) pairs of a system, so ragged direction counts leave no idle lanes
+// except in the last tile. Staging, the per-warp bulk-copy ring, bounded mbarrier waits
+// and the persistent work queue follow the direct kernel.
 #include <algorithm>
 
 #include "common.cuh"
@@ -30,11 +32,16 @@ namespace {
 
 constexpr int kRecWarps = 8, kRecAtoms = 128, kRecStages = 2, kRecBlock = 32;
 
+// Shared memory: per warp a ring of coordinate stages, the stage barriers, the tile
+// slot and the Kahan state (sum re, sum im, compensation re, compensation im) of every
+// (shell, lane) as float4 [warp][k][lane].
+template <int K>
 struct RecLayout {
     static constexpr int kCoordBytes = kRecWarps * kRecStages * kRecAtoms * 16;
     static constexpr int kBarOffset = kCoordBytes;
     static constexpr int kTileOffset = kBarOffset + kRecWarps * kRecStages * 8;
-    static constexpr int kBytes = kTileOffset + 16;
+    static constexpr int kKahanOffset = (kTileOffset + 16 + 127) / 128 * 128;
+    static constexpr int kBytes = kKahanOffset + kRecWarps * K * 32 * 16;
 };
 
 __device__ __forceinline__ void issue_coords(float4* sx, uint64_t* bar, const float4* src) {
@@ -43,42 +50,48 @@ __device__ __forceinline__ void issue_coords(float4* sx, uint64_t* bar, const fl
     bulk_g2s(sx, src, kRecAtoms * 16, bar);
 }
 
-// sin and cos of 2 pi u: explicit reduction of u (revolutions) to [-1/2, 1/2] with the
-// round-to-nearest magic constant 1.5 * 2^23, then the SFU approximation
-__device__ __forceinline__ void sincos_rev(float u, float& s, float& c) {
-    const float n = __fsub_rn(__fadd_rn(u, 12582912.0f), 12582912.0f);
-    __sincosf(__fmul_rn(__fsub_rn(u, n), 6.28318530717958647692f), &s, &c);
+// sin and cos of 2 pi q du (q du in revolutions): explicit reduction to [-1/2, 1/2] with
+// the round-to-nearest constant 1.5 * 2^23 (q du + M rounds to rint(q du) + M), the
+// remainder formed by one fused multiply-add, then the SFU approximation.
+__device__ __forceinline__ void sincos_rev(float q, float du, float& s, float& c) {
+    const float n = __fsub_rn(fmaf(q, du, 12582912.0f), 12582912.0f);
+    const float f = fmaf(q, du, -n);
+    __sincosf(__fmul_rn(f, 6.28318530717958647692f), &s, &c);
 }
 
+// Fold the block sums (minus the padding atoms' exact contribution of 1 each to the
+// real part) times the class factors into the Kahan state and clear them.
 template <int K>
-__device__ __forceinline__ void kahan_fold(float (&sr)[K], float (&si)[K], float (&cr)[K], float (&ci)[K],
-                                           float (&tr)[K], float (&ti)[K], const float* __restrict__ bf) {
+__device__ __forceinline__ void kahan_fold(float4* __restrict__ ks, float (&tr)[K], float (&ti)[K], float npad,
+                                           const float* __restrict__ bf) {
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         const float b = __ldg(bf + k);
-        float y = __fsub_rn(__fmul_rn(b, tr[k]), cr[k]);
-        float t = __fadd_rn(sr[k], y);
-        cr[k] = __fsub_rn(__fsub_rn(t, sr[k]), y);
-        sr[k] = t;
-        y = __fsub_rn(__fmul_rn(b, ti[k]), ci[k]);
-        t = __fadd_rn(si[k], y);
-        ci[k] = __fsub_rn(__fsub_rn(t, si[k]), y);
-        si[k] = t;
+        float4 a = ks[k * 32];
+        float y = fmaf(b, __fsub_rn(tr[k], npad), -a.z);
+        float t = __fadd_rn(a.x, y);
+        a.z = __fsub_rn(__fsub_rn(t, a.x), y);
+        a.x = t;
+        y = fmaf(b, ti[k], -a.w);
+        t = __fadd_rn(a.y, y);
+        a.w = __fsub_rn(__fsub_rn(t, a.y), y);
+        a.y = t;
+        ks[k * 32] = a;
         tr[k] = 0.f;
         ti[k] = 0.f;
     }
 }
 
 template <int K>
-__global__ void __launch_bounds__(kRecWarps * 32, K <= 10 ? 2 : 1)
-    phase_rec_kernel(const RecLaunch a) {
-    using L = RecLayout;
+__global__ void __launch_bounds__(kRecWarps * 32, K <= 20 ? 2 : 1) phase_rec_kernel(const RecLaunch a) {
+    using L = RecLayout<K>;
     constexpr int T = kRecAtoms, S = kRecStages, NB = kRecAtoms / kRecBlock;
     extern __shared__ __align__(128) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* sx = reinterpret_cast<float4*>(smem) + warp * S * T;
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L::kBarOffset) + warp * S;
     volatile int* s_tile = reinterpret_cast<volatile int*>(smem + L::kTileOffset);
+    float4* ks = reinterpret_cast<float4*>(smem + L::kKahanOffset) + warp * K * 32 + lane;
 
     if (lane == 0) {
 #pragma unroll
@@ -109,15 +122,17 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 10 ? 2 : 1)
         const float ux = (float)(u[0] * inv2pi), uy = (float)(u[1] * inv2pi), uz = (float)(u[2] * inv2pi);
         const float q0 = (float)g.lam0, dq = (float)g.dlam;
 
-        float sr[K], si[K], cr[K], ci[K], tr[K], tim[K];
 #pragma unroll
-        for (int k = 0; k < K; ++k) sr[k] = si[k] = cr[k] = ci[k] = tr[k] = tim[k] = 0.f;
+        for (int k = 0; k < K; ++k) ks[k * 32] = make_float4(0.f, 0.f, 0.f, 0.f);
+        float tr[K], tim[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) tr[k] = tim[k] = 0.f;
         const int f = td.f0 + warp;
         const int nst = (td.j_end - td.j_begin) / T;
 
         if (f < nf && nst > 0 && !failed) {
             const float4* row = sys.xyzw + (size_t)f * sys.na_rec + td.j_begin;
-            const int* bcls = sys.block_class + td.j_begin / kRecBlock;
+            const int* binfo = sys.block_class + td.j_begin / kRecBlock;
             if (lane == 0)
                 for (int k = 0; k < S && k < nst; ++k) {
                     const unsigned slot = (used + k) % S;
@@ -129,7 +144,8 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 10 ? 2 : 1)
                 const bool ok = mbar_wait_parity(&bars[slot], ((used + t) / S) & 1u);
                 if (!__all_sync(0xffffffffu, ok)) break;
                 const float4* cx = sx + slot * T;
-                int cls = __ldg(bcls + t * NB);
+                int info = __ldg(binfo + t * NB);
+                float npad = 0.f;
 #pragma unroll 1
                 for (int b = 0; b < NB; ++b) {
 #pragma unroll 2
@@ -137,14 +153,14 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 10 ? 2 : 1)
                         const float4 r = cx[b * kRecBlock + jj];
                         const float du = fmaf(r.z, uz, fmaf(r.y, uy, __fmul_rn(r.x, ux)));
                         float s0, c0, s1, c1;
-                        sincos_rev(__fmul_rn(q0, du), s0, c0);
-                        sincos_rev(__fmul_rn(dq, du), s1, c1);
-                        float zr0 = __fmul_rn(r.w, c0), zi0 = __fmul_rn(r.w, s0);
-                        tr[0] = __fadd_rn(tr[0], zr0);
-                        tim[0] = __fadd_rn(tim[0], zi0);
+                        sincos_rev(q0, du, s0, c0);
+                        sincos_rev(dq, du, s1, c1);
+                        tr[0] = __fadd_rn(tr[0], c0);
+                        tim[0] = __fadd_rn(tim[0], s0);
                         if (K > 1) {
-                            float zr1 = fmaf(zr0, c1, -__fmul_rn(zi0, s1));
-                            float zi1 = fmaf(zr0, s1, __fmul_rn(zi0, c1));
+                            float zr0 = c0, zi0 = s0;
+                            float zr1 = fmaf(c0, c1, -__fmul_rn(s0, s1));
+                            float zi1 = fmaf(s0, c1, __fmul_rn(c0, s1));
                             const float c2 = __fadd_rn(c1, c1);
                             tr[1] = __fadd_rn(tr[1], zr1);
                             tim[1] = __fadd_rn(tim[1], zi1);
@@ -160,11 +176,14 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 10 ? 2 : 1)
                             }
                         }
                     }
-                    const int next = (b + 1 < NB) ? __ldg(bcls + t * NB + b + 1) : -1;
-                    if (next != cls) {  // warp-uniform: every lane reads the same block classes
-                        kahan_fold<K>(sr, si, cr, ci, tr, tim, bf + cls * K);
-                        cls = next;
+                    npad += (float)(info >> 16);
+                    const int next = (b + 1 < NB) ? __ldg(binfo + t * NB + b + 1) : -1;
+                    // warp-uniform: every lane reads the same block information
+                    if (b + 1 == NB || (next & 0xffff) != (info & 0xffff)) {
+                        kahan_fold<K>(ks, tr, tim, npad, bf + (info & 0xffff) * K);
+                        npad = 0.f;
                     }
+                    info = next;
                 }
                 __syncwarp();
                 if (lane == 0 && t + S < nst) issue_coords(sx + slot * T, &bars[slot], row + (t + S) * T);
@@ -185,8 +204,9 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 10 ? 2 : 1)
 #pragma unroll
             for (int k = 0; k < K; ++k) {
                 if (k < g.ks) {
+                    const float4 st = ks[k * 32];
                     const size_t v = (size_t)(g.s0 + k) * sys.nd + d;
-                    const double re = (double)sr[k] - (double)cr[k], im = (double)si[k] - (double)ci[k];
+                    const double re = (double)st.x - (double)st.z, im = (double)st.y - (double)st.w;
                     if (sys.out_f32) sys.out_f32[v * nf + f] = make_float2((float)re, (float)im);
                     else sys.out[(size_t)td.split * sys.split_stride + v * nf + f] = make_double2(re, im);
                 }
@@ -198,7 +218,7 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 10 ? 2 : 1)
 template <int K>
 cudaError_t launch_rec(const RecLaunch& a, cudaStream_t st) {
     auto k = phase_rec_kernel<K>;
-    const int smem = RecLayout::kBytes;
+    const int smem = RecLayout<K>::kBytes;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -235,7 +255,7 @@ __global__ void rec_factors_kernel(const RecSystem* __restrict__ systems, const 
 
 }  // namespace
 
-std::vector<int> rec_shell_counts() { return {4, 6, 8, 10, 12, 16}; }
+std::vector<int> rec_shell_counts() { return {4, 8, 12, 16, 20, 24, 32}; }
 
 bool rec_shells_supported(int K) {
     for (int k : rec_shell_counts())
@@ -255,17 +275,19 @@ cudaError_t launch_phase_rec(const RecLaunch& a, cudaStream_t st) {
     if (a.ntiles <= 0) return cudaSuccess;
     switch (a.K) {
         case 4: return launch_rec<4>(a, st);
-        case 6: return launch_rec<6>(a, st);
         case 8: return launch_rec<8>(a, st);
-        case 10: return launch_rec<10>(a, st);
         case 12: return launch_rec<12>(a, st);
         case 16: return launch_rec<16>(a, st);
+        case 20: return launch_rec<20>(a, st);
+        case 24: return launch_rec<24>(a, st);
+        case 32: return launch_rec<32>(a, st);
     }
     return cudaErrorInvalidValue;
 }
 
-// Class-sorted copy of the staged coordinates: dst[f][j] = src[f][map[j]] with w = 1,
-// or zero with w = 0 where map[j] < 0 (segment padding).
+// Class-sorted copy of the staged coordinates: dst[f][j] = src[f][map[j]] (w = 1), or
+// the origin (w = 0) where map[j] < 0; a padding atom at the origin contributes exactly
+// 1 to the real part of every shell, which the kernel subtracts by count.
 __global__ void permute_stage_kernel(const float4* __restrict__ src, int na_pad_src, const int* __restrict__ map,
                                      int na_dst, int nf, float4* __restrict__ dst) {
     const size_t n = (size_t)nf * na_dst;

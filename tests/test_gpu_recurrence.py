@@ -53,7 +53,7 @@ def linear_case():
     return w, reference(w)
 
 
-@pytest.mark.parametrize("k", [4, 6, 8, 10, 12, 16])
+@pytest.mark.parametrize("k", [4, 8, 12, 16, 20, 24, 32])
 def test_every_width(native_lib, linear_case, k):
     w, ref = linear_case
     sch = {}
@@ -61,6 +61,17 @@ def test_every_width(native_lib, linear_case, k):
     assert sch["rec_shells_per_lane"] == k and sch["rec_shells"] == w.nq and sch["direct_tiles"] == 0
     e = assert_close(got, ref)
     print("K=%d rel err %.2e %.2e %.2e" % ((k,) + e))
+
+
+def test_long_run_several_groups(native_lib):
+    # 45 equally spaced shells: several groups per lane at every width
+    w = synth.small("all", "autocorrelate", seed=38, na=211, nf=24, nq=45, nm=21, box=18.0)
+    ref = reference(w)
+    for k in (8, 20, 32):
+        sch = {}
+        got = abi.compute_workload(w, "fp32", recurrence=k, schedule=sch)
+        assert sch["rec_shells"] == 45 and sch["rec_shells_per_lane"] == k
+        assert_close(got, ref)
 
 
 def test_automatic_width_and_off(native_lib, linear_case):
