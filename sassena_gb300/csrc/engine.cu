@@ -482,10 +482,12 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
             const int per = 32 * shape.q_per_lane;
             // balanced split of the stages: no slice is empty since nsplit <= stages
             const long long nst = (long long)(s.na_pad / shape.atoms), ns = nsplit_[i];
-            for (size_t sh = 0; sh < nq; ++sh) {
-                if (is_rec(i, sh)) continue;
-                for (size_t v = it.offs[sh]; v < it.offs[sh + 1]; v += per)
-                    for (size_t f0 = 0; f0 < s.nf; f0 += shape.warps)
+            // frame tiles outermost: the tiles that read the same frames run together, so
+            // the coordinates stream from HBM about once and the other reads hit L2
+            for (size_t f0 = 0; f0 < s.nf; f0 += shape.warps)
+                for (size_t sh = 0; sh < nq; ++sh) {
+                    if (is_rec(i, sh)) continue;
+                    for (size_t v = it.offs[sh]; v < it.offs[sh + 1]; v += per)
                         for (int sp = 0; sp < nsplit_[i]; ++sp) {
                             PhaseTileDesc t;
                             t.system = (int)i;
@@ -547,8 +549,8 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
         r.g_begin = item_g0[i];
         const int pairs = item_ng[i] * item_nd[i];
         const long long nst = (long long)(s.na_rec / 128), ns = nsplit_[i];
-        for (int p0 = 0; p0 < pairs; p0 += 32)
-            for (size_t f0 = 0; f0 < s.nf; f0 += 8)
+        for (size_t f0 = 0; f0 < s.nf; f0 += 8)  // frame tiles outermost (L2 reuse)
+            for (int p0 = 0; p0 < pairs; p0 += 32)
                 for (int sp = 0; sp < nsplit_[i]; ++sp) {
                     RecTileDesc t{};
                     t.system = (int)i;

@@ -50,35 +50,32 @@ __device__ __forceinline__ void issue_coords(float4* sx, uint64_t* bar, const fl
     bulk_g2s(sx, src, kRecAtoms * 16, bar);
 }
 
-// sin and cos of 2 pi q du (q du in revolutions): explicit reduction to [-1/2, 1/2] with
-// the round-to-nearest constant 1.5 * 2^23 (q du + M rounds to rint(q du) + M), the
-// remainder formed by one fused multiply-add, then the SFU approximation.
-__device__ __forceinline__ void sincos_rev(float q, float du, float& s, float& c) {
-    const float n = __fsub_rn(fmaf(q, du, 12582912.0f), 12582912.0f);
-    const float f = fmaf(q, du, -n);
-    __sincosf(__fmul_rn(f, 6.28318530717958647692f), &s, &c);
-}
+// Per-block sums are kept on the sign-patterned sequence w_k = s_k z_k with
+// s = (+1, +1, -1, -1, +1, +1, ...): then w_{k+1} = r_k 2cos(theta) w_k + w_{k-1} with
+// r_k = -1 for odd k and +1 for even k, so every step is one paired FMA whose addend
+// needs no negation, and the sign s_k is applied once when the block sums are folded.
+__host__ __device__ constexpr float rec_sign(int k) { return ((k >> 1) & 1) ? -1.f : 1.f; }
 
-// Fold the block sums (minus the padding atoms' exact contribution of 1 each to the
-// real part) times the class factors into the Kahan state and clear them.
+// Fold the block sums (minus the padding atoms' exact contribution: z_k = 1 each) times
+// the class factors into the Kahan state (sum re, sum im, compensation re, im) and clear.
 template <int K>
-__device__ __forceinline__ void kahan_fold(float4* __restrict__ ks, float (&tr)[K], float (&ti)[K], float npad,
+__device__ __forceinline__ void kahan_fold(float4* __restrict__ ks, float2 (&acc)[K], float npad,
                                            const float* __restrict__ bf) {
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         const float b = __ldg(bf + k);
+        const float sg = rec_sign(k);
         float4 a = ks[k * 32];
-        float y = fmaf(b, __fsub_rn(tr[k], npad), -a.z);
+        float y = fmaf(b, __fsub_rn(sg * acc[k].x, npad), -a.z);
         float t = __fadd_rn(a.x, y);
         a.z = __fsub_rn(__fsub_rn(t, a.x), y);
         a.x = t;
-        y = fmaf(b, ti[k], -a.w);
+        y = fmaf(b, sg * acc[k].y, -a.w);
         t = __fadd_rn(a.y, y);
         a.w = __fsub_rn(__fsub_rn(t, a.y), y);
         a.y = t;
         ks[k * 32] = a;
-        tr[k] = 0.f;
-        ti[k] = 0.f;
+        acc[k] = make_float2(0.f, 0.f);
     }
 }
 
@@ -124,9 +121,13 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 20 ? 2 : 1) phase_rec_ker
 
 #pragma unroll
         for (int k = 0; k < K; ++k) ks[k * 32] = make_float4(0.f, 0.f, 0.f, 0.f);
-        float tr[K], tim[K];
+        float2 acc[K];
 #pragma unroll
-        for (int k = 0; k < K; ++k) tr[k] = tim[k] = 0.f;
+        for (int k = 0; k < K; ++k) acc[k] = make_float2(0.f, 0.f);
+        const float2 qd = make_float2(q0, dq);
+        const float2 kM = make_float2(12582912.0f, 12582912.0f), kNeg = make_float2(-1.f, -1.f);
+        const float2 k2pi = make_float2(6.28318530717958647692f, 6.28318530717958647692f);
+        const float2 kTwo = make_float2(2.f, -2.f);
         const int f = td.f0 + warp;
         const int nst = (td.j_end - td.j_begin) / T;
 
@@ -152,27 +153,31 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 20 ? 2 : 1) phase_rec_ker
                     for (int jj = 0; jj < kRecBlock; ++jj) {
                         const float4 r = cx[b * kRecBlock + jj];
                         const float du = fmaf(r.z, uz, fmaf(r.y, uy, __fmul_rn(r.x, ux)));
+                        const float2 dd = make_float2(du, du);
+                        // (lam0, dlam) x u.r in revolutions, reduced to [-1/2, 1/2]: the sum with
+                        // 1.5 * 2^23 rounds to the nearest integer n, then f = lam u.r - n by FMA
+                        const float2 nm = __ffma2_rn(qd, dd, kM);
+                        const float2 nn = __ffma2_rn(nm, kNeg, kM);  // -n, exact
+                        const float2 x = __fmul2_rn(__ffma2_rn(qd, dd, nn), k2pi);
                         float s0, c0, s1, c1;
-                        sincos_rev(q0, du, s0, c0);
-                        sincos_rev(dq, du, s1, c1);
-                        tr[0] = __fadd_rn(tr[0], c0);
-                        tim[0] = __fadd_rn(tim[0], s0);
+                        __sincosf(x.x, &s0, &c0);
+                        __sincosf(x.y, &s1, &c1);
+                        const float2 w0 = make_float2(c0, s0);
+                        // w1 = z1 = z0 exp(i theta)
+                        const float2 w1 = __ffma2_rn(make_float2(-s0, c0), make_float2(s1, s1),
+                                                     __fmul2_rn(w0, make_float2(c1, c1)));
+                        const float2 c2 = __fmul2_rn(make_float2(c1, c1), kTwo);  // (2c, -2c)
+                        const float2 cp = make_float2(c2.x, c2.x), cn = make_float2(c2.y, c2.y);
+                        acc[0] = __fadd2_rn(acc[0], w0);
                         if (K > 1) {
-                            float zr0 = c0, zi0 = s0;
-                            float zr1 = fmaf(c0, c1, -__fmul_rn(s0, s1));
-                            float zi1 = fmaf(s0, c1, __fmul_rn(c0, s1));
-                            const float c2 = __fadd_rn(c1, c1);
-                            tr[1] = __fadd_rn(tr[1], zr1);
-                            tim[1] = __fadd_rn(tim[1], zi1);
+                            acc[1] = __fadd2_rn(acc[1], w1);
+                            float2 wa = w0, wb = w1;
 #pragma unroll
                             for (int k = 2; k < K; ++k) {
-                                const float zr2 = fmaf(c2, zr1, -zr0), zi2 = fmaf(c2, zi1, -zi0);
-                                tr[k] = __fadd_rn(tr[k], zr2);
-                                tim[k] = __fadd_rn(tim[k], zi2);
-                                zr0 = zr1;
-                                zi0 = zi1;
-                                zr1 = zr2;
-                                zi1 = zi2;
+                                const float2 wc = __ffma2_rn((k & 1) ? cp : cn, wb, wa);
+                                acc[k] = __fadd2_rn(acc[k], wc);
+                                wa = wb;
+                                wb = wc;
                             }
                         }
                     }
@@ -180,7 +185,7 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 20 ? 2 : 1) phase_rec_ker
                     const int next = (b + 1 < NB) ? __ldg(binfo + t * NB + b + 1) : -1;
                     // warp-uniform: every lane reads the same block information
                     if (b + 1 == NB || (next & 0xffff) != (info & 0xffff)) {
-                        kahan_fold<K>(ks, tr, tim, npad, bf + (info & 0xffff) * K);
+                        kahan_fold<K>(ks, acc, npad, bf + (info & 0xffff) * K);
                         npad = 0.f;
                     }
                     info = next;
