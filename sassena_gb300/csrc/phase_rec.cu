@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 20 ? 2 : 1) phase_rec_ker
                 float npad = 0.f;
 #pragma unroll 1
                 for (int b = 0; b < NB; ++b) {
-#pragma unroll 2
+#pragma unroll 4
                     for (int jj = 0; jj < kRecBlock; ++jj) {
                         const float4 r = cx[b * kRecBlock + jj];
                         const float du = fmaf(r.z, uz, fmaf(r.y, uy, __fmul_rn(r.x, ux)));
@@ -204,17 +204,27 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 20 ? 2 : 1) phase_rec_ker
             }
             used += nst;
         }
-        // every (split, shell, direction, frame) slot is written, also for empty atom ranges
-        if (f < nf && act) {
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                if (k < g.ks) {
-                    const float4 st = ks[k * 32];
-                    const size_t v = (size_t)(g.s0 + k) * sys.nd + d;
-                    const double re = (double)st.x - (double)st.z, im = (double)st.y - (double)st.w;
-                    if (sys.out_f32) sys.out_f32[v * nf + f] = make_float2((float)re, (float)im);
-                    else sys.out[(size_t)td.split * sys.split_stride + v * nf + f] = make_double2(re, im);
-                }
+        // Results from the Kahan state of all warps: 8 consecutive threads write one
+        // (shell, direction) row's frames [f0, f0 + 8) as one contiguous segment. Every
+        // (split, shell, direction, frame) slot is written, also for empty atom ranges.
+        __syncthreads();
+        {
+            const int nfr = min(kRecWarps, nf - td.f0);
+            const float4* ks_all = reinterpret_cast<const float4*>(smem + L::kKahanOffset);
+            for (int i = threadIdx.x; i < K * 32 * kRecWarps; i += kRecWarps * 32) {
+                const int w = i % kRecWarps, row = i / kRecWarps;
+                const int l = row & 31, k = row >> 5;
+                if (w >= nfr || l >= td.np) continue;
+                const int pl = td.p0 + l;
+                const int gw = pl / sys.nd, dw = pl - gw * sys.nd;
+                const RecGroup gr = a.groups[sys.g_begin + gw];
+                if (k >= gr.ks) continue;
+                const float4 st = ks_all[(w * K + k) * 32 + l];
+                const size_t v = (size_t)(gr.s0 + k) * sys.nd + dw;
+                const size_t o = v * nf + td.f0 + w;
+                const double re = (double)st.x - (double)st.z, im = (double)st.y - (double)st.w;
+                if (sys.out_f32) sys.out_f32[o] = make_float2((float)re, (float)im);
+                else sys.out[(size_t)td.split * sys.split_stride + o] = make_double2(re, im);
             }
         }
     }
