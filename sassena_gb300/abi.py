@@ -523,7 +523,7 @@ def host():
         H = ctypes.CDLL(HOST_LIB_PATH)
         H.sass_host_error.restype = ctypes.c_char_p
         H.sass_host_signal_write.argtypes = [ctypes.c_char_p, _sz, _sz, _vp, _vp, _vp, _vp, _vp,
-                                             ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p]
+                                             ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p, _sz]
         H.sass_host_signal_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(_sz),
                                             ctypes.POINTER(_sz), ctypes.POINTER(ctypes.c_int),
                                             _vp, _vp, _vp, _vp, _vp]
@@ -533,8 +533,9 @@ def host():
 
 
 def write_signal(path, qvectors, fqt=None, fq0=None, fq=None, fq2=None, rawconfig="",
-                 database=""):
-    """Write a signal.h5 (complex arrays; None = dataset not written)."""
+                 database="", chunksize=0):
+    """Write a signal.h5 (complex arrays; None = dataset not written; chunksize: rows per
+    chunk, 0 = the reference's default 10000)."""
     H = host()
     q = np.ascontiguousarray(qvectors, dtype=np.float64).reshape(-1, 3)
     nq = len(q)
@@ -550,7 +551,7 @@ def write_signal(path, qvectors, fqt=None, fq0=None, fq=None, fq2=None, rawconfi
     flags = sum(1 << i for i, a in enumerate(arrs) if a is not None)
     ptrs = [a.ctypes.data_as(_vp) if a is not None else None for a in arrs]
     rc = H.sass_host_signal_write(path.encode(), nq, nf, q.ctypes.data_as(_vp), *ptrs, flags,
-                                  rawconfig.encode(), database.encode())
+                                  rawconfig.encode(), database.encode(), chunksize)
     if rc:
         raise RuntimeError(H.sass_host_error().decode())
 

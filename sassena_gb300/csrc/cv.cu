@@ -268,39 +268,55 @@ int sass_compute_cv(sass_plan* p, sass_mlp* net, size_t nq, const double* qlen, 
     std::vector<double> G(nq);
     rc = sass_mlp_sphere_mean(net, qlen, nq, nquad ? nquad : 32768, G.data());
     if (rc) return fail(p->msg, rc, "%s", net->msg.c_str());
-    // two q-entries per shell: directions [0, h) and [h, m)
-    std::vector<size_t> offs(1, 0);
-    std::vector<double> sv(nsub * 3), cf(2 * nq * nclass);
-    for (size_t s = 0; s < nq; ++s) {
-        offs.push_back(s * m + h);
-        offs.push_back((s + 1) * m);
-        for (size_t i = 0; i < m; ++i)
-            for (int k = 0; k < 3; ++k) sv[3 * (s * m + i) + k] = qlen[s] * dirs[3 * i + k];
-        for (int half = 0; half < 2; ++half)
-            memcpy(&cf[(2 * s + half) * nclass], class_factors + s * nclass, nclass * 8);
-    }
+    // Two work items over the same trajectory: every shell's directions [0, h) (half A)
+    // and [h, m) (half B). Each half is a product set (|q_s| times one direction list), so
+    // linear shell scans take the shell-recurrence kernel. Entries: half A rows [0, nq),
+    // half B rows [nq, 2 nq); sub-vectors and sqrt(g) in the same half-major order.
     const size_t ne = 2 * nq;
+    std::vector<double> sv(nsub * 3), wsq_h(nsub);
+    std::vector<size_t> offs_half[2];
+    {
+        size_t k = 0;
+        for (int half = 0; half < 2; ++half) {
+            const size_t i0 = half ? h : 0, i1 = half ? m : h;
+            offs_half[half].push_back(0);
+            for (size_t s = 0; s < nq; ++s) {
+                for (size_t i = i0; i < i1; ++i, ++k) {
+                    for (int c = 0; c < 3; ++c) sv[3 * k + c] = qlen[s] * dirs[3 * i + c];
+                    wsq_h[k] = wsq[s * m + i];
+                }
+                offs_half[half].push_back(offs_half[half].back() + (i1 - i0));
+            }
+        }
+    }
     CK(p->msg, p->qv.ensure(sv.size() * 8));
-    CK(p->msg, p->cf.ensure(cf.size() * 8));
+    CK(p->msg, p->cf.ensure(nq * nclass * 8));
     CK(p->msg, net->wsqrt.ensure(nsub * 8));
     CK(p->msg, net->outs.ensure(2 * ne * (nf + 2) * 16));
     CK(p->msg, cudaMemcpy(p->qv.p, sv.data(), sv.size() * 8, cudaMemcpyHostToDevice));
-    CK(p->msg, cudaMemcpy(p->cf.p, cf.data(), cf.size() * 8, cudaMemcpyHostToDevice));
-    CK(p->msg, cudaMemcpy(net->wsqrt.p, wsq.data(), nsub * 8, cudaMemcpyHostToDevice));
+    CK(p->msg, cudaMemcpy(p->cf.p, class_factors, nq * nclass * 8, cudaMemcpyHostToDevice));
+    CK(p->msg, cudaMemcpy(net->wsqrt.p, wsq_h.data(), nsub * 8, cudaMemcpyHostToDevice));
     double2* o = net->outs.as<double2>();
-    std::vector<WorkItem> items(1);
-    WorkItem& it = items[0];
-    it.sys = &p->sys;
-    it.offs = offs;
-    it.d_qv = p->qv.as<double>();
-    it.d_cf = p->cf.as<double>();
-    it.d_fqt = o;
-    it.d_fq = o + ne * nf;
-    it.d_fq2 = o + ne * (nf + 1);
-    it.d_wsqrt = net->wsqrt.as<double>();
-    it.d_fqt_w = o + ne * (nf + 2);
-    it.d_fq_w = it.d_fqt_w + ne * nf;
-    it.d_fq2_w = it.d_fqt_w + ne * (nf + 1);
+    double2* ow = o + ne * (nf + 2);  // weighted block, same layout
+    std::vector<WorkItem> items(2);
+    for (int half = 0; half < 2; ++half) {
+        WorkItem& it = items[half];
+        const size_t first = half ? offs_half[0].back() : 0;  // sub-vector offset of the half
+        const size_t row = half ? nq : 0;
+        it.sys = &p->sys;
+        it.offs = offs_half[half];
+        it.d_qv = p->qv.as<double>() + 3 * first;
+        if (p->d.precision == SASS_PRECISION_FP32 && p->rec_k >= 0)
+            detect_product(sv.data() + 3 * first, it.offs, it.lam, it.lam_base);
+        it.d_cf = p->cf.as<double>();
+        it.d_fqt = o + row * nf;
+        it.d_fq = o + ne * nf + row;
+        it.d_fq2 = o + ne * nf + ne + row;
+        it.d_wsqrt = net->wsqrt.as<double>() + first;
+        it.d_fqt_w = ow + row * nf;
+        it.d_fq_w = ow + ne * nf + row;
+        it.d_fq2_w = ow + ne * nf + ne + row;
+    }
     EngineConfig cfg;
     cfg.scattering = p->d.scattering;
     cfg.dsp = p->d.dsp_type;
@@ -309,6 +325,7 @@ int sass_compute_cv(sass_plan* p, sass_mlp* net, size_t nq, const double* qlen, 
     cfg.device = p->d.device;
     cfg.shape = p->shape;
     cfg.split_atoms = p->split_atoms;
+    cfg.rec_k = p->rec_k;
     rc = p->eng.prepare(cfg, items, p->msg);
     if (rc) return rc;
     rc = p->eng.enqueue(p->st, p->msg, p->ev);
@@ -353,9 +370,9 @@ int sass_compute_cv(sass_plan* p, sass_mlp* net, size_t nq, const double* qlen, 
             mc[1] = 0.5 * (sA->y + sB->y);
         };
         for (size_t t = 0; t < nf; ++t)
-            combine(S + (2 * s) * nf + t, S + (2 * s + 1) * nf + t, W + (2 * s) * nf + t, W + (2 * s + 1) * nf + t,
+            combine(S + s * nf + t, S + (nq + s) * nf + t, W + s * nf + t, W + (nq + s) * nf + t,
                     fqt_cv + 2 * (s * nf + t), fqt_mc + 2 * (s * nf + t));
-        combine(Sq + 2 * s, Sq + 2 * s + 1, Wq + 2 * s, Wq + 2 * s + 1, fq_cv + 2 * s, fq_mc + 2 * s);
+        combine(Sq + s, Sq + nq + s, Wq + s, Wq + nq + s, fq_cv + 2 * s, fq_mc + 2 * s);
         if (diag) {
             diag[3 * s] = G[s];
             diag[3 * s + 1] = 0.5 * (gb[0] + gb[1]);

@@ -159,6 +159,7 @@ bool run_scatter_device(const Params& p, Database& db, const Sample& s, RunStats
         out.has_fq2 = p.signal_fq2;
     }
     out.nf = nf;
+    out.chunksize = p.chunksize;
     out.rawconfig = p.rawconfig;
     out.config = p.rawconfig;
     out.database = db.rawconfig;

@@ -18,13 +18,15 @@ extern "C" {
 const char* sass_host_error(void) { return g_err.c_str(); }
 
 // Write a signal file. flags: bit0 fqt, bit1 fq0, bit2 fq, bit3 fq2 (datasets written).
-// fqt [nq][nf][2], fq0/fq/fq2 [nq][2]; NULL for datasets not written.
+// fqt [nq][nf][2], fq0/fq/fq2 [nq][2]; NULL for datasets not written. chunksize: rows
+// per chunk (limits.signal.chunksize; 0 = the default 10000).
 int sass_host_signal_write(const char* path, size_t nq, size_t nf, const double* qvectors,
                            const double* fqt, const double* fq0, const double* fq, const double* fq2,
-                           int flags, const char* rawconfig, const char* database) {
+                           int flags, const char* rawconfig, const char* database, size_t chunksize) {
     try {
         SignalData d;
         d.nf = nf;
+        if (chunksize) d.chunksize = chunksize;
         for (size_t i = 0; i < nq; ++i) d.qvectors.push_back(Vec3{qvectors[3 * i], qvectors[3 * i + 1], qvectors[3 * i + 2]});
         d.has_fqt = flags & 1;
         d.has_fq0 = flags & 2;

@@ -45,6 +45,9 @@ struct DatasetSpec {
     const uint8_t* data;
     uint64_t nbytes;
     uint64_t header_addr = 0, data_addr = 0;
+    std::vector<uint64_t> chunk;       // chunked storage, unlimited first dimension (empty: contiguous)
+    std::vector<uint8_t> chunk_region;  // B-tree nodes + chunks, placed at data_addr
+    uint64_t btree_addr = kUndef;
 };
 
 struct Message {
@@ -53,7 +56,7 @@ struct Message {
     std::vector<uint8_t> data;  // unpadded
 };
 
-std::vector<uint8_t> dataspace_msg(const std::vector<uint64_t>& dims) {
+std::vector<uint8_t> dataspace_msg(const std::vector<uint64_t>& dims, bool unlimited0) {
     Out o;
     o.u8(1);                          // version 1
     o.u8(dims.size());                // dimensionality (0 = scalar)
@@ -61,7 +64,7 @@ std::vector<uint8_t> dataspace_msg(const std::vector<uint64_t>& dims) {
     o.u8(0);
     o.u32(0);
     for (uint64_t d : dims) o.u64(d);
-    for (uint64_t d : dims) o.u64(d);  // maximum = current (contiguous storage)
+    for (size_t i = 0; i < dims.size(); ++i) o.u64(i == 0 && unlimited0 ? kUndef : dims[i]);
     return o.b;
 }
 
@@ -119,6 +122,122 @@ std::vector<uint8_t> layout_msg(uint64_t addr, uint64_t size) {
     o.u8(1);  // contiguous
     o.u64(addr);
     o.u64(size);
+    return o.b;
+}
+
+// Layout message, chunked: B-tree address and chunk dimensions plus the element size.
+std::vector<uint8_t> chunked_layout_msg(uint64_t btree, const std::vector<uint64_t>& chunk, uint32_t esize) {
+    Out o;
+    o.u8(3);  // version 3
+    o.u8(2);  // chunked
+    o.u8(chunk.size() + 1);
+    o.u64(btree);
+    for (uint64_t c : chunk) o.u32(c);
+    o.u32(esize);
+    return o.b;
+}
+
+// Chunked storage of a row-major float64 dataset as libhdf5 lays it out: every chunk of
+// the chunk grid over the dataset's extent is stored whole (fill value 0 outside the
+// extent) and indexed by a version-1 B-tree of type 1 (raw data chunks) whose nodes hold
+// up to 2K = 64 entries (K = 32, the default for chunk B-trees). Nodes come first in the
+// region, then the chunks. Returns the region; `root` receives the root node's address.
+std::vector<uint8_t> chunked_region(const DatasetSpec& s, uint64_t base, uint64_t& root) {
+    constexpr int kChunkK = 32;
+    const size_t rank = s.dims.size();
+    const uint64_t es = 8;
+    uint64_t chunk_elems = 1;
+    std::vector<uint64_t> grid(rank);
+    uint64_t nchunks = 1;
+    for (size_t k = 0; k < rank; ++k) {
+        chunk_elems *= s.chunk[k];
+        grid[k] = (s.dims[k] + s.chunk[k] - 1) / s.chunk[k];
+        nchunks *= grid[k];
+    }
+    root = kUndef;
+    if (nchunks == 0) return {};
+    const uint64_t key_bytes = 8 + 8 * (rank + 1);
+    const uint64_t node_bytes = 24 + (2 * kChunkK + 1) * key_bytes + 2 * kChunkK * 8;
+    // chunk offsets (element coordinates) in row-major grid order
+    std::vector<std::vector<uint64_t>> offs(nchunks, std::vector<uint64_t>(rank));
+    for (uint64_t c = 0; c < nchunks; ++c) {
+        uint64_t r = c;
+        for (size_t k = rank; k-- > 0;) {
+            offs[c][k] = (r % grid[k]) * s.chunk[k];
+            r /= grid[k];
+        }
+    }
+    // tree shape: levels of nodes, each over at most 64 children
+    std::vector<uint64_t> level_nodes;
+    for (uint64_t n = nchunks;;) {
+        n = (n + 2 * kChunkK - 1) / (2 * kChunkK);
+        level_nodes.push_back(n);
+        if (n == 1) break;
+    }
+    uint64_t total_nodes = 0;
+    for (uint64_t n : level_nodes) total_nodes += n;
+    const uint64_t chunk_base = base + total_nodes * node_bytes;
+    Out o;
+    auto key = [&](uint64_t csize, const std::vector<uint64_t>& off) {
+        o.u32(csize);
+        o.u32(0);  // filter mask
+        for (uint64_t v : off) o.u64(v);
+        o.u64(0);  // offset in the element-size dimension
+    };
+    std::vector<uint64_t> child_addr(nchunks);
+    std::vector<std::vector<uint64_t>> child_left(offs);  // left key of every child
+    for (uint64_t c = 0; c < nchunks; ++c) child_addr[c] = chunk_base + c * chunk_elems * es;
+    std::vector<uint64_t> right = offs.back();  // right key of the last child
+    right[0] += s.chunk[0];
+    uint64_t node_addr = base;
+    for (size_t lvl = 0; lvl < level_nodes.size(); ++lvl) {
+        std::vector<uint64_t> next_addr;
+        std::vector<std::vector<uint64_t>> next_left;
+        const uint64_t nchild = child_addr.size();
+        for (uint64_t n = 0; n < level_nodes[lvl]; ++n) {
+            const uint64_t c0 = n * 2 * kChunkK, c1 = std::min(nchild, c0 + 2 * kChunkK);
+            const size_t start = o.size();
+            o.raw("TREE", 4);
+            o.u8(1);  // node type: raw data chunks
+            o.u8(lvl);
+            o.u16(c1 - c0);
+            o.u64(kUndef);
+            o.u64(kUndef);
+            for (uint64_t c = c0; c < c1; ++c) {
+                key(lvl == 0 ? chunk_elems * es : 0, child_left[c]);
+                o.u64(child_addr[c]);
+            }
+            key(0, c1 < nchild ? child_left[c1] : right);
+            o.zeros(node_bytes - (o.size() - start));
+            next_addr.push_back(node_addr);
+            next_left.push_back(child_left[c0]);
+            node_addr += node_bytes;
+        }
+        child_addr = next_addr;
+        child_left = next_left;
+    }
+    root = child_addr.front();
+    // chunks, zero outside the dataset's extent
+    const double* src = reinterpret_cast<const double*>(s.data);
+    std::vector<double> buf(chunk_elems);
+    std::vector<uint64_t> idx(rank);
+    for (uint64_t c = 0; c < nchunks; ++c) {
+        for (uint64_t e = 0; e < chunk_elems; ++e) {
+            uint64_t r = e, lin = 0;
+            bool inside = true;
+            for (size_t k = rank; k-- > 0;) {
+                idx[k] = r % s.chunk[k];
+                r /= s.chunk[k];
+            }
+            for (size_t k = 0; k < rank && inside; ++k) {
+                const uint64_t g = offs[c][k] + idx[k];
+                inside = g < s.dims[k];
+                lin = lin * s.dims[k] + g;
+            }
+            buf[e] = inside ? src[lin] : 0.0;
+        }
+        o.raw(buf.data(), chunk_elems * es);
+    }
     return o.b;
 }
 
@@ -432,15 +551,22 @@ void write_signal_file(const std::string& path, const SignalData& d) {
         for (int k = 0; k < 3; ++k) q[3 * i + k] = d.qvectors[i][k];
     if (d.has_fqt && d.fqt.size() != nq * d.nf * 2) throw std::runtime_error("fqt has the wrong size");
     std::vector<DatasetSpec> root_ds;
-    auto f64 = [&](const char* name, const std::vector<double>& v, std::vector<uint64_t> dims) {
-        root_ds.push_back(DatasetSpec{name, F64, dims, reinterpret_cast<const uint8_t*>(v.data()),
-                                      v.size() * 8});
+    auto f64 = [&](const char* name, const std::vector<double>& v, std::vector<uint64_t> dims,
+                   std::vector<uint64_t> chunk) {
+        DatasetSpec ds{name, F64, dims, reinterpret_cast<const uint8_t*>(v.data()), v.size() * 8};
+        ds.chunk = chunk;
+        root_ds.push_back(ds);
     };
-    f64("qvectors", q, {nq, 3});
-    if (d.has_fqt) f64("fqt", d.fqt, {nq, d.nf, 2});
-    if (d.has_fq0) f64("fq0", d.fq0, {nq, 2});
-    if (d.has_fq) f64("fq", d.fq, {nq, 2});
-    if (d.has_fq2) f64("fq2", d.fq2, {nq, 2});
+    // chunk shapes and unlimited first dimension as the reference's writer creates them
+    // (file_writer_service.cpp:68-159): rows of `chunksize`; fqt splits the chunk between
+    // rows and frames when NF < chunksize
+    const uint64_t cs = std::max<size_t>(d.chunksize, 1);
+    const uint64_t c2 = (d.nf > 0 && d.nf < cs) ? d.nf : cs, c1 = std::max<uint64_t>(cs / c2, 1);
+    f64("qvectors", q, {nq, 3}, {cs, 3});
+    if (d.has_fqt) f64("fqt", d.fqt, {nq, d.nf, 2}, {c1, c2, 2});
+    if (d.has_fq0) f64("fq0", d.fq0, {nq, 2}, {cs, 2});
+    if (d.has_fq) f64("fq", d.fq, {nq, 2}, {cs, 2});
+    if (d.has_fq2) f64("fq2", d.fq2, {nq, 2}, {cs, 2});
     std::string cfg = d.config + '\0', db = d.database + '\0';
     std::vector<DatasetSpec> meta_ds = {
         {"config", STR, {}, reinterpret_cast<const uint8_t*>(cfg.data()), cfg.size()},
@@ -470,10 +596,11 @@ void write_signal_file(const std::string& path, const SignalData& d) {
     pos += meta.bytes();
     auto ds_messages = [](const DatasetSpec& s) {
         std::vector<Message> m;
-        m.push_back({0x0001, 0, dataspace_msg(s.dims)});
+        m.push_back({0x0001, 0, dataspace_msg(s.dims, !s.chunk.empty())});
         m.push_back({0x0003, 1, datatype_msg(s.kind, s.nbytes)});
         m.push_back({0x0005, 1, fill_msg(s.kind)});
-        m.push_back({0x0008, 0, layout_msg(s.data_addr, s.nbytes)});
+        if (s.chunk.empty()) m.push_back({0x0008, 0, layout_msg(s.data_addr, s.nbytes)});
+        else m.push_back({0x0008, 0, chunked_layout_msg(s.btree_addr, s.chunk, 8)});
         return m;
     };
     std::vector<DatasetSpec*> all;
@@ -485,6 +612,12 @@ void write_signal_file(const std::string& path, const SignalData& d) {
     }
     for (DatasetSpec* s : all) {
         pos = (pos + 7) & ~(uint64_t)7;
+        if (!s->chunk.empty()) {
+            s->chunk_region = chunked_region(*s, pos, s->btree_addr);
+            s->data_addr = s->chunk_region.empty() ? kUndef : pos;
+            pos += s->chunk_region.size();
+            continue;
+        }
         s->data_addr = s->nbytes ? pos : kUndef;
         pos += s->nbytes;
     }
@@ -541,6 +674,11 @@ void write_signal_file(const std::string& path, const SignalData& d) {
     }
     for (DatasetSpec* s : all) {
         o.pad8();
+        if (!s->chunk.empty()) {
+            if (!s->chunk_region.empty() && o.size() != s->data_addr) throw std::logic_error("chunk placement");
+            o.raw(s->chunk_region.data(), s->chunk_region.size());
+            continue;
+        }
         if (s->nbytes && o.size() != s->data_addr) throw std::logic_error("data placement");
         o.raw(s->data, s->nbytes);
     }

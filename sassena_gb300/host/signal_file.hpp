@@ -7,10 +7,12 @@
 // each of fqt, fq0, fq, fq2 only if its scattering.signal.* flag is set, rows in
 // completion order. This module writes the same names, shapes, element types and
 // row order in the HDF5 file format's classic encoding (superblock version 0,
-// symbol-table groups, version-1 object headers, contiguous data). Appending rewrites
-// the file with the new rows after the old ones. The reader understands that
-// encoding and the chunked (version-1 B-tree) datasets the reference's writer
-// creates, so a run can resume from either.
+// symbol-table groups, version-1 object headers). Like the reference's writer, the
+// root datasets are chunked with an unlimited first dimension (rows of
+// limits.signal.chunksize, a version-1 B-tree chunk index); the /meta datasets are
+// contiguous. Appending rewrites the file with the new rows after the old ones. The
+// reader understands contiguous and chunked datasets, so a run can resume from a file
+// written by either program.
 #pragma once
 
 #include <string>
@@ -22,6 +24,7 @@ namespace sassgpu {
 
 struct SignalData {
     size_t nf = 0;
+    size_t chunksize = 10000;  // limits.signal.chunksize (rows per chunk)
     std::vector<Vec3> qvectors;
     bool has_fqt = true, has_fq0 = true, has_fq = true, has_fq2 = true;
     std::vector<double> fqt;  // [NQ][NF][2]

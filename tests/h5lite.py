@@ -129,6 +129,8 @@ class File:
                 ver, rank, fl = d[0], d[1], d[2]
                 off = 8 if ver == 1 else 4
                 shape = tuple(struct.unpack_from("<%dQ" % rank, d, off)) if rank else ()
+                maxdims = (tuple(struct.unpack_from("<%dQ" % rank, d, off + 8 * rank))
+                           if rank and fl & 1 else shape)
             elif t == 0x03:
                 cls, size = d[0] & 0x0F, struct.unpack_from("<I", d, 4)[0]
                 if cls == 1 and size == 8:
@@ -157,6 +159,9 @@ class File:
                 raise H5Error("filters not supported")
         if shape is None or dtype is None or layout is None:
             raise H5Error("dataset header incomplete")
+        self.last_info = {"shape": shape, "maxdims": maxdims, "layout": layout[0],
+                          "chunk": tuple(layout[2]) if layout[0] == "chunked" else None,
+                          "btree": layout[1] if layout[0] == "chunked" else None}
         n = int(np.prod(shape)) if shape else 1
         if layout[0] == "contiguous":
             a, size = layout[1], layout[2]
@@ -169,27 +174,50 @@ class File:
         else:
             arr = np.zeros(n, dtype=dtype)
             bt, cd = layout[1], layout[2][:-1]
-            self._chunks(bt, len(shape), cd, shape, arr, dtype)
+            if layout[2][-1] != dtype.itemsize:
+                raise H5Error("chunk element size %d" % layout[2][-1])
+            if bt != UNDEF:
+                self.tree_depth = 0
+                self._chunks(bt, len(shape), cd, shape, arr, dtype)
+            elif n:
+                raise H5Error("chunked dataset with rows but no chunk index")
         return arr.reshape(shape) if shape else arr[0]
 
-    def _chunks(self, node, rank, cd, shape, arr, dtype):
+    def _chunks(self, node, rank, cd, shape, arr, dtype, depth=0):
         b = self.b
         if b[node:node + 4] != b"TREE" or b[node + 4] != 1:
             raise H5Error("bad chunk B-tree node")
         level, used = b[node + 5], struct.unpack_from("<H", b, node + 6)[0]
+        self.tree_depth = max(self.tree_depth, depth + 1)
+        if used > 64:
+            raise H5Error("chunk B-tree node over-full (%d > 2K = 64)" % used)
         kb = 8 + 8 * (rank + 1)
         full = arr.reshape(shape)
+        keys = [struct.unpack_from("<%dQ" % rank, b, node + 24 + i * (kb + 8) + 8)
+                for i in range(used + 1)]
+        if any(keys[i] >= keys[i + 1] for i in range(used)):
+            raise H5Error("chunk B-tree keys not increasing")
         for i in range(used):
             k = node + 24 + i * (kb + 8)
             child = struct.unpack_from("<Q", b, k + kb)[0]
             if level:
-                self._chunks(child, rank, cd, shape, arr, dtype)
+                first = struct.unpack_from("<%dQ" % rank, b, child + 24 + 8)
+                if first != keys[i]:
+                    raise H5Error("internal chunk key differs from the child's first key")
+                self._chunks(child, rank, cd, shape, arr, dtype, depth + 1)
                 continue
+            if struct.unpack_from("<I", b, k)[0] != int(np.prod(cd)) * dtype.itemsize:
+                raise H5Error("chunk size field")
             offs = struct.unpack_from("<%dQ" % rank, b, k + 8)
             cnt = int(np.prod(cd))
             chunk = np.frombuffer(b[child:child + cnt * dtype.itemsize], dtype=dtype).reshape(cd)
             sl = tuple(slice(o, min(o + c, s)) for o, c, s in zip(offs, cd, shape))
             full[sl] = chunk[tuple(slice(0, s.stop - s.start) for s in sl)]
+
+    def info(self, path):
+        """Shape, maximum dimensions, layout and chunk dimensions of a dataset."""
+        self.read(path)
+        return self.last_info
 
     def read(self, path):
         parts = [p for p in path.split("/") if p]

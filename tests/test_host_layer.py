@@ -53,6 +53,55 @@ def test_signal_roundtrip_and_structure(tmp_path):
     assert raw.dtype == np.int8 and raw.tobytes() == b"<root>cfg</root>"
 
 
+def test_signal_chunked_like_reference(tmp_path):
+    # root datasets: chunked, unlimited first dimension, the reference's chunk shapes
+    # (file_writer_service.cpp:68-159); /meta stays contiguous
+    rng = np.random.default_rng(1)
+    nq, nf = 5, 13
+    q = rng.normal(size=(nq, 3))
+    fqt = rng.normal(size=(nq, nf)) + 1j * rng.normal(size=(nq, nf))
+    path = str(tmp_path / "c.h5")
+    abi.write_signal(path, q, fqt, fqt[:, 0], fqt[:, 1], fqt[:, 2])
+    f = h5lite.File(path)
+    unlimited = 0xFFFFFFFFFFFFFFFF
+    qi = f.info("qvectors")
+    assert qi["layout"] == "chunked" and qi["chunk"] == (10000, 3, 8)
+    assert qi["maxdims"] == (unlimited, 3) and qi["shape"] == (nq, 3)
+    ti = f.info("fqt")
+    assert ti["chunk"] == (10000 // nf, nf, 2, 8) and ti["maxdims"] == (unlimited, nf, 2)
+    for n in ("fq0", "fq", "fq2"):
+        assert f.info(n)["chunk"] == (10000, 2, 8)
+    assert f.info("meta/rawconfig")["layout"] == "contiguous"
+    got = f.read("fqt")
+    assert np.array_equal(got[..., 0] + 1j * got[..., 1], fqt)
+
+
+def test_signal_multilevel_chunk_index(tmp_path):
+    # small chunks: 300 rows of qvectors in 75 chunks (two-level B-tree); fqt with NF above
+    # the chunk size is chunked along frames too (1 x 4 x 2 chunks, 600 of them)
+    rng = np.random.default_rng(2)
+    nq, nf = 300, 5
+    q = rng.normal(size=(nq, 3))
+    fqt = rng.normal(size=(nq, nf)) + 1j * rng.normal(size=(nq, nf))
+    fq = rng.normal(size=nq) + 1j * rng.normal(size=nq)
+    path = str(tmp_path / "m.h5")
+    abi.write_signal(path, q, fqt, fqt[:, 0], fq, fq, chunksize=4)
+    f = h5lite.File(path)
+    assert np.array_equal(f.read("qvectors"), q)
+    assert f.tree_depth == 2
+    got = f.read("fqt")
+    assert f.info("fqt")["chunk"] == (1, 4, 2, 8) and f.tree_depth == 2
+    assert np.array_equal(got[..., 0] + 1j * got[..., 1], fqt)
+    d = abi.read_signal(path)
+    assert np.array_equal(d["fqt"], fqt) and np.array_equal(d["fq"], fq)
+    # zero rows: no chunk index at all
+    empty = str(tmp_path / "e.h5")
+    abi.write_signal(empty, np.zeros((0, 3)), np.zeros((0, nf), complex), np.zeros(0, complex),
+                     np.zeros(0, complex), np.zeros(0, complex))
+    assert h5lite.File(empty).read("fqt").shape == (0, nf, 2)
+    assert abi.read_signal(empty)["qvectors"].shape == (0, 3)
+
+
 def test_signal_optional_datasets(tmp_path):
     path = str(tmp_path / "s.h5")
     abi.write_signal(path, np.ones((2, 3)), fqt=None, fq0=None, fq=np.array([1 + 2j, 3]),
