@@ -199,15 +199,19 @@ int autotune_engine(std::string& m, Engine& eng, const EngineConfig& base, const
         if (rc) return rc;
         if (ms >= 0 && ms < best_ms) {
             best_ms = ms;
-            best.shape = c.shape;
+            // the shape the engine resolved (an automatic shape depends on the items, so a
+            // choice made on a representative subset must name the shape it timed)
+            best.shape = eng.stats().shape;
             best.split_atoms = c.split_atoms;
             best.rec_k = c.rec_k;
             any = true;
         }
         return SASS_OK;
     };
+    // the recurrence widths are worth timing only where some shells form runs
     bool product = false;
-    for (const WorkItem& it : items) product = product || !it.lam.empty();
+    for (const WorkItem& it : items)
+        product = product || (!it.lam.empty() && !arithmetic_runs(it.lam, 3).empty());
     int rec_k = -1;
     bool all_rec = false;
     if (base.precision == PREC_FP32 && product) {
