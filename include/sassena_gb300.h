@@ -144,6 +144,13 @@ int sass_last_timing(const sass_plan* plan, sass_timing* out);
  * this build does not instantiate. */
 int sass_set_phase_tile(sass_plan* plan, int q_per_lane, int warps, int atoms, int atom_splits);
 
+/* FP32 direct kernel: pairs of each lane's q-vectors whose sin/cos are evaluated on the
+ * FP32 pipe (Taylor series of the half angle and the double-angle formulas, truncation
+ * below 6e-8) instead of the SFU, so that both units carry load; 0 = all on the SFU. Needs
+ * the explicit tile shape set by sass_set_phase_tile to instantiate that split
+ * (SASS_ERR_UNSUPPORTED otherwise). No counterpart in the reference (libm sin/cos). */
+int sass_set_phase_poly(sass_plan* plan, int poly_pairs);
+
 /* Frame centre used by the FP32 form (frame-0 bounding-box midpoint). */
 int sass_frame_center(const sass_plan* plan, double* center3);
 
@@ -165,6 +172,7 @@ typedef struct sass_schedule {
     int rec_shells_per_lane;       /* 0: recurrence not used */
     int q_per_lane, warps, atoms;  /* direct kernel tile shape */
     int atom_splits;               /* largest atom-split count */
+    int poly_pairs;                /* direct kernel: q-vector pairs per lane on the FP32 pipe */
 } sass_schedule;
 int sass_plan_schedule(const sass_plan* plan, sass_schedule* out);
 
@@ -208,6 +216,8 @@ int sass_batch_info(const sass_batch* batch, double* terms, uint64_t* phase_tile
                     int* warps, int* atoms, int* split_atoms);
 /* Shell recurrence for the batch (as sass_set_shell_recurrence) and its schedule. */
 int sass_batch_set_shell_recurrence(sass_batch* batch, int shells_per_lane);
+/* Polynomial sin/cos pairs of the batch's tile shape (as sass_set_phase_poly). */
+int sass_batch_set_phase_poly(sass_batch* batch, int poly_pairs);
 int sass_batch_schedule(const sass_batch* batch, sass_schedule* out);
 const char* sass_batch_error(const sass_batch* batch);
 void sass_batch_destroy(sass_batch* batch);

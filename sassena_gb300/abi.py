@@ -36,7 +36,7 @@ EXPORTS = [
     "sass_mlp_set_scaling", "sass_mlp_get_params", "sass_mlp_set_params", "sass_mlp_gradient",
     "sass_mlp_train", "sass_mlp_predict", "sass_mlp_sphere_mean", "sass_compute_cv",
     "sass_set_shell_recurrence", "sass_plan_schedule", "sass_batch_set_shell_recurrence",
-    "sass_batch_schedule",
+    "sass_batch_schedule", "sass_set_phase_poly", "sass_batch_set_phase_poly",
 ]
 
 
@@ -76,7 +76,8 @@ class Schedule(ctypes.Structure):
     _fields_ = [("terms", ctypes.c_double), ("direct_tiles", ctypes.c_uint64),
                 ("rec_tiles", ctypes.c_uint64), ("rec_shells", ctypes.c_uint64),
                 ("rec_shells_per_lane", ctypes.c_int), ("q_per_lane", ctypes.c_int),
-                ("warps", ctypes.c_int), ("atoms", ctypes.c_int), ("atom_splits", ctypes.c_int)]
+                ("warps", ctypes.c_int), ("atoms", ctypes.c_int), ("atom_splits", ctypes.c_int),
+                ("poly_pairs", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -153,6 +154,8 @@ def load(path=LIB_PATH):
     L.sass_plan_schedule.argtypes = [_vp, ctypes.POINTER(Schedule)]
     L.sass_batch_set_shell_recurrence.argtypes = [_vp, ctypes.c_int]
     L.sass_batch_schedule.argtypes = [_vp, ctypes.POINTER(Schedule)]
+    L.sass_set_phase_poly.argtypes = [_vp, ctypes.c_int]
+    L.sass_batch_set_phase_poly.argtypes = [_vp, ctypes.c_int]
     _lib = L
     return L
 
@@ -221,6 +224,10 @@ class Plan:
 
     def set_tile(self, q_per_lane=0, warps=0, atoms=0, atom_splits=0):
         self._check(self.lib.sass_set_phase_tile(self._h, q_per_lane, warps, atoms, atom_splits))
+
+    def set_poly(self, poly_pairs):
+        """Pairs of each lane's q-vectors whose sin/cos use the FP32 pipe (direct kernel)."""
+        self._check(self.lib.sass_set_phase_poly(self._h, poly_pairs))
 
     def set_recurrence(self, shells_per_lane=0):
         """Shell recurrence of the FP32 form: 0 automatic, -1 off, else 4/8/12/16/20/24/32."""
@@ -352,6 +359,9 @@ class Batch:
 
     def set_recurrence(self, shells_per_lane=0):
         self._check(self.lib.sass_batch_set_shell_recurrence(self._h, shells_per_lane))
+
+    def set_poly(self, poly_pairs):
+        self._check(self.lib.sass_batch_set_phase_poly(self._h, poly_pairs))
 
     def schedule(self):
         s = Schedule()

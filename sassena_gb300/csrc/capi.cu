@@ -278,6 +278,7 @@ void fill_schedule(const EngineStats& s, sass_schedule* out) {
     out->warps = s.shape.warps;
     out->atoms = s.shape.atoms;
     out->atom_splits = s.max_split;
+    out->poly_pairs = s.phase_tiles ? s.shape.poly_pairs : 0;
 }
 
 std::string signature(const sass_plan_desc& d, const std::vector<WorkItem>& items) {
@@ -388,6 +389,17 @@ int sass_frame_center(const sass_plan* p, double* c) {
 }
 
 static bool rec_width_ok(int k) { return k == 0 || k == -1 || rec_shells_supported(k); }
+
+int sass_set_phase_poly(sass_plan* p, int poly_pairs) {
+    if (!p) return SASS_ERR_ARG;
+    PhaseShape t = p->shape;
+    t.poly_pairs = poly_pairs;
+    if (poly_pairs != 0 && (t.q_per_lane == 0 || !phase_shape_supported(p->d.precision, t)))
+        return set_msg(p->msg, SASS_ERR_UNSUPPORTED, "no instantiated tile shape Q=%d W=%d T=%d with %d polynomial pairs",
+                       t.q_per_lane, t.warps, t.atoms, poly_pairs);
+    p->shape.poly_pairs = poly_pairs;
+    return SASS_OK;
+}
 
 int sass_set_shell_recurrence(sass_plan* p, int shells_per_lane) {
     if (!p) return SASS_ERR_ARG;
@@ -899,6 +911,19 @@ int sass_batch_set_shell_recurrence(sass_batch* b, int shells_per_lane) {
     if (!rec_width_ok(shells_per_lane))
         return set_msg(b->msg, SASS_ERR_UNSUPPORTED, "shell recurrence width %d not instantiated", shells_per_lane);
     b->rec_k = shells_per_lane;
+    b->prepared = false;
+    drop_graph(b);
+    return SASS_OK;
+}
+
+int sass_batch_set_phase_poly(sass_batch* b, int poly_pairs) {
+    if (!b) return SASS_ERR_ARG;
+    PhaseShape t = b->shape;
+    t.poly_pairs = poly_pairs;
+    if (poly_pairs != 0 && (t.q_per_lane == 0 || !phase_shape_supported(b->d.precision, t)))
+        return set_msg(b->msg, SASS_ERR_UNSUPPORTED, "no instantiated tile shape Q=%d W=%d T=%d with %d polynomial pairs",
+                       t.q_per_lane, t.warps, t.atoms, poly_pairs);
+    b->shape.poly_pairs = poly_pairs;
     b->prepared = false;
     drop_graph(b);
     return SASS_OK;

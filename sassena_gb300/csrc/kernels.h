@@ -31,11 +31,13 @@ constexpr int kMaxLg = 13;
 // ---------------------------------------------------------------------------------------
 // Phase sum
 // ---------------------------------------------------------------------------------------
-// Tile shape: q-vectors per lane, warps (= frames) per CTA, atoms per pipeline stage.
+// Tile shape: q-vectors per lane, warps (= frames) per CTA, atoms per pipeline stage, and
+// (FP32 form) pairs of a lane's q-vectors whose sin/cos are evaluated on the FP32 pipe.
 struct PhaseShape {
     int q_per_lane;
     int warps;
     int atoms;
+    int poly_pairs;
 };
 
 struct PhaseSystem {

@@ -57,7 +57,8 @@ __device__ __forceinline__ void issue_stage(float4* sx, void* sb, uint64_t* bar,
     bulk_g2s(sb, src_b, T * BBYTES, bar);
 }
 
-template <int Q>
+// FP32 form, Q = 1: one sub-vector per lane, scalar arithmetic.
+template <int Q, int PP>
 struct Fp32Acc {
     float qx[Q], qy[Q], qz[Q], sr[Q], si[Q], cr[Q], ci[Q];
     __device__ void load_q(const double* qv, int v0, int nv, int lane) {
@@ -115,6 +116,113 @@ struct Fp32Acc {
     }
 };
 
+// sin and cos of 2 pi f for a pair of reduced angles f in [-1/2, 1/2] revolutions on the
+// FP32 pipe instead of the SFU: Taylor series of the half angle h = pi f in
+// [-pi/2, pi/2] (sin through h^11, cos through h^12: truncation below 6e-8) and the
+// double-angle formulas sin 2h = 2 sin h cos h, cos 2h = cos^2 h - sin^2 h (absolute error
+// below 4.3e-7 over the range in float32, under the SFU approximation's 2^-21). Returns
+// (cos 2h) and (sin h cos h) = (sin 2h) / 2.
+__device__ __forceinline__ void sincos2_poly(float2 f, float2& c2h, float2& shch) {
+    const float2 kPi = make_float2(3.14159265358979323846f, 3.14159265358979323846f);
+    const float2 h = __fmul2_rn(f, kPi);
+    const float2 h2 = __fmul2_rn(h, h);
+    auto cst = [](float v) { return make_float2(v, v); };
+    float2 ps = __ffma2_rn(cst(-1.f / 39916800.f), h2, cst(1.f / 362880.f));
+    ps = __ffma2_rn(ps, h2, cst(-1.f / 5040.f));
+    ps = __ffma2_rn(ps, h2, cst(1.f / 120.f));
+    ps = __ffma2_rn(ps, h2, cst(-1.f / 6.f));
+    ps = __ffma2_rn(ps, h2, cst(1.f));
+    const float2 sh = __fmul2_rn(ps, h);
+    float2 pc = __ffma2_rn(cst(1.f / 479001600.f), h2, cst(-1.f / 3628800.f));
+    pc = __ffma2_rn(pc, h2, cst(1.f / 40320.f));
+    pc = __ffma2_rn(pc, h2, cst(-1.f / 720.f));
+    pc = __ffma2_rn(pc, h2, cst(1.f / 24.f));
+    pc = __ffma2_rn(pc, h2, cst(-0.5f));
+    const float2 ch = __ffma2_rn(pc, h2, cst(1.f));
+    shch = __fmul2_rn(sh, ch);
+    c2h = __ffma2_rn(ch, ch, __fmul2_rn(__fmul2_rn(sh, cst(-1.f)), sh));
+}
+
+// FP32 form, even Q: sub-vectors in pairs (lane + 32 (2j), lane + 32 (2j + 1)) evaluated
+// with paired FP32 operations (FFMA2/FADD2/FMUL2). The last PP pairs take sin/cos from
+// sincos2_poly on the FP32 pipe, the others from the SFU, so both units carry load.
+template <int Q, int PP>
+struct Fp32PairAcc {
+    static constexpr int NP = Q / 2;
+    static_assert(Q % 2 == 0 && PP <= NP, "pairs");
+    float2 qx[NP], qy[NP], qz[NP], sr[NP], si[NP], cr[NP], ci[NP];
+    __device__ void load_q(const double* qv, int v0, int nv, int lane) {
+        const double inv2pi = 0.15915494309189533577;
+#pragma unroll
+        for (int j = 0; j < NP; ++j) {
+            float q[2][3];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int vl = lane + 32 * (2 * j + h);
+                const double* p = qv + 3 * (size_t)(v0 + vl);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) q[h][c] = vl < nv ? (float)(p[c] * inv2pi) : 0.f;
+            }
+            qx[j] = make_float2(q[0][0], q[1][0]);
+            qy[j] = make_float2(q[0][1], q[1][1]);
+            qz[j] = make_float2(q[0][2], q[1][2]);
+            sr[j] = si[j] = cr[j] = ci[j] = make_float2(0.f, 0.f);
+        }
+    }
+    template <int T>
+    __device__ __forceinline__ void stage(const float4* cx, const float* cb) {
+        const float2 kM = make_float2(12582912.0f, 12582912.0f), kNM = make_float2(-12582912.0f, -12582912.0f);
+        const float2 kNeg = make_float2(-1.f, -1.f);
+        const float2 kTwoPi = make_float2(6.28318530717958647692f, 6.28318530717958647692f);
+        float2 tr[NP], ti[NP];
+#pragma unroll
+        for (int j = 0; j < NP; ++j) tr[j] = ti[j] = make_float2(0.f, 0.f);
+#pragma unroll 2
+        for (int jj = 0; jj < T; ++jj) {
+            const float4 r = cx[jj];
+            const float2 rx = make_float2(r.x, r.x), ry = make_float2(r.y, r.y), rz = make_float2(r.z, r.z);
+            const float2 b = make_float2(cb[jj], cb[jj]);
+            const float2 b2 = __fadd2_rn(b, b);
+#pragma unroll
+            for (int j = 0; j < NP; ++j) {
+                const float2 u = __ffma2_rn(rz, qz[j], __ffma2_rn(ry, qy[j], __fmul2_rn(rx, qx[j])));
+                const float2 n = __fadd2_rn(__fadd2_rn(u, kM), kNM);  // rint(u)
+                const float2 fr = __ffma2_rn(n, kNeg, u);              // u - n in [-1/2, 1/2], exact
+                if (j < NP - PP) {
+                    const float2 x = __fmul2_rn(fr, kTwoPi);
+                    float s0, c0, s1, c1;
+                    __sincosf(x.x, &s0, &c0);
+                    __sincosf(x.y, &s1, &c1);
+                    tr[j] = __ffma2_rn(b, make_float2(c0, c1), tr[j]);
+                    ti[j] = __ffma2_rn(b, make_float2(s0, s1), ti[j]);
+                } else {
+                    float2 c, sc;
+                    sincos2_poly(fr, c, sc);
+                    tr[j] = __ffma2_rn(b, c, tr[j]);
+                    ti[j] = __ffma2_rn(b2, sc, ti[j]);
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < NP; ++j) {  // Kahan: fold the stage sums into (s, c)
+            float2 y = __ffma2_rn(cr[j], kNeg, tr[j]);
+            float2 t = __fadd2_rn(sr[j], y);
+            cr[j] = __ffma2_rn(y, kNeg, __ffma2_rn(sr[j], kNeg, t));
+            sr[j] = t;
+            y = __ffma2_rn(ci[j], kNeg, ti[j]);
+            t = __fadd2_rn(si[j], y);
+            ci[j] = __ffma2_rn(y, kNeg, __ffma2_rn(si[j], kNeg, t));
+            si[j] = t;
+        }
+    }
+    __device__ double2 result(int k) const {
+        const int j = k >> 1;
+        const float s_r = (k & 1) ? sr[j].y : sr[j].x, c_r = (k & 1) ? cr[j].y : cr[j].x;
+        const float s_i = (k & 1) ? si[j].y : si[j].x, c_i = (k & 1) ? ci[j].y : ci[j].x;
+        return make_double2((double)s_r - (double)c_r, (double)s_i - (double)c_i);
+    }
+};
+
 template <int Q>
 struct Fp64Acc {
     double qx[Q], qy[Q], qz[Q], ar[Q], ai[Q];
@@ -153,25 +261,30 @@ struct Fp64Acc {
     __device__ double2 result(int k) const { return make_double2(ar[k], ai[k]); }
 };
 
-template <bool F32, int Q>
+template <bool F32, int Q, int PP, bool PAIRED = (Q % 2 == 0)>
 struct AccSel;
-template <int Q>
-struct AccSel<true, Q> {
-    typedef Fp32Acc<Q> type;
+template <int Q, int PP>
+struct AccSel<true, Q, PP, false> {
+    typedef Fp32Acc<Q, PP> type;
     typedef float B;
 };
-template <int Q>
-struct AccSel<false, Q> {
+template <int Q, int PP>
+struct AccSel<true, Q, PP, true> {
+    typedef Fp32PairAcc<Q, PP> type;
+    typedef float B;
+};
+template <int Q, int PP, bool PAIRED>
+struct AccSel<false, Q, PP, PAIRED> {
     typedef Fp64Acc<Q> type;
     typedef double B;
 };
 
-template <bool F32, int Q, int W, int T, int S>
+template <bool F32, int Q, int W, int T, int S, int PP>
 __global__ void __launch_bounds__(W * 32)
     phase_sum_kernel(const PhaseSystem* __restrict__ systems, const PhaseTileDesc* __restrict__ tiles,
                      int ntiles, unsigned int* __restrict__ counter, unsigned int* err) {
-    typedef typename AccSel<F32, Q>::type Acc;
-    typedef typename AccSel<F32, Q>::B B;
+    typedef typename AccSel<F32, Q, PP>::type Acc;
+    typedef typename AccSel<F32, Q, PP>::B B;
     constexpr int BB = sizeof(B);
     using L = PipeLayout<W, T, S, BB>;
     static_assert(S * T >= 32 * Q, "output staging must fit in the coordinate ring");
@@ -288,9 +401,9 @@ __global__ void split_reduce_kernel(const double2* __restrict__ part, int nsplit
     }
 }
 
-template <bool F32, int Q, int W, int T, int S>
+template <bool F32, int Q, int W, int T, int S, int PP>
 cudaError_t launch_tiles(const PhaseLaunch& a, cudaStream_t st) {
-    auto k = phase_sum_kernel<F32, Q, W, T, S>;
+    auto k = phase_sum_kernel<F32, Q, W, T, S, PP>;
     const int smem = PipeLayout<W, T, S, F32 ? 4 : 8>::kBytes;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
@@ -310,14 +423,16 @@ cudaError_t launch_tiles(const PhaseLaunch& a, cudaStream_t st) {
 
 }  // namespace
 
-// Instantiated tile shapes (q per lane, warps = frames per CTA, atoms per stage).
-#define SASS_FP32_SHAPES(X) \
-    X(1, 8, 128) X(2, 8, 128) X(4, 8, 128) X(8, 8, 128) X(4, 4, 128) X(8, 4, 128) X(2, 8, 64) X(4, 8, 64)
-#define SASS_FP64_SHAPES(X) X(1, 4, 64) X(2, 4, 64) X(2, 8, 64)
+// Instantiated tile shapes (q per lane, warps = frames per CTA, atoms per stage, pairs of
+// q-vectors whose sin/cos come from the FP32 pipe instead of the SFU).
+#define SASS_FP32_SHAPES(X)                                                                  \
+    X(1, 8, 128, 0) X(2, 8, 128, 0) X(4, 8, 128, 0) X(8, 8, 128, 0) X(8, 8, 128, 1) X(4, 4, 128, 0) \
+        X(8, 4, 128, 0) X(8, 4, 128, 1) X(2, 8, 64, 0) X(4, 8, 64, 0)
+#define SASS_FP64_SHAPES(X) X(1, 4, 64, 0) X(2, 4, 64, 0) X(2, 8, 64, 0)
 
 bool phase_shape_supported(int precision, PhaseShape t) {
-#define CHECK(Q, W, T) \
-    if (t.q_per_lane == Q && t.warps == W && t.atoms == T) return true;
+#define CHECK(Q, W, T, PP) \
+    if (t.q_per_lane == Q && t.warps == W && t.atoms == T && t.poly_pairs == PP) return true;
     if (precision == PREC_FP32) {
         SASS_FP32_SHAPES(CHECK)
     } else {
@@ -329,7 +444,7 @@ bool phase_shape_supported(int precision, PhaseShape t) {
 
 std::vector<PhaseShape> phase_shapes(int precision) {
     std::vector<PhaseShape> v;
-#define ADD(Q, W, T) v.push_back(PhaseShape{Q, W, T});
+#define ADD(Q, W, T, PP) v.push_back(PhaseShape{Q, W, T, PP});
     if (precision == PREC_FP32) {
         SASS_FP32_SHAPES(ADD)
     } else {
@@ -342,10 +457,12 @@ std::vector<PhaseShape> phase_shapes(int precision) {
 cudaError_t launch_phase_sum(const PhaseLaunch& a, cudaStream_t st) {
     if (a.ntiles <= 0) return cudaSuccess;
     const PhaseShape& t = a.shape;
-#define L32(Q, W, T) \
-    if (t.q_per_lane == Q && t.warps == W && t.atoms == T) return launch_tiles<true, Q, W, T, 2>(a, st);
-#define L64(Q, W, T) \
-    if (t.q_per_lane == Q && t.warps == W && t.atoms == T) return launch_tiles<false, Q, W, T, 2>(a, st);
+#define L32(Q, W, T, PP)                                                                       \
+    if (t.q_per_lane == Q && t.warps == W && t.atoms == T && t.poly_pairs == PP)               \
+        return launch_tiles<true, Q, W, T, 2, PP>(a, st);
+#define L64(Q, W, T, PP)                                                                       \
+    if (t.q_per_lane == Q && t.warps == W && t.atoms == T && t.poly_pairs == PP)               \
+        return launch_tiles<false, Q, W, T, 2, PP>(a, st);
     if (a.precision == PREC_FP32) {
         SASS_FP32_SHAPES(L32)
     } else {

@@ -108,6 +108,30 @@ def test_amplitudes_and_atom_splits(native_lib, precision, splits):
     assert err <= (1e-13 if precision == "fp64" else 2e-5), err
 
 
+FP32_SHAPES = [(1, 8, 128, 0), (2, 8, 128, 0), (4, 8, 128, 0), (8, 8, 128, 0), (8, 8, 128, 1),
+               (4, 4, 128, 0), (8, 4, 128, 0), (8, 4, 128, 1), (2, 8, 64, 0), (4, 8, 64, 0)]
+
+
+@pytest.mark.parametrize("shape", FP32_SHAPES)
+def test_fp32_direct_shapes(native_lib, shape):
+    # every instantiated FP32 tile of the direct kernel: scalar (Q=1), paired SFU, and paired
+    # with one pair of polynomial sin/cos per lane, on ragged sizes
+    w = synth.small("all", "autocorrelate", seed=17, na=450, nf=21, nq=3, nm=70, box=25.0)
+    sv = w.subvectors()
+    shell = np.repeat(np.arange(w.nq), w.nm).astype(np.int32)
+    ref = oracle.amplitudes(w.coords, sv, shell.astype(np.uintp), w.factors(), nthreads=8)
+    with abi.Plan(w.na, w.nf, len(w.class_names), "all", precision="fp32") as p:
+        p.stage(w.coords)
+        p.set_classes(w.atom_class)
+        p.set_tile(*shape[:3])
+        p.set_poly(shape[3])
+        amp = p.amplitudes(sv, shell, w.class_factors)
+        assert p.schedule()["poly_pairs"] == shape[3]
+    scale = np.abs(w.factors()).sum(axis=1).max()
+    err = np.abs(amp - ref).max() / scale
+    assert err <= 2e-6, err
+
+
 def test_static_single_atom(native_lib):
     # One static atom: |A|^2 = b^2 for every q and t (known answer).
     nf = 16
