@@ -320,6 +320,157 @@ __global__ void __launch_bounds__(NT) self_fft_kernel(CorrLaunch a) {
 }
 
 // ---------------------------------------------------------------------------------------
+// Warp-per-series form for padded lengths L <= 512: every warp transforms its own series
+// in a private shared-memory buffer with warp-level barriers only, keeps its share of the
+// power spectrum (bins lane + 32 r) in registers and its series sums in lane 0. The
+// warps' partials are added in warp order at the end of the chunk. Same outputs as the
+// CTA-per-series kernels above (used for longer series).
+// ---------------------------------------------------------------------------------------
+constexpr int kWarpFftMaxLg = 9, kWarpFftWarps = 8;
+
+template <class T>
+size_t warp_fft_smem(int lg_max, int nf, bool self) {
+    typedef typename cplx<T>::type T2;
+    const size_t Lm = (size_t)1 << lg_max;
+    size_t b = (sizeof(T) == 4 ? Lm / 2 : 0) * sizeof(T2);           // twiddles (FP32)
+    b += std::max(kWarpFftWarps * Lm * sizeof(T2), kWarpFftWarps * Lm * sizeof(double));  // buffers / reduce
+    b += kWarpFftWarps * sizeof(double2) + kWarpFftWarps * sizeof(double);
+    if (self) b += (size_t)nf * sizeof(float4);
+    return b;
+}
+
+template <class T>
+__device__ __forceinline__ double2 warp_sum2(T x, T y) {
+    double dx = (double)x, dy = (double)y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        dx += __shfl_xor_sync(0xffffffffu, dx, o);
+        dy += __shfl_xor_sync(0xffffffffu, dy, o);
+    }
+    return make_double2(dx, dy);
+}
+
+template <class T, bool SELF>
+__global__ void __launch_bounds__(kWarpFftWarps * 32) warp_fft_kernel(CorrLaunch a) {
+    typedef typename cplx<T>::type T2;
+    constexpr int NW = kWarpFftWarps, NT = NW * 32, MAXR = (1 << kWarpFftMaxLg) / 32;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const CorrChunk c = a.chunks[blockIdx.x];
+    const CorrSystem sys = a.systems[c.system];
+    const int lg = sys.lg, L = 1 << lg, half = L >> 1, tws = a.lg_max - lg, nf = sys.nf;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int Lm = 1 << a.lg_max;
+    T2* twsm = reinterpret_cast<T2*>(smem);
+    unsigned char* region = smem + (sizeof(T) == 4 ? (size_t)(Lm / 2) * sizeof(T2) : 0);
+    T2* buf = reinterpret_cast<T2*>(region) + (size_t)warp * Lm;
+    const size_t region_bytes = NW * (size_t)Lm * (sizeof(T2) > sizeof(double) ? sizeof(T2) : sizeof(double));
+    double2* red = reinterpret_cast<double2*>(region + region_bytes);
+    double* red2 = reinterpret_cast<double*>(red + NW);
+    float4* rj = reinterpret_cast<float4*>(red2 + NW);
+    const T2* tw = stage_twiddles<T, NT>(twsm, a.tw, a.lg_max);
+    const T2* kbr = reinterpret_cast<const T2*>(sys.kbr);
+    PowerAcc<T, MAXR> acc;
+    acc.clear();
+    double2 asum = make_double2(0.0, 0.0);
+    double a2sum = 0.0;
+    __syncthreads();
+
+    // one series: folded first DIF stage on load, the other stages, power + K-weighted sum
+    auto transform = [&](auto gen) {
+        for (int p = lane; p < half; p += 32) {
+            T2 x = zero2<T2>();
+            if (p < nf) x = gen(p);
+            buf[p] = x;
+            buf[p + half] = cmul(x, tw[p << tws]);
+        }
+        __syncwarp();
+        for (int lh = lg - 2; lh >= 0; --lh) {
+            const int h = 1 << lh, sh = lg - 1 - lh + tws;
+            for (int b = lane; b < half; b += 32) {
+                const int q = b & (h - 1);
+                const int i0 = ((b >> lh) << (lh + 1)) + q;
+                const T2 u = buf[i0], w = buf[i0 + h];
+                buf[i0] = cadd(u, w);
+                buf[i0 + h] = cmul(csub(u, w), tw[q << sh]);
+            }
+            __syncwarp();
+        }
+        T ax = 0, ay = 0;
+#pragma unroll
+        for (int r = 0; r < MAXR; ++r) {
+            const int i = lane + 32 * r;
+            if (i < L) {
+                const T2 X = buf[i];
+                const T P = X.x * X.x + X.y * X.y;
+                acc.add(r, P);
+                const T2 k = kbr[i];
+                ax += P * k.x;
+                ay += P * k.y;
+            }
+        }
+        const double2 av = warp_sum2<T>(ax, ay);
+        if (lane == 0) {
+            asum.x += av.x;
+            asum.y += av.y;
+            a2sum += av.x * av.x + av.y * av.y;
+        }
+        __syncwarp();  // the buffer is free for the next series
+    };
+
+    if (SELF) {
+        const T* bfac = reinterpret_cast<const T*>(sys.bfac);
+        const int v0 = sys.shell_v[c.shell], v1 = sys.shell_v[c.shell + 1];
+        for (int j = c.v_begin; j < c.v_end; ++j) {
+            __syncthreads();  // every warp is done with the previous atom's trajectory
+            for (int t = threadIdx.x; t < nf; t += NT) rj[t] = sys.xyz[(size_t)t * sys.na_pad + j];
+            const T b = bfac[(size_t)c.shell * sys.na_pad + j];
+            __syncthreads();
+            for (int v = v0 + warp; v < v1; v += NW) {
+                T qx, qy, qz;
+                load_q(sys.qv + 3 * (size_t)v, qx, qy, qz);
+                transform([&](int p) { return self_term(b, rj[p], qx, qy, qz); });
+            }
+        }
+    } else {
+        for (int v = c.v_begin + warp; v < c.v_end; v += NW) {
+            const T2* src = reinterpret_cast<const T2*>(sys.A) + (size_t)v * sys.nf;
+            transform([&](int p) { return src[p]; });
+        }
+    }
+
+    // partials of the warps, added in warp order
+    __syncthreads();
+    double* pw = reinterpret_cast<double*>(region);  // [NW][L]
+#pragma unroll
+    for (int r = 0; r < MAXR; ++r) {
+        const int i = lane + 32 * r;
+        if (i < L) pw[(size_t)warp * L + i] = acc.get(r);
+    }
+    if (lane == 0) {
+        red[warp] = asum;
+        red2[warp] = a2sum;
+    }
+    __syncthreads();
+    double* dst = a.ppart + c.part_off;
+    for (int i = threadIdx.x; i < L; i += NT) {
+        double s = 0.0;
+        for (int w = 0; w < NW; ++w) s += pw[(size_t)w * L + i];
+        dst[i] = s;
+    }
+    if (threadIdx.x == 0) {
+        double2 as = make_double2(0.0, 0.0);
+        double a2 = 0.0;
+        for (int w = 0; w < NW; ++w) {
+            as.x += red[w].x;
+            as.y += red[w].y;
+            a2 += red2[w];
+        }
+        a.apart[c.slot] = as;
+        a.a2part[c.slot] = a2;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
 // dsp = square | plain (no transform): C_v(t) = |A_v(t)|^2 or A_v(t) * exp(i q_v.c).
 // Partials are complex per frame (double2 [nf] at part_off).
 // ---------------------------------------------------------------------------------------
@@ -576,13 +727,24 @@ cudaError_t launch_fft(const CorrLaunch& a, bool self, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+template <class T>
+cudaError_t launch_warp_fft(const CorrLaunch& a, bool self, cudaStream_t st) {
+    const size_t sm = warp_fft_smem<T>(a.lg_max, a.nf_max, self);
+    auto k = self ? warp_fft_kernel<T, true> : warp_fft_kernel<T, false>;
+    cudaError_t e = set_smem(k, sm);
+    if (e != cudaSuccess) return e;
+    k<<<a.nchunks, kWarpFftWarps * 32, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_accumulate(const CorrLaunch& a, bool self, cudaStream_t st) {
     if (a.nchunks == 0) return cudaSuccess;
     if (a.dsp == DSP_AUTOCORRELATE) {
         if (a.lg_max < 2 || a.lg_max > kMaxLg) return cudaErrorInvalidValue;
-        if (a.precision == PREC_FP32)
-            return a.lg_max <= 9 ? launch_fft<float, 64, 8>(a, self, st) : launch_fft<float, 256, 32>(a, self, st);
-        return a.lg_max <= 9 ? launch_fft<double, 64, 8>(a, self, st) : launch_fft<double, 256, 32>(a, self, st);
+        if (a.lg_max <= kWarpFftMaxLg)
+            return a.precision == PREC_FP32 ? launch_warp_fft<float>(a, self, st) : launch_warp_fft<double>(a, self, st);
+        if (a.precision == PREC_FP32) return launch_fft<float, 256, 32>(a, self, st);
+        return launch_fft<double, 256, 32>(a, self, st);
     }
     if (a.nf_max > 256 * 16) return cudaErrorInvalidValue;
     if (self) {
@@ -598,8 +760,9 @@ cudaError_t launch_accumulate(const CorrLaunch& a, bool self, cudaStream_t st) {
 }  // namespace
 
 size_t fft_smem_bytes(int precision, int lg, int nf, bool self) {
-    const int nt = lg <= 9 ? 64 : 256;
-    return precision == PREC_FP32 ? fft_smem<float>(lg, nt, nf, self) : fft_smem<double>(lg, nt, nf, self);
+    if (lg <= kWarpFftMaxLg)
+        return precision == PREC_FP32 ? warp_fft_smem<float>(lg, nf, self) : warp_fft_smem<double>(lg, nf, self);
+    return precision == PREC_FP32 ? fft_smem<float>(lg, 256, nf, self) : fft_smem<double>(lg, 256, nf, self);
 }
 
 cudaError_t launch_corr_accumulate(const CorrLaunch& a, cudaStream_t st) { return launch_accumulate(a, false, st); }
