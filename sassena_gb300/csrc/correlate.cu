@@ -727,6 +727,185 @@ cudaError_t launch_fft(const CorrLaunch& a, bool self, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------------------
+// Register-resident warp FFT for one padded length L = 32 E (64 <= L <= 512) shared by
+// every system of the launch. Lane l holds elements l + 32 m (m < E), generated or loaded
+// in place: the folded first DIF stage and the stages of span >= 32 pair elements inside
+// a lane; the five stages of span 16 .. 1 pair lanes l and l ^ h through shuffles. The
+// output is in bit-reversed order at the same positions l + 32 m, which are exactly the
+// power-spectrum bins this lane accumulates, so no shared memory holds series data.
+// ---------------------------------------------------------------------------------------
+__host__ __device__ constexpr int ilog2c(int v) { return v <= 1 ? 0 : 1 + ilog2c(v >> 1); }
+
+template <class T2>
+__device__ __forceinline__ T2 shfl_xor2(T2 v, int m) {
+    v.x = __shfl_xor_sync(0xffffffffu, v.x, m);
+    v.y = __shfl_xor_sync(0xffffffffu, v.y, m);
+    return v;
+}
+
+template <class T>
+size_t reg_fft_smem(int lg, int nf, bool self) {
+    typedef typename cplx<T>::type T2;
+    size_t b = (sizeof(T) == 4 ? ((size_t)1 << lg) / 2 : 0) * sizeof(T2);
+    b += (size_t)kWarpFftWarps * (kWarpFftWarps > 0 ? ((size_t)1 << lg) : 0) * sizeof(double);  // reduce
+    b += kWarpFftWarps * sizeof(double2) + kWarpFftWarps * sizeof(double);
+    if (self) b += (size_t)nf * sizeof(float4);
+    return b;
+}
+
+template <class T, int LG, bool SELF>
+__global__ void __launch_bounds__(kWarpFftWarps * 32) reg_fft_kernel(CorrLaunch a) {
+    typedef typename cplx<T>::type T2;
+    constexpr int NW = kWarpFftWarps, NT = NW * 32, L = 1 << LG, E = L / 32, EH = E / 2;
+    static_assert(E >= 2 && E <= 16, "register FFT lengths 64 .. 512");
+    extern __shared__ __align__(16) unsigned char smem[];
+    const CorrChunk c = a.chunks[blockIdx.x];
+    const CorrSystem sys = a.systems[c.system];
+    const int nf = sys.nf, tws = a.lg_max - LG;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    T2* twsm = reinterpret_cast<T2*>(smem);
+    unsigned char* region = smem + (sizeof(T) == 4 ? (size_t)(L / 2) * sizeof(T2) : 0);
+    double* pw = reinterpret_cast<double*>(region);  // [NW][L] warp partials at the end
+    double2* red = reinterpret_cast<double2*>(pw + (size_t)NW * L);
+    double* red2 = reinterpret_cast<double*>(red + NW);
+    float4* rj = reinterpret_cast<float4*>(red2 + NW);
+    const T2* tw = stage_twiddles<T, NT>(twsm, a.tw, a.lg_max);
+    const T2* kbr = reinterpret_cast<const T2*>(sys.kbr);
+    PowerAcc<T, E> acc;
+    acc.clear();
+    T2 kv[E];  // this lane's bins of the store kernel
+#pragma unroll
+    for (int m = 0; m < E; ++m) kv[m] = kbr[lane + 32 * m];
+    double2 asum = make_double2(0.0, 0.0);
+    double a2sum = 0.0;
+    __syncthreads();
+
+    auto transform = [&](auto gen) {
+        T2 x[E];
+#pragma unroll
+        for (int m = 0; m < EH; ++m) {  // load with the folded first stage (upper half zero)
+            const int p = lane + 32 * m;
+            const T2 v = p < nf ? gen(p) : zero2<T2>();
+            x[m] = v;
+            x[m + EH] = cmul(v, tw[p << tws]);
+        }
+#pragma unroll
+        for (int hm = E / 4; hm >= 1; hm >>= 1) {  // spans 32 hm inside the lane
+            const int sh = LG - 1 - (5 + ilog2c(hm)) + tws;
+#pragma unroll
+            for (int m = 0; m < E; ++m) {
+                if ((m & hm) == 0) {
+                    const T2 u = x[m], w = x[m + hm];
+                    x[m] = cadd(u, w);
+                    x[m + hm] = cmul(csub(u, w), tw[(lane + 32 * (m & (hm - 1))) << sh]);
+                }
+            }
+        }
+#pragma unroll
+        for (int lh = 4; lh >= 0; --lh) {  // spans 16 .. 1 across lanes
+            const int h = 1 << lh, sh = LG - 1 - lh + tws;
+            const bool upper = (lane & h) != 0;
+            const T sg = upper ? T(-1) : T(1);
+            T2 tv = tw[(lane & (h - 1)) << sh];
+            if (!upper) {
+                tv.x = T(1);
+                tv.y = T(0);
+            }
+#pragma unroll
+            for (int m = 0; m < E; ++m) {
+                const T2 o = shfl_xor2(x[m], h);
+                T2 d;  // lower lane: x + o; upper lane: o - x (then times the twiddle)
+                d.x = fma(sg, x[m].x, o.x);
+                d.y = fma(sg, x[m].y, o.y);
+                x[m] = cmul(d, tv);
+            }
+        }
+        T ax = 0, ay = 0;
+#pragma unroll
+        for (int m = 0; m < E; ++m) {
+            const T P = x[m].x * x[m].x + x[m].y * x[m].y;
+            acc.add(m, P);
+            ax += P * kv[m].x;
+            ay += P * kv[m].y;
+        }
+        const double2 av = warp_sum2<T>(ax, ay);
+        if (lane == 0) {
+            asum.x += av.x;
+            asum.y += av.y;
+            a2sum += av.x * av.x + av.y * av.y;
+        }
+    };
+
+    if (SELF) {
+        const T* bfac = reinterpret_cast<const T*>(sys.bfac);
+        const int v0 = sys.shell_v[c.shell], v1 = sys.shell_v[c.shell + 1];
+        for (int j = c.v_begin; j < c.v_end; ++j) {
+            __syncthreads();  // every warp is done with the previous atom's trajectory
+            for (int t = threadIdx.x; t < nf; t += NT) rj[t] = sys.xyz[(size_t)t * sys.na_pad + j];
+            const T b = bfac[(size_t)c.shell * sys.na_pad + j];
+            __syncthreads();
+            for (int v = v0 + warp; v < v1; v += NW) {
+                T qx, qy, qz;
+                load_q(sys.qv + 3 * (size_t)v, qx, qy, qz);
+                transform([&](int p) { return self_term(b, rj[p], qx, qy, qz); });
+            }
+        }
+    } else {
+        for (int v = c.v_begin + warp; v < c.v_end; v += NW) {
+            const T2* src = reinterpret_cast<const T2*>(sys.A) + (size_t)v * sys.nf;
+            transform([&](int p) { return src[p]; });
+        }
+    }
+
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < E; ++m) pw[(size_t)warp * L + lane + 32 * m] = acc.get(m);
+    if (lane == 0) {
+        red[warp] = asum;
+        red2[warp] = a2sum;
+    }
+    __syncthreads();
+    double* dst = a.ppart + c.part_off;
+    for (int i = threadIdx.x; i < L; i += NT) {
+        double s = 0.0;
+        for (int w = 0; w < NW; ++w) s += pw[(size_t)w * L + i];
+        dst[i] = s;
+    }
+    if (threadIdx.x == 0) {
+        double2 as = make_double2(0.0, 0.0);
+        double a2 = 0.0;
+        for (int w = 0; w < NW; ++w) {
+            as.x += red[w].x;
+            as.y += red[w].y;
+            a2 += red2[w];
+        }
+        a.apart[c.slot] = as;
+        a.a2part[c.slot] = a2;
+    }
+}
+
+template <class T, int LG>
+cudaError_t launch_reg_fft_lg(const CorrLaunch& a, bool self, cudaStream_t st) {
+    const size_t sm = reg_fft_smem<T>(LG, a.nf_max, self);
+    auto k = self ? reg_fft_kernel<T, LG, true> : reg_fft_kernel<T, LG, false>;
+    cudaError_t e = set_smem(k, sm);
+    if (e != cudaSuccess) return e;
+    k<<<a.nchunks, kWarpFftWarps * 32, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_reg_fft(const CorrLaunch& a, bool self, cudaStream_t st) {
+    switch (a.lg_max) {
+        case 6: return launch_reg_fft_lg<T, 6>(a, self, st);
+        case 7: return launch_reg_fft_lg<T, 7>(a, self, st);
+        case 8: return launch_reg_fft_lg<T, 8>(a, self, st);
+        case 9: return launch_reg_fft_lg<T, 9>(a, self, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
 template <class T>
 cudaError_t launch_warp_fft(const CorrLaunch& a, bool self, cudaStream_t st) {
     const size_t sm = warp_fft_smem<T>(a.lg_max, a.nf_max, self);
@@ -741,6 +920,8 @@ cudaError_t launch_accumulate(const CorrLaunch& a, bool self, cudaStream_t st) {
     if (a.nchunks == 0) return cudaSuccess;
     if (a.dsp == DSP_AUTOCORRELATE) {
         if (a.lg_max < 2 || a.lg_max > kMaxLg) return cudaErrorInvalidValue;
+        if (a.lg_min == a.lg_max && a.lg_max >= 6 && a.lg_max <= kWarpFftMaxLg)
+            return a.precision == PREC_FP32 ? launch_reg_fft<float>(a, self, st) : launch_reg_fft<double>(a, self, st);
         if (a.lg_max <= kWarpFftMaxLg)
             return a.precision == PREC_FP32 ? launch_warp_fft<float>(a, self, st) : launch_warp_fft<double>(a, self, st);
         if (a.precision == PREC_FP32) return launch_fft<float, 256, 32>(a, self, st);

@@ -321,11 +321,13 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
     // ---- shape and sizes ----------------------------------------------------------------
     size_t min_nm = (size_t)-1, total_shells = 0;
     lg_max_ = 2;
+    lg_min_ = kMaxLg;
     nf_max_ = 1;
     for (const WorkItem& it : items) {
         for (size_t s = 0; s + 1 < it.offs.size(); ++s) min_nm = std::min(min_nm, it.offs[s + 1] - it.offs[s]);
         total_shells += it.offs.size() - 1;
         lg_max_ = std::max(lg_max_, it.sys->lg);
+        lg_min_ = std::min(lg_min_, it.sys->lg);
         nf_max_ = std::max(nf_max_, (int)it.sys->nf);
     }
     PhaseShape shape = cfg.shape.q_per_lane ? cfg.shape : default_shape(cfg.precision, min_nm);
@@ -588,7 +590,7 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
             weighted_ = true;
             item_wsqrt_[i] = items[i].d_wsqrt;
         }
-    const size_t per_shell = std::max<size_t>(1, ((size_t)sms * 4 + total_shells - 1) / total_shells);
+    const size_t per_shell = std::max<size_t>(1, ((size_t)sms * 8 + total_shells - 1) / total_shells);
     size_t poff = 0;
     int slot = 0;
     for (size_t i = 0; i < items.size(); ++i) {
@@ -745,6 +747,7 @@ int Engine::enqueue(cudaStream_t st, std::string& err, cudaEvent_t* ev) {
     cl.chunks = d_chunks_;
     cl.nchunks = nchunks_;
     cl.lg_max = lg_max_;
+    cl.lg_min = lg_min_;
     cl.nf_max = nf_max_;
     cl.tw = f32 ? (const void*)tw32_.p : (const void*)tw64_.p;
     cl.restore_phase = f32;

@@ -124,7 +124,7 @@ public:
 private:
     EngineConfig cfg_;
     EngineStats stats_;
-    int lg_max_ = 2, nf_max_ = 1, nitems_ = 0;
+    int lg_max_ = 2, lg_min_ = 2, nf_max_ = 1, nitems_ = 0;
     std::vector<int> nsplit_;
     std::vector<size_t> item_nv_, item_nf_;
     std::vector<std::pair<double2*, double2*>> split_part_;  // (partials, FP64 out) per item

@@ -165,6 +165,7 @@ struct CorrLaunch {
     const CorrChunk* chunks;
     int nchunks;
     int lg_max;             // largest padded length of the batch (shared memory sizing)
+    int lg_min;             // smallest padded length (0: not known)
     int nf_max;
     const void* tw;         // [L_max/2] exp(-2 pi i k / L_max), float2 or double2
     int restore_phase;      // FP32 form with dsp=plain: multiply by exp(i q.c)

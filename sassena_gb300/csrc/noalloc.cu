@@ -206,6 +206,7 @@ extern "C" int sass_correlate_noalloc(int device, void* stream, const double* am
     ca.chunks = chunks;
     ca.nchunks = (int)nq * g;
     ca.lg_max = lg;
+    ca.lg_min = lg;
     ca.nf_max = (int)nf;
     ca.tw = tw;
     ca.ppart = reinterpret_cast<double*>(b + kOffPart);
