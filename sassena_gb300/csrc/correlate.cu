@@ -339,15 +339,16 @@ size_t warp_fft_smem(int lg_max, int nf, bool self) {
     return b;
 }
 
+// Sum over the warp in the form's own precision (a float shuffle moves one word, a
+// double shuffle two), returned in FP64 for the cross-series accumulation.
 template <class T>
 __device__ __forceinline__ double2 warp_sum2(T x, T y) {
-    double dx = (double)x, dy = (double)y;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        dx += __shfl_xor_sync(0xffffffffu, dx, o);
-        dy += __shfl_xor_sync(0xffffffffu, dy, o);
+        x += __shfl_xor_sync(0xffffffffu, x, o);
+        y += __shfl_xor_sync(0xffffffffu, y, o);
     }
-    return make_double2(dx, dy);
+    return make_double2((double)x, (double)y);
 }
 
 template <class T, bool SELF>
@@ -744,18 +745,20 @@ __device__ __forceinline__ T2 shfl_xor2(T2 v, int m) {
     return v;
 }
 
+constexpr int kRegFftAtoms = 8;  // incoherent: atoms whose trajectories are staged together
+
 template <class T>
 size_t reg_fft_smem(int lg, int nf, bool self) {
     typedef typename cplx<T>::type T2;
     size_t b = (sizeof(T) == 4 ? ((size_t)1 << lg) / 2 : 0) * sizeof(T2);
-    b += (size_t)kWarpFftWarps * (kWarpFftWarps > 0 ? ((size_t)1 << lg) : 0) * sizeof(double);  // reduce
+    b += (size_t)kWarpFftWarps * ((size_t)1 << lg) * sizeof(double);  // warp partials
     b += kWarpFftWarps * sizeof(double2) + kWarpFftWarps * sizeof(double);
-    if (self) b += (size_t)nf * sizeof(float4);
+    if (self) b += (size_t)kRegFftAtoms * nf * sizeof(float4) + kRegFftAtoms * sizeof(double);
     return b;
 }
 
 template <class T, int LG, bool SELF>
-__global__ void __launch_bounds__(kWarpFftWarps * 32) reg_fft_kernel(CorrLaunch a) {
+__global__ void __launch_bounds__(kWarpFftWarps * 32, (LG <= 8 && sizeof(T) == 4) ? 3 : 2) reg_fft_kernel(CorrLaunch a) {
     typedef typename cplx<T>::type T2;
     constexpr int NW = kWarpFftWarps, NT = NW * 32, L = 1 << LG, E = L / 32, EH = E / 2;
     static_assert(E >= 2 && E <= 16, "register FFT lengths 64 .. 512");
@@ -774,9 +777,6 @@ __global__ void __launch_bounds__(kWarpFftWarps * 32) reg_fft_kernel(CorrLaunch 
     const T2* kbr = reinterpret_cast<const T2*>(sys.kbr);
     PowerAcc<T, E> acc;
     acc.clear();
-    T2 kv[E];  // this lane's bins of the store kernel
-#pragma unroll
-    for (int m = 0; m < E; ++m) kv[m] = kbr[lane + 32 * m];
     double2 asum = make_double2(0.0, 0.0);
     double a2sum = 0.0;
     __syncthreads();
@@ -826,8 +826,9 @@ __global__ void __launch_bounds__(kWarpFftWarps * 32) reg_fft_kernel(CorrLaunch 
         for (int m = 0; m < E; ++m) {
             const T P = x[m].x * x[m].x + x[m].y * x[m].y;
             acc.add(m, P);
-            ax += P * kv[m].x;
-            ay += P * kv[m].y;
+            const T2 kv = __ldg(kbr + lane + 32 * m);  // this lane's bins of the store kernel (L1)
+            ax += P * kv.x;
+            ay += P * kv.y;
         }
         const double2 av = warp_sum2<T>(ax, ay);
         if (lane == 0) {
@@ -838,17 +839,28 @@ __global__ void __launch_bounds__(kWarpFftWarps * 32) reg_fft_kernel(CorrLaunch 
     };
 
     if (SELF) {
+        // trajectories of up to kRegFftAtoms atoms staged at once (coalesced over atoms);
+        // the warps share out their (atom, direction) pairs evenly
+        constexpr int NAS = kRegFftAtoms;
+        T* bsm = reinterpret_cast<T*>(rj + (size_t)NAS * nf);
         const T* bfac = reinterpret_cast<const T*>(sys.bfac);
-        const int v0 = sys.shell_v[c.shell], v1 = sys.shell_v[c.shell + 1];
-        for (int j = c.v_begin; j < c.v_end; ++j) {
-            __syncthreads();  // every warp is done with the previous atom's trajectory
-            for (int t = threadIdx.x; t < nf; t += NT) rj[t] = sys.xyz[(size_t)t * sys.na_pad + j];
-            const T b = bfac[(size_t)c.shell * sys.na_pad + j];
+        const int v0 = sys.shell_v[c.shell], nd = sys.shell_v[c.shell + 1] - v0;
+        for (int j0 = c.v_begin; j0 < c.v_end; j0 += NAS) {
+            const int na = min(NAS, c.v_end - j0);
+            __syncthreads();  // every warp is done with the previous atoms' trajectories
+            for (int i = threadIdx.x; i < na * nf; i += NT) {
+                const int t = i / na, at = i - t * na;
+                rj[at * nf + t] = sys.xyz[(size_t)t * sys.na_pad + j0 + at];
+            }
+            if (threadIdx.x < na) bsm[threadIdx.x] = bfac[(size_t)c.shell * sys.na_pad + j0 + threadIdx.x];
             __syncthreads();
-            for (int v = v0 + warp; v < v1; v += NW) {
+            for (int pr = warp; pr < na * nd; pr += NW) {
+                const int at = pr / nd, v = v0 + (pr - at * nd);
                 T qx, qy, qz;
                 load_q(sys.qv + 3 * (size_t)v, qx, qy, qz);
-                transform([&](int p) { return self_term(b, rj[p], qx, qy, qz); });
+                const T b = bsm[at];
+                const float4* ra = rj + (size_t)at * nf;
+                transform([&](int p) { return self_term(b, ra[p], qx, qy, qz); });
             }
         }
     } else {
