@@ -187,7 +187,14 @@ def cpu_sample(w, seconds, nthreads):
 def run_reference(args, dist):
     if dist.rank != 0:
         return
-    w = make_workload(args.workload, args.nq, args.nf)
+    if args.workload == "batched_uneven":  # the CPU rate per term: one system of the batch
+        from sassena_gb300 import synth
+        w = synth.batched_uneven(seed=4, nsys=args.nsys or 64)[0]
+    elif args.workload == "layered_cv":
+        from sassena_gb300 import synth
+        w = synth.layered()
+    else:
+        w = make_workload(args.workload, args.nq, args.nf)
     nthreads = os.cpu_count() or 1
     vals = []
     for i in range(args.warmup + args.steps):
