@@ -190,10 +190,19 @@ bool run_scatter_device(const Params& p, Database& db, const Sample& s, RunStats
         ~Guard() { sass_plan_destroy(p); }
     } guard{plan};
 
-    // sd:stage
+    // sd:stage: frames read straight into page-locked memory, one copy to the device
     double ts = now_s();
-    std::vector<float> coords = s.stage(p.target);
-    check(plan, sass_stage_frames(plan, coords.data(), 0), "sass_stage_frames");
+    {
+        const size_t bytes = nf * na * 3 * sizeof(float);
+        float* pinned = static_cast<float*>(sass_host_alloc(bytes));
+        if (!pinned) throw std::runtime_error("sass_host_alloc: cannot allocate page-locked staging memory");
+        struct Free {
+            float* q;
+            ~Free() { sass_host_free(q); }
+        } release{pinned};
+        s.stage_into(p.target, pinned);
+        check(plan, sass_stage_frames(plan, pinned, 0), "sass_stage_frames");
+    }
     check(plan, sass_set_atom_classes(plan, cls.atom_class.data(), 0), "sass_set_atom_classes");
     st.stage_s = now_s() - ts;
     info("Staged " + std::to_string(nf) + " frames x " + std::to_string(na) + " atoms (sd:stage " +

@@ -157,22 +157,26 @@ const std::vector<size_t>& Sample::selection(const std::string& name) const {
 }
 
 std::vector<float> Sample::stage(const std::string& target) const {
+    std::vector<float> out(nframes * selection(target).size() * 3);
+    stage_into(target, out.data());
+    return out;
+}
+
+void Sample::stage_into(const std::string& target, float* out) const {
     const std::vector<size_t>& sel = selection(target);
     const size_t na_all = atom_ids.size(), na = sel.size();
-    std::vector<float> out(nframes * na * 3);
     std::vector<float> x(na_all), y(na_all), z(na_all);
     size_t f = 0;
     for (const DcdFile& d : framesets)
         for (size_t i = 0; i < d.frame_pos.size(); ++i, ++f) {
             d.read_frame(i, x.data(), y.data(), z.data());
-            float* o = out.data() + f * na * 3;
+            float* o = out + f * na * 3;
             for (size_t n = 0; n < na; ++n) {
                 o[3 * n] = x[sel[n]];
                 o[3 * n + 1] = y[sel[n]];
                 o[3 * n + 2] = z[sel[n]];
             }
         }
-    return out;
 }
 
 }  // namespace sassgpu

@@ -46,6 +46,8 @@ public:
     // frame-major float32 [nf][na][3] of the atoms in `target`
     // (CoordinateSets::load without motions/alignments reduces to the selection)
     std::vector<float> stage(const std::string& target) const;
+    // The same frames written to `out` ([nframes][na][3]), e.g. page-locked host memory.
+    void stage_into(const std::string& target, float* out) const;
 };
 
 }  // namespace sassgpu
