@@ -61,6 +61,19 @@ def lib():
         L.oracle_exclusion.restype = ctypes.c_double
         L.oracle_exclusion.argtypes = [ctypes.c_int, _dp, ctypes.c_size_t, ctypes.c_double,
                                        ctypes.c_double]
+        _ip = ctypes.POINTER(ctypes.c_int)
+        L.oracle_mp_sphere.restype = ctypes.c_int
+        L.oracle_mp_sphere.argtypes = [_fp, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t, _dp,
+                                       _dp, ctypes.c_size_t, _ip, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, _dp, _dp, _dp]
+        L.oracle_mp_cylinder.restype = ctypes.c_int
+        L.oracle_mp_cylinder.argtypes = [_fp, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t,
+                                         _dp, _dp, ctypes.c_size_t, _ip, _dp, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
+        L.oracle_sph_bessel.argtypes = [ctypes.c_int, ctypes.c_double, _dp]
+        L.oracle_cyl_bessel.argtypes = [ctypes.c_int, ctypes.c_double, _dp]
+        L.oracle_conj_ylm.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp]
+        L.oracle_to_spherical.argtypes = [_fp, ctypes.c_size_t, _fp]
         L.oracle_scan.restype = ctypes.c_size_t
         L.oracle_scan.argtypes = [_dp, ctypes.c_double, ctypes.c_double, ctypes.c_size_t,
                                   ctypes.c_double, _dp]
@@ -162,3 +175,72 @@ def scan(base, frm, to, points, exponent=1.0):
     out = np.zeros((max(points, 1), 3))
     n = lib().oracle_scan(_ptr(base, _dp), frm, to, points, exponent, _ptr(out, _dp))
     return out[:n]
+
+
+def _mp(kind, coords, qvectors, factors, moments, axis, dsp_type, dsp_method, nthreads):
+    coords = np.ascontiguousarray(coords, dtype=np.float32)
+    nf, na = coords.shape[0], coords.shape[1]
+    q = np.ascontiguousarray(qvectors, dtype=np.float64).reshape(-1, 3)
+    nq = len(q)
+    factors = np.ascontiguousarray(factors, dtype=np.float64).reshape(nq, na)
+    mom = np.ascontiguousarray(moments, dtype=np.int32).reshape(-1, 2)
+    fqt, fq, fq2 = np.zeros((nq, nf, 2)), np.zeros((nq, 2)), np.zeros((nq, 2))
+    ip = ctypes.POINTER(ctypes.c_int)
+    args = [_ptr(coords, _fp), nf, na, nq, _ptr(q, _dp), _ptr(factors, _dp), len(mom), _ptr(mom, ip)]
+    if kind == "cylinder":
+        args.append(_ptr(np.ascontiguousarray(axis, np.float64), _dp))
+    args += [dsp_type, dsp_method, nthreads or os.cpu_count(), _ptr(fqt, _dp), _ptr(fq, _dp),
+             _ptr(fq2, _dp)]
+    rc = getattr(lib(), "oracle_mp_" + kind)(*args)
+    if rc != 0:
+        raise ValueError("oracle_mp_%s rejected its arguments" % kind)
+    return fqt, fq, fq2
+
+
+def mp_sphere(coords, qvectors, factors, moments, dsp_type=DSP_AUTOCORRELATE,
+              dsp_method=METHOD_FFTW, nthreads=None):
+    """Multipole sphere device: (fqt [nq,nf,2], fq [nq,2], fq2 [nq,2])."""
+    return _mp("sphere", coords, qvectors, factors, moments, None, dsp_type, dsp_method, nthreads)
+
+
+def mp_cylinder(coords, qvectors, factors, moments, axis, dsp_type=DSP_AUTOCORRELATE,
+                dsp_method=METHOD_FFTW, nthreads=None):
+    """Multipole cylinder device around `axis`: (fqt, fq, fq2)."""
+    return _mp("cylinder", coords, qvectors, factors, moments, axis, dsp_type, dsp_method,
+               nthreads)
+
+
+def sph_bessel(L, x):
+    out = np.zeros(L + 1)
+    lib().oracle_sph_bessel(L, float(x), _ptr(out, _dp))
+    return out
+
+
+def cyl_bessel(N, x):
+    out = np.zeros(N + 1)
+    lib().oracle_cyl_bessel(N, float(x), _ptr(out, _dp))
+    return out
+
+
+def conj_ylm(L, theta, phi):
+    """conj(Y_l^m(theta, phi)) for (l, m) = (0,0), (1,-1), (1,0), (1,1), ... as complex."""
+    out = np.zeros(((L + 1) ** 2, 2))
+    lib().oracle_conj_ylm(L, float(theta), float(phi), _ptr(out, _dp))
+    return out[:, 0] + 1j * out[:, 1]
+
+
+def to_spherical(xyz):
+    xyz = np.ascontiguousarray(xyz, np.float32).reshape(-1, 3)
+    out = np.zeros_like(xyz)
+    lib().oracle_to_spherical(_ptr(xyz, _fp), len(xyz), _ptr(out, _fp))
+    return out
+
+
+def sphere_moments(resolution):
+    """Moments (0,0), (1,-1..1), ..., (L,-L..L) (parameters.cpp:1049-1058)."""
+    return [(0, 0)] + [(l, m) for l in range(1, resolution + 1) for m in range(-l, l + 1)]
+
+
+def cylinder_moments(resolution):
+    """Moments (0,0), (l,0..3) for l = 1..L (parameters.cpp:1060-1068)."""
+    return [(0, 0)] + [(l, m) for l in range(1, resolution + 1) for m in range(4)]

@@ -189,6 +189,232 @@ void parallel_for(size_t n, int nthreads, F&& fn) {
     for (auto& th : pool) th.join();
 }
 
+// ---------------------------------------------------------------------------
+// Multipole devices: coordinate representations and special functions.
+// ---------------------------------------------------------------------------
+
+// SphericalCoor3D(CartesianCoor3D), src/math/coor3d.cpp:168-215: r, theta = acos(z/r),
+// phi in [0, 2 pi) from atan(y/x) with quadrant corrections; the staged values are
+// rounded to float (coor_t, include/common.hpp:38; data_stager.cpp:110-114).
+void to_spherical(float xf, float yf, float zf, float& r_out, float& phi_out, float& theta_out) {
+    double x = xf, y = yf, z = zf;
+    double r = sqrt(pow(x, 2) + pow(y, 2) + pow(z, 2));
+    double theta = 0, phi = 0;
+    if (r != 0) {
+        theta = acos(z / r);
+        if (x != 0.0) {
+            phi = atan(y / x);
+            if (x < 0.0) phi += M_PI;
+            else if (y < 0.0) phi += 2 * M_PI;
+        } else if (y != 0.0) {
+            if (y > 0) phi = M_PI_2;
+            if (y < 0) phi = 3 * M_PI_2;
+        }
+    }
+    r_out = (float)r;
+    phi_out = (float)phi;
+    theta_out = (float)theta;
+}
+
+struct V3 {
+    double x, y, z;
+};
+V3 cross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+double length(V3 a) { return sqrt(pow(a.x, 2) + pow(a.y, 2) + pow(a.z, 2)); }
+V3 divide(V3 a, double l) { return {a.x / l, a.y / l, a.z / l}; }
+
+// CartesianVectorBase(axis), coor3d.cpp:278-295: e_r, e_phi, e_z.
+void axis_base(const double* axis, V3* base) {
+    V3 ek{0, 0, 1}, ej{0, 1, 0};
+    V3 a{axis[0], axis[1], axis[2]};
+    V3 ez = divide(a, length(a));
+    V3 ekez = cross(ek, ez);
+    if (length(ekez) == 0) ekez = cross(ej, ez);
+    V3 er = divide(ekez, length(ekez));
+    V3 ezer = cross(ez, er);
+    V3 ephi = divide(ezer, length(ezer));
+    base[0] = er;
+    base[1] = ephi;
+    base[2] = ez;
+}
+
+// CylinderCoor3D(CartesianCoor3D), coor3d.cpp:116-141, with the reference's float
+// sign(float, float) (include/math/coor3d.hpp:30) for the x < 0 branch.
+void to_cylinder(V3 c, double& r, double& phi, double& z) {
+    r = sqrt(pow(c.x, 2) + pow(c.y, 2));
+    auto fsign = [](float a, float b) { return (b < 0.0) ? -a : a; };
+    if (c.x != 0.0) {
+        phi = atan(c.y / c.x);
+        if (c.x < 0.0) phi = fsign((float)M_PI, (float)c.y) + phi;
+    } else if (c.y != 0.0) {
+        phi = fsign((float)M_PI_2, (float)c.y);
+    } else {
+        phi = 0.0;
+    }
+    phi = phi < 0 ? 2 * M_PI + phi : phi;
+    z = c.z;
+}
+
+// Spherical Bessel functions j_0 .. j_L at x >= 0 (the reference calls
+// boost::math::sph_bessel, multipole_scatter_device.cpp:484; Boost is absent here and
+// this is an independent implementation): power series for x < 1/2, the upward
+// recurrence j_{l+1} = (2l+1)/x j_l - j_{l-1} where it is stable (every l < x), and
+// otherwise Miller's downward recurrence from order L + 32, normalised by j_0 or j_1.
+void sph_bessel_all(int L, double x, double* j) {
+    if (x == 0) {
+        j[0] = 1;
+        for (int l = 1; l <= L; ++l) j[l] = 0;
+        return;
+    }
+    if (x < 0.5) {
+        double xl = 1;  // x^l / (2l+1)!!
+        for (int l = 0; l <= L; ++l) {
+            if (l > 0) xl *= x / (2 * l + 1);
+            double term = 1, sum = 1;
+            for (int k = 1; k < 40; ++k) {
+                term *= -x * x / (2.0 * k * (2 * l + 2 * k + 1));
+                sum += term;
+                if (fabs(term) < 1e-18 * fabs(sum)) break;
+            }
+            j[l] = xl * sum;
+        }
+        return;
+    }
+    const double j0 = sin(x) / x, j1 = sin(x) / (x * x) - cos(x) / x;
+    if (x > L) {
+        j[0] = j0;
+        if (L >= 1) j[1] = j1;
+        for (int l = 1; l < L; ++l) j[l + 1] = (2 * l + 1) / x * j[l] - j[l - 1];
+        return;
+    }
+    const int N = L + 32;
+    double fp = 0, f = 1e-250;  // f_{n+1}, f_n
+    for (int n = N; n >= 1; --n) {
+        double fm = (2 * n + 1) / x * f - fp;  // f_{n-1}
+        fp = f;
+        f = fm;
+        if (n - 1 <= L) j[n - 1] = f;
+        if (fabs(f) > 1e200) {
+            for (int l = n - 1; l <= L; ++l) j[l] *= 1e-200;
+            fp *= 1e-200;
+            f *= 1e-200;
+        }
+    }
+    const double scale = fabs(j0) >= fabs(j1) ? j0 / j[0] : j1 / j[1];
+    for (int l = 0; l <= L; ++l) j[l] *= scale;
+}
+
+// Normalised associated Legendre functions with the Condon-Shortley phase,
+// Pbar_l^m(x) = sqrt((2l+1)/(4 pi) (l-m)!/(l+m)!) P_l^m(x), 0 <= m <= l <= L, by the
+// standard recurrences: Pbar_m^m = -sqrt((2m+1)/(2m)) sqrt(1-x^2) Pbar_{m-1}^{m-1},
+// Pbar_{m+1}^m = sqrt(2m+3) x Pbar_m^m and
+// Pbar_l^m = a_lm (x Pbar_{l-1}^m - b_lm Pbar_{l-2}^m). P is indexed l(l+1)/2 + m.
+void legendre_norm(int L, double x, double* P) {
+    auto at = [](int l, int m) { return l * (l + 1) / 2 + m; };
+    const double s = sqrt((1 - x) * (1 + x));
+    P[0] = sqrt(1.0 / (4 * M_PI));
+    for (int m = 1; m <= L; ++m) P[at(m, m)] = -sqrt((2.0 * m + 1) / (2.0 * m)) * s * P[at(m - 1, m - 1)];
+    for (int m = 0; m < L; ++m) P[at(m + 1, m)] = sqrt(2.0 * m + 3) * x * P[at(m, m)];
+    for (int m = 0; m <= L; ++m)
+        for (int l = m + 2; l <= L; ++l) {
+            const double a = sqrt((4.0 * l * l - 1) / ((double)l * l - (double)m * m));
+            const double b = sqrt((((double)l - 1) * (l - 1) - (double)m * m) / (4.0 * (l - 1) * (l - 1) - 1));
+            P[at(l, m)] = a * (x * P[at(l - 1, m)] - b * P[at(l - 2, m)]);
+        }
+}
+
+// conj(Y_l^m(theta, phi)) with Y_l^{-m} = (-1)^m conj(Y_l^m) (the reference calls
+// conj(boost::math::spherical_harmonic(l, m, theta, phi)), multipole_scatter_device.cpp:488).
+cd conj_ylm(const double* P, int l, int m, double phi) {
+    const int am = m < 0 ? -m : m;
+    double v = P[l * (l + 1) / 2 + am];
+    if (m < 0 && (am & 1)) v = -v;
+    return cd(v * cos(m * phi), -v * sin(m * phi));
+}
+
+// J_0(x) and J_1(x) for x >= 25 from Hankel's asymptotic expansion,
+// J_nu(x) = sqrt(2/(pi x)) (P cos chi - Q sin chi), chi = x - (nu/2 + 1/4) pi, with
+// P, Q the alternating series in a_k(nu) = prod_{i<=k} (4 nu^2 - (2i-1)^2) / (k! 8^k x^k);
+// cos chi and sin chi are formed from cos x and sin x so that no multiple of pi is
+// subtracted from x.
+void bessel01_asymptotic(double x, double& j0, double& j1) {
+    double pq[2][2];
+    for (int nu = 0; nu < 2; ++nu) {
+        const double mu = 4.0 * nu * nu;
+        double a = 1, P = 1, Q = 0;
+        for (int k = 1; k < 60; ++k) {
+            const double next = a * (mu - (2.0 * k - 1) * (2.0 * k - 1)) / (k * 8.0 * x);
+            if (fabs(next) > fabs(a) && k > 2) break;  // the asymptotic series starts to diverge
+            a = next;
+            // k odd: into Q with sign (-1)^((k-1)/2); k even: into P with sign (-1)^(k/2)
+            if (k & 1) Q += (((k - 1) / 2) & 1 ? -a : a);
+            else P += ((k / 2) & 1 ? -a : a);
+            if (fabs(a) < 1e-18) break;
+        }
+        pq[nu][0] = P;
+        pq[nu][1] = Q;
+    }
+    const double c = cos(x), s = sin(x), h = sqrt(0.5), amp = sqrt(2.0 / (M_PI * x));
+    const double c0 = h * (c + s), s0 = h * (s - c);   // cos, sin of x - pi/4
+    const double c1 = h * (s - c), s1 = -h * (s + c);  // cos, sin of x - 3 pi/4
+    j0 = amp * (pq[0][0] * c0 - pq[0][1] * s0);
+    j1 = amp * (pq[1][0] * c1 - pq[1][1] * s1);
+}
+
+// Bessel functions of the first kind J_0 .. J_N at x >= 0 (the reference calls
+// boost::math::cyl_bessel_j, multipole_scatter_device.cpp:956-975; independent
+// implementation). For x >= 25 above every order needed: J_0, J_1 from the asymptotic
+// expansion and the upward recurrence J_{n+1} = (2n/x) J_n - J_{n-1}, stable for n < x.
+// Otherwise Miller's downward recurrence J_{n-1} = (2n/x) J_n - J_{n+1} from an even
+// order M above max(N, x), normalised by J_0 + 2 sum_k J_2k = 1.
+void cyl_bessel_all(int N, double x, double* J) {
+    if (x == 0) {
+        J[0] = 1;
+        for (int n = 1; n <= N; ++n) J[n] = 0;
+        return;
+    }
+    if (x >= 25 && x > N) {
+        double j0, j1;
+        bessel01_asymptotic(x, j0, j1);
+        J[0] = j0;
+        if (N >= 1) J[1] = j1;
+        for (int n = 1; n < N; ++n) J[n + 1] = 2.0 * n / x * J[n] - J[n - 1];
+        return;
+    }
+    const double top = std::max((double)N, x);
+    int M = (int)(top + 20 + 2 * sqrt(top + 10));
+    M += M & 1;
+    double fp = 0, f = 1e-250, norm = 0;  // f_{n+1}, f_n
+    if (M <= N) J[M] = f;
+    for (int n = M; n >= 1; --n) {
+        double fm = 2.0 * n / x * f - fp;  // f_{n-1}
+        fp = f;
+        f = fm;
+        if (n - 1 <= N) J[n - 1] = f;
+        if ((n - 1) % 2 == 0) norm += (n - 1 == 0 ? 1.0 : 2.0) * f;
+        if (fabs(f) > 1e200) {
+            for (int k = n - 1; k <= N && k <= M; ++k) J[k] *= 1e-200;
+            fp *= 1e-200;
+            f *= 1e-200;
+            norm *= 1e-200;
+        }
+    }
+    for (int n = 0; n <= N; ++n) J[n] /= norm;
+}
+
+void finish_factor(Accum& acc, double factor, double* fqt, double* fq, double* fq2) {
+    for (size_t n = 0; n < acc.atfinal.size(); ++n) {
+        fqt[2 * n] = acc.atfinal[n].real() * factor;
+        fqt[2 * n + 1] = acc.atfinal[n].imag() * factor;
+    }
+    cd a = acc.afinal * factor, a2 = acc.a2final * factor;
+    fq[0] = a.real();
+    fq[1] = a.imag();
+    fq2[0] = a2.real();
+    fq2[1] = a2.imag();
+}
+
 }  // namespace
 
 extern "C" {
@@ -388,6 +614,163 @@ size_t oracle_scan(const double* base, double from, double to, size_t points,
     }
     push(to);
     return n;
+}
+
+// ---------------------------------------------------------------------------
+// Multipole devices (coherent). coords are Cartesian float32 frames [nf][na][3]
+// as the stager delivers them; the representation the reference stages instead
+// (SPHERICAL / CYLINDRICAL, multipole_scatter_device.cpp:53, :524, converted by
+// coordinate_sets.cpp:359-363 and rounded to float) is formed here.
+//   qvectors [nq][3], factors [nq][na], moments [nmom][2] (major, minor)
+// ---------------------------------------------------------------------------
+
+// MPSphereScatterDevice::compute / ::scatter, multipole_scatter_device.cpp:278-401,
+// 428-497: A_lm(t) = sum_j 4 pi i^l b_j j_l(|q| r_j) conj(Y_l^m(theta_j, phi_j)), dsp
+// and store per moment, all results times 1/(4 pi).
+int oracle_mp_sphere(const float* coords, size_t nf, size_t na, size_t nq, const double* qvectors,
+                     const double* factors, size_t nmom, const int* moments, int dsp_type,
+                     int dsp_method, int nthreads, double* fqt, double* fq, double* fq2) {
+    if (nf == 0 || na == 0 || nmom == 0) return 1;
+    int L = 0;
+    for (size_t k = 0; k < nmom; ++k) {
+        if (moments[2 * k] < 0 || abs(moments[2 * k + 1]) > moments[2 * k]) return 1;
+        L = std::max(L, moments[2 * k]);
+    }
+    std::vector<float> sph(nf * na * 3);  // r, phi, theta
+    for (size_t i = 0; i < nf * na; ++i)
+        to_spherical(coords[3 * i], coords[3 * i + 1], coords[3 * i + 2], sph[3 * i], sph[3 * i + 1],
+                     sph[3 * i + 2]);
+    Dft fwd(2 * nf, -1), bwd(2 * nf, +1);
+    const size_t np = (size_t)(L + 1) * (L + 2) / 2;
+    for (size_t iq = 0; iq < nq; ++iq) {
+        const double* q = qvectors + 3 * iq;
+        const double ql = sqrt(pow(q[0], 2) + pow(q[1], 2) + pow(q[2], 2));
+        const double* sfs = factors + iq * na;
+        Accum acc(nf);
+        std::vector<cd> at(nmom * 2 * nf);
+        parallel_for(nf, nthreads, [&](size_t fi) {
+            std::vector<double> jl(L + 1), P(np);
+            std::vector<cd> A(nmom, 0.0);
+            for (size_t j = 0; j < na; ++j) {
+                const float* c = &sph[(fi * na + j) * 3];
+                double r = c[0], phi = c[1], theta = c[2];
+                sph_bessel_all(L, ql * r, jl.data());
+                legendre_norm(L, cos(theta), P.data());
+                for (size_t k = 0; k < nmom; ++k) {
+                    int l = moments[2 * k], m = moments[2 * k + 1];
+                    static const cd il[4] = {cd(1, 0), cd(0, 1), cd(-1, 0), cd(0, -1)};
+                    cd fmpiilesf = 4 * M_PI * il[l & 3] * sfs[j];
+                    A[k] += fmpiilesf * jl[l] * conj_ylm(P.data(), l, m, phi);
+                }
+            }
+            for (size_t k = 0; k < nmom; ++k) at[k * 2 * nf + fi] = A[k];
+        });
+        parallel_for(nmom, nthreads, [&](size_t k) {
+            cd* p = &at[k * 2 * nf];
+            for (size_t fi = nf; fi < 2 * nf; ++fi) p[fi] = 0;
+            dsp(p, nf, dsp_type, dsp_method, fwd, bwd);
+        });
+        for (size_t k = 0; k < nmom; ++k) acc.store(&at[k * 2 * nf], nf);
+        finish_factor(acc, 1.0 / (4 * M_PI), fqt + iq * nf * 2, fq + iq * 2, fq2 + iq * 2);
+    }
+    return 0;
+}
+
+// MPCylinderScatterDevice::compute / ::scatter, multipole_scatter_device.cpp:750-872,
+// 900-986: coordinates and q in the cylinder frame of `axis`; per moment (l, m) with
+// m in 0..3 a Bessel J_{2l} (m = 0, 1) or J_{2l-1} (m = 2, 3) term times cos / sin of the
+// order times (phi - phi_q), the phase exp(i s z q_z) with s the sign of z q_z (the
+// reference's parallel_sign), the factor sqrt(2 pi); all results times 1/(2 pi).
+int oracle_mp_cylinder(const float* coords, size_t nf, size_t na, size_t nq, const double* qvectors,
+                       const double* factors, size_t nmom, const int* moments, const double* axis,
+                       int dsp_type, int dsp_method, int nthreads, double* fqt, double* fq, double* fq2) {
+    if (nf == 0 || na == 0 || nmom == 0) return 1;
+    int N = 0;
+    for (size_t k = 0; k < nmom; ++k) {
+        int l = moments[2 * k], m = moments[2 * k + 1];
+        if (l < 0 || m < 0 || m > 3 || (l == 0 && m != 0)) return 1;
+        N = std::max(N, 2 * l);
+    }
+    V3 base[3];
+    axis_base(axis, base);
+    std::vector<float> cyl(nf * na * 3);  // r, phi, z (float, as staged)
+    for (size_t i = 0; i < nf * na; ++i) {
+        V3 c{(double)coords[3 * i], (double)coords[3 * i + 1], (double)coords[3 * i + 2]};
+        V3 pr{dot(c, base[0]), dot(c, base[1]), dot(c, base[2])};
+        double r, phi, z;
+        to_cylinder(pr, r, phi, z);
+        cyl[3 * i] = (float)r;
+        cyl[3 * i + 1] = (float)phi;
+        cyl[3 * i + 2] = (float)z;
+    }
+    Dft fwd(2 * nf, -1), bwd(2 * nf, +1);
+    for (size_t iq = 0; iq < nq; ++iq) {
+        V3 qv{qvectors[3 * iq], qvectors[3 * iq + 1], qvectors[3 * iq + 2]};
+        V3 qp{dot(qv, base[0]), dot(qv, base[1]), dot(qv, base[2])};
+        double qr, qphi, qz;
+        to_cylinder(qp, qr, qphi, qz);
+        const double* sfs = factors + iq * na;
+        Accum acc(nf);
+        std::vector<cd> at(nmom * 2 * nf);
+        parallel_for(nf, nthreads, [&](size_t fi) {
+            std::vector<double> J(N + 1);
+            std::vector<cd> A(nmom, 0.0);
+            for (size_t j = 0; j < na; ++j) {
+                const float* c = &cyl[(fi * na + j) * 3];
+                double r = c[0], phi = c[1], z = c[2];
+                double esf = sfs[j];
+                double parallel_sign = 1.0;
+                if ((z != 0) && (qz != 0)) parallel_sign = (z * qz) / (fabs(z) * fabs(qz));
+                cd expi = std::exp(cd(0, parallel_sign * z * qz));
+                double p = r * qr;
+                double psiphi = phi - qphi;
+                cyl_bessel_all(N, p, J.data());
+                for (size_t k = 0; k < nmom; ++k) {
+                    int l = moments[2 * k], m = moments[2 * k + 1];
+                    if (m == 0 && l == 0) {
+                        A[k] += expi * J[0] * esf;
+                    } else if (m == 0 || m == 1) {
+                        cd fac1 = 2.0 * ((l & 1) ? -1.0 : 1.0) * J[2 * l];
+                        double t = m == 0 ? cos(2 * l * psiphi) : sin(2 * l * psiphi);
+                        A[k] += sqrt(0.5) * fac1 * expi * t * esf;
+                    } else {
+                        cd fac2 = cd(0, 1.0) * (2.0 * (((l - 1) & 1) ? -1.0 : 1.0) * J[2 * l - 1]);
+                        double t = m == 2 ? cos((2 * l - 1) * psiphi) : sin((2 * l - 1) * psiphi);
+                        A[k] += sqrt(0.5) * fac2 * expi * t * esf;
+                    }
+                }
+            }
+            const double norm = sqrt(2 * M_PI);
+            for (size_t k = 0; k < nmom; ++k) at[k * 2 * nf + fi] = norm * A[k];
+        });
+        parallel_for(nmom, nthreads, [&](size_t k) {
+            cd* p = &at[k * 2 * nf];
+            for (size_t fi = nf; fi < 2 * nf; ++fi) p[fi] = 0;
+            dsp(p, nf, dsp_type, dsp_method, fwd, bwd);
+        });
+        for (size_t k = 0; k < nmom; ++k) acc.store(&at[k * 2 * nf], nf);
+        finish_factor(acc, 1.0 / (2 * M_PI), fqt + iq * nf * 2, fq + iq * 2, fq2 + iq * 2);
+    }
+    return 0;
+}
+
+// Special functions and coordinate conversions on their own (for the tests).
+void oracle_sph_bessel(int L, double x, double* out) { sph_bessel_all(L, x, out); }
+void oracle_cyl_bessel(int N, double x, double* out) { cyl_bessel_all(N, x, out); }
+// conj(Y_l^m(theta, phi)) for l <= L, m = -l..l in order (l, m): out [(L+1)^2][2]
+void oracle_conj_ylm(int L, double theta, double phi, double* out) {
+    std::vector<double> P((size_t)(L + 1) * (L + 2) / 2);
+    legendre_norm(L, cos(theta), P.data());
+    size_t k = 0;
+    for (int l = 0; l <= L; ++l)
+        for (int m = -l; m <= l; ++m, ++k) {
+            cd v = conj_ylm(P.data(), l, m, phi);
+            out[2 * k] = v.real();
+            out[2 * k + 1] = v.imag();
+        }
+}
+void oracle_to_spherical(const float* xyz, size_t n, float* out) {
+    for (size_t i = 0; i < n; ++i) to_spherical(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], out[3 * i], out[3 * i + 1], out[3 * i + 2]);
 }
 
 }  // extern "C"
