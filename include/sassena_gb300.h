@@ -176,6 +176,26 @@ typedef struct sass_schedule {
 } sass_schedule;
 int sass_plan_schedule(const sass_plan* plan, sass_schedule* out);
 
+/* ---- Multipole orientational averages ----
+ * The reference's multipole devices (orientation type "multipole",
+ * scatter_device_factory.cpp:167-190): MPSphereScatterDevice and MPCylinderScatterDevice
+ * (multipole_scatter_device.cpp:278-497, 750-986). For each q and each moment (major l,
+ * minor m) the amplitude over frames is summed over atoms, correlated (dsp) and stored
+ * as by the vectors devices; the sums over moments are scaled by 1/(4 pi) (sphere) or
+ * 1/(2 pi) (cylinder).
+ *   sphere:   A_lm(t) = sum_j 4 pi i^l b_j j_l(|q| r_j) conj(Y_l^m(theta_j, phi_j)), |m| <= l
+ *   cylinder: A_lm(t) = sqrt(2 pi) sum_j b_j exp(i |z_j q_z|) c_lm J_n(q_r r_j) T_m(n (phi_j - phi_q)),
+ *             n = 2l for m = 0, 1 (T = cos, sin) and 2l - 1 for m = 2, 3, in the cylinder frame
+ *             of `axis` (CartesianVectorBase, coor3d.cpp:278-295).
+ * moments [nmoments][2] (major, minor) as ScatteringAverageOrientationMultipoleMoments
+ * lists them (parameters.cpp:1037-1122; the same validity checks, major <= 40 here).
+ * Coherent FP64 plans only (SASS_ERR_UNSUPPORTED otherwise). qvectors [nq][3],
+ * class_factors [nq][nclass], outputs as sass_compute; all host arrays. */
+enum { SASS_MULTIPOLE_SPHERE = 0, SASS_MULTIPOLE_CYLINDER = 1 };
+int sass_multipole_compute(sass_plan* plan, int type, size_t nq, const double* qvectors,
+                           const double* class_factors, size_t nmoments, const int32_t* moments,
+                           const double* axis, double* fqt, double* fq, double* fq2);
+
 /* ---- Batches: many independent systems in one graph-captured launch sequence ----
  * Each system has its own trajectory, atom classes, q-vectors and sub-vector sets of
  * any size. The batch stages everything once; sass_batch_run replays one CUDA graph

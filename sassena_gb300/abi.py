@@ -37,6 +37,7 @@ EXPORTS = [
     "sass_mlp_train", "sass_mlp_predict", "sass_mlp_sphere_mean", "sass_compute_cv",
     "sass_set_shell_recurrence", "sass_plan_schedule", "sass_batch_set_shell_recurrence",
     "sass_batch_schedule", "sass_set_phase_poly", "sass_batch_set_phase_poly",
+    "sass_multipole_compute",
 ]
 
 
@@ -155,6 +156,8 @@ def load(path=LIB_PATH):
     L.sass_batch_set_shell_recurrence.argtypes = [_vp, ctypes.c_int]
     L.sass_batch_schedule.argtypes = [_vp, ctypes.POINTER(Schedule)]
     L.sass_set_phase_poly.argtypes = [_vp, ctypes.c_int]
+    L.sass_multipole_compute.argtypes = [_vp, ctypes.c_int, _sz, _vp, _vp, _sz, _vp, _vp, _vp, _vp,
+                                         _vp]
     L.sass_batch_set_phase_poly.argtypes = [_vp, ctypes.c_int]
     _lib = L
     return L
@@ -224,6 +227,23 @@ class Plan:
 
     def set_tile(self, q_per_lane=0, warps=0, atoms=0, atom_splits=0):
         self._check(self.lib.sass_set_phase_tile(self._h, q_per_lane, warps, atoms, atom_splits))
+
+    def multipole(self, kind, qvectors, class_factors, moments, axis=(0.0, 0.0, 1.0)):
+        """Multipole orientational average ("sphere" or "cylinder"): (fqt, fq, fq2) per q."""
+        q = np.ascontiguousarray(qvectors, dtype=np.float64).reshape(-1, 3)
+        nq = len(q)
+        cf = np.ascontiguousarray(class_factors, dtype=np.float64).reshape(nq, self.nclass)
+        mom = np.ascontiguousarray(moments, dtype=np.int32).reshape(-1, 2)
+        ax = np.ascontiguousarray(axis, dtype=np.float64)
+        fqt = np.zeros((nq, self.nf, 2))
+        fq = np.zeros((nq, 2))
+        fq2 = np.zeros((nq, 2))
+        t = {"sphere": 0, "cylinder": 1}[kind]
+        self._check(self.lib.sass_multipole_compute(self._h, t, nq, _ptr(q), _ptr(cf), len(mom),
+                                                    _ptr(mom), _ptr(ax), _ptr(fqt), _ptr(fq),
+                                                    _ptr(fq2)))
+        return (fqt[..., 0] + 1j * fqt[..., 1], fq[:, 0] + 1j * fq[:, 1],
+                fq2[:, 0] + 1j * fq2[:, 1])
 
     def set_poly(self, poly_pairs):
         """Pairs of each lane's q-vectors whose sin/cos use the FP32 pipe (direct kernel)."""

@@ -31,7 +31,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + INCLUDE, "-I" + HOST]
 
 CUDA_SOURCES = [
     "capi.cu", "engine.cu", "phase_sum.cu", "phase_rec.cu", "correlate.cu", "peaks.cu", "noalloc.cu", "mlp.cu",
-    "cv.cu",
+    "cv.cu", "multipole.cu",
 ]
 HOST_SOURCES = []  # filled when the host layer exists (see host_sources())
 

@@ -140,6 +140,7 @@ int stage_system(SystemState& s, const float* coords, bool on_device, int precis
     ECK(cudaStreamSynchronize(st));
     s.staged = true;
     s.rec_valid = false;
+    s.mp_valid = false;
     return kOk;
 }
 
@@ -410,7 +411,7 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
         int ns = 1;
         if (cfg.split_atoms > 0) ns = (int)((items[i].sys->na_pad + cfg.split_atoms - 1) / cfg.split_atoms);
         else if (base_tiles < target) ns = (int)((target + base_tiles - 1) / std::max<size_t>(base_tiles, 1));
-        nsplit_[i] = std::max(1, std::min(ns, max_split));
+        nsplit_[i] = items[i].d_amp_given ? 1 : std::max(1, std::min(ns, max_split));
         stats_.max_split = std::max(stats_.max_split, nsplit_[i]);
     }
     stats_.split_atoms = cfg.split_atoms;
@@ -425,7 +426,7 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
         const size_t nq = it.offs.size() - 1, nv = it.offs.back(), nf = it.sys->nf;
         bfac_off_[i] = bfac_bytes;
         bfac_bytes += ((nq * it.sys->na_pad * bsz + 255) & ~(size_t)255);
-        if (coherent) {
+        if (coherent && !it.d_amp_given) {
             amp_off_[i] = amp_bytes;
             amp_bytes += ((nv * nf * (f32 ? 8 : 16) + 255) & ~(size_t)255);
             if (nsplit_[i] > 1) {
@@ -470,7 +471,8 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
         p.nf = (int)s.nf;
         p.split_stride = nv * s.nf;
         void* amp = coherent ? (void*)(amp_.as<unsigned char>() + amp_off_[i]) : nullptr;
-        if (coherent) {
+        if (it.d_amp_given) amp = const_cast<double2*>(it.d_amp_given);
+        if (coherent && !it.d_amp_given) {
             if (nsplit_[i] > 1) {
                 double2* part = reinterpret_cast<double2*>(part_.as<unsigned char>() + part_off_[i]);
                 p.out = part;
@@ -605,7 +607,7 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
             e.part_len = plen;
             e.nf = (int)s.nf;
             e.lg = s.lg;
-            e.inv_nm = 1.0 / (double)(it.offs[sh + 1] - it.offs[sh]);
+            e.inv_nm = it.norm > 0 ? it.norm : 1.0 / (double)(it.offs[sh + 1] - it.offs[sh]);
             e.fqt = it.d_fqt + sh * s.nf;
             e.fq = it.d_fq + sh;
             e.fq2 = it.d_fq2 + sh;

@@ -52,6 +52,11 @@ struct SystemState {
     DevBuf xyz_rec, block_class;  // [nf][na_rec] float4 with w; [na_rec / 32] int
     size_t na_rec = 0;
     bool rec_valid = false;
+    // multipole devices: coordinates in the spherical or cylindrical representation
+    DevBuf mp_xyz;  // [nf][na_pad] float4
+    int mp_type = -1;
+    bool mp_valid = false;
+    double mp_axis[3] = {0, 0, 0};
 };
 
 struct EngineConfig {
@@ -81,6 +86,11 @@ struct WorkItem {
     double2* d_fqt_w = nullptr;
     double2* d_fq_w = nullptr;
     double2* d_fq2_w = nullptr;
+    // optional (coherent, FP64): amplitudes computed elsewhere ([nv][nf] double2, e.g. the
+    // multipole devices); the engine runs no phase sum for the item, only the correlation
+    // and the average, scaled by `norm` instead of 1/NM
+    const double2* d_amp_given = nullptr;
+    double norm = 0;
 };
 
 struct EngineStats {

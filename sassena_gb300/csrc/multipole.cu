@@ -1,0 +1,761 @@
+// Multipole orientational averages (coherent, FP64 form).
+//
+// Replaces MPSphereScatterDevice and MPCylinderScatterDevice
+// (src/scatter_devices/multipole_scatter_device.cpp). Per q and per moment (l, m) the
+// reference sums over atoms, for every frame:
+//   sphere   A_lm(t) = sum_j 4 pi i^l b_j j_l(|q| r_j) conj(Y_l^m(theta_j, phi_j))   (:428-497)
+//   cylinder A_lm(t) = sqrt(2 pi) sum_j b_j exp(i s z_j q_z) c_lm J_n(q_r r_j) T_m(n (phi_j - phi_q))
+//            with n = 2l (m = 0, 1: T = cos, sin) or 2l - 1 (m = 2, 3), c = sqrt(1/2) 2 (-1)^l or
+//            i sqrt(1/2) 2 (-1)^(l-1), (l, m) = (0, 0): J_0, and s the sign of z q_z  (:900-986)
+// then correlates each moment like the vectors devices and scales the sum by 1/(4 pi)
+// (sphere, :396-400) or 1/(2 pi) (cylinder, :865-870). Coordinates are in the spherical or
+// cylindrical representation the reference stages (coordinate_sets.cpp:359-363), converted
+// here on the device from the staged Cartesian frames in FP64 and rounded to float as the
+// reference's float staging does (data_stager.cpp:110-114).
+//
+// GB300 layout.
+//   sphere: the sum over atoms is, for one frame and one l, a product of the matrix
+//     b_j(q) j_l(|q| r_j) [q x atom] with conj(Y_l^m(j)) [atom x m]. A basis kernel writes both
+//     factors for a batch of frames to HBM (every Y_l^m once, not once per q); a tiled
+//     contraction kernel stages atom tiles of both in shared memory and accumulates every
+//     (q, m) output of one (frame, l) in FP64.
+//   cylinder: one CTA per (q, frame) stages, for a tile of atoms, J_n(q_r r) for every
+//     order n <= 2L, cos(n phi), sin(n phi) and b exp(i s z q_z) in shared memory; threads
+//     then own orders n and accumulate sum_j X_j J_n cos(n phi_j) and ... sin(n phi_j);
+//     each moment is formed from them with cos(n phi_q), sin(n phi_q).
+// The special functions are this project's own FP64 implementations (Boost, which the
+// reference calls, is not used): spherical Bessel functions by power series, upward
+// recurrence where stable or Miller's downward recurrence; normalised associated Legendre
+// functions by the standard three-term recurrences; cylinder Bessel functions by Hankel's
+// asymptotic expansion plus upward recurrence for large arguments, Miller's algorithm
+// otherwise. The amplitudes then go through the engine's correlation and average.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "engine.h"
+#include "kernels.h"
+#include "plan.h"
+
+namespace sassgpu {
+
+namespace {
+
+constexpr int kMpMaxL = 40;  // largest major moment (sphere) / half order (cylinder)
+constexpr int kMpTileAtoms = 32, kMpCylAtoms = 64, kMpCylThreads = 64;
+
+// ---------------------------------------------------------------------------------------
+// coordinate representations
+// ---------------------------------------------------------------------------------------
+// SphericalCoor3D(CartesianCoor3D), coor3d.cpp:168-215 -> (r, phi, theta) as float.
+__device__ float4 to_spherical(float xf, float yf, float zf) {
+    const double x = xf, y = yf, z = zf;
+    const double r = sqrt(x * x + y * y + z * z);  // squares of float values are exact
+    double theta = 0, phi = 0;
+    if (r != 0) {
+        theta = acos(z / r);
+        if (x != 0.0) {
+            phi = atan(y / x);
+            if (x < 0.0) phi += 3.14159265358979323846;
+            else if (y < 0.0) phi += 2 * 3.14159265358979323846;
+        } else if (y != 0.0) {
+            if (y > 0) phi = 1.57079632679489661923;
+            if (y < 0) phi = 3 * 1.57079632679489661923;
+        }
+    }
+    return make_float4((float)r, (float)phi, (float)theta, 0.f);
+}
+
+// CylinderCoor3D(CartesianCoor3D) of the projected vector, coor3d.cpp:116-141, with the
+// reference's float sign() for the x < 0 branch.
+__host__ __device__ inline void to_cylinder(double x, double y, double z, double& r, double& phi, double& zz) {
+    r = sqrt(x * x + y * y);
+    const double kPi = 3.14159265358979323846, kPi2 = 1.57079632679489661923;
+    if (x != 0.0) {
+        phi = atan(y / x);
+        if (x < 0.0) phi = (double)((float)y < 0.0f ? -(float)kPi : (float)kPi) + phi;
+    } else if (y != 0.0) {
+        phi = (double)((float)y < 0.0f ? -(float)kPi2 : (float)kPi2);
+    } else {
+        phi = 0.0;
+    }
+    phi = phi < 0 ? 2 * kPi + phi : phi;
+    zz = z;
+}
+
+struct MpBase {
+    double e[9];  // e_r, e_phi, e_z of CartesianVectorBase(axis), coor3d.cpp:278-295
+};
+
+__global__ void mp_convert_kernel(const float4* __restrict__ xyz, int na_pad, int na, int nf, int cylinder,
+                                  MpBase b, float4* __restrict__ out) {
+    const size_t n = (size_t)nf * na_pad;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int j = (int)(i % na_pad);
+        if (j >= na) {
+            out[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            continue;
+        }
+        const float4 c = xyz[i];
+        if (!cylinder) {
+            out[i] = to_spherical(c.x, c.y, c.z);
+        } else {
+            const double x = c.x, y = c.y, z = c.z;
+            const double px = x * b.e[0] + y * b.e[1] + z * b.e[2];
+            const double py = x * b.e[3] + y * b.e[4] + z * b.e[5];
+            const double pz = x * b.e[6] + y * b.e[7] + z * b.e[8];
+            double r, phi, zz;
+            to_cylinder(px, py, pz, r, phi, zz);
+            out[i] = make_float4((float)r, (float)phi, (float)zz, 0.f);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// special functions (FP64)
+// ---------------------------------------------------------------------------------------
+// b * j_l(x) for l = 0..L written to out[l * stride].
+__device__ void sph_bessel_row(int L, double x, double b, double* out, size_t stride) {
+    if (x == 0) {
+        out[0] = b;
+        for (int l = 1; l <= L; ++l) out[l * stride] = 0;
+        return;
+    }
+    if (x < 0.5) {  // power series
+        double xl = 1;
+        for (int l = 0; l <= L; ++l) {
+            if (l > 0) xl *= x / (2 * l + 1);
+            double term = 1, sum = 1;
+            for (int k = 1; k < 40; ++k) {
+                term *= -x * x / (2.0 * k * (2 * l + 2 * k + 1));
+                sum += term;
+                if (fabs(term) < 1e-18 * fabs(sum)) break;
+            }
+            out[l * stride] = b * xl * sum;
+        }
+        return;
+    }
+    double sx, cx;
+    sincos(x, &sx, &cx);
+    const double j0 = sx / x, j1 = sx / (x * x) - cx / x;
+    if (x > L) {  // upward recurrence, stable for every l < x
+        double jm = j0, jc = j1;
+        out[0] = b * j0;
+        if (L >= 1) out[stride] = b * j1;
+        for (int l = 1; l < L; ++l) {
+            const double jn = (2 * l + 1) / x * jc - jm;
+            out[(l + 1) * stride] = b * jn;
+            jm = jc;
+            jc = jn;
+        }
+        return;
+    }
+    // Miller's downward recurrence from order L + 32, normalised by j_0 or j_1
+    const int N = L + 32;
+    double fp = 0, f = 1e-250;
+    for (int n = N; n >= 1; --n) {
+        const double fm = (2 * n + 1) / x * f - fp;
+        fp = f;
+        f = fm;
+        if (n - 1 <= L) out[(n - 1) * stride] = f;
+        if (fabs(f) > 1e200) {
+            for (int l = n - 1; l <= L; ++l) out[l * stride] *= 1e-200;
+            fp *= 1e-200;
+            f *= 1e-200;
+        }
+    }
+    const double scale = b * (fabs(j0) >= fabs(j1) ? j0 / out[0] : j1 / out[stride]);
+    for (int l = 0; l <= L; ++l) out[l * stride] *= scale;
+}
+
+// conj(Y_l^m(theta, phi)) for the requested moments (idx[l (2L+1) + L + m] -> moment, or -1)
+// written to out[k * stride]; m outer, l inner, so the Legendre recurrence carries two values.
+__device__ void conj_ylm_row(int L, double theta, double phi, const int* __restrict__ idx, double2* out,
+                             size_t stride) {
+    const double x = cos(theta), s = sqrt((1 - x) * (1 + x));
+    double pmm = sqrt(1.0 / (4 * 3.14159265358979323846));
+    const int W = 2 * L + 1;
+    for (int m = 0; m <= L; ++m) {
+        if (m > 0) pmm = -sqrt((2.0 * m + 1) / (2.0 * m)) * s * pmm;
+        double sm, cm;
+        sincos(m * phi, &sm, &cm);
+        auto emit = [&](int l, double P) {
+            const int kp = idx[l * W + L + m];
+            if (kp >= 0) out[kp * stride] = make_double2(P * cm, -P * sm);
+            if (m > 0) {
+                const int kn = idx[l * W + L - m];
+                const double v = (m & 1) ? -P : P;  // conj(Y_l^{-m}) = (-1)^m Pbar e^{i m phi}
+                if (kn >= 0) out[kn * stride] = make_double2(v * cm, v * sm);
+            }
+        };
+        emit(m, pmm);
+        if (m < L) {
+            double p2 = pmm, p1 = sqrt(2.0 * m + 3) * x * pmm;
+            emit(m + 1, p1);
+            for (int l = m + 2; l <= L; ++l) {
+                const double a = sqrt((4.0 * l * l - 1) / ((double)l * l - (double)m * m));
+                const double bb = sqrt((((double)l - 1) * (l - 1) - (double)m * m) / (4.0 * (l - 1) * (l - 1) - 1));
+                const double p = a * (x * p1 - bb * p2);
+                emit(l, p);
+                p2 = p1;
+                p1 = p;
+            }
+        }
+    }
+}
+
+// J_0(x), J_1(x) for x >= 25 by Hankel's asymptotic expansion (cos, sin of x - pi/4 and
+// x - 3 pi/4 formed from cos x, sin x).
+__device__ void bessel01_asymptotic(double x, double& j0, double& j1) {
+    double P0 = 1, Q0 = 0, P1 = 1, Q1 = 0;
+    for (int nu = 0; nu < 2; ++nu) {
+        const double mu = 4.0 * nu * nu;
+        double a = 1, P = 1, Q = 0;
+        for (int k = 1; k < 60; ++k) {
+            const double next = a * (mu - (2.0 * k - 1) * (2.0 * k - 1)) / (k * 8.0 * x);
+            if (fabs(next) > fabs(a) && k > 2) break;
+            a = next;
+            if (k & 1) Q += (((k - 1) / 2) & 1 ? -a : a);
+            else P += ((k / 2) & 1 ? -a : a);
+            if (fabs(a) < 1e-18) break;
+        }
+        if (nu == 0) {
+            P0 = P;
+            Q0 = Q;
+        } else {
+            P1 = P;
+            Q1 = Q;
+        }
+    }
+    double s, c;
+    sincos(x, &s, &c);
+    const double h = 0.70710678118654752440, amp = sqrt(2.0 / (3.14159265358979323846 * x));
+    j0 = amp * (P0 * h * (c + s) - Q0 * h * (s - c));
+    j1 = amp * (P1 * h * (s - c) + Q1 * h * (s + c));
+}
+
+// J_n(x), n = 0..N, written to out[n * stride].
+__device__ void cyl_bessel_row(int N, double x, double* out, int stride) {
+    if (x == 0) {
+        out[0] = 1;
+        for (int n = 1; n <= N; ++n) out[n * stride] = 0;
+        return;
+    }
+    if (x >= 25 && x > N) {
+        double j0, j1;
+        bessel01_asymptotic(x, j0, j1);
+        out[0] = j0;
+        if (N >= 1) out[stride] = j1;
+        double jm = j0, jc = j1;
+        for (int n = 1; n < N; ++n) {
+            const double jn = 2.0 * n / x * jc - jm;
+            out[(n + 1) * stride] = jn;
+            jm = jc;
+            jc = jn;
+        }
+        return;
+    }
+    const double top = fmax((double)N, x);
+    int M = (int)(top + 20 + 2 * sqrt(top + 10));
+    M += M & 1;
+    double fp = 0, f = 1e-250, norm = 0;
+    for (int n = M; n >= 1; --n) {
+        const double fm = 2.0 * n / x * f - fp;
+        fp = f;
+        f = fm;
+        if (n - 1 <= N) out[(n - 1) * stride] = f;
+        if (((n - 1) & 1) == 0) norm += (n - 1 == 0 ? 1.0 : 2.0) * f;
+        if (fabs(f) > 1e200) {
+            for (int k = n - 1; k <= N; ++k) out[k * stride] *= 1e-200;
+            fp *= 1e-200;
+            f *= 1e-200;
+            norm *= 1e-200;
+        }
+    }
+    for (int n = 0; n <= N; ++n) out[n * stride] /= norm;
+}
+
+// ---------------------------------------------------------------------------------------
+// sphere: basis and contraction
+// ---------------------------------------------------------------------------------------
+struct MpSphereBasis {
+    const float4* sph;  // [nf][na_pad] (r, phi, theta)
+    const int* cls;     // [na_pad] (-1 padding)
+    const double* cf;   // [nq][nclass]
+    const double* qlen; // [nq]
+    const int* idx;     // [(L+1)(2L+1)]
+    double* Jb;         // [nfb][nq][L+1][na_pad]  b_j(q) j_l(|q| r_j)
+    double2* Yc;        // [nfb][nmom][na_pad]     conj(Y_l^m(j))
+    int na_pad, nclass, nq, L, nmom, f0, nfb;
+};
+
+__global__ void __launch_bounds__(128) mp_sphere_basis_kernel(MpSphereBasis a) {
+    const size_t n = (size_t)a.nfb * a.na_pad;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int fl = (int)(i / a.na_pad), j = (int)(i - (size_t)fl * a.na_pad);
+        const float4 c = a.sph[(size_t)(a.f0 + fl) * a.na_pad + j];
+        conj_ylm_row(a.L, (double)c.z, (double)c.y, a.idx, a.Yc + (size_t)fl * a.nmom * a.na_pad + j, a.na_pad);
+        const int cl = a.cls[j];
+        for (int q = 0; q < a.nq; ++q) {
+            const double b = cl >= 0 ? a.cf[(size_t)q * a.nclass + cl] : 0.0;
+            sph_bessel_row(a.L, a.qlen[q] * (double)c.x, b,
+                           a.Jb + ((size_t)(fl * a.nq + q) * (a.L + 1)) * a.na_pad + j, a.na_pad);
+        }
+    }
+}
+
+struct MpSphereContract {
+    const double* Jb;
+    const double2* Yc;
+    const int* perm;    // moments grouped by l
+    const int* gl;      // [ngroups] l of the group
+    const int* gstart;  // [ngroups] first entry in perm
+    const int* gcount;  // [ngroups]
+    double2* A;         // [nq][nmom][nf]
+    int na_pad, na, nq, L, nmom, nf, f0;
+};
+
+constexpr int kContractThreads = 256, kContractOutputs = 4;
+
+__global__ void __launch_bounds__(kContractThreads) mp_sphere_contract_kernel(MpSphereContract a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int g = blockIdx.x, fl = blockIdx.y;
+    const int l = a.gl[g], k0 = a.gstart[g], cnt = a.gcount[g];
+    const int nout = a.nq * cnt;
+    const int obase = blockIdx.z * kContractThreads * kContractOutputs;
+    if (obase >= nout) return;
+    double* Js = reinterpret_cast<double*>(smem);                    // [nq][T]
+    double2* Ys = reinterpret_cast<double2*>(Js + (size_t)a.nq * kMpTileAtoms);  // [cnt][T]
+    double2 acc[kContractOutputs];
+#pragma unroll
+    for (int r = 0; r < kContractOutputs; ++r) acc[r] = make_double2(0.0, 0.0);
+    const double* jrow = a.Jb + (size_t)fl * a.nq * (a.L + 1) * a.na_pad;
+    const double2* yrow = a.Yc + (size_t)fl * a.nmom * a.na_pad;
+    const int jend = (a.na + kMpTileAtoms - 1) / kMpTileAtoms * kMpTileAtoms;  // <= na_pad
+    for (int j0 = 0; j0 < jend; j0 += kMpTileAtoms) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < a.nq * kMpTileAtoms; t += kContractThreads) {
+            const int q = t / kMpTileAtoms, jj = t - q * kMpTileAtoms;
+            Js[t] = jrow[((size_t)q * (a.L + 1) + l) * a.na_pad + j0 + jj];
+        }
+        for (int t = threadIdx.x; t < cnt * kMpTileAtoms; t += kContractThreads) {
+            const int kk = t / kMpTileAtoms, jj = t - kk * kMpTileAtoms;
+            Ys[t] = yrow[(size_t)a.perm[k0 + kk] * a.na_pad + j0 + jj];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < kContractOutputs; ++r) {
+            const int o = obase + threadIdx.x + r * kContractThreads;
+            if (o < nout) {
+                const int q = o / cnt, kk = o - q * cnt;
+                const double* jq = Js + q * kMpTileAtoms;
+                const double2* yk = Ys + kk * kMpTileAtoms;
+                double2 s = acc[r];
+                for (int jj = 0; jj < kMpTileAtoms; ++jj) {
+                    s.x = fma(jq[jj], yk[jj].x, s.x);
+                    s.y = fma(jq[jj], yk[jj].y, s.y);
+                }
+                acc[r] = s;
+            }
+        }
+    }
+    // times 4 pi i^l
+    const double f4 = 4 * 3.14159265358979323846;
+#pragma unroll
+    for (int r = 0; r < kContractOutputs; ++r) {
+        const int o = obase + threadIdx.x + r * kContractThreads;
+        if (o < nout) {
+            const int q = o / cnt, kk = o - q * cnt, mom = a.perm[k0 + kk];
+            double2 v = acc[r], w;
+            switch (l & 3) {
+                case 0: w = make_double2(v.x, v.y); break;
+                case 1: w = make_double2(-v.y, v.x); break;
+                case 2: w = make_double2(-v.x, -v.y); break;
+                default: w = make_double2(v.y, -v.x); break;
+            }
+            a.A[((size_t)q * a.nmom + mom) * a.nf + a.f0 + fl] = make_double2(f4 * w.x, f4 * w.y);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// cylinder
+// ---------------------------------------------------------------------------------------
+struct MpCylinder {
+    const float4* cyl;   // [nf][na_pad] (r, phi, z)
+    const int* cls;
+    const double* cf;    // [nq][nclass]
+    const double* qcyl;  // [nq][3] (q_r, phi_q, q_z)
+    const int* mom;      // [nmom][2]
+    double2* A;          // [nq][nmom][nf]
+    int na_pad, na, nclass, nq, N, nmom, nf;
+};
+
+__global__ void __launch_bounds__(kMpCylThreads) mp_cylinder_kernel(MpCylinder a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int q = blockIdx.x, f = blockIdx.y, N = a.N, W = N + 1;
+    double* Jn = reinterpret_cast<double*>(smem);        // [W][TA]
+    double* cn = Jn + (size_t)W * kMpCylAtoms;            // [W][TA] cos(n phi)
+    double* sn = cn + (size_t)W * kMpCylAtoms;            // [W][TA] sin(n phi)
+    double2* X = reinterpret_cast<double2*>(sn + (size_t)W * kMpCylAtoms);  // [TA]
+    double2* Sc = X + kMpCylAtoms;                         // [W] after the atom loop
+    double2* Ss = Sc + W;
+    const double qr = a.qcyl[3 * q], qphi = a.qcyl[3 * q + 1], qz = a.qcyl[3 * q + 2];
+    // this thread's orders: n = threadIdx.x + 64 k
+    constexpr int NPT = (2 * kMpMaxL + 1 + kMpCylThreads - 1) / kMpCylThreads;
+    double2 ac[NPT], as[NPT];
+#pragma unroll
+    for (int k = 0; k < NPT; ++k) ac[k] = as[k] = make_double2(0.0, 0.0);
+    const float4* row = a.cyl + (size_t)f * a.na_pad;
+    for (int j0 = 0; j0 < a.na; j0 += kMpCylAtoms) {
+        __syncthreads();
+        {
+            const int jj = threadIdx.x, j = j0 + jj;
+            if (j < a.na) {
+                const float4 c = row[j];
+                const double r = c.x, phi = c.y, z = c.z;
+                const int cl = a.cls[j];
+                const double b = cl >= 0 ? a.cf[(size_t)q * a.nclass + cl] : 0.0;
+                double sgn = 1.0;  // parallel_sign, multipole_scatter_device.cpp:944-948
+                if (z != 0 && qz != 0) sgn = (z * qz) / (fabs(z) * fabs(qz));
+                double es, ec;
+                sincos(sgn * z * qz, &es, &ec);
+                X[jj] = make_double2(b * ec, b * es);
+                cyl_bessel_row(N, r * qr, Jn + jj, kMpCylAtoms);
+                double s1, c1;
+                sincos(phi, &s1, &c1);
+                double cp = 1, sp = 0;  // cos, sin of n phi by rotation
+                for (int n = 0; n <= N; ++n) {
+                    cn[n * kMpCylAtoms + jj] = cp;
+                    sn[n * kMpCylAtoms + jj] = sp;
+                    const double cq = cp * c1 - sp * s1;
+                    sp = sp * c1 + cp * s1;
+                    cp = cq;
+                }
+            } else {
+                X[jj] = make_double2(0.0, 0.0);
+                for (int n = 0; n <= N; ++n) Jn[n * kMpCylAtoms + jj] = cn[n * kMpCylAtoms + jj] = sn[n * kMpCylAtoms + jj] = 0;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < NPT; ++k) {
+            const int n = threadIdx.x + k * kMpCylThreads;
+            if (n <= N) {
+                double2 sc = ac[k], ss = as[k];
+                for (int jj = 0; jj < kMpCylAtoms; ++jj) {
+                    const double2 x = X[jj];
+                    const double jv = Jn[n * kMpCylAtoms + jj];
+                    const double wc = jv * cn[n * kMpCylAtoms + jj], ws = jv * sn[n * kMpCylAtoms + jj];
+                    sc.x = fma(x.x, wc, sc.x);
+                    sc.y = fma(x.y, wc, sc.y);
+                    ss.x = fma(x.x, ws, ss.x);
+                    ss.y = fma(x.y, ws, ss.y);
+                }
+                ac[k] = sc;
+                as[k] = ss;
+            }
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NPT; ++k) {
+        const int n = threadIdx.x + k * kMpCylThreads;
+        if (n <= N) {
+            Sc[n] = ac[k];
+            Ss[n] = as[k];
+        }
+    }
+    __syncthreads();
+    const double norm = sqrt(2 * 3.14159265358979323846), h = 0.70710678118654752440;
+    for (int k = threadIdx.x; k < a.nmom; k += kMpCylThreads) {
+        const int l = a.mom[2 * k], m = a.mom[2 * k + 1];
+        double2 v;
+        if (l == 0 && m == 0) {
+            v = Sc[0];
+        } else {
+            const int n = m < 2 ? 2 * l : 2 * l - 1;
+            double snq, cnq;
+            sincos(n * qphi, &snq, &cnq);
+            const double2 C = Sc[n], S = Ss[n];
+            double2 t;  // sum_j X_j J_n cos / sin (n (phi_j - phi_q))
+            if (m == 0 || m == 2) t = make_double2(cnq * C.x + snq * S.x, cnq * C.y + snq * S.y);
+            else t = make_double2(cnq * S.x - snq * C.x, cnq * S.y - snq * C.y);
+            if (m < 2) {
+                const double c = h * 2.0 * ((l & 1) ? -1.0 : 1.0);
+                v = make_double2(c * t.x, c * t.y);
+            } else {  // times i sqrt(1/2) 2 (-1)^(l-1)
+                const double c = h * 2.0 * (((l - 1) & 1) ? -1.0 : 1.0);
+                v = make_double2(-c * t.y, c * t.x);
+            }
+        }
+        a.A[((size_t)q * a.nmom + k) * a.nf + f] = make_double2(norm * v.x, norm * v.y);
+    }
+}
+
+size_t cylinder_smem(int N) {
+    const size_t W = (size_t)N + 1;
+    return 3 * W * kMpCylAtoms * sizeof(double) + kMpCylAtoms * sizeof(double2) + 2 * W * sizeof(double2);
+}
+
+// ---------------------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------------------
+struct V3 {
+    double x, y, z;
+};
+V3 cross3(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+double len3(V3 a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+V3 div3(V3 a, double l) { return {a.x / l, a.y / l, a.z / l}; }
+
+// CartesianVectorBase(axis), coor3d.cpp:278-295
+bool axis_base(const double* axis, MpBase& b) {
+    V3 a{axis[0], axis[1], axis[2]};
+    if (!(len3(a) > 0)) return false;
+    V3 ez = div3(a, len3(a));
+    V3 ekez = cross3(V3{0, 0, 1}, ez);
+    if (len3(ekez) == 0) ekez = cross3(V3{0, 1, 0}, ez);
+    V3 er = div3(ekez, len3(ekez));
+    V3 ezer = cross3(ez, er);
+    V3 ephi = div3(ezer, len3(ezer));
+    const V3 e[3] = {er, ephi, ez};
+    for (int k = 0; k < 3; ++k) {
+        b.e[3 * k] = e[k].x;
+        b.e[3 * k + 1] = e[k].y;
+        b.e[3 * k + 2] = e[k].z;
+    }
+    return true;
+}
+
+int fail(std::string& m, int code, const std::string& what) {
+    m = what;
+    return code;
+}
+
+}  // namespace
+
+}  // namespace sassgpu
+
+using namespace sassgpu;
+
+extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const double* qvectors,
+                                      const double* class_factors, size_t nmom, const int32_t* moments,
+                                      const double* axis, double* fqt, double* fq, double* fq2) {
+    if (!p) return SASS_ERR_ARG;
+    if (nq == 0) return SASS_OK;
+    if (!qvectors || !class_factors || !moments || !fqt || !fq || !fq2 || nmom == 0)
+        return fail(p->msg, SASS_ERR_ARG, "NULL argument or no moments");
+    if (type != SASS_MULTIPOLE_SPHERE && type != SASS_MULTIPOLE_CYLINDER)
+        return fail(p->msg, SASS_ERR_ARG, "multipole type must be sphere or cylinder");
+    if (p->d.precision != SASS_PRECISION_FP64 || p->d.scattering != SASS_SCATTERING_ALL)
+        return fail(p->msg, SASS_ERR_UNSUPPORTED, "multipole devices need a coherent FP64 plan");
+    if (!p->sys.staged || !p->sys.classes_set) return fail(p->msg, SASS_ERR_STATE, "plan not staged");
+    const bool cyl = type == SASS_MULTIPOLE_CYLINDER;
+    int L = 0;  // largest major moment
+    for (size_t k = 0; k < nmom; ++k) {
+        const int l = moments[2 * k], m = moments[2 * k + 1];
+        // the reference's checks, parameters.cpp:1076-1114
+        if (l < 0) return fail(p->msg, SASS_ERR_ARG, "major multipole moment must be >= 0");
+        if (!cyl && std::abs(m) > l) return fail(p->msg, SASS_ERR_ARG, "minor multipole moment must be within -major..major");
+        if (cyl && (m < 0 || m > 3)) return fail(p->msg, SASS_ERR_ARG, "minor multipole moment must be between 0 and 3");
+        if (cyl && l == 0 && m != 0) return fail(p->msg, SASS_ERR_ARG, "minor multipole moment must be 0 for major 0");
+        L = std::max(L, l);
+    }
+    if (L > kMpMaxL) return fail(p->msg, SASS_ERR_UNSUPPORTED, "major multipole moments above 40 are not supported");
+    MpBase base{};
+    if (cyl && (!axis || !axis_base(axis, base))) return fail(p->msg, SASS_ERR_ARG, "cylinder axis must be a nonzero vector");
+
+    std::string& m = p->msg;
+    auto cuda_fail = [&](cudaError_t e, const char* what) {
+        cudaGetLastError();
+        m = std::string(what) + ": " + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? SASS_ERR_OOM : SASS_ERR_CUDA;
+    };
+#define MCK(expr)                                  \
+    do {                                           \
+        cudaError_t e_ = (expr);                   \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #expr); \
+    } while (0)
+    MCK(cudaSetDevice(p->d.device));
+    memset(&p->timing, 0, sizeof(p->timing));
+    SystemState& s = p->sys;
+    const size_t nf = s.nf, na_pad = s.na_pad, nclass = s.nclass;
+    cudaStream_t st = p->st;
+
+    // representation cache
+    if (s.mp_type != type || !s.mp_valid || (cyl && memcmp(s.mp_axis, axis, sizeof(s.mp_axis)) != 0)) {
+        MCK(s.mp_xyz.ensure(nf * na_pad * sizeof(float4)));
+        const size_t n = nf * na_pad;
+        const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+        mp_convert_kernel<<<std::max(blocks, 1), 256, 0, st>>>(s.xyz.as<float4>(), (int)na_pad, (int)s.na, (int)nf, cyl,
+                                                                base, s.mp_xyz.as<float4>());
+        MCK(cudaGetLastError());
+        s.mp_type = type;
+        s.mp_valid = true;
+        if (cyl) memcpy(s.mp_axis, axis, sizeof(s.mp_axis));
+    }
+
+    // per-q inputs, moments, outputs
+    std::vector<double> qin(cyl ? 3 * nq : nq);
+    for (size_t i = 0; i < nq; ++i) {
+        const double* qv = qvectors + 3 * i;
+        if (!cyl) {
+            qin[i] = sqrt(qv[0] * qv[0] + qv[1] * qv[1] + qv[2] * qv[2]);  // q.length()
+        } else {
+            const double px = qv[0] * base.e[0] + qv[1] * base.e[1] + qv[2] * base.e[2];
+            const double py = qv[0] * base.e[3] + qv[1] * base.e[4] + qv[2] * base.e[5];
+            const double pz = qv[0] * base.e[6] + qv[1] * base.e[7] + qv[2] * base.e[8];
+            to_cylinder(px, py, pz, qin[3 * i], qin[3 * i + 1], qin[3 * i + 2]);
+        }
+    }
+    // sphere: lookup (l, m) -> moment and moments grouped by l
+    const int W = 2 * L + 1;
+    std::vector<int> idx((size_t)(L + 1) * W, -1), perm, gl, gstart, gcount;
+    if (!cyl) {
+        for (size_t k = 0; k < nmom; ++k) idx[moments[2 * k] * W + L + moments[2 * k + 1]] = (int)k;
+        for (int l = 0; l <= L; ++l) {
+            const int start = (int)perm.size();
+            for (size_t k = 0; k < nmom; ++k)
+                if (moments[2 * k] == l) perm.push_back((int)k);
+            if ((int)perm.size() > start) {
+                gl.push_back(l);
+                gstart.push_back(start);
+                gcount.push_back((int)perm.size() - start);
+            }
+        }
+    }
+    DevBuf d_qin, d_cf, d_mom, d_idx, d_perm, d_gl, d_gs, d_gc, d_amp, d_out, d_Jb, d_Yc;
+    auto up = [&](DevBuf& b, const void* h, size_t bytes) -> cudaError_t {
+        cudaError_t e = b.ensure(bytes);
+        if (e != cudaSuccess) return e;
+        return cudaMemcpy(b.p, h, bytes, cudaMemcpyHostToDevice);
+    };
+    MCK(up(d_qin, qin.data(), qin.size() * sizeof(double)));
+    MCK(up(d_cf, class_factors, nq * nclass * sizeof(double)));
+    MCK(up(d_mom, moments, nmom * 2 * sizeof(int)));
+    MCK(d_amp.ensure(nq * nmom * nf * sizeof(double2)));
+    MCK(d_out.ensure(nq * (nf + 2) * sizeof(double2)));
+    MCK(cudaEventRecord(p->ev[0], st));
+    if (!cyl) {
+        MCK(up(d_idx, idx.data(), idx.size() * sizeof(int)));
+        MCK(up(d_perm, perm.data(), perm.size() * sizeof(int)));
+        MCK(up(d_gl, gl.data(), gl.size() * sizeof(int)));
+        MCK(up(d_gs, gstart.data(), gstart.size() * sizeof(int)));
+        MCK(up(d_gc, gcount.data(), gcount.size() * sizeof(int)));
+        // frame batches sized to about 1 GB of basis
+        const size_t per_frame = na_pad * (nq * (L + 1) * sizeof(double) + nmom * sizeof(double2));
+        const size_t nfb = std::max<size_t>(1, std::min<size_t>(nf, ((size_t)1 << 30) / per_frame));
+        MCK(d_Jb.ensure(nfb * nq * (L + 1) * na_pad * sizeof(double)));
+        MCK(d_Yc.ensure(nfb * nmom * na_pad * sizeof(double2)));
+        int maxcnt = 0;
+        for (int c : gcount) maxcnt = std::max(maxcnt, c);
+        const size_t csm = nq * kMpTileAtoms * sizeof(double) + (size_t)maxcnt * kMpTileAtoms * sizeof(double2);
+        if (csm > 48 * 1024)
+            MCK(cudaFuncSetAttribute(mp_sphere_contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
+        const int zchunks = (int)((nq * maxcnt + kContractThreads * kContractOutputs - 1) /
+                                  (kContractThreads * kContractOutputs));
+        for (size_t f0 = 0; f0 < nf; f0 += nfb) {
+            const int nb = (int)std::min(nfb, nf - f0);
+            MpSphereBasis ba{};
+            ba.sph = s.mp_xyz.as<float4>();
+            ba.cls = s.cls.as<int>();
+            ba.cf = d_cf.as<double>();
+            ba.qlen = d_qin.as<double>();
+            ba.idx = d_idx.as<int>();
+            ba.Jb = d_Jb.as<double>();
+            ba.Yc = d_Yc.as<double2>();
+            ba.na_pad = (int)na_pad;
+            ba.nclass = (int)nclass;
+            ba.nq = (int)nq;
+            ba.L = L;
+            ba.nmom = (int)nmom;
+            ba.f0 = (int)f0;
+            ba.nfb = nb;
+            const size_t nthreads = (size_t)nb * na_pad;
+            mp_sphere_basis_kernel<<<(unsigned)std::min<size_t>((nthreads + 127) / 128, 152 * 64), 128, 0, st>>>(ba);
+            MCK(cudaGetLastError());
+            MpSphereContract ca{};
+            ca.Jb = d_Jb.as<double>();
+            ca.Yc = d_Yc.as<double2>();
+            ca.perm = d_perm.as<int>();
+            ca.gl = d_gl.as<int>();
+            ca.gstart = d_gs.as<int>();
+            ca.gcount = d_gc.as<int>();
+            ca.A = d_amp.as<double2>();
+            ca.na_pad = (int)na_pad;
+            ca.na = (int)s.na;
+            ca.nq = (int)nq;
+            ca.L = L;
+            ca.nmom = (int)nmom;
+            ca.nf = (int)nf;
+            ca.f0 = (int)f0;
+            dim3 grid((unsigned)gl.size(), (unsigned)nb, (unsigned)zchunks);
+            mp_sphere_contract_kernel<<<grid, kContractThreads, csm, st>>>(ca);
+            MCK(cudaGetLastError());
+        }
+    } else {
+        MpCylinder ca{};
+        ca.cyl = s.mp_xyz.as<float4>();
+        ca.cls = s.cls.as<int>();
+        ca.cf = d_cf.as<double>();
+        ca.qcyl = d_qin.as<double>();
+        ca.mom = d_mom.as<int>();
+        ca.A = d_amp.as<double2>();
+        ca.na_pad = (int)na_pad;
+        ca.na = (int)s.na;
+        ca.nclass = (int)nclass;
+        ca.nq = (int)nq;
+        ca.N = 2 * L;
+        ca.nmom = (int)nmom;
+        ca.nf = (int)nf;
+        const size_t sm = cylinder_smem(2 * L);
+        if (sm > 48 * 1024) MCK(cudaFuncSetAttribute(mp_cylinder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        mp_cylinder_kernel<<<dim3((unsigned)nq, (unsigned)nf), kMpCylThreads, sm, st>>>(ca);
+        MCK(cudaGetLastError());
+    }
+    // correlation and average of the amplitudes: moments play the sub-vectors
+    EngineConfig cfg;
+    cfg.scattering = p->d.scattering;
+    cfg.dsp = p->d.dsp_type;
+    cfg.method = p->d.dsp_method;
+    cfg.precision = p->d.precision;
+    cfg.device = p->d.device;
+    std::vector<WorkItem> items(1);
+    WorkItem& it = items[0];
+    it.sys = &s;
+    for (size_t i = 0; i <= nq; ++i) it.offs.push_back(i * nmom);
+    it.d_cf = d_cf.as<double>();
+    double2* o = d_out.as<double2>();
+    it.d_fqt = o;
+    it.d_fq = o + nq * nf;
+    it.d_fq2 = o + nq * (nf + 1);
+    it.d_amp_given = d_amp.as<double2>();
+    it.norm = cyl ? 1.0 / (2 * 3.14159265358979323846) : 1.0 / (4 * 3.14159265358979323846);
+    int rc = p->eng.prepare(cfg, items, p->msg);
+    if (rc) return rc;
+    MCK(cudaEventRecord(p->ev[1], st));
+    cudaEvent_t ev[4] = {p->ev[8], p->ev[9], p->ev[2], p->ev[3]};
+    rc = p->eng.enqueue(st, p->msg, ev);
+    if (rc) return rc;
+    std::vector<double2> host(nq * (nf + 2));
+    MCK(cudaMemcpyAsync(host.data(), o, host.size() * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    MCK(cudaStreamSynchronize(st));
+    unsigned flag = 0;
+    MCK(cudaMemcpy(&flag, p->eng.err_word(), sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (flag) return fail(p->msg, SASS_ERR_TIMEOUT, "device error flag " + std::to_string(flag));
+    memcpy(fqt, host.data(), nq * nf * sizeof(double2));
+    memcpy(fq, host.data() + nq * nf, nq * sizeof(double2));
+    memcpy(fq2, host.data() + nq * (nf + 1), nq * sizeof(double2));
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, p->ev[0], p->ev[1]) == cudaSuccess) p->timing.phase_ms = ms;
+    if (cudaEventElapsedTime(&ms, p->ev[9], p->ev[2]) == cudaSuccess) p->timing.corr_ms = ms;
+    if (cudaEventElapsedTime(&ms, p->ev[2], p->ev[3]) == cudaSuccess) p->timing.finalize_ms = ms;
+    if (cudaEventElapsedTime(&ms, p->ev[0], p->ev[3]) == cudaSuccess) p->timing.total_ms = ms;
+    cudaGetLastError();
+    p->msg.clear();
+    return SASS_OK;
+#undef MCK
+}
