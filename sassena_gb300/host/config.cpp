@@ -2,6 +2,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <fstream>
 #include <regex>
 #include <sstream>
@@ -193,7 +194,13 @@ void Params::read_xml(const std::string& path) {
             vectors_filepath = get_filepath(vectors_file);
             orientations = create_orientations(*this);
         } else if (orientation_type == "multipole") {
-            throw std::runtime_error("Orientation averaging type multipole is not supported by this build");
+            const std::string b = "//scattering/average/orientation/multipole/";
+            if (x.exists(b + "type")) multipole_type = x.get_string(b + "type");
+            if (x.exists(b + "moments/type")) moments_type = x.get_string(b + "moments/type");
+            if (x.exists(b + "moments/resolution")) moments_resolution = (long)x.get_long(b + "moments/resolution");
+            if (x.exists(b + "moments/file")) moments_file = x.get_string(b + "moments/file");
+            moments_filepath = get_filepath(moments_file);
+            moments = create_moments(*this);
         } else if (orientation_type != "none") {
             throw std::runtime_error("Orientation averaging type not understood: " + orientation_type);
         }
@@ -296,6 +303,43 @@ std::vector<Vec3> create_from_scans(const std::vector<ScanParams>& scans) {
             for (auto& b : q[1])
                 for (auto& c : q[2]) out.push_back(add(add(a, b), c));
     return out;
+}
+
+std::vector<std::pair<long, long>> create_moments(const Params& p) {
+    std::vector<std::pair<long, long>> m;
+    if (p.moments_type == "file") {
+        std::ifstream f(p.moments_filepath);
+        if (!f) throw std::runtime_error("cannot open multipole moments file " + p.moments_filepath);
+        long major, minor;
+        while (f >> major >> minor) m.emplace_back(major, minor);
+    } else if (p.moments_type == "resolution") {
+        if (p.multipole_type == "sphere") {
+            m.emplace_back(0, 0);
+            for (long l = 1; l <= p.moments_resolution; ++l)
+                for (long k = -l; k <= l; ++k) m.emplace_back(l, k);
+        } else if (p.multipole_type == "cylinder") {
+            m.emplace_back(0, 0);
+            for (long l = 1; l <= p.moments_resolution; ++l)
+                for (long k = 0; k < 4; ++k) m.emplace_back(l, k);
+        } else {
+            throw std::runtime_error("Type not understood: scattering.average.orientation.multipole.moments.type=" +
+                                     p.moments_type);
+        }
+    } else {
+        throw std::runtime_error("Type not understood: scattering.average.orientation.multipole.type=" +
+                                 p.multipole_type);
+    }
+    for (const auto& mm : m) {
+        if (mm.first < 0) throw std::runtime_error("Major multipole moment must be >= 0!");
+        if (p.multipole_type == "cylinder") {
+            if (mm.second < 0 || mm.second > 3) throw std::runtime_error("Minor multipole moment must be between 0 and 3!");
+            if (mm.first == 0 && mm.second != 0) throw std::runtime_error("Minor multipole moment must be 0 for Major 0!");
+        } else if (p.multipole_type == "sphere") {
+            if (std::labs(mm.second) > mm.first)
+                throw std::runtime_error("Minor multipole moment must be between -Major and +Major!");
+        }
+    }
+    return m;
 }
 
 std::vector<Vec3> create_orientations(const Params& p) {

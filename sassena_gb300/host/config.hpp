@@ -64,6 +64,11 @@ struct Params {
     unsigned long seed = 0;
     std::string vectors_file = "qvector-orientations.txt", vectors_filepath;
     std::vector<Vec3> orientations;  // unit vectors (file, sphere) or 2-D (cylinder)
+    // orientation type "multipole" (parameters.cpp:386-389, 552-576)
+    std::string multipole_type = "sphere", moments_type;
+    long moments_resolution = 20;
+    std::string moments_file = "moments.txt", moments_filepath;
+    std::vector<std::pair<long, long>> moments;  // (major, minor)
     std::string signal_file = "signal.h5", signal_filepath;
     bool signal_fqt = true, signal_fq0 = true, signal_fq = true, signal_fq2 = true;
     // limits
@@ -88,6 +93,9 @@ std::vector<Vec3> create_from_scans(const std::vector<ScanParams>& scans);
 // cylinder raster_linear as the reference; sphere/cylinder random draws use this
 // project's seeded generator, not Boost's mt19937 stream).
 std::vector<Vec3> create_orientations(const Params& p);
+// ScatteringAverageOrientationMultipoleMomentsParameters::create, parameters.cpp:1037-1122
+// (file or resolution, then the validity checks).
+std::vector<std::pair<long, long>> create_moments(const Params& p);
 
 struct FunctionEntry {
     size_t type = 0;

@@ -165,6 +165,11 @@ bool run_scatter_device(const Params& p, Database& db, const Sample& s, RunStats
     out.database = db.rawconfig;
 
     // ---- device -------------------------------------------------------------------------------
+    // ScatterDeviceFactory::create, scatter_device_factory.cpp:145-201
+    const bool multipole = p.scattering_type == "all" && p.orientation_type == "multipole";
+    if (multipole && p.multipole_type != "sphere" && p.multipole_type != "cylinder")
+        throw std::runtime_error("scattering.average.orientation.multipole.type not understood: " + p.multipole_type);
+    if (multipole && p.precision != "fp64") info("The multipole devices run the FP64 form.");
     ScatterClasses cls = build_classes(p, db, s);
     sass_plan_desc d{};
     d.scattering = p.scattering_type == "self" ? SASS_SCATTERING_SELF : SASS_SCATTERING_ALL;
@@ -172,7 +177,7 @@ bool run_scatter_device(const Params& p, Database& db, const Sample& s, RunStats
                  : p.dsp_type == "plain" ? SASS_DSP_PLAIN
                                          : SASS_DSP_AUTOCORRELATE;
     d.dsp_method = p.dsp_method == "direct" ? SASS_METHOD_DIRECT : SASS_METHOD_FFTW;
-    d.precision = p.precision == "fp32" ? SASS_PRECISION_FP32 : SASS_PRECISION_FP64;
+    d.precision = (p.precision == "fp32" && !multipole) ? SASS_PRECISION_FP32 : SASS_PRECISION_FP64;
     d.na = na;
     d.nf = nf;
     d.nclass = cls.id.size();
@@ -208,24 +213,43 @@ bool run_scatter_device(const Params& p, Database& db, const Sample& s, RunStats
     info("Staged " + std::to_string(nf) + " frames x " + std::to_string(na) + " atoms (sd:stage " +
          std::to_string(st.stage_s) + " s)");
 
+    std::vector<int32_t> moments;
+    for (const auto& mm : p.moments) {
+        moments.push_back((int32_t)mm.first);
+        moments.push_back((int32_t)mm.second);
+    }
+    const double axis[3] = {p.axis[0], p.axis[1], p.axis[2]};
+
     // sd:compute in batches of whole q-vectors
     const size_t batch = p.batch_q ? p.batch_q : todo.size();
     double last_flush = now_s();
     for (size_t i0 = 0; i0 < todo.size(); i0 += batch) {
         const size_t i1 = std::min(todo.size(), i0 + batch), nq = i1 - i0;
         std::vector<size_t> offs(1, 0);
-        std::vector<double> sv, cf;
+        std::vector<double> sv, cf, qv;
         for (size_t i = i0; i < i1; ++i) {
-            std::vector<Vec3> sub = subvectors_for(p, todo[i]);
-            for (const Vec3& v : sub) sv.insert(sv.end(), v.begin(), v.end());
-            offs.push_back(offs.back() + sub.size());
+            if (multipole) {
+                qv.insert(qv.end(), todo[i].begin(), todo[i].end());
+                offs.push_back(offs.back() + p.moments.size());
+            } else {
+                std::vector<Vec3> sub = subvectors_for(p, todo[i]);
+                for (const Vec3& v : sub) sv.insert(sv.end(), v.begin(), v.end());
+                offs.push_back(offs.back() + sub.size());
+            }
             std::vector<double> f = cls.factors(db, p.background_factor, len(todo[i]));
             cf.insert(cf.end(), f.begin(), f.end());
         }
         std::vector<double> fqt(nq * nf * 2), fq(nq * 2), fq2(nq * 2);
         double tc = now_s();
-        check(plan, sass_compute(plan, nq, offs.data(), sv.data(), cf.data(), fqt.data(), fq.data(), fq2.data(), 0),
-              "sass_compute");
+        if (multipole)
+            check(plan,
+                  sass_multipole_compute(plan, p.multipole_type == "sphere" ? SASS_MULTIPOLE_SPHERE : SASS_MULTIPOLE_CYLINDER,
+                                         nq, qv.data(), cf.data(), p.moments.size(), moments.data(), axis, fqt.data(),
+                                         fq.data(), fq2.data()),
+                  "sass_multipole_compute");
+        else
+            check(plan, sass_compute(plan, nq, offs.data(), sv.data(), cf.data(), fqt.data(), fq.data(), fq2.data(), 0),
+                  "sass_compute");
         st.compute_s += now_s() - tc;
         st.nsub += offs.back();
         st.terms += (double)offs.back() * (double)na * (double)nf;

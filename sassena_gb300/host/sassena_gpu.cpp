@@ -45,7 +45,7 @@ void dry_run(const Params& p, Database& db, const Sample& s, const std::string& 
     o << ",\"orientations\":";
     json_vecs(o, p.orientations);
     o << ",\"subvectors_q0\":";
-    json_vecs(o, subvectors_for(p, p.qvectors.at(0)));
+    json_vecs(o, p.orientation_type == "multipole" ? std::vector<Vec3>() : subvectors_for(p, p.qvectors.at(0)));
     o << ",\"atom_class\":[";
     for (size_t i = 0; i < c.atom_class.size(); ++i) o << (i ? "," : "") << c.atom_class[i];
     o << "],\"class_labels\":[";
@@ -68,6 +68,11 @@ void dry_run(const Params& p, Database& db, const Sample& s, const std::string& 
     char b[64];
     snprintf(b, sizeof(b), "%.17g", sum);
     o << "],\"coord_sum\":" << b;
+    o << ",\"orientation\":\"" << p.orientation_type << "\",\"multipole\":\"" << p.multipole_type
+      << "\",\"moments\":[";
+    for (size_t i = 0; i < p.moments.size(); ++i)
+        o << (i ? "," : "") << "[" << p.moments[i].first << "," << p.moments[i].second << "]";
+    o << "]";
     o << ",\"scattering\":\"" << p.scattering_type << "\",\"dsp\":\"" << p.dsp_type << "\",\"method\":\""
       << p.dsp_method << "\",\"precision\":\"" << p.precision << "\",\"signal\":\"" << p.signal_filepath
       << "\"}\n";

@@ -288,13 +288,14 @@ def write_database(path, w, sfactor_params=None):
 
 
 def write_files(directory, w, precision="fp64", method="fftw", qvectors_file=True,
-                signal="signal.h5", sfactor_params=None, extra=""):
+                signal="signal.h5", sfactor_params=None, extra="", average=None):
     """Write sample.pdb, sample.dcd, db.xml, qvectors.txt, orientations.txt and scatter.xml
     for workload `w` into `directory`; returns the scatter.xml path.
 
     q-vectors are |q_s| along x (the orientation set ignores the q direction,
     abstract_vectors_scatter_device.cpp:123-129) and the directions come from a file
-    (vectors.type=file, parameters.cpp:932-943)."""
+    (vectors.type=file, parameters.cpp:932-943). `average` replaces the <average> element
+    (e.g. a multipole orientation)."""
     import os
     if sfactor_params is None and not np.all(w.class_factors == w.class_factors[:1]):
         raise ValueError("type-0 database factors cannot vary with |q|; pass sfactor_params")
@@ -319,16 +320,16 @@ def write_files(directory, w, precision="fp64", method="fftw", qvectors_file=Tru
     <type>%(type)s</type>
     <vectors><type>file</type><file>qvectors.txt</file></vectors>
     <dsp><type>%(dsp)s</type><method>%(method)s</method></dsp>
-    <average><orientation><type>vectors</type>
-      <vectors><type>file</type><file>orientations.txt</file></vectors>
-    </orientation></average>
+    %(average)s
     <signal><file>%(signal)s</file></signal>
   </scattering>
   <gpu><precision>%(precision)s</precision></gpu>
   %(extra)s
 </root>
 """ % dict(type=w.scattering, dsp=w.dsp, method=method, signal=signal, precision=precision,
-           extra=extra)
+           extra=extra, average=average or """<average><orientation><type>vectors</type>
+      <vectors><type>file</type><file>orientations.txt</file></vectors>
+    </orientation></average>""")
     path = os.path.join(directory, "scatter.xml")
     with open(path, "w") as f:
         f.write(xml)

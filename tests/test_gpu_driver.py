@@ -110,3 +110,36 @@ def test_driver_rejects_nf_mismatch_on_resume(native_lib, tmp_path):
         f.write("0.77 0 0\n")
     r = subprocess.run([abi.DRIVER_PATH, "--config", cfg], capture_output=True, text=True)
     assert r.returncode == 1 and "NF=" in r.stderr
+
+
+@pytest.mark.parametrize("kind,resolution,axis", [("sphere", 6, None), ("cylinder", 5, (1.0, -0.5, 0.7))])
+def test_driver_multipole_matches_oracle(native_lib, tmp_path, kind, resolution, axis):
+    # scattering.average.orientation.type = multipole (scatter_device_factory.cpp:145-201):
+    # the q-vectors themselves enter, so the file gets general 3-vectors of the scan's lengths
+    w = small("all", "autocorrelate", seed=54, na=37, nf=16, nq=3, nm=4)
+    rng = np.random.default_rng(54)
+    q = rng.normal(size=(len(w.shells), 3))
+    q *= (w.shells / np.linalg.norm(q, axis=1))[:, None]
+    ax = "" if axis is None else "<axis><x>%r</x><y>%r</y><z>%r</z></axis>" % axis
+    average = ("<average><orientation><type>multipole</type><multipole><type>%s</type><moments>"
+               "<type>resolution</type><resolution>%d</resolution></moments></multipole>%s"
+               "</orientation></average>" % (kind, resolution, ax))
+    d = str(tmp_path / "run")
+    cfg = synth.write_files(d, w, precision="fp64", average=average)
+    with open(os.path.join(d, "qvectors.txt"), "w") as f:
+        for v in q:
+            f.write("%.17g %.17g %.17g\n" % tuple(v))
+    run(cfg)
+    qo, fqt, fq0, fq, _ = read_rows(os.path.join(d, "signal.h5"))
+    if kind == "sphere":
+        ref = oracle.mp_sphere(w.coords, q, w.factors(), oracle.sphere_moments(resolution))
+    else:
+        ref = oracle.mp_cylinder(w.coords, q, w.factors(), oracle.cylinder_moments(resolution), axis)
+    # rows in completion order: match them to the q-vectors
+    order = [int(np.argmin(np.abs(q - v).sum(axis=1))) for v in qo]
+    assert sorted(order) == list(range(len(q)))
+    rfqt = (ref[0][..., 0] + 1j * ref[0][..., 1])[order]
+    err = (np.abs(fqt - rfqt).max(axis=1) / np.abs(rfqt[:, 0])).max()
+    assert err <= 1e-12, err
+    assert np.array_equal(fq0, fqt[:, 0])
+    assert np.allclose(fq, (ref[1][:, 0] + 1j * ref[1][:, 1])[order], rtol=1e-12, atol=1e-14)

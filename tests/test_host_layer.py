@@ -239,3 +239,39 @@ def test_command_line_overrides(small_files, tmp_path):
     assert d["signal"].endswith("other.h5") and d["precision"] == "fp32"
     r = run_driver("--config", cfg, "--dry-run", str(tmp_path / "o.json"), "--no.such=1")
     assert r.returncode == 1 and "unknown option" in r.stderr
+
+
+def multipole_xml(kind, moments_type="resolution", resolution=3, extra=""):
+    return ("<average><orientation><type>multipole</type><multipole><type>%s</type><moments>"
+            "<type>%s</type><resolution>%d</resolution><file>moments.txt</file></moments>"
+            "</multipole>%s</orientation></average>" % (kind, moments_type, resolution, extra))
+
+
+def test_multipole_moments_from_configuration(small_files, tmp_path):
+    w, _ = small_files
+    d = str(tmp_path / "mp")
+    cfg = synth.write_files(d, w, average=multipole_xml("sphere", resolution=3))
+    j = dry(cfg, tmp_path)
+    assert j["orientation"] == "multipole" and j["multipole"] == "sphere"
+    assert [tuple(m) for m in j["moments"]] == oracle.sphere_moments(3)
+    cfg = synth.write_files(d, w, average=multipole_xml("cylinder", resolution=2))
+    assert [tuple(m) for m in dry(cfg, tmp_path)["moments"]] == oracle.cylinder_moments(2)
+    with open(os.path.join(d, "moments.txt"), "w") as f:
+        f.write("0 0\n4 -3\n2 1\n")
+    cfg = synth.write_files(d, w, average=multipole_xml("sphere", moments_type="file"))
+    assert [tuple(m) for m in dry(cfg, tmp_path)["moments"]] == [(0, 0), (4, -3), (2, 1)]
+
+
+@pytest.mark.parametrize("kind,lines,needle", [
+    ("sphere", "2 3\n", "between -Major and +Major"),
+    ("cylinder", "1 4\n", "between 0 and 3"),
+    ("cylinder", "0 2\n", "must be 0 for Major 0"),
+    ("sphere", "-1 0\n", "must be >= 0"),
+])
+def test_multipole_moment_checks(small_files, tmp_path, kind, lines, needle):
+    d = str(tmp_path / "mp")
+    cfg = synth.write_files(d, small_files[0], average=multipole_xml(kind, moments_type="file"))
+    with open(os.path.join(d, "moments.txt"), "w") as f:
+        f.write(lines)
+    r = run_driver("--config", cfg, "--dry-run", str(tmp_path / "x.json"))
+    assert r.returncode != 0 and needle in r.stderr, r.stderr
