@@ -18,6 +18,10 @@ lengths, 20 shells 0.05-3.0 1/A x 500 directions, FFT autocorrelation (padded le
   cpu_baseline  the CPU oracle (FP64 restatement of the reference, all host threads) on
              a bounded sample of the same workload.
 
+Other workloads (--workload): incoherent_fqt, static_xray, batched_uneven, layered_cv, and
+multipole_sphere / multipole_cylinder (the multipole devices on the coherent trajectory, FP64,
+terms = atoms x q-vectors x moments x frames).
+
 --impl reference times that CPU restatement (the reference itself cannot be built:
 MPI, Boost, FFTW3, HDF5 and libxml2 are absent) and prints its own line.
 Multi-GPU: replicas only — every rank runs the full workload on its own GPU (weak scaling).
@@ -41,6 +45,7 @@ if ROOT not in sys.path:
 
 METRIC = "atom*q*frame terms/s; time to 1e-3 rel err in S(q,t), chosen vs plain, same GPU"
 UNIT = "terms/s"
+MP_METRIC = "atom*q*moment*frame terms/s of the multipole orientational average (FP64)"
 
 
 def parse():
@@ -66,6 +71,8 @@ def parse():
                     help="directions of the dense reference average (layered_cv)")
     ap.add_argument("--cv-samples", type=int, default=100000,
                     help="exact |A|^2 training samples of the control variate (layered_cv)")
+    ap.add_argument("--resolution", type=int, default=20,
+                    help="largest major moment (multipole_sphere / multipole_cylinder)")
     ap.add_argument("--cv-steps", type=int, default=2500, help="training steps (layered_cv)")
     return ap.parse_args()
 
@@ -184,8 +191,80 @@ def cpu_sample(w, seconds, nthreads):
         m = min(w.nm, max(m * 2, int(m * seconds * 0.6 / max(dt, 1e-3))))
 
 
+MP_WORKLOADS = ("multipole_sphere", "multipole_cylinder")
+MP_AXIS = (0.0, 0.0, 1.0)
+
+
+def multipole_workload(args):
+    """The coherent_sqt trajectory (10,000 atoms, 1,024 frames) with one q-vector per shell
+    in a seeded random direction, and the moments of `--resolution` (default 20, the
+    reference's default)."""
+    import oracle
+    w = make_workload("coherent_sqt", args.nq, args.nf)
+    rng = np.random.default_rng(7)
+    d = rng.normal(size=(w.nq, 3))
+    qv = w.shells[:, None] * d / np.linalg.norm(d, axis=1)[:, None]
+    kind = args.workload.split("_")[1]
+    res = args.resolution
+    moments = oracle.sphere_moments(res) if kind == "sphere" else oracle.cylinder_moments(res)
+    return w, qv, kind, moments
+
+
+def mp_terms(w, moments):
+    return float(w.na) * w.nq * len(moments) * w.nf
+
+
+def cpu_sample_mp(w, qv, kind, moments, seconds, nthreads):
+    """Time the oracle's multipole device on one q-vector, all atoms and moments, over a
+    growing prefix of the frames (~`seconds`)."""
+    import oracle
+    s = w.nq // 2
+    fac = w.factors()[s:s + 1]
+    nf = min(w.nf, 2 * nthreads)
+    while True:
+        t0 = time.perf_counter()
+        if kind == "sphere":
+            oracle.mp_sphere(w.coords[:nf], qv[s:s + 1], fac, moments, nthreads=nthreads)
+        else:
+            oracle.mp_cylinder(w.coords[:nf], qv[s:s + 1], fac, moments, MP_AXIS, nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        terms = float(w.na) * len(moments) * nf
+        if dt >= seconds * 0.4 or nf >= w.nf:
+            return {"value": terms / dt, "unit": "terms/s", "cores": nthreads, "kind": "port",
+                    "sample": "oracle multipole %s (FP64 restatement) on q-vector %d/%d, all %d "
+                              "atoms x %d moments x %d of %d frames (%.3g terms, %.1f s)"
+                              % (kind, s, w.nq, w.na, len(moments), nf, w.nf, terms, dt)}
+        nf = min(w.nf, max(nf * 2, int(nf * seconds * 0.6 / max(dt, 1e-3))))
+
+
 def run_reference(args, dist):
     if dist.rank != 0:
+        return
+    if args.workload in MP_WORKLOADS:
+        w, qv, kind, moments = multipole_workload(args)
+        nthreads = os.cpu_count() or 1
+        vals = []
+        for i in range(args.warmup + args.steps):
+            r = cpu_sample_mp(w, qv, kind, moments, args.cpu_seconds / max(1, args.steps), nthreads)
+            if i >= args.warmup:
+                vals.append(r["value"])
+        v = statistics.median(vals)
+        terms = mp_terms(w, moments)
+        print(json.dumps({"impl": "reference", "metric": MP_METRIC, "value": v, "unit": "terms/s",
+                          "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": terms / v * 1e3, "higher_is_better": True,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic (seeded)",
+                          "config": {"workload": args.workload, "na": w.na, "nf": w.nf, "nq": w.nq,
+                                     "moments": len(moments), "resolution": args.resolution,
+                                     "terms_per_step": terms},
+                          "cpu_baseline": {"value": v, "unit": "terms/s", "cores": nthreads,
+                                           "kind": "port", "sample": r["sample"]},
+                          "e2e": {"value": v, "unit": "terms/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0},
+                          "note": "reference unbuildable here (MPI/Boost/FFTW3/HDF5/libxml2 "
+                                  "absent); timed its CPU restatement, ms_per_step extrapolated "
+                                  "by terms"}))
         return
     if args.workload == "batched_uneven":  # the CPU rate per term: one system of the batch
         from sassena_gb300 import synth
@@ -384,6 +463,112 @@ def run_ours(args, dist):
 
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu:
         out["cpu_baseline"] = cpu_sample(w, args.cpu_seconds, os.cpu_count() or 1)
+    if dist.rank == 0:
+        print(json.dumps(out))
+    plan.close()
+
+
+def run_multipole(args, dist):
+    """Multipole sphere / cylinder devices (FP64): terms = atoms x q-vectors x moments x
+    frames. `value`: sass_multipole_compute with the frames resident in HBM (q-vectors,
+    factors and moments are host inputs of that call, a few KB); `e2e`: staging from pinned
+    host memory plus the same call."""
+    import torch
+
+    from sassena_gb300 import abi
+
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    w, qv, kind, moments = multipole_workload(args)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    nclass = len(w.class_names)
+    terms = mp_terms(w, moments)
+    cf = np.ascontiguousarray(w.class_factors)
+    plan = abi.Plan(w.na, w.nf, nclass, "all", w.dsp, "fftw", "fp64", device=dev,
+                    stream=stream.cuda_stream)
+    plan.stage(w.coords)
+    plan.set_classes(w.atom_class)
+
+    def step():
+        plan.multipole(kind, qv, cf, moments, MP_AXIS)
+        return plan.timing()
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    steps = max(1, min(args.steps, 5))
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(dev)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    phase_ms, corr_ms, launches = [], [], 0
+    e0.record(stream)
+    for _ in range(steps):
+        t = step()
+        phase_ms.append(t["phase_ms"])
+        corr_ms.append(t["corr_ms"] + t["finalize_ms"])
+        launches += t["kernel_launches"]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    dist.barrier()
+    ms = dist.max(e0.elapsed_time(e1) / steps)
+    value = terms * dist.world / (ms * 1e-3)
+
+    lib = abi.load()
+    nbytes = w.coords.nbytes
+    hp = lib.sass_host_alloc(nbytes)
+    host_coords = np.ctypeslib.as_array((np.ctypeslib.ctypes.c_float * w.coords.size)
+                                        .from_address(hp)).reshape(w.coords.shape)
+    host_coords[...] = w.coords
+    e2e_ms = []
+    for i in range(0 if args.no_e2e else 1 + steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        plan.stage(host_coords)
+        plan.multipole(kind, qv, cf, moments, MP_AXIS)
+        torch.cuda.synchronize()
+        if i >= 1:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    lib.sass_host_free(hp)
+    e2e_step = dist.max(statistics.median(e2e_ms) if e2e_ms else float("nan"))
+    t = plan.timing()
+
+    fp64 = abi.probe_fp64(dev)
+    ph = statistics.median(phase_ms)
+    # algorithmic FP64 work of the moment sums: sphere 2 FMA per term (real j_l b times a
+    # complex Y); cylinder 6 operations per atom, q, frame and order (J cos, J sin, 4 FMA)
+    if kind == "sphere":
+        ops = 2.0 * terms
+        per = "2 FMA per term (sum_j b j_l(qr) conj(Y_lm))"
+    else:
+        ops = 6.0 * w.na * w.nq * w.nf * (2 * args.resolution + 1)
+        per = "6 FP64 operations per atom, q, frame and order n <= 2L"
+    achieved = ops / (ph * 1e-3)
+    roof = {"bound": "fp64", "achieved": achieved, "peak": fp64, "unit": "FP64 op/s",
+            "frac": achieved / fp64, "traffic": None,
+            "kernel": "mp_sphere_basis+contract" if kind == "sphere" else "mp_cylinder_kernel",
+            "kernel_ms": ph, "peak_source": "measured live: sass_probe_fp64 %.4g FMA/s; "
+                                            "algorithmic work %s" % (fp64, per)}
+    out = {"metric": MP_METRIC, "value": value, "unit": "terms/s", "n_gpus": dist.world,
+           "steps": steps, "warmup": max(3, args.warmup), "ms_per_step": ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded random walk, coherent_sqt trajectory)",
+           "config": {"workload": args.workload, "na": w.na, "nf": w.nf, "nq": w.nq,
+                      "moments": len(moments), "resolution": args.resolution,
+                      "axis": list(MP_AXIS) if kind == "cylinder" else None,
+                      "terms_per_step": terms, "dsp": w.dsp,
+                      "l2": "inputs larger than L2 (coordinates %.0f MB)" % (w.na * w.nf * 16 / 1e6),
+                      "parallelism": "replicas x%d" % dist.world},
+           "e2e": {"value": terms * dist.world / (e2e_step * 1e-3), "unit": "terms/s",
+                   "h2d_bytes_per_step": nbytes + t["h2d_bytes"],
+                   "d2h_bytes_per_step": t["d2h_bytes"], "ms_per_step": e2e_step},
+           "roofline": roof, "phase_ms": ph, "correlation_ms": statistics.median(corr_ms),
+           "gpu_launches": int(launches), "clocks": clk}
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_sample_mp(w, qv, kind, moments, args.cpu_seconds,
+                                            os.cpu_count() or 1)
     if dist.rank == 0:
         print(json.dumps(out))
     plan.close()
@@ -592,6 +777,8 @@ def main():
             run_batched(args, dist)
         elif args.workload == "layered_cv":
             run_cv(args, dist)
+        elif args.workload in MP_WORKLOADS:
+            run_multipole(args, dist)
         else:
             run_ours(args, dist)
     finally:

@@ -281,6 +281,9 @@ void sass_host_free(void* p);
 /* Measure the SFU (sin/cos results per second) and FP32 FMA (per second)
  * throughput of `device` with pipe microbenchmarks; the phase sum's roofline. */
 int sass_probe_pipes(int device, double* sfu_ops_per_s, double* fp32_fma_per_s);
+/* FP64 FMA rate of the device (independent fma chains over every SM), FMA/s: the
+ * ceiling of the FP64 forms and of the multipole devices. */
+int sass_probe_fp64(int device, double* fp64_fma_per_s);
 
 /* Allocation-free coherent autocorrelation + orientational average (FP64), for
  * callers that must not allocate GPU memory while they run: programs that reserve

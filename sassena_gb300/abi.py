@@ -28,7 +28,7 @@ EXPORTS = [
     "sass_plan_create", "sass_plan_destroy", "sass_plan_error", "sass_status_name",
     "sass_stage_frames", "sass_set_atom_classes", "sass_compute", "sass_amplitudes",
     "sass_last_timing", "sass_set_phase_tile", "sass_frame_center", "sass_host_alloc",
-    "sass_host_free", "sass_probe_pipes", "sass_correlate_noalloc", "sass_version",
+    "sass_host_free", "sass_probe_pipes", "sass_probe_fp64", "sass_correlate_noalloc", "sass_version",
     "sass_autotune", "sass_batch_create", "sass_batch_autotune", "sass_batch_run",
     "sass_batch_sync", "sass_batch_results", "sass_batch_timing", "sass_batch_info",
     "sass_batch_error", "sass_batch_destroy", "sass_batch_set_tile",
@@ -119,6 +119,7 @@ def load(path=LIB_PATH):
     L.sass_host_free.restype = None
     L.sass_version.restype = ctypes.c_char_p
     L.sass_probe_pipes.argtypes = [ctypes.c_int, _dp, _dp]
+    L.sass_probe_fp64.argtypes = [ctypes.c_int, _dp]
     _ip = ctypes.POINTER(ctypes.c_int)
     L.sass_autotune.argtypes = [_vp, _sz, _vp, _vp, _vp, ctypes.c_int, _ip, _ip, _ip, _ip]
     L.sass_batch_create.argtypes = [ctypes.POINTER(PlanDesc), _sz, ctypes.POINTER(System),
@@ -515,6 +516,16 @@ def probe_pipes(device=0):
     if rc != SASS_OK:
         raise SassError(rc, "sass_probe_pipes failed")
     return a.value, b.value
+
+
+def probe_fp64(device=0):
+    """Measured FP64 FMA/s of the device."""
+    L = load()
+    a = ctypes.c_double()
+    rc = L.sass_probe_fp64(device, ctypes.byref(a))
+    if rc != SASS_OK:
+        raise SassError(rc, "sass_probe_fp64 failed")
+    return a.value
 
 
 def compute_workload(w, precision="fp64", method="fftw", device=0, tile=None, recurrence=None,

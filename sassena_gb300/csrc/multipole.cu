@@ -584,21 +584,9 @@ extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const d
     SystemState& s = p->sys;
     const size_t nf = s.nf, na_pad = s.na_pad, nclass = s.nclass;
     cudaStream_t st = p->st;
+    size_t launches = 0;
 
-    // representation cache
-    if (s.mp_type != type || !s.mp_valid || (cyl && memcmp(s.mp_axis, axis, sizeof(s.mp_axis)) != 0)) {
-        MCK(s.mp_xyz.ensure(nf * na_pad * sizeof(float4)));
-        const size_t n = nf * na_pad;
-        const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
-        mp_convert_kernel<<<std::max(blocks, 1), 256, 0, st>>>(s.xyz.as<float4>(), (int)na_pad, (int)s.na, (int)nf, cyl,
-                                                                base, s.mp_xyz.as<float4>());
-        MCK(cudaGetLastError());
-        s.mp_type = type;
-        s.mp_valid = true;
-        if (cyl) memcpy(s.mp_axis, axis, sizeof(s.mp_axis));
-    }
-
-    // per-q inputs, moments, outputs
+    // per-q inputs: |q| (sphere) or the projected q in cylinder coordinates
     std::vector<double> qin(cyl ? 3 * nq : nq);
     for (size_t i = 0; i < nq; ++i) {
         const double* qv = qvectors + 3 * i;
@@ -627,29 +615,51 @@ extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const d
             }
         }
     }
-    DevBuf d_qin, d_cf, d_mom, d_idx, d_perm, d_gl, d_gs, d_gc, d_amp, d_out, d_Jb, d_Yc;
-    auto up = [&](DevBuf& b, const void* h, size_t bytes) -> cudaError_t {
-        cudaError_t e = b.ensure(bytes);
-        if (e != cudaSuccess) return e;
-        return cudaMemcpy(b.p, h, bytes, cudaMemcpyHostToDevice);
+    // one packed upload of every small input (16-byte aligned pieces)
+    std::vector<unsigned char> blob;
+    auto put = [&](const void* h, size_t bytes) {
+        const size_t off = (blob.size() + 15) / 16 * 16;
+        blob.resize(off + bytes);
+        if (bytes) memcpy(blob.data() + off, h, bytes);
+        return off;
     };
-    MCK(up(d_qin, qin.data(), qin.size() * sizeof(double)));
-    MCK(up(d_cf, class_factors, nq * nclass * sizeof(double)));
-    MCK(up(d_mom, moments, nmom * 2 * sizeof(int)));
-    MCK(d_amp.ensure(nq * nmom * nf * sizeof(double2)));
-    MCK(d_out.ensure(nq * (nf + 2) * sizeof(double2)));
+    const size_t o_qin = put(qin.data(), qin.size() * sizeof(double));
+    const size_t o_cf = put(class_factors, nq * nclass * sizeof(double));
+    const size_t o_mom = put(moments, nmom * 2 * sizeof(int32_t));
+    const size_t o_idx = put(idx.data(), idx.size() * sizeof(int));
+    const size_t o_perm = put(perm.data(), perm.size() * sizeof(int));
+    const size_t o_gl = put(gl.data(), gl.size() * sizeof(int));
+    const size_t o_gs = put(gstart.data(), gstart.size() * sizeof(int));
+    const size_t o_gc = put(gcount.data(), gcount.size() * sizeof(int));
+    MCK(p->mp_in.ensure(blob.size()));
+    MCK(p->mp_amp.ensure(nq * nmom * nf * sizeof(double2)));
+    MCK(p->mp_out.ensure(nq * (nf + 2) * sizeof(double2)));
+    unsigned char* din = p->mp_in.as<unsigned char>();
+    auto dptr = [&](size_t off) { return din + off; };
+    MCK(cudaEventRecord(p->ev[4], st));
+    MCK(cudaMemcpyAsync(din, blob.data(), blob.size(), cudaMemcpyHostToDevice, st));
     MCK(cudaEventRecord(p->ev[0], st));
+
+    // representation cache (rebuilt after staging or for another device type / axis)
+    if (s.mp_type != type || !s.mp_valid || (cyl && memcmp(s.mp_axis, axis, sizeof(s.mp_axis)) != 0)) {
+        MCK(s.mp_xyz.ensure(nf * na_pad * sizeof(float4)));
+        const size_t n = nf * na_pad;
+        const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+        mp_convert_kernel<<<std::max(blocks, 1), 256, 0, st>>>(s.xyz.as<float4>(), (int)na_pad, (int)s.na, (int)nf, cyl,
+                                                                base, s.mp_xyz.as<float4>());
+        MCK(cudaGetLastError());
+        ++launches;
+        s.mp_type = type;
+        s.mp_valid = true;
+        if (cyl) memcpy(s.mp_axis, axis, sizeof(s.mp_axis));
+    }
+    const double* d_cf = reinterpret_cast<const double*>(dptr(o_cf));
     if (!cyl) {
-        MCK(up(d_idx, idx.data(), idx.size() * sizeof(int)));
-        MCK(up(d_perm, perm.data(), perm.size() * sizeof(int)));
-        MCK(up(d_gl, gl.data(), gl.size() * sizeof(int)));
-        MCK(up(d_gs, gstart.data(), gstart.size() * sizeof(int)));
-        MCK(up(d_gc, gcount.data(), gcount.size() * sizeof(int)));
         // frame batches sized to about 1 GB of basis
         const size_t per_frame = na_pad * (nq * (L + 1) * sizeof(double) + nmom * sizeof(double2));
         const size_t nfb = std::max<size_t>(1, std::min<size_t>(nf, ((size_t)1 << 30) / per_frame));
-        MCK(d_Jb.ensure(nfb * nq * (L + 1) * na_pad * sizeof(double)));
-        MCK(d_Yc.ensure(nfb * nmom * na_pad * sizeof(double2)));
+        MCK(p->mp_Jb.ensure(nfb * nq * (L + 1) * na_pad * sizeof(double)));
+        MCK(p->mp_Yc.ensure(nfb * nmom * na_pad * sizeof(double2)));
         int maxcnt = 0;
         for (int c : gcount) maxcnt = std::max(maxcnt, c);
         const size_t csm = nq * kMpTileAtoms * sizeof(double) + (size_t)maxcnt * kMpTileAtoms * sizeof(double2);
@@ -662,11 +672,11 @@ extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const d
             MpSphereBasis ba{};
             ba.sph = s.mp_xyz.as<float4>();
             ba.cls = s.cls.as<int>();
-            ba.cf = d_cf.as<double>();
-            ba.qlen = d_qin.as<double>();
-            ba.idx = d_idx.as<int>();
-            ba.Jb = d_Jb.as<double>();
-            ba.Yc = d_Yc.as<double2>();
+            ba.cf = d_cf;
+            ba.qlen = reinterpret_cast<const double*>(dptr(o_qin));
+            ba.idx = reinterpret_cast<const int*>(dptr(o_idx));
+            ba.Jb = p->mp_Jb.as<double>();
+            ba.Yc = p->mp_Yc.as<double2>();
             ba.na_pad = (int)na_pad;
             ba.nclass = (int)nclass;
             ba.nq = (int)nq;
@@ -678,13 +688,13 @@ extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const d
             mp_sphere_basis_kernel<<<(unsigned)std::min<size_t>((nthreads + 127) / 128, 152 * 64), 128, 0, st>>>(ba);
             MCK(cudaGetLastError());
             MpSphereContract ca{};
-            ca.Jb = d_Jb.as<double>();
-            ca.Yc = d_Yc.as<double2>();
-            ca.perm = d_perm.as<int>();
-            ca.gl = d_gl.as<int>();
-            ca.gstart = d_gs.as<int>();
-            ca.gcount = d_gc.as<int>();
-            ca.A = d_amp.as<double2>();
+            ca.Jb = p->mp_Jb.as<double>();
+            ca.Yc = p->mp_Yc.as<double2>();
+            ca.perm = reinterpret_cast<const int*>(dptr(o_perm));
+            ca.gl = reinterpret_cast<const int*>(dptr(o_gl));
+            ca.gstart = reinterpret_cast<const int*>(dptr(o_gs));
+            ca.gcount = reinterpret_cast<const int*>(dptr(o_gc));
+            ca.A = p->mp_amp.as<double2>();
             ca.na_pad = (int)na_pad;
             ca.na = (int)s.na;
             ca.nq = (int)nq;
@@ -695,15 +705,16 @@ extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const d
             dim3 grid((unsigned)gl.size(), (unsigned)nb, (unsigned)zchunks);
             mp_sphere_contract_kernel<<<grid, kContractThreads, csm, st>>>(ca);
             MCK(cudaGetLastError());
+            launches += 2;
         }
     } else {
         MpCylinder ca{};
         ca.cyl = s.mp_xyz.as<float4>();
         ca.cls = s.cls.as<int>();
-        ca.cf = d_cf.as<double>();
-        ca.qcyl = d_qin.as<double>();
-        ca.mom = d_mom.as<int>();
-        ca.A = d_amp.as<double2>();
+        ca.cf = d_cf;
+        ca.qcyl = reinterpret_cast<const double*>(dptr(o_qin));
+        ca.mom = reinterpret_cast<const int*>(dptr(o_mom));
+        ca.A = p->mp_amp.as<double2>();
         ca.na_pad = (int)na_pad;
         ca.na = (int)s.na;
         ca.nclass = (int)nclass;
@@ -715,7 +726,9 @@ extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const d
         if (sm > 48 * 1024) MCK(cudaFuncSetAttribute(mp_cylinder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         mp_cylinder_kernel<<<dim3((unsigned)nq, (unsigned)nf), kMpCylThreads, sm, st>>>(ca);
         MCK(cudaGetLastError());
+        ++launches;
     }
+    const size_t phase_launches = launches;
     // correlation and average of the amplitudes: moments play the sub-vectors
     EngineConfig cfg;
     cfg.scattering = p->d.scattering;
@@ -727,12 +740,12 @@ extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const d
     WorkItem& it = items[0];
     it.sys = &s;
     for (size_t i = 0; i <= nq; ++i) it.offs.push_back(i * nmom);
-    it.d_cf = d_cf.as<double>();
-    double2* o = d_out.as<double2>();
+    it.d_cf = d_cf;
+    double2* o = p->mp_out.as<double2>();
     it.d_fqt = o;
     it.d_fq = o + nq * nf;
     it.d_fq2 = o + nq * (nf + 1);
-    it.d_amp_given = d_amp.as<double2>();
+    it.d_amp_given = p->mp_amp.as<double2>();
     it.norm = cyl ? 1.0 / (2 * 3.14159265358979323846) : 1.0 / (4 * 3.14159265358979323846);
     int rc = p->eng.prepare(cfg, items, p->msg);
     if (rc) return rc;
@@ -740,8 +753,11 @@ extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const d
     cudaEvent_t ev[4] = {p->ev[8], p->ev[9], p->ev[2], p->ev[3]};
     rc = p->eng.enqueue(st, p->msg, ev);
     if (rc) return rc;
+    launches += p->eng.stats().launches;
     std::vector<double2> host(nq * (nf + 2));
+    MCK(cudaEventRecord(p->ev[6], st));
     MCK(cudaMemcpyAsync(host.data(), o, host.size() * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    MCK(cudaEventRecord(p->ev[7], st));
     MCK(cudaStreamSynchronize(st));
     unsigned flag = 0;
     MCK(cudaMemcpy(&flag, p->eng.err_word(), sizeof(unsigned), cudaMemcpyDeviceToHost));
@@ -753,7 +769,13 @@ extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const d
     if (cudaEventElapsedTime(&ms, p->ev[0], p->ev[1]) == cudaSuccess) p->timing.phase_ms = ms;
     if (cudaEventElapsedTime(&ms, p->ev[9], p->ev[2]) == cudaSuccess) p->timing.corr_ms = ms;
     if (cudaEventElapsedTime(&ms, p->ev[2], p->ev[3]) == cudaSuccess) p->timing.finalize_ms = ms;
-    if (cudaEventElapsedTime(&ms, p->ev[0], p->ev[3]) == cudaSuccess) p->timing.total_ms = ms;
+    if (cudaEventElapsedTime(&ms, p->ev[4], p->ev[0]) == cudaSuccess) p->timing.h2d_ms = ms;
+    if (cudaEventElapsedTime(&ms, p->ev[6], p->ev[7]) == cudaSuccess) p->timing.d2h_ms = ms;
+    if (cudaEventElapsedTime(&ms, p->ev[4], p->ev[7]) == cudaSuccess) p->timing.total_ms = ms;
+    p->timing.kernel_launches = launches;
+    p->timing.phase_launches = phase_launches;
+    p->timing.h2d_bytes = blob.size();
+    p->timing.d2h_bytes = host.size() * sizeof(double2);
     cudaGetLastError();
     p->msg.clear();
     return SASS_OK;

@@ -23,4 +23,6 @@ struct sass_plan {
     int split_atoms = 0;
     int rec_k = 0;  // shell recurrence: 0 automatic, -1 off, else shells per lane
     sassgpu::DevBuf qv, cf, fqt, fq, fq2, amp_tmp;
+    // multipole devices: packed per-call inputs, basis batch, amplitudes, results
+    sassgpu::DevBuf mp_in, mp_Jb, mp_Yc, mp_amp, mp_out;
 };
