@@ -106,6 +106,57 @@ const char* sass_status_name(int status);
  * buffer). coords_on_device != 0 means `coords` is a device pointer. */
 int sass_stage_frames(sass_plan* plan, const float* coords, int coords_on_device);
 
+/* ---- Staging pre-pass: alignments and motions ------------------------------------
+ * Replaces the per-frame work of CoordinateSets::load (src/sample/coordinate_sets.cpp:
+ * 244-368): pre-alignments, motions and post-alignments applied in FP64 to the whole
+ * system's coordinates, then the reduction to the stager target and the float32
+ * staging of DataStagerByFrame (src/stager/data_stager.cpp:102-118). Steps run in the
+ * order given (the caller lists pre-alignments, motions, then post-alignments).
+ *
+ * Every step names atoms by system index. The reference structure of a step is
+ * `reference` ([nreference][3], a frame or a file read by the caller) or, when it is
+ * NULL, the current frame's atoms reference_selection ("instant"); its centre of mass
+ * is sum_i m[reference_selection[i]] R_i / sum_i m[...], summed in list order.
+ *   CENTER       (type "center"): translate `selection` by -COM(reference structure).
+ *   FITTRANS     translate `selection` by COM(reference structure) - COM(selection).
+ *   FITROTTRANS  Fit (center_of_mass.cpp:53-157): the frame's atoms reference_selection
+ *                are rotated (Kabsch, SVD of the mass-weighted correlation matrix with
+ *                the reflection correction) and moved onto the reference structure;
+ *                atom fit_target[k] then takes fitted atom fit_source[k].
+ *   FITROT       as FITROTTRANS, then `selection` is translated by its centre of mass
+ *                from before the fit (coordinate_sets.cpp:283-287).
+ *   MOTION       translation motions (linear, fixed, oscillation; motion_walker.cpp):
+ *                x -> ((x - c) + t_f) + c for the atoms of `selection`, c = COM of the
+ *                reference structure, t_f = translations[f].
+ * Empty lists are allowed (a centre of mass of nothing is 0, as in the reference). */
+#define SASS_STEP_CENTER 0
+#define SASS_STEP_FITTRANS 1
+#define SASS_STEP_FITROTTRANS 2
+#define SASS_STEP_FITROT 3
+#define SASS_STEP_MOTION 4
+
+typedef struct sass_prepass_step {
+    int type;
+    int reserved;
+    const size_t* selection;            /* atoms translated (and FITTRANS / FITROT centres) */
+    size_t nselection;
+    const size_t* reference_selection;  /* atoms of the reference structure (masses) */
+    size_t nreference;
+    const double* reference;            /* [nreference][3] or NULL (the current frame) */
+    const size_t* fit_target;           /* fits: atoms written from the fitted copy ... */
+    const size_t* fit_source;           /* ... positions in reference_selection they take */
+    size_t nfit;
+    const double* translations;         /* MOTION: [nf][3] */
+} sass_prepass_step;
+
+/* frames: host float32 [nf][nsys][3] of the whole system; masses [nsys]; target [na]
+ * system indices of the plan's atoms; staged (optional) receives the float32 frames
+ * [nf][na][3] as staged. Replaces sass_stage_frames for configurations with alignments
+ * or motions. */
+int sass_stage_frames_prepass(sass_plan* plan, const float* frames, size_t nsys, const double* masses,
+                              const sass_prepass_step* steps, size_t nsteps, const size_t* target,
+                              float* staged);
+
 /* Class index per atom of the selection, int32 [na], each in [0, nclass). */
 int sass_set_atom_classes(sass_plan* plan, const int32_t* atom_class, int on_device);
 

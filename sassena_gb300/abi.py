@@ -37,7 +37,7 @@ EXPORTS = [
     "sass_mlp_train", "sass_mlp_predict", "sass_mlp_sphere_mean", "sass_compute_cv",
     "sass_set_shell_recurrence", "sass_plan_schedule", "sass_batch_set_shell_recurrence",
     "sass_batch_schedule", "sass_set_phase_poly", "sass_batch_set_phase_poly",
-    "sass_multipole_compute",
+    "sass_multipole_compute", "sass_stage_frames_prepass",
 ]
 
 
@@ -60,6 +60,18 @@ class System(ctypes.Structure):
                 ("coords", ctypes.c_void_p), ("atom_class", ctypes.c_void_p),
                 ("nq", ctypes.c_size_t), ("sub_offsets", ctypes.c_void_p),
                 ("subvectors", ctypes.c_void_p), ("class_factors", ctypes.c_void_p)]
+
+
+STEP = {"center": 0, "fittrans": 1, "fitrottrans": 2, "fitrot": 3, "motion": 4}
+
+
+class PrepassStep(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int), ("reserved", ctypes.c_int),
+                ("selection", ctypes.c_void_p), ("nselection", ctypes.c_size_t),
+                ("reference_selection", ctypes.c_void_p), ("nreference", ctypes.c_size_t),
+                ("reference", ctypes.c_void_p),
+                ("fit_target", ctypes.c_void_p), ("fit_source", ctypes.c_void_p),
+                ("nfit", ctypes.c_size_t), ("translations", ctypes.c_void_p)]
 
 
 class Timing(ctypes.Structure):
@@ -107,6 +119,8 @@ def load(path=LIB_PATH):
     L.sass_status_name.argtypes = [ctypes.c_int]
     L.sass_status_name.restype = ctypes.c_char_p
     L.sass_stage_frames.argtypes = [_vp, _vp, ctypes.c_int]
+    L.sass_stage_frames_prepass.argtypes = [_vp, _vp, ctypes.c_size_t, _vp, ctypes.POINTER(PrepassStep),
+                                            ctypes.c_size_t, _vp, _vp]
     L.sass_set_atom_classes.argtypes = [_vp, _vp, ctypes.c_int]
     L.sass_compute.argtypes = [_vp, _sz, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int]
     L.sass_amplitudes.argtypes = [_vp, _sz, _vp, _vp, _sz, _vp, _vp]
@@ -219,6 +233,45 @@ class Plan:
         if c.shape != (self.nf, self.na, 3):
             raise ValueError("coords must be [nf, na, 3]")
         self._check(self.lib.sass_stage_frames(self._h, _ptr(c), 0))
+
+    def stage_prepass(self, frames, masses, steps, target):
+        """Alignments / motions on the whole system, then staging of the target atoms.
+
+        frames: float32 [nf, nsys, 3]; masses [nsys]; target [na] system indices;
+        steps: dicts with "type" (center, fittrans, fitrottrans, fitrot, motion),
+        "selection", "reference_selection", optional "reference" ([nref, 3]),
+        "fit_target" and "fit_source" (fits) and "translations" ([nf, 3], motions).
+        Returns the staged float32 frames [nf, na, 3]."""
+        fr = np.ascontiguousarray(frames, dtype=np.float32)
+        nsys = fr.shape[1]
+        if fr.shape != (self.nf, nsys, 3):
+            raise ValueError("frames must be [nf, nsys, 3]")
+        ms = np.ascontiguousarray(masses, dtype=np.float64)
+        tg = np.ascontiguousarray(target, dtype=np.uintp)
+        keep = []
+        arr = (PrepassStep * max(1, len(steps)))()
+        for k, st in enumerate(steps):
+            def lst(key, dtype=np.uintp, shape=None):
+                v = st.get(key)
+                if v is None:
+                    return None, 0
+                a = np.ascontiguousarray(v, dtype=dtype)
+                if shape is not None:
+                    a = a.reshape(shape)
+                keep.append(a)
+                return a.ctypes.data, len(a)
+            e = arr[k]
+            e.type = STEP[st["type"]]
+            e.selection, e.nselection = lst("selection")
+            e.reference_selection, e.nreference = lst("reference_selection")
+            e.reference, _ = lst("reference", np.float64, (-1, 3))
+            e.fit_target, e.nfit = lst("fit_target")
+            e.fit_source, _ = lst("fit_source")
+            e.translations, _ = lst("translations", np.float64, (-1, 3))
+        out = np.zeros((self.nf, self.na, 3), dtype=np.float32)
+        self._check(self.lib.sass_stage_frames_prepass(self._h, _ptr(fr), nsys, _ptr(ms), arr, len(steps),
+                                                       _ptr(tg), _ptr(out)))
+        return out
 
     def set_classes(self, atom_class):
         c = np.ascontiguousarray(atom_class, dtype=np.int32)

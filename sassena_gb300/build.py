@@ -24,14 +24,16 @@ INCLUDE = os.path.join(ROOT, "include")
 
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE,
-                     "-Xptxas", "-warn-spills"]
+# host code without FP contraction (the reference's x86-64 build has no fused multiply-add,
+# and the Arm compiler would contract by default)
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+                     "-I" + INCLUDE, "-Xptxas", "-warn-spills"]
 CXX = os.environ.get("CXX", "g++")
-CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + INCLUDE, "-I" + HOST]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-ffp-contract=off", "-I" + INCLUDE, "-I" + HOST]
 
 CUDA_SOURCES = [
     "capi.cu", "engine.cu", "phase_sum.cu", "phase_rec.cu", "correlate.cu", "peaks.cu", "noalloc.cu", "mlp.cu",
-    "cv.cu", "multipole.cu",
+    "cv.cu", "multipole.cu", "align.cu",
 ]
 HOST_SOURCES = []  # filled when the host layer exists (see host_sources())
 

@@ -124,10 +124,54 @@ void Params::read_xml(const std::string& path) {
             framesets.push_back(fs);
         }
     }
-    if (x.exists("//sample/motions") && !x.query("//sample/motions/motion").empty())
-        throw std::runtime_error("sample.motions are not supported by this build");
-    if (x.exists("//sample/alignments") && !x.query("//sample/alignments/alignment").empty())
-        throw std::runtime_error("sample.alignments are not supported by this build");
+    for (const XmlNode* e : x.query("//sample/motions/motion")) {
+        MotionParams m;
+        m.ref_file = structure_file;
+        m.ref_filepath = structure_filepath;
+        m.ref_format = structure_format;
+        if (x.exists("./type", e)) m.type = x.get_string("./type", e);
+        if (x.exists("./displace", e)) m.displace = x.get_double("./displace", e);
+        if (x.exists("./frequency", e)) m.frequency = x.get_double("./frequency", e);
+        if (x.exists("./seed", e)) m.seed = (unsigned long)x.get_size("./seed", e);
+        if (x.exists("./sampling", e)) m.sampling = (long)x.get_long("./sampling", e);
+        if (x.exists("./selection", e)) m.selection = x.get_string("./selection", e);
+        if (x.exists("./direction/x", e)) m.direction[0] = x.get_double("./direction/x", e);
+        if (x.exists("./direction/y", e)) m.direction[1] = x.get_double("./direction/y", e);
+        if (x.exists("./direction/z", e)) m.direction[2] = x.get_double("./direction/z", e);
+        m.radius = m.displace * 10;
+        if (x.exists("./radius", e)) m.radius = x.get_double("./radius", e);
+        m.ref_selection = m.selection;
+        if (x.exists("./reference/type", e)) m.ref_type = x.get_string("./reference/type", e);
+        if (x.exists("./reference/frame", e)) m.ref_frame = x.get_size("./reference/frame", e);
+        if (x.exists("./reference/file", e)) {
+            m.ref_file = x.get_string("./reference/file", e);
+            m.ref_filepath = get_filepath(m.ref_file);
+        }
+        if (x.exists("./reference/format", e)) m.ref_format = x.get_string("./reference/format", e);
+        if (x.exists("./reference/selection", e)) m.ref_selection = x.get_string("./reference/selection", e);
+        motions.push_back(m);
+    }
+    for (const XmlNode* e : x.query("//sample/alignments/alignment")) {
+        AlignmentParams a;
+        if (x.exists("./type", e)) a.type = x.get_string("./type", e);
+        if (x.exists("./selection", e)) a.selection = x.get_string("./selection", e);
+        if (x.exists("./order", e)) a.order = x.get_string("./order", e);
+        a.ref_file = structure_file;
+        a.ref_filepath = structure_filepath;
+        a.ref_format = structure_format;
+        a.ref_selection = a.selection;
+        if (x.exists("./reference/type", e)) a.ref_type = x.get_string("./reference/type", e);
+        if (x.exists("./reference/frame", e)) a.ref_frame = x.get_size("./reference/frame", e);
+        if (x.exists("./reference/file", e)) {
+            a.ref_file = x.get_string("./reference/file", e);
+            a.ref_filepath = get_filepath(a.ref_file);
+        }
+        if (x.exists("./reference/format", e)) a.ref_format = x.get_string("./reference/format", e);
+        if (x.exists("./reference/selection", e)) a.ref_selection = x.get_string("./reference/selection", e);
+        if (a.order != "pre" && a.order != "post")
+            throw std::runtime_error("Ordering of alignment not understood. Must be pre or post.");
+        alignments.push_back(a);
+    }
 
     // ---- stager (parameters.cpp:340-369) ---------------------------------------------------
     if (x.exists("//stager/target")) target = x.get_string("//stager/target");

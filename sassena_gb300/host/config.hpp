@@ -31,6 +31,24 @@ struct SelectionParams {
     std::string expression;
 };
 
+// sample.alignments.alignment (parameters.cpp:298-340)
+struct AlignmentParams {
+    std::string type = "center", selection = "system", order = "pre";
+    std::string ref_type = "frame", ref_file, ref_filepath, ref_format, ref_selection;
+    size_t ref_frame = 0;
+};
+
+// sample.motions.motion (parameters.cpp:234-296)
+struct MotionParams {
+    std::string type = "linear", selection = "system";
+    double displace = 0.0, frequency = 0.001, radius = 0.0;
+    Vec3 direction{1.0, 0.0, 0.0};
+    unsigned long seed = 0;
+    long sampling = 1;
+    std::string ref_type = "instant", ref_file, ref_filepath, ref_format, ref_selection;
+    size_t ref_frame = 0;
+};
+
 struct ScanParams {
     Vec3 base{1.0, 0.0, 0.0};
     double from = 0.0, to = 1.0;
@@ -46,6 +64,8 @@ struct Params {
     std::string structure_file = "sample.pdb", structure_filepath, structure_format = "pdb";
     std::vector<SelectionParams> selections;
     std::vector<FramesetParams> framesets;
+    std::vector<MotionParams> motions;
+    std::vector<AlignmentParams> alignments;
     // stager
     std::string target = "system";
     // database

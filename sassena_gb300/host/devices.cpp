@@ -7,6 +7,7 @@
 #include <set>
 #include <stdexcept>
 
+#include "prepass.hpp"
 #include "sassena_gb300.h"
 
 namespace sassgpu {
@@ -195,18 +196,47 @@ bool run_scatter_device(const Params& p, Database& db, const Sample& s, RunStats
         ~Guard() { sass_plan_destroy(p); }
     } guard{plan};
 
-    // sd:stage: frames read straight into page-locked memory, one copy to the device
+    // sd:stage: frames read straight into page-locked memory, one copy to the device; with
+    // alignments or motions the whole system goes up and the device applies them first
     double ts = now_s();
     {
-        const size_t bytes = nf * na * 3 * sizeof(float);
+        const bool prepass = !p.alignments.empty() || !p.motions.empty();
+        const size_t nsys = s.atom_ids.size();
+        const size_t bytes = nf * (prepass ? nsys : na) * 3 * sizeof(float);
         float* pinned = static_cast<float*>(sass_host_alloc(bytes));
         if (!pinned) throw std::runtime_error("sass_host_alloc: cannot allocate page-locked staging memory");
         struct Free {
             float* q;
             ~Free() { sass_host_free(q); }
         } release{pinned};
-        s.stage_into(p.target, pinned);
-        check(plan, sass_stage_frames(plan, pinned, 0), "sass_stage_frames");
+        if (!prepass) {
+            s.stage_into(p.target, pinned);
+            check(plan, sass_stage_frames(plan, pinned, 0), "sass_stage_frames");
+        } else {
+            s.stage_into("system", pinned);
+            Prepass pp = build_prepass(p, db, s, pinned);
+            std::vector<sass_prepass_step> steps(pp.steps.size());
+            for (size_t i = 0; i < pp.steps.size(); ++i) {
+                const PrepassStep& q = pp.steps[i];
+                sass_prepass_step& e = steps[i];
+                e = sass_prepass_step{};
+                e.type = q.type;
+                e.selection = q.selection.data();
+                e.nselection = q.selection.size();
+                e.reference_selection = q.reference_selection.data();
+                e.nreference = q.reference_selection.size();
+                e.reference = q.reference.empty() ? nullptr : q.reference.data();
+                e.fit_target = q.fit_target.data();
+                e.fit_source = q.fit_source.data();
+                e.nfit = q.fit_target.size();
+                e.translations = q.translations.empty() ? nullptr : q.translations.data();
+                info("Staging pre-pass step: " + q.label);
+            }
+            const std::vector<size_t>& target = s.selection(p.target);
+            check(plan, sass_stage_frames_prepass(plan, pinned, nsys, pp.masses.data(), steps.data(), steps.size(),
+                                                  target.data(), nullptr),
+                  "sass_stage_frames_prepass");
+        }
     }
     check(plan, sass_set_atom_classes(plan, cls.atom_class.data(), 0), "sass_set_atom_classes");
     st.stage_s = now_s() - ts;

@@ -20,6 +20,7 @@
 
 #include "config.hpp"
 #include "devices.hpp"
+#include "prepass.hpp"
 #include "sample.hpp"
 
 using namespace sassgpu;
@@ -72,6 +73,44 @@ void dry_run(const Params& p, Database& db, const Sample& s, const std::string& 
       << "\",\"moments\":[";
     for (size_t i = 0; i < p.moments.size(); ++i)
         o << (i ? "," : "") << "[" << p.moments[i].first << "," << p.moments[i].second << "]";
+    o << "]";
+    // staging pre-pass steps (alignments, motions) as the device receives them
+    o << ",\"prepass\":[";
+    if (!p.alignments.empty() || !p.motions.empty()) {
+        std::vector<float> sys = s.stage("system");
+        Prepass pp = build_prepass(p, db, s, sys.data());
+        auto ints = [&](const char* key, const std::vector<size_t>& v) {
+            o << ",\"" << key << "\":[";
+            for (size_t i = 0; i < v.size(); ++i) o << (i ? "," : "") << v[i];
+            o << "]";
+        };
+        auto dbls = [&](const char* key, const std::vector<double>& v) {
+            o << ",\"" << key << "\":[";
+            for (size_t i = 0; i < v.size(); ++i) {
+                char b[64];
+                snprintf(b, sizeof(b), "%s%.17g", i ? "," : "", v[i]);
+                o << b;
+            }
+            o << "]";
+        };
+        for (size_t i = 0; i < pp.steps.size(); ++i) {
+            const PrepassStep& q = pp.steps[i];
+            o << (i ? "," : "") << "{\"type\":" << q.type << ",\"label\":\"" << q.label << "\"";
+            ints("selection", q.selection);
+            ints("reference_selection", q.reference_selection);
+            dbls("reference", q.reference);
+            ints("fit_target", q.fit_target);
+            ints("fit_source", q.fit_source);
+            dbls("translations", q.translations);
+            o << "}";
+        }
+        o << "],\"masses\":[";
+        for (size_t i = 0; i < pp.masses.size(); ++i) {
+            char b[64];
+            snprintf(b, sizeof(b), "%s%.17g", i ? "," : "", pp.masses[i]);
+            o << b;
+        }
+    }
     o << "]";
     o << ",\"scattering\":\"" << p.scattering_type << "\",\"dsp\":\"" << p.dsp_type << "\",\"method\":\""
       << p.dsp_method << "\",\"precision\":\"" << p.precision << "\",\"signal\":\"" << p.signal_filepath

@@ -259,15 +259,17 @@ def write_dcd(path, coords):
                 f.write(rec)
 
 
-def write_database(path, w, sfactor_params=None):
-    """db.xml: names/pdb regexes, masses, sizes, exclusion factors and scattering factors
-    (type 0 constants from the workload's class factors, or type 2 parameter vectors)."""
+def write_database(path, w, sfactor_params=None, masses=None):
+    """db.xml: names/pdb regexes, masses (1.0, or `masses` per class), sizes, exclusion
+    factors and scattering factors (type 0 constants from the workload's class factors, or
+    type 2 parameter vectors)."""
     lines = ["<?xml version=\"1.0\"?>", "<root>", "<names><pdb>"]
     for c in w.class_names:
         lines.append("<element><name>%s</name><param>%s[0-9]*</param></element>" % (c, c))
     lines.append("</pdb></names><masses>")
-    for c in w.class_names:
-        lines.append("<element><name>%s</name><param>1.0</param></element>" % c)
+    for i, c in enumerate(w.class_names):
+        m = 1.0 if masses is None else masses[i]
+        lines.append("<element><name>%s</name><param>%.17g</param></element>" % (c, m))
     lines.append("</masses><sizes>")
     for c in w.class_names:
         lines.append("<element><name>%s</name><type>0</type><param>1.0</param></element>" % c)
@@ -288,21 +290,23 @@ def write_database(path, w, sfactor_params=None):
 
 
 def write_files(directory, w, precision="fp64", method="fftw", qvectors_file=True,
-                signal="signal.h5", sfactor_params=None, extra="", average=None):
+                signal="signal.h5", sfactor_params=None, extra="", average=None, sample_extra="",
+                masses=None):
     """Write sample.pdb, sample.dcd, db.xml, qvectors.txt, orientations.txt and scatter.xml
     for workload `w` into `directory`; returns the scatter.xml path.
 
     q-vectors are |q_s| along x (the orientation set ignores the q direction,
     abstract_vectors_scatter_device.cpp:123-129) and the directions come from a file
     (vectors.type=file, parameters.cpp:932-943). `average` replaces the <average> element
-    (e.g. a multipole orientation)."""
+    (e.g. a multipole orientation); `sample_extra` goes inside <sample> (alignments,
+    motions, selections); `masses` are the database masses per class."""
     import os
     if sfactor_params is None and not np.all(w.class_factors == w.class_factors[:1]):
         raise ValueError("type-0 database factors cannot vary with |q|; pass sfactor_params")
     os.makedirs(directory, exist_ok=True)
     write_pdb(os.path.join(directory, "sample.pdb"), w)
     write_dcd(os.path.join(directory, "sample.dcd"), w.coords)
-    write_database(os.path.join(directory, "db.xml"), w, sfactor_params)
+    write_database(os.path.join(directory, "db.xml"), w, sfactor_params, masses)
     with open(os.path.join(directory, "qvectors.txt"), "w") as f:
         for q in w.shells:
             f.write("%.17g 0 0\n" % q)
@@ -314,6 +318,7 @@ def write_files(directory, w, precision="fp64", method="fftw", qvectors_file=Tru
   <sample>
     <structure><file>sample.pdb</file><format>pdb</format></structure>
     <framesets><frameset><file>sample.dcd</file><format>dcd</format></frameset></framesets>
+    %(sample_extra)s
   </sample>
   <database><type>file</type><file>db.xml</file></database>
   <scattering>
@@ -327,7 +332,7 @@ def write_files(directory, w, precision="fp64", method="fftw", qvectors_file=Tru
   %(extra)s
 </root>
 """ % dict(type=w.scattering, dsp=w.dsp, method=method, signal=signal, precision=precision,
-           extra=extra, average=average or """<average><orientation><type>vectors</type>
+           extra=extra, sample_extra=sample_extra, average=average or """<average><orientation><type>vectors</type>
       <vectors><type>file</type><file>orientations.txt</file></vectors>
     </orientation></average>""")
     path = os.path.join(directory, "scatter.xml")

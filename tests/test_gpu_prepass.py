@@ -1,0 +1,98 @@
+"""Staging pre-pass on the GPU (sass_stage_frames_prepass) against oracle.alignment: the
+steps sassena-gpu builds for each configuration are applied on the device and the staged
+float32 frames compared with the oracle's CoordinateSets::load. Centres of mass,
+translations and motions are summed in the reference's order, so those frames are equal
+bit for bit; fits go through an SVD (LAPACK in the oracle, Jacobi here), so they may differ
+by one float32 ulp. End to end, the driver's S(q,t) for aligned configurations matches the
+FP64 oracle run on the oracle's aligned frames (bar 1e-12)."""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle import alignment as al
+from sassena_gb300 import abi
+
+import h5lite
+import prepass_cases as pc
+
+pytestmark = pytest.mark.gpu
+
+FITS = {"fitrottrans", "fitrot_file", "fit_instant", "pre_post"}
+
+
+def host_steps(cfg, tmp_path):
+    out = str(tmp_path / "dry.json")
+    r = subprocess.run([abi.DRIVER_PATH, "--config", cfg, "--dry-run", out], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    j = json.load(open(out))
+    types = {0: "center", 1: "fittrans", 2: "fitrottrans", 3: "fitrot", 4: "motion"}
+    steps = []
+    for s in j["prepass"]:
+        d = {"type": types[s["type"]], "selection": s["selection"], "reference_selection": s["reference_selection"],
+             "fit_target": s["fit_target"], "fit_source": s["fit_source"]}
+        if s["reference"]:
+            d["reference"] = np.reshape(s["reference"], (-1, 3))
+        if s["translations"]:
+            d["translations"] = np.reshape(s["translations"], (-1, 3))
+        steps.append(d)
+    return steps, np.array(j["masses"])
+
+
+@pytest.mark.parametrize("name", pc.CASES)
+def test_prepass_matches_oracle(native_lib, tmp_path, name):
+    w, cfg, o = pc.build(name, str(tmp_path / "run"))
+    steps, masses = host_steps(cfg, tmp_path)
+    want = al.load(w.coords, o["masses"], o["alignments"], o["motions"], o["target"])
+    target = o["target"] if o["target"] is not None else list(range(pc.NA))
+    for precision in ("fp64", "fp32"):
+        with abi.Plan(len(target), pc.NF, 4, "all", "autocorrelate", "fftw", precision) as p:
+            got = p.stage_prepass(w.coords, masses, steps, target)
+        if name in FITS:
+            ulp = np.spacing(np.abs(want).astype(np.float32))
+            assert (np.abs(got - want) <= ulp).all(), np.abs(got - want).max()
+        else:
+            np.testing.assert_array_equal(got, want)
+
+
+def test_prepass_empty_and_errors(native_lib):
+    w = pc.workload()
+    m = np.ones(pc.NA)
+    with abi.Plan(pc.NA, pc.NF, 4, "all") as p:
+        # no steps: the target atoms staged unchanged
+        np.testing.assert_array_equal(p.stage_prepass(w.coords, m, [], list(range(pc.NA))), w.coords)
+        # empty lists are allowed (a centre of nothing is 0)
+        got = p.stage_prepass(w.coords, m, [{"type": "center", "selection": list(range(5)),
+                                             "reference_selection": []}], list(range(pc.NA)))
+        np.testing.assert_array_equal(got, w.coords)
+        with pytest.raises(abi.SassError):
+            p.stage_prepass(w.coords, m, [{"type": "center", "selection": [pc.NA], "reference_selection": []}],
+                            list(range(pc.NA)))
+        with pytest.raises(abi.SassError):
+            p.stage_prepass(w.coords, m, [{"type": "fitrottrans", "selection": [], "reference_selection": [0, 1],
+                                           "fit_target": [0], "fit_source": [2]}], list(range(pc.NA)))
+        with pytest.raises(abi.SassError):
+            p.stage_prepass(w.coords, m, [{"type": "motion", "selection": [0], "reference_selection": [0]}],
+                            list(range(pc.NA)))
+
+
+@pytest.mark.parametrize("name", ["pre_post", "motions", "fittrans"])
+def test_driver_with_alignments_matches_oracle(native_lib, tmp_path, name):
+    d = str(tmp_path / "run")
+    w, cfg, o = pc.build(name, d)
+    r = subprocess.run([abi.DRIVER_PATH, "--config", cfg], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    aligned = al.load(w.coords, o["masses"], o["alignments"], o["motions"], o["target"])
+    target = o["target"] if o["target"] is not None else list(range(pc.NA))
+    cls = w.atom_class[target]
+    sv = (w.shells[:, None, None] * w.directions[None]).reshape(-1, 3)
+    ref = oracle.all_vectors(aligned, w.sub_offsets(), sv, w.class_factors[:, cls], 0, 0, nthreads=8)
+    f = h5lite.File(os.path.join(d, "signal.h5"))
+    fqt = f.read("fqt")
+    fqt = fqt[..., 0] + 1j * fqt[..., 1]
+    rfqt = ref[0][..., 0] + 1j * ref[0][..., 1]
+    err = (np.abs(fqt - rfqt).max(axis=1) / np.abs(rfqt[:, 0])).max()
+    assert err <= 1e-12, err
