@@ -20,7 +20,7 @@ lengths, 20 shells 0.05-3.0 1/A x 500 directions, FFT autocorrelation (padded le
 
 Other workloads (--workload): incoherent_fqt, static_xray, batched_uneven, layered_cv, and
 multipole_sphere / multipole_cylinder (the multipole devices on the coherent trajectory, FP64,
-terms = atoms x q-vectors x moments x frames).
+terms = atoms x q-vectors x moments x frames), prepass (sample alignments on the device).
 
 --impl reference times that CPU restatement (the reference itself cannot be built:
 MPI, Boost, FFTW3, HDF5 and libxml2 are absent) and prints its own line.
@@ -239,6 +239,36 @@ def cpu_sample_mp(w, qv, kind, moments, seconds, nthreads):
 
 def run_reference(args, dist):
     if dist.rank != 0:
+        return
+    if args.workload == "prepass":
+        from oracle import alignment as al
+        w = make_workload("coherent_sqt", args.nq, args.nf)
+        masses, _ = prepass_case(w)
+        allat = list(range(w.na))
+        al_steps = [{"type": "center", "selection": allat, "reference_selection": allat, "reference": None},
+                    {"type": "fitrottrans", "selection": allat, "reference_selection": allat,
+                     "reference": w.coords[0].astype(np.float64)}]
+        vals, nfs = [], 2
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            al.load(w.coords[:nfs], masses, al_steps)
+            dt = time.perf_counter() - t0
+            if i >= args.warmup:
+                vals.append(w.na * nfs / dt)
+        v = statistics.median(vals)
+        units = float(w.na) * w.nf
+        print(json.dumps({"impl": "reference", "metric": "atom*frame/s through the staging pre-pass "
+                          "(center + fitrottrans onto frame 0)", "value": v, "unit": "atom-frames/s",
+                          "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": units / v * 1e3, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+                          "config": {"workload": "prepass", "na": w.na, "nf": w.nf},
+                          "cpu_baseline": {"value": v, "unit": "atom-frames/s", "cores": 1, "kind": "port",
+                                           "sample": "oracle.alignment.load on %d of %d frames" % (nfs, w.nf)},
+                          "e2e": {"value": v, "unit": "atom-frames/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0},
+                          "note": "reference unbuildable here; timed the numpy restatement of "
+                                  "CoordinateSets::load (one core), ms_per_step extrapolated by frames"}))
         return
     if args.workload in MP_WORKLOADS:
         w, qv, kind, moments = multipole_workload(args)
@@ -574,6 +604,84 @@ def run_multipole(args, dist):
     plan.close()
 
 
+def prepass_case(w, nframes=None):
+    """Steps of the prepass workload: centre the system, then fit every frame onto frame 0
+    (all atoms); masses by class."""
+    na = w.na
+    allat = np.arange(na, dtype=np.uintp)
+    masses = np.array([1.008, 12.011, 14.007, 15.999, 32.06])[w.atom_class % 5]
+    steps = [{"type": "center", "selection": allat, "reference_selection": allat},
+             {"type": "fitrottrans", "selection": allat, "reference_selection": allat,
+              "reference": w.coords[0].astype(np.float64), "fit_target": allat, "fit_source": allat}]
+    return masses, steps
+
+
+def run_prepass(args, dist):
+    """Staging pre-pass (sample alignments): the coherent_sqt trajectory (10,000 atoms x
+    1,024 frames) centred and fitted onto frame 0 on the device, then staged. value =
+    atom-frames per second through sass_stage_frames_prepass from host frames (the host
+    copy is part of the call)."""
+    import torch
+
+    from sassena_gb300 import abi
+
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    w = make_workload("coherent_sqt", args.nq, args.nf)
+    masses, steps = prepass_case(w)
+    lib = abi.load()
+    nbytes = w.coords.nbytes
+    hp = lib.sass_host_alloc(nbytes)
+    frames = np.ctypeslib.as_array((np.ctypeslib.ctypes.c_float * w.coords.size)
+                                   .from_address(hp)).reshape(w.coords.shape)
+    frames[...] = w.coords
+    target = np.arange(w.na, dtype=np.uintp)
+    plan = abi.Plan(w.na, w.nf, len(w.class_names), "all", w.dsp, "fftw", "fp32", device=dev)
+    for _ in range(max(3, args.warmup)):
+        plan.stage_prepass(frames, masses, steps, target, return_staged=False)
+    steps_n = max(1, min(args.steps, 10))
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(dev)
+    clocks.start()
+    t0 = time.perf_counter()
+    for _ in range(steps_n):
+        plan.stage_prepass(frames, masses, steps, target, return_staged=False)
+    torch.cuda.synchronize()
+    ms = dist.max((time.perf_counter() - t0) * 1e3 / steps_n)
+    clk = clocks.stop()
+    units = float(w.na) * w.nf
+    out = {"metric": "atom*frame/s through the staging pre-pass (center + fitrottrans onto frame 0)",
+           "value": units * dist.world / (ms * 1e-3), "unit": "atom-frames/s", "n_gpus": dist.world,
+           "steps": steps_n, "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded random walk, coherent_sqt trajectory)",
+           "config": {"workload": "prepass", "na": w.na, "nf": w.nf,
+                      "steps": ["center", "fitrottrans"], "timing": "host clock around the C-ABI call "
+                      "(host frames in page-locked memory; upload, pre-pass, staging, synchronised)"},
+           "e2e": {"value": units * dist.world / (ms * 1e-3), "unit": "atom-frames/s",
+                   "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": w.nf * 9 * 8 * 2,
+                   "ms_per_step": ms},
+           "gpu_launches": None, "clocks": clk}
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu:
+        from oracle import alignment as al
+        nfs = 2
+        t0 = time.perf_counter()
+        al.load(w.coords[:nfs], masses,
+                [{"type": "center", "selection": list(range(w.na)), "reference_selection": list(range(w.na)),
+                  "reference": None},
+                 {"type": "fitrottrans", "selection": list(range(w.na)),
+                  "reference_selection": list(range(w.na)), "reference": w.coords[0].astype(np.float64)}])
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": w.na * nfs / dt, "unit": "atom-frames/s", "cores": 1, "kind": "port",
+                               "sample": "oracle.alignment.load (numpy restatement) on %d frames x %d atoms, "
+                                         "%.2f s" % (nfs, w.na, dt)}
+    if dist.rank == 0:
+        print(json.dumps(out))
+    lib.sass_host_free(hp)
+    plan.close()
+
+
 def run_batched(args, dist):
     """The batched form: 64 systems of uneven size in one graph-captured launch sequence."""
     import torch
@@ -779,6 +887,8 @@ def main():
             run_cv(args, dist)
         elif args.workload in MP_WORKLOADS:
             run_multipole(args, dist)
+        elif args.workload == "prepass":
+            run_prepass(args, dist)
         else:
             run_ours(args, dist)
     finally:

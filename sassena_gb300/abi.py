@@ -234,14 +234,14 @@ class Plan:
             raise ValueError("coords must be [nf, na, 3]")
         self._check(self.lib.sass_stage_frames(self._h, _ptr(c), 0))
 
-    def stage_prepass(self, frames, masses, steps, target):
+    def stage_prepass(self, frames, masses, steps, target, return_staged=True):
         """Alignments / motions on the whole system, then staging of the target atoms.
 
         frames: float32 [nf, nsys, 3]; masses [nsys]; target [na] system indices;
         steps: dicts with "type" (center, fittrans, fitrottrans, fitrot, motion),
         "selection", "reference_selection", optional "reference" ([nref, 3]),
         "fit_target" and "fit_source" (fits) and "translations" ([nf, 3], motions).
-        Returns the staged float32 frames [nf, na, 3]."""
+        Returns the staged float32 frames [nf, na, 3] (None with return_staged=False)."""
         fr = np.ascontiguousarray(frames, dtype=np.float32)
         nsys = fr.shape[1]
         if fr.shape != (self.nf, nsys, 3):
@@ -268,9 +268,9 @@ class Plan:
             e.fit_target, e.nfit = lst("fit_target")
             e.fit_source, _ = lst("fit_source")
             e.translations, _ = lst("translations", np.float64, (-1, 3))
-        out = np.zeros((self.nf, self.na, 3), dtype=np.float32)
+        out = np.zeros((self.nf, self.na, 3), dtype=np.float32) if return_staged else None
         self._check(self.lib.sass_stage_frames_prepass(self._h, _ptr(fr), nsys, _ptr(ms), arr, len(steps),
-                                                       _ptr(tg), _ptr(out)))
+                                                       _ptr(tg), _ptr(out) if return_staged else None))
         return out
 
     def set_classes(self, atom_class):
