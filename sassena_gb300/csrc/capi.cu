@@ -38,14 +38,14 @@ int validate_desc(const sass_plan_desc& d, int& lg, std::string& msg) {
     if (d.na == 0 || d.nf == 0 || d.nclass == 0) return SASS_ERR_ARG;
     if (d.na > (size_t)1 << 30 || d.nf > (size_t)1 << 24) return SASS_ERR_ARG;
     lg = std::max(2, ceil_log2(2 * d.nf));
-    if (d.dsp_type == SASS_DSP_AUTOCORRELATE && lg > kMaxLg) {
-        char b[160];
-        snprintf(b, sizeof(b), "autocorrelation supports NF <= 4096 (padded FFT length <= 8192), got NF=%zu", d.nf);
+    // coherent autocorrelation: shared-memory transforms up to 2^kMaxLg, the four-step
+    // transform through HBM up to 2^kLongLgMax; incoherent: shared memory only
+    const int lg_limit = d.scattering == SASS_SCATTERING_ALL ? kLongLgMax : kMaxLg;
+    if (d.dsp_type == SASS_DSP_AUTOCORRELATE && lg > lg_limit) {
+        char b[200];
+        snprintf(b, sizeof(b), "autocorrelation supports NF <= %zu for this scattering type (padded FFT length <= %zu), got NF=%zu",
+                 ((size_t)1 << lg_limit) / 2, (size_t)1 << lg_limit, d.nf);
         msg = b;
-        return SASS_ERR_UNSUPPORTED;
-    }
-    if (d.dsp_type != SASS_DSP_AUTOCORRELATE && d.nf > 4096) {
-        msg = "dsp square/plain supports NF <= 4096";
         return SASS_ERR_UNSUPPORTED;
     }
     if (d.scattering == SASS_SCATTERING_SELF && d.dsp_type == SASS_DSP_AUTOCORRELATE &&

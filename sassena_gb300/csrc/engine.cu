@@ -93,6 +93,14 @@ int build_system_tables(SystemState& s, cudaStream_t st, std::string& err) {
     ECK(s.k64.ensure(L * sizeof(double2)));
     ECK(s.k32.ensure(L * sizeof(float2)));
     ECK(launch_twiddles(s.tw64.as<double2>(), s.tw32.as<float2>(), s.lg, st));
+    if (s.lg > kMaxLg) {  // long layout, built by the four-step transform of the window
+        DevBuf scratch;
+        ECK(scratch.ensure((s.nf + L) * sizeof(double2)));
+        ECK(launch_long_store_kernel(s.tw64.as<double2>(), s.lg, (int)s.nf, scratch.as<double2>(),
+                                     s.k64.as<double2>(), s.k32.as<float2>(), st));
+        ECK(cudaStreamSynchronize(st));
+        return kOk;
+    }
     ECK(launch_store_kernel(s.tw64.as<double2>(), s.lg, s.k64.as<double2>(), s.k32.as<float2>(), (int)s.nf, s.lg,
                             st));
     ECK(cudaStreamSynchronize(st));
@@ -324,9 +332,24 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
     lg_max_ = 2;
     lg_min_ = kMaxLg;
     nf_max_ = 1;
-    for (const WorkItem& it : items) {
+    // systems whose padded length exceeds the shared-memory transforms take the long path
+    std::vector<char> long_item(items.size(), 0);
+    for (size_t i = 0; i < items.size(); ++i) {
+        const WorkItem& it = items[i];
         for (size_t s = 0; s + 1 < it.offs.size(); ++s) min_nm = std::min(min_nm, it.offs[s + 1] - it.offs[s]);
         total_shells += it.offs.size() - 1;
+        if (autoc && it.sys->lg > kMaxLg) {
+            if (!coherent || it.sys->lg > kLongLgMax) {
+                err = "autocorrelation of this length is not supported for this scattering type";
+                return kErrUnsupported;
+            }
+            if (it.d_wsqrt) {
+                err = "weighted averages need NF <= 4096";
+                return kErrUnsupported;
+            }
+            long_item[i] = 1;
+            continue;
+        }
         lg_max_ = std::max(lg_max_, it.sys->lg);
         lg_min_ = std::min(lg_min_, it.sys->lg);
         nf_max_ = std::max(nf_max_, (int)it.sys->nf);
@@ -452,6 +475,7 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
     item_cf_.assign(items.size(), nullptr);
     item_sys_.assign(items.size(), nullptr);
     item_nq_.assign(items.size(), 0);
+    item_amp_.assign(items.size(), nullptr);
     for (size_t i = 0; i < items.size(); ++i) {
         const WorkItem& it = items[i];
         SystemState& s = *it.sys;
@@ -472,6 +496,7 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
         p.split_stride = nv * s.nf;
         void* amp = coherent ? (void*)(amp_.as<unsigned char>() + amp_off_[i]) : nullptr;
         if (it.d_amp_given) amp = const_cast<double2*>(it.d_amp_given);
+        item_amp_[i] = amp;
         if (coherent && !it.d_amp_given) {
             if (nsplit_[i] > 1) {
                 double2* part = reinterpret_cast<double2*>(part_.as<unsigned char>() + part_off_[i]);
@@ -596,6 +621,7 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
     size_t poff = 0;
     int slot = 0;
     for (size_t i = 0; i < items.size(); ++i) {
+        if (long_item[i]) continue;
         const WorkItem& it = items[i];
         SystemState& s = *it.sys;
         const size_t L = (size_t)1 << s.lg;
@@ -636,6 +662,77 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
             }
         }
     }
+    // long series: chunks of one shell's series (about 2 CTAs per SM over all rows), batches
+    // of consecutive chunks whose series fit the column-pass scratch, one entry per shell
+    std::vector<CorrChunk> lchunks;
+    std::vector<FinalEntry> lentries;
+    long_batches_.clear();
+    long_items_.clear();
+    size_t mpart_total = 0, ybytes = 0, zbytes = 0;
+    for (size_t i = 0; i < items.size(); ++i) {
+        if (!long_item[i]) continue;
+        const WorkItem& it = items[i];
+        SystemState& s = *it.sys;
+        const size_t L = (size_t)1 << s.lg, R = L >> kLongRowLg, nq = it.offs.size() - 1;
+        const size_t esz = f32 ? sizeof(float2) : sizeof(double2);
+        const size_t S = std::max<size_t>(1, kLongScratchBytes / (L * esz));
+        LongItem li{};
+        li.item = (int)i;
+        li.lg = s.lg;
+        li.mpart_off = mpart_total;
+        li.chunk_begin = (int)lchunks.size();
+        li.entry_begin = (int)lentries.size();
+        li.batch_begin = (int)long_batches_.size();
+        mpart_total += it.offs.back() * R;
+        const size_t per = std::max<size_t>(1, (2 * (size_t)sms + R * nq - 1) / (R * nq));
+        std::vector<CorrChunk> ic;
+        for (size_t sh = 0; sh < nq; ++sh) {
+            FinalEntry e{};
+            e.slot_begin = slot;
+            e.part_off = poff;
+            e.part_len = L;
+            e.nf = (int)s.nf;
+            e.lg = s.lg;
+            e.inv_nm = it.norm > 0 ? it.norm : 1.0 / (double)(it.offs[sh + 1] - it.offs[sh]);
+            e.fqt = it.d_fqt + sh * s.nf;
+            e.fq = it.d_fq + sh;
+            e.fq2 = it.d_fq2 + sh;
+            const size_t units = it.offs[sh + 1] - it.offs[sh];
+            const size_t len = std::min(S, (units + std::min(per, units) - 1) / std::min(per, units));
+            for (size_t u = 0; u < units; u += len) {
+                CorrChunk c{};
+                c.system = (int)i;
+                c.shell = (int)sh;
+                c.v_begin = (int)(it.offs[sh] + u);
+                c.v_end = (int)(it.offs[sh] + std::min(units, u + len));
+                c.part_off = poff;
+                c.slot = slot++;
+                poff += L;
+                ic.push_back(c);
+            }
+            e.slot_end = slot;
+            lentries.push_back(e);
+        }
+        for (size_t cb = 0; cb < ic.size();) {
+            size_t ce = cb + 1;
+            while (ce < ic.size() && (size_t)(ic[ce].v_end - ic[cb].v_begin) <= S) ++ce;
+            LongBatch b{(int)i, ic[cb].v_begin, ic[ce - 1].v_end, li.chunk_begin + (int)cb, li.chunk_begin + (int)ce};
+            long_batches_.push_back(b);
+            ybytes = std::max(ybytes, (size_t)(b.v1 - b.v0) * L * esz);
+            cb = ce;
+        }
+        lchunks.insert(lchunks.end(), ic.begin(), ic.end());
+        li.chunk_end = (int)lchunks.size();
+        li.entry_end = (int)lentries.size();
+        li.batch_end = (int)long_batches_.size();
+        zbytes = std::max(zbytes, (size_t)(li.entry_end - li.entry_begin) * L * sizeof(double2));
+        long_items_.push_back(li);
+    }
+    if (!long_items_.empty()) {
+        ECK(long_Y_.ensure(ybytes));
+        ECK(long_mpart_.ensure(mpart_total * sizeof(double2)));
+        ECK(long_Z_.ensure(zbytes));
+    }
     nchunks_ = (int)chunks.size();
     nentries_ = (int)entries.size();
     ECK(ppart_.ensure(poff * sizeof(double)));
@@ -660,12 +757,14 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
     size_t o_psys = push(blob, psys), o_tiles = push(blob, tiles);
     size_t o_rsys = push(blob, rsys), o_rgroups = push(blob, rgroups), o_rtiles = push(blob, rtiles);
     // CorrSystem.shell_v points into the blob: patch with the final device address
-    ECK(blob_.ensure(blob.size() + 4096 + csys.size() * sizeof(CorrSystem) + chunks.size() * sizeof(CorrChunk) +
-                     (entries.size() + entries_w.size()) * sizeof(FinalEntry) + 4096));
+    ECK(blob_.ensure(blob.size() + 8192 + csys.size() * sizeof(CorrSystem) +
+                     (chunks.size() + lchunks.size()) * sizeof(CorrChunk) +
+                     (entries.size() + entries_w.size() + lentries.size()) * sizeof(FinalEntry) + 4096));
     for (size_t i = 0; i < items.size(); ++i)
         csys[i].shell_v = reinterpret_cast<const int*>(blob_.as<unsigned char>() + shell_off[i]);
     size_t o_csys = push(blob, csys), o_chunks = push(blob, chunks), o_entries = push(blob, entries);
     size_t o_entries_w = push(blob, entries_w);
+    size_t o_lchunks = push(blob, lchunks), o_lentries = push(blob, lentries);
     if (blob.size() > blob_.bytes) {
         err = "descriptor blob sizing";
         return kErrArg;
@@ -683,11 +782,13 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
     d_chunks_ = reinterpret_cast<CorrChunk*>(base + o_chunks);
     d_entries_ = reinterpret_cast<FinalEntry*>(base + o_entries);
     d_entries_w_ = reinterpret_cast<FinalEntry*>(base + o_entries_w);
+    d_long_chunks_ = reinterpret_cast<CorrChunk*>(base + o_lchunks);
+    d_long_entries_ = reinterpret_cast<FinalEntry*>(base + o_lentries);
     ECK(cudaDeviceSynchronize());
     stats_.phase_tiles = tiles.size();
     stats_.rec_tiles = rtiles.size();
-    stats_.corr_chunks = chunks.size();
-    stats_.final_entries = entries.size();
+    stats_.corr_chunks = chunks.size() + lchunks.size();
+    stats_.final_entries = entries.size() + lentries.size();
     return kOk;
 }
 
@@ -759,6 +860,34 @@ int Engine::enqueue(cudaStream_t st, std::string& err, cudaEvent_t* ev) {
     cl.err = err_.as<unsigned>();
     ECK(coherent ? launch_corr_accumulate(cl, st) : launch_self_accumulate(cl, st));
     ++launches;
+    for (const LongItem& li : long_items_) {
+        SystemState& s = *item_sys_[li.item];
+        const size_t esz = f32 ? sizeof(float2) : sizeof(double2);
+        for (int b = li.batch_begin; b < li.batch_end; ++b) {
+            const LongBatch& lb = long_batches_[b];
+            LongArgs la{};
+            la.precision = cfg_.precision;
+            la.lg = s.lg;
+            la.nf = (int)s.nf;
+            la.A = static_cast<const unsigned char*>(item_amp_[li.item]) + (size_t)lb.v0 * s.nf * esz;
+            la.Y = long_Y_.p;
+            la.nseries = lb.v1 - lb.v0;
+            la.tw = f32 ? s.tw32.p : s.tw64.p;
+            la.chunks = d_long_chunks_ + lb.chunk_begin;
+            la.nchunks = lb.chunk_end - lb.chunk_begin;
+            la.v0 = lb.v0;
+            la.kbr = f32 ? s.k32.p : s.k64.p;
+            la.ppart = ppart_.as<double>();
+            la.mpart = long_mpart_.as<double2>() + li.mpart_off;
+            ECK(launch_long_columns(la, st));
+            ECK(launch_long_rows(la, st));
+            launches += 2;
+        }
+        ECK(launch_long_means(d_long_chunks_ + li.chunk_begin, li.chunk_end - li.chunk_begin,
+                              long_mpart_.as<double2>() + li.mpart_off, 1 << (s.lg - kLongRowLg), apart_.as<double2>(),
+                              a2part_.as<double>(), st));
+        ++launches;
+    }
     if (ev) ECK(cudaEventRecord(ev[2], st));
     FinalLaunch fl{};
     fl.dsp = cfg_.dsp;
@@ -772,6 +901,21 @@ int Engine::enqueue(cudaStream_t st, std::string& err, cudaEvent_t* ev) {
     fl.tw = tw64_.as<double2>();
     ECK(launch_finalize(fl, st));
     ++launches;
+    for (const LongItem& li : long_items_) {
+        SystemState& s = *item_sys_[li.item];
+        LongFinal lf{};
+        lf.entries = d_long_entries_ + li.entry_begin;
+        lf.nentries = li.entry_end - li.entry_begin;
+        lf.lg = s.lg;
+        lf.conj_out = fl.conj_out;
+        lf.ppart = ppart_.as<double>();
+        lf.apart = apart_.as<double2>();
+        lf.a2part = a2part_.as<double>();
+        lf.tw = s.tw64.as<double2>();
+        lf.Z = long_Z_.as<double2>();
+        ECK(launch_long_finalize(lf, st));
+        launches += 2;
+    }
     if (weighted_) {
         // the autocorrelation is quadratic in A: scaling A_v by sqrt(w_v) turns the same
         // correlation pass into (1/NM) sum_v w_v C_v(t)

@@ -159,7 +159,25 @@ private:
     std::vector<const double*> item_wsqrt_;
     bool weighted_ = false;
     int tw_lg_ = 0;
+    // long series (autocorrelation, padded length above 2^kMaxLg): four-step transform
+    struct LongBatch {
+        int item, v0, v1, chunk_begin, chunk_end;  // series [v0, v1) in Y; chunks of the batch
+    };
+    struct LongItem {
+        int item, lg;
+        int chunk_begin, chunk_end, entry_begin, entry_end, batch_begin, batch_end;
+        size_t mpart_off;  // double2 offset of the item's [nv][R] mean parts
+    };
+    std::vector<LongBatch> long_batches_;
+    std::vector<LongItem> long_items_;
+    std::vector<const void*> item_amp_;
+    CorrChunk* d_long_chunks_ = nullptr;
+    FinalEntry* d_long_entries_ = nullptr;
+    DevBuf long_Y_, long_mpart_, long_Z_;
 };
+
+// HBM scratch for the column-pass output of one batch of long series.
+constexpr size_t kLongScratchBytes = (size_t)2 << 30;
 
 int sm_count(int device);
 

@@ -205,6 +205,51 @@ cudaError_t launch_finalize(const FinalLaunch& a, cudaStream_t st);
 // Shared memory of the FFT accumulate kernels for padded length 2^lg.
 size_t fft_smem_bytes(int precision, int lg, int nf, bool self);
 
+// ---------------------------------------------------------------------------------------
+// Long series (autocorrelation with padded length 2^14 .. 2^20): four-step FFT through HBM,
+// L = R x C with C = 2^kLongRowLg and R = L / C. Spectra are kept in (k1, bit-reversed k2)
+// order: index k1 * C + bitrev(k2) holds frequency k1 + R k2.
+// ---------------------------------------------------------------------------------------
+constexpr int kLongRowLg = 12;
+constexpr int kLongLgMax = 20;
+
+struct LongArgs {
+    int precision, lg, nf;
+    const void* A;             // series [nseries][nf] (T2): the batch's first series
+    void* Y;                   // [nseries][L] T2 scratch (column-pass output)
+    int nseries;
+    const void* tw;            // W_L^j for j < L/2 (T2 of the precision)
+    const CorrChunk* chunks;   // row pass: chunk series v reads Y[v - v0]
+    int nchunks, v0;
+    const void* kbr;           // store kernel K in the long order (T2)
+    double* ppart;             // power partial slots (chunk.part_off, L doubles per slot)
+    double2* mpart;            // [nv][R] row parts of the series means
+    void* xout;                // transform mode: conj(X) in the long order (T2)
+};
+// Column pass over the batch's series; row pass over its chunks (power, means).
+cudaError_t launch_long_columns(const LongArgs& a, cudaStream_t st);
+cudaError_t launch_long_rows(const LongArgs& a, cudaStream_t st);
+// One series' transform (nseries = 1): xout = conj(FFT_L(x)).
+cudaError_t launch_long_transform(const LongArgs& a, cudaStream_t st);
+// afinal / a2final partials of every long chunk from the row parts of its series means.
+cudaError_t launch_long_means(const CorrChunk* chunks, int nchunks, const double2* mpart, int R, double2* apart,
+                              double* a2part, cudaStream_t st);
+
+struct LongFinal {
+    const FinalEntry* entries;
+    int nentries, lg, conj_out;
+    const double* ppart;
+    const double2* apart;
+    const double* a2part;
+    const double2* tw;         // W_L^j, j < L/2, FP64
+    double2* Z;                // [nentries][L] scratch
+};
+cudaError_t launch_long_finalize(const LongFinal& a, cudaStream_t st);
+// K of a long system: K(k) = sum_{tau<nf} exp(+2 pi i k tau / L) / (nf L (nf - tau)) in the long
+// order, FP64 and FP32 copies; scratch holds nf + L double2.
+cudaError_t launch_long_store_kernel(const double2* tw64, int lg, int nf, double2* scratch, double2* k64,
+                                     float2* k32, cudaStream_t st);
+
 // FFT tables on the device: tw[k] = exp(-2 pi i k / L) (k < L/2) in FP64 and FP32, and
 // the store kernel K at bit-reversed positions for (nf, lg).
 cudaError_t launch_twiddles(double2* tw64, float2* tw32, int lg, cudaStream_t st);
