@@ -38,9 +38,9 @@ int validate_desc(const sass_plan_desc& d, int& lg, std::string& msg) {
     if (d.na == 0 || d.nf == 0 || d.nclass == 0) return SASS_ERR_ARG;
     if (d.na > (size_t)1 << 30 || d.nf > (size_t)1 << 24) return SASS_ERR_ARG;
     lg = std::max(2, ceil_log2(2 * d.nf));
-    // coherent autocorrelation: shared-memory transforms up to 2^kMaxLg, the four-step
-    // transform through HBM up to 2^kLongLgMax; incoherent: shared memory only
-    const int lg_limit = d.scattering == SASS_SCATTERING_ALL ? kLongLgMax : kMaxLg;
+    // autocorrelation: shared-memory transforms up to 2^kMaxLg, the four-step transform
+    // through HBM up to 2^kLongLgMax
+    const int lg_limit = kLongLgMax;
     if (d.dsp_type == SASS_DSP_AUTOCORRELATE && lg > lg_limit) {
         char b[200];
         snprintf(b, sizeof(b), "autocorrelation supports NF <= %zu for this scattering type (padded FFT length <= %zu), got NF=%zu",
@@ -48,7 +48,7 @@ int validate_desc(const sass_plan_desc& d, int& lg, std::string& msg) {
         msg = b;
         return SASS_ERR_UNSUPPORTED;
     }
-    if (d.scattering == SASS_SCATTERING_SELF && d.dsp_type == SASS_DSP_AUTOCORRELATE &&
+    if (d.scattering == SASS_SCATTERING_SELF && d.dsp_type == SASS_DSP_AUTOCORRELATE && lg <= kMaxLg &&
         fft_smem_bytes(d.precision, lg, (int)d.nf, true) > 227 * 1024) {
         msg = "incoherent FP64 autocorrelation with this NF exceeds shared memory";
         return SASS_ERR_UNSUPPORTED;

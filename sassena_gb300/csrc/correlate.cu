@@ -1294,6 +1294,21 @@ __global__ void __launch_bounds__(kLongNT) long_final_cols_kernel(LongFinal a) {
     }
 }
 
+template <class T>
+__global__ void long_self_series_kernel(LongSelfArgs a) {
+    typedef typename cplx<T>::type T2;
+    const T* b = reinterpret_cast<const T*>(a.bfac);
+    T2* G = reinterpret_cast<T2*>(a.G);
+    const size_t n = (size_t)a.nseries * a.nf;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+        const int s = (int)(idx / a.nf), t = (int)(idx - (size_t)s * a.nf);
+        const int p = a.p0 + s, j = p / a.nm, m = p - j * a.nm;
+        T qx, qy, qz;
+        load_q(a.qv + 3 * (size_t)m, qx, qy, qz);
+        G[idx] = self_term(b[j], a.xyz[(size_t)t * a.na_pad + j], qx, qy, qz);
+    }
+}
+
 __global__ void long_window_kernel(int nf, int L, double2* w) {
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += gridDim.x * blockDim.x)
         w[t] = make_double2(1.0 / ((double)nf * (double)L * (double)(nf - t)), 0.0);
@@ -1361,6 +1376,14 @@ cudaError_t launch_long_transform(const LongArgs& a, cudaStream_t st) {
     e = set_smem(long_row_kernel<double, 1>, sm);
     if (e != cudaSuccess) return e;
     long_row_kernel<double, 1><<<dim3((unsigned)(1 << (a.lg - kLongRowLg)), 1), kLongNT, sm, st>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_long_self_series(const LongSelfArgs& a, cudaStream_t st) {
+    const size_t n = (size_t)a.nseries * a.nf;
+    if (n == 0) return cudaSuccess;
+    if (a.precision == PREC_FP32) long_self_series_kernel<float><<<grid_for(n, 256), 256, 0, st>>>(a);
+    else long_self_series_kernel<double><<<grid_for(n, 256), 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -339,8 +339,8 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
         for (size_t s = 0; s + 1 < it.offs.size(); ++s) min_nm = std::min(min_nm, it.offs[s + 1] - it.offs[s]);
         total_shells += it.offs.size() - 1;
         if (autoc && it.sys->lg > kMaxLg) {
-            if (!coherent || it.sys->lg > kLongLgMax) {
-                err = "autocorrelation of this length is not supported for this scattering type";
+            if (it.sys->lg > kLongLgMax) {
+                err = "autocorrelation supports NF <= 524288";
                 return kErrUnsupported;
             }
             if (it.d_wsqrt) {
@@ -476,6 +476,12 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
     item_sys_.assign(items.size(), nullptr);
     item_nq_.assign(items.size(), 0);
     item_amp_.assign(items.size(), nullptr);
+    item_offs_.assign(items.size(), {});
+    item_qv_.assign(items.size(), nullptr);
+    for (size_t i = 0; i < items.size(); ++i) {
+        item_offs_[i] = items[i].offs;
+        item_qv_[i] = items[i].d_qv;
+    }
     for (size_t i = 0; i < items.size(); ++i) {
         const WorkItem& it = items[i];
         SystemState& s = *it.sys;
@@ -668,14 +674,15 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
     std::vector<FinalEntry> lentries;
     long_batches_.clear();
     long_items_.clear();
-    size_t mpart_total = 0, ybytes = 0, zbytes = 0;
+    size_t mpart_total = 0, ybytes = 0, zbytes = 0, gbytes = 0;
     for (size_t i = 0; i < items.size(); ++i) {
         if (!long_item[i]) continue;
         const WorkItem& it = items[i];
         SystemState& s = *it.sys;
         const size_t L = (size_t)1 << s.lg, R = L >> kLongRowLg, nq = it.offs.size() - 1;
         const size_t esz = f32 ? sizeof(float2) : sizeof(double2);
-        const size_t S = std::max<size_t>(1, kLongScratchBytes / (L * esz));
+        // incoherent: the (atom, direction) series are generated per batch next to Y
+        const size_t S = std::max<size_t>(1, kLongScratchBytes / ((L + (coherent ? 0 : s.nf)) * esz));
         LongItem li{};
         li.item = (int)i;
         li.lg = s.lg;
@@ -683,9 +690,9 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
         li.chunk_begin = (int)lchunks.size();
         li.entry_begin = (int)lentries.size();
         li.batch_begin = (int)long_batches_.size();
-        mpart_total += it.offs.back() * R;
         const size_t per = std::max<size_t>(1, (2 * (size_t)sms + R * nq - 1) / (R * nq));
         std::vector<CorrChunk> ic;
+        size_t vbase = 0;  // incoherent: first series of the shell (pairs of earlier shells)
         for (size_t sh = 0; sh < nq; ++sh) {
             FinalEntry e{};
             e.slot_begin = slot;
@@ -697,14 +704,17 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
             e.fqt = it.d_fqt + sh * s.nf;
             e.fq = it.d_fq + sh;
             e.fq2 = it.d_fq2 + sh;
-            const size_t units = it.offs[sh + 1] - it.offs[sh];
+            const size_t nm = it.offs[sh + 1] - it.offs[sh];
+            const size_t units = coherent ? nm : s.na * nm;
+            const size_t first = coherent ? it.offs[sh] : vbase;
+            vbase += units;
             const size_t len = std::min(S, (units + std::min(per, units) - 1) / std::min(per, units));
             for (size_t u = 0; u < units; u += len) {
                 CorrChunk c{};
                 c.system = (int)i;
                 c.shell = (int)sh;
-                c.v_begin = (int)(it.offs[sh] + u);
-                c.v_end = (int)(it.offs[sh] + std::min(units, u + len));
+                c.v_begin = (int)(first + u);
+                c.v_end = (int)(first + std::min(units, u + len));
                 c.part_off = poff;
                 c.slot = slot++;
                 poff += L;
@@ -713,12 +723,24 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
             e.slot_end = slot;
             lentries.push_back(e);
         }
+        if (vbase > (size_t)INT32_MAX) {
+            err = "too many (atom, direction) series for one call; split the q-vectors";
+            return kErrArg;
+        }
+        mpart_total += (coherent ? it.offs.back() : vbase) * R;
+        // batches of consecutive chunks within S series (incoherent: within one shell)
+        std::vector<size_t> shell_first(nq + 1, 0);
+        for (size_t sh = 0; sh < nq; ++sh) shell_first[sh + 1] = shell_first[sh] + s.na * (it.offs[sh + 1] - it.offs[sh]);
         for (size_t cb = 0; cb < ic.size();) {
             size_t ce = cb + 1;
-            while (ce < ic.size() && (size_t)(ic[ce].v_end - ic[cb].v_begin) <= S) ++ce;
-            LongBatch b{(int)i, ic[cb].v_begin, ic[ce - 1].v_end, li.chunk_begin + (int)cb, li.chunk_begin + (int)ce};
+            while (ce < ic.size() && (size_t)(ic[ce].v_end - ic[cb].v_begin) <= S &&
+                   (coherent || ic[ce].shell == ic[cb].shell))
+                ++ce;
+            LongBatch b{(int)i, ic[cb].v_begin, ic[ce - 1].v_end, li.chunk_begin + (int)cb, li.chunk_begin + (int)ce,
+                        ic[cb].shell, coherent ? 0 : ic[cb].v_begin - (int)shell_first[ic[cb].shell]};
             long_batches_.push_back(b);
             ybytes = std::max(ybytes, (size_t)(b.v1 - b.v0) * L * esz);
+            if (!coherent) gbytes = std::max(gbytes, (size_t)(b.v1 - b.v0) * s.nf * esz);
             cb = ce;
         }
         lchunks.insert(lchunks.end(), ic.begin(), ic.end());
@@ -732,6 +754,7 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
         ECK(long_Y_.ensure(ybytes));
         ECK(long_mpart_.ensure(mpart_total * sizeof(double2)));
         ECK(long_Z_.ensure(zbytes));
+        if (gbytes) ECK(long_G_.ensure(gbytes));
     }
     nchunks_ = (int)chunks.size();
     nentries_ = (int)entries.size();
@@ -869,7 +892,24 @@ int Engine::enqueue(cudaStream_t st, std::string& err, cudaEvent_t* ev) {
             la.precision = cfg_.precision;
             la.lg = s.lg;
             la.nf = (int)s.nf;
-            la.A = static_cast<const unsigned char*>(item_amp_[li.item]) + (size_t)lb.v0 * s.nf * esz;
+            if (coherent) {
+                la.A = static_cast<const unsigned char*>(item_amp_[li.item]) + (size_t)lb.v0 * s.nf * esz;
+            } else {  // generate the batch's (atom, direction) series
+                LongSelfArgs g{};
+                g.precision = cfg_.precision;
+                g.nf = (int)s.nf;
+                g.na_pad = (int)s.na_pad;
+                g.nm = (int)(item_offs_[li.item][lb.shell + 1] - item_offs_[li.item][lb.shell]);
+                g.p0 = lb.p0;
+                g.nseries = lb.v1 - lb.v0;
+                g.xyz = s.xyz.as<float4>();
+                g.bfac = bfac_.as<unsigned char>() + bfac_off_[li.item] + (size_t)lb.shell * s.na_pad * (f32 ? 4 : 8);
+                g.qv = item_qv_[li.item] + 3 * item_offs_[li.item][lb.shell];
+                g.G = long_G_.p;
+                ECK(launch_long_self_series(g, st));
+                ++launches;
+                la.A = long_G_.p;
+            }
             la.Y = long_Y_.p;
             la.nseries = lb.v1 - lb.v0;
             la.tw = f32 ? s.tw32.p : s.tw64.p;

@@ -162,6 +162,7 @@ private:
     // long series (autocorrelation, padded length above 2^kMaxLg): four-step transform
     struct LongBatch {
         int item, v0, v1, chunk_begin, chunk_end;  // series [v0, v1) in Y; chunks of the batch
+        int shell, p0;                             // incoherent: the shell and its first pair
     };
     struct LongItem {
         int item, lg;
@@ -171,9 +172,11 @@ private:
     std::vector<LongBatch> long_batches_;
     std::vector<LongItem> long_items_;
     std::vector<const void*> item_amp_;
+    std::vector<std::vector<size_t>> item_offs_;
+    std::vector<const double*> item_qv_;
     CorrChunk* d_long_chunks_ = nullptr;
     FinalEntry* d_long_entries_ = nullptr;
-    DevBuf long_Y_, long_mpart_, long_Z_;
+    DevBuf long_Y_, long_mpart_, long_Z_, long_G_;
 };
 
 // HBM scratch for the column-pass output of one batch of long series.

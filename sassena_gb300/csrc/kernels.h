@@ -231,6 +231,16 @@ cudaError_t launch_long_columns(const LongArgs& a, cudaStream_t st);
 cudaError_t launch_long_rows(const LongArgs& a, cudaStream_t st);
 // One series' transform (nseries = 1): xout = conj(FFT_L(x)).
 cudaError_t launch_long_transform(const LongArgs& a, cudaStream_t st);
+// Incoherent long series: G[p - p0][t] = b_j exp(i q_m . r_j(t)) for pairs p = j * nm + m of
+// one shell, p in [p0, p0 + nseries).
+struct LongSelfArgs {
+    int precision, nf, na_pad, nm, p0, nseries;
+    const float4* xyz;         // [nf][na_pad]
+    const void* bfac;          // the shell's factor row [na_pad] (T)
+    const double* qv;          // the shell's q-vectors [nm][3]
+    void* G;                   // [nseries][nf] T2
+};
+cudaError_t launch_long_self_series(const LongSelfArgs& a, cudaStream_t st);
 // afinal / a2final partials of every long chunk from the row parts of its series means.
 cudaError_t launch_long_means(const CorrChunk* chunks, int nchunks, const double2* mpart, int R, double2* apart,
                               double* a2part, cudaStream_t st);

@@ -56,10 +56,23 @@ def test_long_square_plain(native_lib, scattering, dsp):
     check(w, "fp32")
 
 
-def test_incoherent_long_autocorrelation_is_refused(native_lib):
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("nf", [4100, 8300])
+def test_incoherent_long_autocorrelation(native_lib, precision, nf):
+    # (atom, direction) series generated per batch, then the same four-step passes
+    w = synth.small("self", "autocorrelate", seed=76, na=13, nf=nf, nq=2, nm=3, box=10.0)
+    check(w, precision)
+
+
+def test_incoherent_long_direct_method(native_lib):
+    w = synth.small("self", "autocorrelate", seed=77, na=7, nf=4400, nq=2, nm=2, box=10.0)
+    check(w, "fp64", method="direct")
+
+
+def test_longest_series_refused(native_lib):
     with pytest.raises(abi.SassError) as e:
-        abi.Plan(10, 5000, 1, "self", "autocorrelate", "fftw", "fp64")
-    assert "NF <=" in str(e.value) or e.value.code == 3
+        abi.Plan(10, 600000, 1, "all", "autocorrelate", "fftw", "fp64")
+    assert e.value.code == 3
 
 
 def test_multipole_long(native_lib):
