@@ -171,8 +171,8 @@ def test_error_paths(native_lib):
     with pytest.raises(abi.SassError) as e:
         abi.Plan(10, 0, 1)
     assert e.value.code == 1
-    with pytest.raises(abi.SassError) as e:
-        abi.Plan(10, 5000, 1, "all", "autocorrelate")
+    with pytest.raises(abi.SassError) as e:  # beyond the long-series transform (NF <= 524,288)
+        abi.Plan(10, 600000, 1, "all", "autocorrelate")
     assert e.value.code == 3
     with abi.Plan(4, 4, 2) as p:
         with pytest.raises(abi.SassError) as e:
