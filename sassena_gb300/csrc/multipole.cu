@@ -117,7 +117,8 @@ __global__ void mp_convert_kernel(const float4* __restrict__ xyz, int na_pad, in
 // ---------------------------------------------------------------------------------------
 // special functions (FP64)
 // ---------------------------------------------------------------------------------------
-// b * j_l(x) for l = 0..L written to out[l * stride].
+// b * j_l(x) for l = 0..L written to out[l * stride]. Divisions are hoisted (1/x once):
+// GB300's FP64 pipe makes every division or square root a dozen FMAs.
 __device__ void sph_bessel_row(int L, double x, double b, double* out, size_t stride) {
     if (x == 0) {
         out[0] = b;
@@ -126,11 +127,12 @@ __device__ void sph_bessel_row(int L, double x, double b, double* out, size_t st
     }
     if (x < 0.5) {  // power series
         double xl = 1;
+        const double x2 = x * x;
         for (int l = 0; l <= L; ++l) {
             if (l > 0) xl *= x / (2 * l + 1);
             double term = 1, sum = 1;
             for (int k = 1; k < 40; ++k) {
-                term *= -x * x / (2.0 * k * (2 * l + 2 * k + 1));
+                term *= -x2 / (2.0 * k * (2 * l + 2 * k + 1));
                 sum += term;
                 if (fabs(term) < 1e-18 * fabs(sum)) break;
             }
@@ -138,15 +140,16 @@ __device__ void sph_bessel_row(int L, double x, double b, double* out, size_t st
         }
         return;
     }
+    const double ix = 1.0 / x;
     double sx, cx;
     sincos(x, &sx, &cx);
-    const double j0 = sx / x, j1 = sx / (x * x) - cx / x;
+    const double j0 = sx * ix, j1 = (sx * ix - cx) * ix;
     if (x > L) {  // upward recurrence, stable for every l < x
         double jm = j0, jc = j1;
         out[0] = b * j0;
         if (L >= 1) out[stride] = b * j1;
         for (int l = 1; l < L; ++l) {
-            const double jn = (2 * l + 1) / x * jc - jm;
+            const double jn = (2 * l + 1) * ix * jc - jm;
             out[(l + 1) * stride] = b * jn;
             jm = jc;
             jc = jn;
@@ -157,7 +160,7 @@ __device__ void sph_bessel_row(int L, double x, double b, double* out, size_t st
     const int N = L + 32;
     double fp = 0, f = 1e-250;
     for (int n = N; n >= 1; --n) {
-        const double fm = (2 * n + 1) / x * f - fp;
+        const double fm = (2 * n + 1) * ix * f - fp;
         fp = f;
         f = fm;
         if (n - 1 <= L) out[(n - 1) * stride] = f;
@@ -171,17 +174,44 @@ __device__ void sph_bessel_row(int L, double x, double b, double* out, size_t st
     for (int l = 0; l <= L; ++l) out[l * stride] *= scale;
 }
 
+// Coefficients of the normalised associated Legendre recurrences, per (l, m) with m <= l:
+//   cf[(l (l + 1)) / 2 + m] = (a_lm, b_lm), a = sqrt((4l^2 - 1)/(l^2 - m^2)),
+//   b = sqrt(((l-1)^2 - m^2)/(4 (l-1)^2 - 1)) (l >= m + 2); the seeds per m:
+//   sd[m] = (-sqrt((2m + 1)/(2m)), sqrt(2m + 3)).
+__global__ void ylm_coeff_kernel(int L, double2* cf, double2* sd) {
+    const int n = (L + 1) * (L + 2) / 2;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int l = 0;
+        while ((l + 1) * (l + 2) / 2 <= i) ++l;
+        const int m = i - l * (l + 1) / 2;
+        double a = 0, bb = 0;
+        if (l >= m + 2) {
+            a = sqrt((4.0 * l * l - 1) / ((double)l * l - (double)m * m));
+            bb = sqrt((((double)l - 1) * (l - 1) - (double)m * m) / (4.0 * (l - 1) * (l - 1) - 1));
+        }
+        cf[i] = make_double2(a, bb);
+        if (l == m) sd[m] = make_double2(m > 0 ? -sqrt((2.0 * m + 1) / (2.0 * m)) : 0.0, sqrt(2.0 * m + 3));
+    }
+}
+
 // conj(Y_l^m(theta, phi)) for the requested moments (idx[l (2L+1) + L + m] -> moment, or -1)
 // written to out[k * stride]; m outer, l inner, so the Legendre recurrence carries two values.
-__device__ void conj_ylm_row(int L, double theta, double phi, const int* __restrict__ idx, double2* out,
-                             size_t stride) {
+// e^{i m phi} by rotation (m multiplications of e^{i phi}).
+__device__ void conj_ylm_row(int L, double theta, double phi, const int* __restrict__ idx, const double2* cf,
+                             const double2* sd, double2* out, size_t stride) {
     const double x = cos(theta), s = sqrt((1 - x) * (1 + x));
     double pmm = sqrt(1.0 / (4 * 3.14159265358979323846));
     const int W = 2 * L + 1;
+    double s1, c1;
+    sincos(phi, &s1, &c1);
+    double cm = 1.0, sm = 0.0;
     for (int m = 0; m <= L; ++m) {
-        if (m > 0) pmm = -sqrt((2.0 * m + 1) / (2.0 * m)) * s * pmm;
-        double sm, cm;
-        sincos(m * phi, &sm, &cm);
+        if (m > 0) {
+            pmm = sd[m].x * s * pmm;
+            const double cn = cm * c1 - sm * s1;
+            sm = sm * c1 + cm * s1;
+            cm = cn;
+        }
         auto emit = [&](int l, double P) {
             const int kp = idx[l * W + L + m];
             if (kp >= 0) out[kp * stride] = make_double2(P * cm, -P * sm);
@@ -193,12 +223,11 @@ __device__ void conj_ylm_row(int L, double theta, double phi, const int* __restr
         };
         emit(m, pmm);
         if (m < L) {
-            double p2 = pmm, p1 = sqrt(2.0 * m + 3) * x * pmm;
+            double p2 = pmm, p1 = sd[m].y * x * pmm;
             emit(m + 1, p1);
             for (int l = m + 2; l <= L; ++l) {
-                const double a = sqrt((4.0 * l * l - 1) / ((double)l * l - (double)m * m));
-                const double bb = sqrt((((double)l - 1) * (l - 1) - (double)m * m) / (4.0 * (l - 1) * (l - 1) - 1));
-                const double p = a * (x * p1 - bb * p2);
+                const double2 ab = cf[l * (l + 1) / 2 + m];
+                const double p = ab.x * (x * p1 - ab.y * p2);
                 emit(l, p);
                 p2 = p1;
                 p1 = p;
@@ -214,8 +243,9 @@ __device__ void bessel01_asymptotic(double x, double& j0, double& j1) {
     for (int nu = 0; nu < 2; ++nu) {
         const double mu = 4.0 * nu * nu;
         double a = 1, P = 1, Q = 0;
+        const double i8x = 1.0 / (8.0 * x);
         for (int k = 1; k < 60; ++k) {
-            const double next = a * (mu - (2.0 * k - 1) * (2.0 * k - 1)) / (k * 8.0 * x);
+            const double next = a * (mu - (2.0 * k - 1) * (2.0 * k - 1)) * i8x / k;
             if (fabs(next) > fabs(a) && k > 2) break;
             a = next;
             if (k & 1) Q += (((k - 1) / 2) & 1 ? -a : a);
@@ -250,8 +280,9 @@ __device__ void cyl_bessel_row(int N, double x, double* out, int stride) {
         out[0] = j0;
         if (N >= 1) out[stride] = j1;
         double jm = j0, jc = j1;
+        const double ix2 = 2.0 / x;
         for (int n = 1; n < N; ++n) {
-            const double jn = 2.0 * n / x * jc - jm;
+            const double jn = n * ix2 * jc - jm;
             out[(n + 1) * stride] = jn;
             jm = jc;
             jc = jn;
@@ -261,9 +292,10 @@ __device__ void cyl_bessel_row(int N, double x, double* out, int stride) {
     const double top = fmax((double)N, x);
     int M = (int)(top + 20 + 2 * sqrt(top + 10));
     M += M & 1;
+    const double ix2 = 2.0 / x;
     double fp = 0, f = 1e-250, norm = 0;
     for (int n = M; n >= 1; --n) {
-        const double fm = 2.0 * n / x * f - fp;
+        const double fm = n * ix2 * f - fp;
         fp = f;
         f = fm;
         if (n - 1 <= N) out[(n - 1) * stride] = f;
@@ -275,7 +307,8 @@ __device__ void cyl_bessel_row(int N, double x, double* out, int stride) {
             norm *= 1e-200;
         }
     }
-    for (int n = 0; n <= N; ++n) out[n * stride] /= norm;
+    const double inorm = 1.0 / norm;
+    for (int n = 0; n <= N; ++n) out[n * stride] *= inorm;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -287,23 +320,41 @@ struct MpSphereBasis {
     const double* cf;   // [nq][nclass]
     const double* qlen; // [nq]
     const int* idx;     // [(L+1)(2L+1)]
+    const double2* ycf; // Legendre coefficients [(L+1)(L+2)/2] and seeds [L+1] (ylm_coeff_kernel)
+    const double2* ysd;
     double* Jb;         // [nfb][nq][L+1][na_pad]  b_j(q) j_l(|q| r_j)
     double2* Yc;        // [nfb][nmom][na_pad]     conj(Y_l^m(j))
     int na_pad, nclass, nq, L, nmom, f0, nfb;
 };
 
-__global__ void __launch_bounds__(128) mp_sphere_basis_kernel(MpSphereBasis a) {
+// conj(Y_l^m) of every (frame, atom) of the batch; the coefficient tables live in shared memory.
+__global__ void __launch_bounds__(128) mp_ylm_kernel(MpSphereBasis a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    double2* cf = reinterpret_cast<double2*>(smem);
+    const int ncf = (a.L + 1) * (a.L + 2) / 2;
+    double2* sd = cf + ncf;
+    for (int i = threadIdx.x; i < ncf; i += blockDim.x) cf[i] = a.ycf[i];
+    for (int i = threadIdx.x; i <= a.L; i += blockDim.x) sd[i] = a.ysd[i];
+    __syncthreads();
     const size_t n = (size_t)a.nfb * a.na_pad;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const int fl = (int)(i / a.na_pad), j = (int)(i - (size_t)fl * a.na_pad);
         const float4 c = a.sph[(size_t)(a.f0 + fl) * a.na_pad + j];
-        conj_ylm_row(a.L, (double)c.z, (double)c.y, a.idx, a.Yc + (size_t)fl * a.nmom * a.na_pad + j, a.na_pad);
+        conj_ylm_row(a.L, (double)c.z, (double)c.y, a.idx, cf, sd, a.Yc + (size_t)fl * a.nmom * a.na_pad + j,
+                     a.na_pad);
+    }
+}
+
+// b_j(q) j_l(|q| r_j) of every (frame, q, atom) of the batch.
+__global__ void __launch_bounds__(128) mp_jl_kernel(MpSphereBasis a) {
+    const size_t n = (size_t)a.nfb * a.nq * a.na_pad;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t fq = i / a.na_pad;
+        const int j = (int)(i - fq * a.na_pad), fl = (int)(fq / a.nq), q = (int)(fq - (size_t)fl * a.nq);
+        const float4 c = a.sph[(size_t)(a.f0 + fl) * a.na_pad + j];
         const int cl = a.cls[j];
-        for (int q = 0; q < a.nq; ++q) {
-            const double b = cl >= 0 ? a.cf[(size_t)q * a.nclass + cl] : 0.0;
-            sph_bessel_row(a.L, a.qlen[q] * (double)c.x, b,
-                           a.Jb + ((size_t)(fl * a.nq + q) * (a.L + 1)) * a.na_pad + j, a.na_pad);
-        }
+        const double b = cl >= 0 ? a.cf[(size_t)q * a.nclass + cl] : 0.0;
+        sph_bessel_row(a.L, a.qlen[q] * (double)c.x, b, a.Jb + (fq * (a.L + 1)) * a.na_pad + j, a.na_pad);
     }
 }
 
@@ -655,9 +706,19 @@ extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const d
     }
     const double* d_cf = reinterpret_cast<const double*>(dptr(o_cf));
     if (!cyl) {
-        // frame batches sized to about 1 GB of basis
+        // frame batches: basis of up to a quarter of the free memory (at most 16 GB), so that
+        // one contraction launch has thousands of CTAs
+        size_t free_b = 0, total_b = 0;
+        MCK(cudaMemGetInfo(&free_b, &total_b));
+        const size_t budget = std::max<size_t>((size_t)1 << 28, std::min<size_t>((size_t)16 << 30, free_b / 4));
         const size_t per_frame = na_pad * (nq * (L + 1) * sizeof(double) + nmom * sizeof(double2));
-        const size_t nfb = std::max<size_t>(1, std::min<size_t>(nf, ((size_t)1 << 30) / per_frame));
+        const size_t nfb = std::max<size_t>(1, std::min<size_t>(nf, budget / per_frame));
+        const int ncf = (L + 1) * (L + 2) / 2;
+        MCK(p->mp_ycf.ensure((size_t)(ncf + L + 1) * sizeof(double2)));
+        ylm_coeff_kernel<<<(ncf + 127) / 128, 128, 0, st>>>(L, p->mp_ycf.as<double2>(), p->mp_ycf.as<double2>() + ncf);
+        MCK(cudaGetLastError());
+        ++launches;
+        const size_t ysm = (size_t)(ncf + L + 1) * sizeof(double2);
         MCK(p->mp_Jb.ensure(nfb * nq * (L + 1) * na_pad * sizeof(double)));
         MCK(p->mp_Yc.ensure(nfb * nmom * na_pad * sizeof(double2)));
         int maxcnt = 0;
@@ -675,6 +736,8 @@ extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const d
             ba.cf = d_cf;
             ba.qlen = reinterpret_cast<const double*>(dptr(o_qin));
             ba.idx = reinterpret_cast<const int*>(dptr(o_idx));
+            ba.ycf = p->mp_ycf.as<double2>();
+            ba.ysd = p->mp_ycf.as<double2>() + ncf;
             ba.Jb = p->mp_Jb.as<double>();
             ba.Yc = p->mp_Yc.as<double2>();
             ba.na_pad = (int)na_pad;
@@ -684,9 +747,12 @@ extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const d
             ba.nmom = (int)nmom;
             ba.f0 = (int)f0;
             ba.nfb = nb;
-            const size_t nthreads = (size_t)nb * na_pad;
-            mp_sphere_basis_kernel<<<(unsigned)std::min<size_t>((nthreads + 127) / 128, 152 * 64), 128, 0, st>>>(ba);
+            const size_t ny = (size_t)nb * na_pad, nj = ny * nq;
+            mp_ylm_kernel<<<(unsigned)std::min<size_t>((ny + 127) / 128, 152 * 64), 128, ysm, st>>>(ba);
             MCK(cudaGetLastError());
+            mp_jl_kernel<<<(unsigned)std::min<size_t>((nj + 127) / 128, 152 * 64), 128, 0, st>>>(ba);
+            MCK(cudaGetLastError());
+            ++launches;
             MpSphereContract ca{};
             ca.Jb = p->mp_Jb.as<double>();
             ca.Yc = p->mp_Yc.as<double2>();
