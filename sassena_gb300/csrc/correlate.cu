@@ -1118,20 +1118,25 @@ __device__ __forceinline__ int brev_bits(int x, int bits) {
     return bits ? (int)(__brev((unsigned)x) >> (32 - bits)) : 0;
 }
 
-template <class T>
+__device__ __forceinline__ float2 as_t2(float2 x, float2) { return x; }
+__device__ __forceinline__ double2 as_t2(float2 x, double2) { return make_double2(x.x, x.y); }
+__device__ __forceinline__ double2 as_t2(double2 x, double2) { return x; }
+__device__ __forceinline__ float2 as_t2(double2 x, float2) { return make_float2((float)x.x, (float)x.y); }
+
+template <class T, class AT2>
 __global__ void __launch_bounds__(kLongNT) long_col_kernel(LongArgs a) {
     typedef typename cplx<T>::type T2;
     extern __shared__ __align__(16) unsigned char smem[];
     T2* buf = reinterpret_cast<T2*>(smem);  // [kLongTile][R]
     const int r = a.lg - kLongRowLg, R = 1 << r, half = R >> 1, L = 1 << a.lg;
     const int n2base = blockIdx.x * kLongTile;
-    const T2* A = reinterpret_cast<const T2*>(a.A) + (size_t)blockIdx.y * a.nf;
+    const AT2* A = reinterpret_cast<const AT2*>(a.A) + (size_t)blockIdx.y * a.nf;
     const T2* tw = reinterpret_cast<const T2*>(a.tw);
     // first stage folded into the load: x[C n1 + n2] = 0 for n1 >= R/2 (C R / 2 = L / 2 >= nf)
     for (int idx = threadIdx.x; idx < kLongTile * half; idx += kLongNT) {
         const int c = idx % kLongTile, n1 = idx / kLongTile;
         const int t = kLongC * n1 + n2base + c;
-        const T2 x = t < a.nf ? A[t] : zero2<T2>();
+        const T2 x = t < a.nf ? as_t2(A[t], T2()) : zero2<T2>();
         buf[c * R + n1] = x;
         buf[c * R + n1 + half] = cmul(x, tw[n1 << kLongRowLg]);  // W_R^n1 = W_L^{n1 C}
     }
@@ -1337,15 +1342,11 @@ cudaError_t launch_long_columns(const LongArgs& a, cudaStream_t st) {
     if (a.nseries == 0) return cudaSuccess;
     const size_t sm = long_col_smem(a.precision, a.lg);
     dim3 grid(kLongC / kLongTile, (unsigned)a.nseries);
-    if (a.precision == PREC_FP32) {
-        cudaError_t e = set_smem(long_col_kernel<float>, sm);
-        if (e != cudaSuccess) return e;
-        long_col_kernel<float><<<grid, kLongNT, sm, st>>>(a);
-    } else {
-        cudaError_t e = set_smem(long_col_kernel<double>, sm);
-        if (e != cudaSuccess) return e;
-        long_col_kernel<double><<<grid, kLongNT, sm, st>>>(a);
-    }
+    auto k = a.precision == PREC_FP32 ? (a.amp_f32 ? long_col_kernel<float, float2> : long_col_kernel<float, double2>)
+                                      : (a.amp_f32 ? long_col_kernel<double, float2> : long_col_kernel<double, double2>);
+    cudaError_t e = set_smem(k, sm);
+    if (e != cudaSuccess) return e;
+    k<<<grid, kLongNT, sm, st>>>(a);
     return cudaGetLastError();
 }
 

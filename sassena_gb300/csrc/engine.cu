@@ -680,9 +680,10 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
         const WorkItem& it = items[i];
         SystemState& s = *it.sys;
         const size_t L = (size_t)1 << s.lg, R = L >> kLongRowLg, nq = it.offs.size() - 1;
-        const size_t esz = f32 ? sizeof(float2) : sizeof(double2);
+        const size_t esz = sizeof(double2);  // FP64 transforms (see enqueue)
+        const size_t gsz = f32 ? sizeof(float2) : sizeof(double2);
         // incoherent: the (atom, direction) series are generated per batch next to Y
-        const size_t S = std::max<size_t>(1, kLongScratchBytes / ((L + (coherent ? 0 : s.nf)) * esz));
+        const size_t S = std::max<size_t>(1, kLongScratchBytes / (L * esz + (coherent ? 0 : s.nf * gsz)));
         LongItem li{};
         li.item = (int)i;
         li.lg = s.lg;
@@ -740,7 +741,7 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
                         ic[cb].shell, coherent ? 0 : ic[cb].v_begin - (int)shell_first[ic[cb].shell]};
             long_batches_.push_back(b);
             ybytes = std::max(ybytes, (size_t)(b.v1 - b.v0) * L * esz);
-            if (!coherent) gbytes = std::max(gbytes, (size_t)(b.v1 - b.v0) * s.nf * esz);
+            if (!coherent) gbytes = std::max(gbytes, (size_t)(b.v1 - b.v0) * s.nf * gsz);
             cb = ce;
         }
         lchunks.insert(lchunks.end(), ic.begin(), ic.end());
@@ -888,8 +889,11 @@ int Engine::enqueue(cudaStream_t st, std::string& err, cudaEvent_t* ev) {
         const size_t esz = f32 ? sizeof(float2) : sizeof(double2);
         for (int b = li.batch_begin; b < li.batch_end; ++b) {
             const LongBatch& lb = long_batches_[b];
+            // the transforms run in FP64 in both forms: the 1/(NF - tau) normalisation
+            // amplifies transform rounding at large lags in proportion to NF
             LongArgs la{};
-            la.precision = cfg_.precision;
+            la.precision = PREC_FP64;
+            la.amp_f32 = f32;
             la.lg = s.lg;
             la.nf = (int)s.nf;
             if (coherent) {
@@ -912,11 +916,11 @@ int Engine::enqueue(cudaStream_t st, std::string& err, cudaEvent_t* ev) {
             }
             la.Y = long_Y_.p;
             la.nseries = lb.v1 - lb.v0;
-            la.tw = f32 ? s.tw32.p : s.tw64.p;
+            la.tw = s.tw64.p;
             la.chunks = d_long_chunks_ + lb.chunk_begin;
             la.nchunks = lb.chunk_end - lb.chunk_begin;
             la.v0 = lb.v0;
-            la.kbr = f32 ? s.k32.p : s.k64.p;
+            la.kbr = s.k64.p;
             la.ppart = ppart_.as<double>();
             la.mpart = long_mpart_.as<double2>() + li.mpart_off;
             ECK(launch_long_columns(la, st));

@@ -214,8 +214,9 @@ constexpr int kLongRowLg = 12;
 constexpr int kLongLgMax = 20;
 
 struct LongArgs {
-    int precision, lg, nf;
-    const void* A;             // series [nseries][nf] (T2): the batch's first series
+    int precision, lg, nf;     // precision of the transforms (Y, twiddles, K)
+    int amp_f32;               // the series are float2 (else double2)
+    const void* A;             // series [nseries][nf]: the batch's first series
     void* Y;                   // [nseries][L] T2 scratch (column-pass output)
     int nseries;
     const void* tw;            // W_L^j for j < L/2 (T2 of the precision)

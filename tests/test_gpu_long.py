@@ -29,9 +29,9 @@ def check(w, precision, method="fftw", tol=None):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
-@pytest.mark.parametrize("nf", [4097, 5000, 9000])
+@pytest.mark.parametrize("nf", [4097, 5000, 9000, 30000])
 def test_coherent_long_autocorrelation(native_lib, precision, nf):
-    # padded lengths 2^14, 2^14, 2^15: R = 4, 4, 8 rows of 4,096
+    # padded lengths 2^14, 2^14, 2^15, 2^16: R = 4, 4, 8, 16 rows of 4,096
     w = synth.small("all", "autocorrelate", seed=71, na=23, nf=nf, nq=2, nm=3, box=10.0)
     check(w, precision)
 
