@@ -45,7 +45,7 @@ namespace sassgpu {
 namespace {
 
 constexpr int kMpMaxL = 40;  // largest major moment (sphere) / half order (cylinder)
-constexpr int kMpTileAtoms = 32, kMpCylAtoms = 64, kMpCylThreads = 64;
+constexpr int kMpTileAtoms = 32;
 
 // ---------------------------------------------------------------------------------------
 // coordinate representations
@@ -445,93 +445,102 @@ struct MpCylinder {
     int na_pad, na, nclass, nq, N, nmom, nf;
 };
 
-__global__ void __launch_bounds__(kMpCylThreads) mp_cylinder_kernel(MpCylinder a) {
+// One CTA per (frame, block of kCylQB q-vectors), kCylThreads threads, tiles of kCylTA atoms.
+// Per tile, threads [0, QB TA) evaluate one (q, atom) pair each: the Bessel row J_n(q_r r) and
+// X = b e^{i s z q_z}; threads [QB TA, QB TA + TA) evaluate cos(n phi), sin(n phi) of one atom
+// (shared by the block's q-vectors). Then every thread owns (q, order, cos|sin) sums.
+constexpr int kCylQB = 3, kCylTA = 32, kCylThreads = 128;
+static_assert(kCylQB * kCylTA + kCylTA <= kCylThreads, "tile roles exceed the CTA");
+
+__global__ void __launch_bounds__(kCylThreads) mp_cylinder_kernel(MpCylinder a) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const int q = blockIdx.x, f = blockIdx.y, N = a.N, W = N + 1;
-    double* Jn = reinterpret_cast<double*>(smem);        // [W][TA]
-    double* cn = Jn + (size_t)W * kMpCylAtoms;            // [W][TA] cos(n phi)
-    double* sn = cn + (size_t)W * kMpCylAtoms;            // [W][TA] sin(n phi)
-    double2* X = reinterpret_cast<double2*>(sn + (size_t)W * kMpCylAtoms);  // [TA]
-    double2* Sc = X + kMpCylAtoms;                         // [W] after the atom loop
-    double2* Ss = Sc + W;
-    const double qr = a.qcyl[3 * q], qphi = a.qcyl[3 * q + 1], qz = a.qcyl[3 * q + 2];
-    // this thread's orders: n = threadIdx.x + 64 k
-    constexpr int NPT = (2 * kMpMaxL + 1 + kMpCylThreads - 1) / kMpCylThreads;
-    double2 ac[NPT], as[NPT];
+    const int f = blockIdx.y, q0 = blockIdx.x * kCylQB, nqb = min(kCylQB, a.nq - q0);
+    const int N = a.N, W = N + 1, ntask = nqb * 2 * W;
+    double* Jn = reinterpret_cast<double*>(smem);                         // [QB][W][TA]
+    double* cn = Jn + (size_t)kCylQB * W * kCylTA;                          // [W][TA]
+    double* sn = cn + (size_t)W * kCylTA;                                   // [W][TA]
+    double2* X = reinterpret_cast<double2*>(sn + (size_t)W * kCylTA);      // [QB][TA]
+    constexpr int NPT = (kCylQB * 2 * (2 * kMpMaxL + 1) + kCylThreads - 1) / kCylThreads;
+    double2 acc[NPT];
 #pragma unroll
-    for (int k = 0; k < NPT; ++k) ac[k] = as[k] = make_double2(0.0, 0.0);
+    for (int k = 0; k < NPT; ++k) acc[k] = make_double2(0.0, 0.0);
     const float4* row = a.cyl + (size_t)f * a.na_pad;
-    for (int j0 = 0; j0 < a.na; j0 += kMpCylAtoms) {
+    const int tid = threadIdx.x;
+    for (int j0 = 0; j0 < a.na; j0 += kCylTA) {
         __syncthreads();
-        {
-            const int jj = threadIdx.x, j = j0 + jj;
-            if (j < a.na) {
+        if (tid < kCylQB * kCylTA) {
+            const int qq = tid / kCylTA, jj = tid - qq * kCylTA, j = j0 + jj;
+            double* jrow = Jn + (size_t)qq * W * kCylTA + jj;
+            if (qq < nqb && j < a.na) {
+                const int q = q0 + qq;
+                const double qr = a.qcyl[3 * q], qz = a.qcyl[3 * q + 2];
                 const float4 c = row[j];
-                const double r = c.x, phi = c.y, z = c.z;
+                const double r = c.x, z = c.z;
                 const int cl = a.cls[j];
                 const double b = cl >= 0 ? a.cf[(size_t)q * a.nclass + cl] : 0.0;
                 double sgn = 1.0;  // parallel_sign, multipole_scatter_device.cpp:944-948
                 if (z != 0 && qz != 0) sgn = (z * qz) / (fabs(z) * fabs(qz));
                 double es, ec;
                 sincos(sgn * z * qz, &es, &ec);
-                X[jj] = make_double2(b * ec, b * es);
-                cyl_bessel_row(N, r * qr, Jn + jj, kMpCylAtoms);
-                double s1, c1;
-                sincos(phi, &s1, &c1);
-                double cp = 1, sp = 0;  // cos, sin of n phi by rotation
-                for (int n = 0; n <= N; ++n) {
-                    cn[n * kMpCylAtoms + jj] = cp;
-                    sn[n * kMpCylAtoms + jj] = sp;
-                    const double cq = cp * c1 - sp * s1;
-                    sp = sp * c1 + cp * s1;
-                    cp = cq;
-                }
+                X[qq * kCylTA + jj] = make_double2(b * ec, b * es);
+                cyl_bessel_row(N, r * qr, jrow, kCylTA);
             } else {
-                X[jj] = make_double2(0.0, 0.0);
-                for (int n = 0; n <= N; ++n) Jn[n * kMpCylAtoms + jj] = cn[n * kMpCylAtoms + jj] = sn[n * kMpCylAtoms + jj] = 0;
+                X[qq * kCylTA + jj] = make_double2(0.0, 0.0);
+                for (int n = 0; n <= N; ++n) jrow[n * kCylTA] = 0;
+            }
+        } else if (tid < kCylQB * kCylTA + kCylTA) {
+            const int jj = tid - kCylQB * kCylTA, j = j0 + jj;
+            double cp = 1, sp = 0, s1 = 0, c1 = 1;  // cos, sin of n phi by rotation
+            if (j < a.na) sincos((double)row[j].y, &s1, &c1);
+            for (int n = 0; n <= N; ++n) {
+                cn[n * kCylTA + jj] = cp;
+                sn[n * kCylTA + jj] = sp;
+                const double cq = cp * c1 - sp * s1;
+                sp = sp * c1 + cp * s1;
+                cp = cq;
             }
         }
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < NPT; ++k) {
-            const int n = threadIdx.x + k * kMpCylThreads;
-            if (n <= N) {
-                double2 sc = ac[k], ss = as[k];
-                for (int jj = 0; jj < kMpCylAtoms; ++jj) {
-                    const double2 x = X[jj];
-                    const double jv = Jn[n * kMpCylAtoms + jj];
-                    const double wc = jv * cn[n * kMpCylAtoms + jj], ws = jv * sn[n * kMpCylAtoms + jj];
-                    sc.x = fma(x.x, wc, sc.x);
-                    sc.y = fma(x.y, wc, sc.y);
-                    ss.x = fma(x.x, ws, ss.x);
-                    ss.y = fma(x.y, ws, ss.y);
+            const int t = tid + k * kCylThreads;
+            if (t < ntask) {
+                const int qq = t / (2 * W), rem = t - qq * 2 * W, n = rem >> 1;
+                const double* jv = Jn + ((size_t)qq * W + n) * kCylTA;
+                const double* tr = ((rem & 1) ? sn : cn) + (size_t)n * kCylTA;
+                const double2* x = X + qq * kCylTA;
+                double2 sacc = acc[k];
+                for (int jj = 0; jj < kCylTA; ++jj) {
+                    const double w = jv[jj] * tr[jj];
+                    sacc.x = fma(x[jj].x, w, sacc.x);
+                    sacc.y = fma(x[jj].y, w, sacc.y);
                 }
-                ac[k] = sc;
-                as[k] = ss;
+                acc[k] = sacc;
             }
         }
     }
     __syncthreads();
+    double2* Sv = reinterpret_cast<double2*>(smem);  // [QB][W][cos, sin]
 #pragma unroll
     for (int k = 0; k < NPT; ++k) {
-        const int n = threadIdx.x + k * kMpCylThreads;
-        if (n <= N) {
-            Sc[n] = ac[k];
-            Ss[n] = as[k];
-        }
+        const int t = tid + k * kCylThreads;
+        if (t < ntask) Sv[t] = acc[k];
     }
     __syncthreads();
     const double norm = sqrt(2 * 3.14159265358979323846), h = 0.70710678118654752440;
-    for (int k = threadIdx.x; k < a.nmom; k += kMpCylThreads) {
+    for (int idx = tid; idx < nqb * a.nmom; idx += kCylThreads) {
+        const int qq = idx / a.nmom, k = idx - qq * a.nmom, q = q0 + qq;
+        const double qphi = a.qcyl[3 * q + 1];
+        const double2* S2 = Sv + (size_t)qq * 2 * W;
         const int l = a.mom[2 * k], m = a.mom[2 * k + 1];
         double2 v;
         if (l == 0 && m == 0) {
-            v = Sc[0];
+            v = S2[0];
         } else {
             const int n = m < 2 ? 2 * l : 2 * l - 1;
             double snq, cnq;
             sincos(n * qphi, &snq, &cnq);
-            const double2 C = Sc[n], S = Ss[n];
+            const double2 C = S2[2 * n], S = S2[2 * n + 1];
             double2 t;  // sum_j X_j J_n cos / sin (n (phi_j - phi_q))
             if (m == 0 || m == 2) t = make_double2(cnq * C.x + snq * S.x, cnq * C.y + snq * S.y);
             else t = make_double2(cnq * S.x - snq * C.x, cnq * S.y - snq * C.y);
@@ -549,7 +558,8 @@ __global__ void __launch_bounds__(kMpCylThreads) mp_cylinder_kernel(MpCylinder a
 
 size_t cylinder_smem(int N) {
     const size_t W = (size_t)N + 1;
-    return 3 * W * kMpCylAtoms * sizeof(double) + kMpCylAtoms * sizeof(double2) + 2 * W * sizeof(double2);
+    const size_t tiles = (size_t)(kCylQB + 2) * W * kCylTA * sizeof(double) + (size_t)kCylQB * kCylTA * sizeof(double2);
+    return std::max(tiles, (size_t)kCylQB * 2 * W * sizeof(double2));
 }
 
 // ---------------------------------------------------------------------------------------
@@ -790,7 +800,7 @@ extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const d
         ca.nf = (int)nf;
         const size_t sm = cylinder_smem(2 * L);
         if (sm > 48 * 1024) MCK(cudaFuncSetAttribute(mp_cylinder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        mp_cylinder_kernel<<<dim3((unsigned)nq, (unsigned)nf), kMpCylThreads, sm, st>>>(ca);
+        mp_cylinder_kernel<<<dim3((unsigned)((nq + kCylQB - 1) / kCylQB), (unsigned)nf), kCylThreads, sm, st>>>(ca);
         MCK(cudaGetLastError());
         ++launches;
     }
