@@ -65,3 +65,22 @@ def test_plan_autotune(native_lib):
         # q_per_lane 0: the automatic tile shape won (or the recurrence covers every shell)
         assert shape["q_per_lane"] in (0, 1, 2, 4, 8)
     assert rel_err_sqt(fqt, r[0]).max() <= 1e-3
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("scattering", ["all", "self"])
+def test_batch_mixes_long_and_short_series(native_lib, precision, scattering):
+    # one captured launch sequence with a long system (four-step transform through HBM,
+    # NF > 4096) next to short ones (shared-memory transforms)
+    ws = [synth.small(scattering, "autocorrelate", seed=81, na=9, nf=4500, nq=2, nm=3, box=10.0),
+          synth.small(scattering, "autocorrelate", seed=82, na=31, nf=40, nq=3, nm=5),
+          synth.small(scattering, "autocorrelate", seed=83, na=12, nf=9000, nq=1, nm=2, box=10.0)]
+    refs = [ref(w) for w in ws]
+    with abi.Batch(ws, precision=precision) as b:
+        for replay in range(2):
+            b.run()
+            b.sync()
+            for i, r in enumerate(refs):
+                fqt, fq, fq2 = b.results(i)
+                assert rel_err_sqt(fqt, r[0]).max() <= TOL[precision]
+                assert rel_err_vec(fq, cplx(r[1])) <= TOL[precision]
