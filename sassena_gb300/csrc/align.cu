@@ -31,7 +31,8 @@
 namespace sassgpu {
 namespace {
 
-constexpr int kPerFrameThreads = 32;
+constexpr int kPerFrameThreads = 32;   // one thread per frame (small per-frame kernels)
+constexpr int kWarpFrameThreads = 128; // one warp per frame (sums over atom lists)
 
 __global__ void pp_promote_kernel(const float* __restrict__ in, size_t n, double* __restrict__ out) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -39,28 +40,43 @@ __global__ void pp_promote_kernel(const float* __restrict__ in, size_t n, double
 }
 
 // com[f] = sum_i m_i r_i / sum_i m_i over the list, r_i = base[f * stride + 3 idx[i]]
-// (idx NULL: i), summed in list order without fused multiply-adds.
+// (idx NULL: i), summed in list order without fused multiply-adds. One warp per frame: the
+// lanes load 32 list entries at a time (coalesced) and form the products m_i r_i; the sums
+// then run through the entries in order (broadcast by shuffles), so every partial sum is the
+// reference's.
 __global__ void pp_com_kernel(const double* __restrict__ base, size_t stride, const size_t* __restrict__ idx,
                               const double* __restrict__ mass, size_t n, int nf, double* __restrict__ com) {
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    const int f = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
     if (f >= nf) return;
     const double* fr = base + (size_t)f * stride;
     double m = 0.0, x = 0.0, y = 0.0, z = 0.0;
-    for (size_t i = 0; i < n; ++i) {
-        const size_t j = idx ? idx[i] : i;
-        const double mi = mass[i];
-        m = __dadd_rn(m, mi);
-        x = __dadd_rn(x, __dmul_rn(fr[3 * j], mi));
-        y = __dadd_rn(y, __dmul_rn(fr[3 * j + 1], mi));
-        z = __dadd_rn(z, __dmul_rn(fr[3 * j + 2], mi));
+    for (size_t i0 = 0; i0 < n; i0 += 32) {
+        const size_t i = i0 + lane;
+        double mi = 0.0, px = 0.0, py = 0.0, pz = 0.0;
+        if (i < n) {
+            const size_t j = idx ? idx[i] : i;
+            mi = mass[i];
+            px = __dmul_rn(fr[3 * j], mi);
+            py = __dmul_rn(fr[3 * j + 1], mi);
+            pz = __dmul_rn(fr[3 * j + 2], mi);
+        }
+        const int cnt = (int)min((size_t)32, n - i0);
+        for (int k = 0; k < cnt; ++k) {
+            m = __dadd_rn(m, __shfl_sync(0xffffffffu, mi, k));
+            x = __dadd_rn(x, __shfl_sync(0xffffffffu, px, k));
+            y = __dadd_rn(y, __shfl_sync(0xffffffffu, py, k));
+            z = __dadd_rn(z, __shfl_sync(0xffffffffu, pz, k));
+        }
     }
-    double* o = com + 3 * (size_t)f;
-    if (n == 0) {
-        o[0] = o[1] = o[2] = 0.0;
-    } else {
-        o[0] = __ddiv_rn(x, m);
-        o[1] = __ddiv_rn(y, m);
-        o[2] = __ddiv_rn(z, m);
+    if (lane == 0) {
+        double* o = com + 3 * (size_t)f;
+        if (n == 0) {
+            o[0] = o[1] = o[2] = 0.0;
+        } else {
+            o[0] = __ddiv_rn(x, m);
+            o[1] = __ddiv_rn(y, m);
+            o[2] = __ddiv_rn(z, m);
+        }
     }
 }
 
@@ -116,28 +132,38 @@ __global__ void pp_gather_kernel(const double* __restrict__ W, size_t nsys, cons
 }
 
 // K[f] = sum_i m_i (u_i v_i^T), u_i = R_i - ref, v_i = C[f][i] - pos[f] (center_of_mass.cpp:79-98),
-// R_i = reference[i] or (NULL) C[f][i]; each element m_i * (u_r * v_c), summed in order.
+// R_i = reference[i] or (NULL) C[f][i]; each element m_i * (u_r * v_c), summed in order. One warp
+// per frame as in pp_com_kernel: lanes form the nine products of 32 entries, the sums run in order.
 __global__ void pp_kmat_kernel(const double* __restrict__ C, const double* __restrict__ ref_xyz,
                                const double* __restrict__ mass, size_t n, int nf, const double* __restrict__ pos,
                                const double* __restrict__ ref, int ref_one, double* __restrict__ K) {
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    const int f = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
     if (f >= nf) return;
     const double* cf = C + (size_t)f * n * 3;
     const double* rr = ref_xyz ? ref_xyz : cf;
     const double* pf = pos + 3 * f;
     const double* qf = ref + 3 * (ref_one ? 0 : f);
     double k[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (size_t i = 0; i < n; ++i) {
-        const double mi = mass[i];
-        double u[3], v[3];
-        for (int d = 0; d < 3; ++d) {
-            v[d] = __dsub_rn(cf[3 * i + d], pf[d]);
-            u[d] = __dsub_rn(rr[3 * i + d], qf[d]);
+    for (size_t i0 = 0; i0 < n; i0 += 32) {
+        const size_t i = i0 + lane;
+        double t[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        if (i < n) {
+            const double mi = mass[i];
+            double u[3], v[3];
+            for (int d = 0; d < 3; ++d) {
+                v[d] = __dsub_rn(cf[3 * i + d], pf[d]);
+                u[d] = __dsub_rn(rr[3 * i + d], qf[d]);
+            }
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) t[3 * r + c] = __dmul_rn(mi, __dmul_rn(u[r], v[c]));
         }
-        for (int r = 0; r < 3; ++r)
-            for (int c = 0; c < 3; ++c) k[3 * r + c] = __dadd_rn(k[3 * r + c], __dmul_rn(mi, __dmul_rn(u[r], v[c])));
+        const int cnt = (int)min((size_t)32, n - i0);
+        for (int s = 0; s < cnt; ++s)
+#pragma unroll
+            for (int e = 0; e < 9; ++e) k[e] = __dadd_rn(k[e], __shfl_sync(0xffffffffu, t[e], s));
     }
-    for (int e = 0; e < 9; ++e) K[9 * (size_t)f + e] = k[e];
+    if (lane == 0)
+        for (int e = 0; e < 9; ++e) K[9 * (size_t)f + e] = k[e];
 }
 
 // C[f][i] = R[f] (C[f][i] - pos[f]) + ref (center_of_mass.cpp:114-128; ublas prod order).
@@ -391,6 +417,7 @@ extern "C" int sass_stage_frames_prepass(sass_plan* p, const float* frames, size
     double* C = p->pp_C.as<double>();
     const int nfi = (int)nf;
     const unsigned gf = (unsigned)((nf + kPerFrameThreads - 1) / kPerFrameThreads);
+    const unsigned gw = (unsigned)((nf * 32 + kWarpFrameThreads - 1) / kWarpFrameThreads);  // warp per frame
     auto L = [&](size_t off) { return reinterpret_cast<const size_t*>(dl + off); };
     auto D = [&](size_t off) { return reinterpret_cast<const double*>(dl + off); };
     std::vector<double> hK(nf * 9), hR(nf * 9);
@@ -403,9 +430,9 @@ extern "C" int sass_stage_frames_prepass(sass_plan* p, const float* frames, size
         const bool ref_one = q.reference != nullptr;
         auto com_ref = [&](double* out) {
             if (ref_one)
-                pp_com_kernel<<<1, kPerFrameThreads, 0, st>>>(D(o.refxyz), 0, nullptr, D(o.rmass), nref, 1, out);
+                pp_com_kernel<<<1, 32, 0, st>>>(D(o.refxyz), 0, nullptr, D(o.rmass), nref, 1, out);
             else
-                pp_com_kernel<<<gf, kPerFrameThreads, 0, st>>>(W, nsys * 3, L(o.ref), D(o.rmass), nref, nfi, out);
+                pp_com_kernel<<<gw, kWarpFrameThreads, 0, st>>>(W, nsys * 3, L(o.ref), D(o.rmass), nref, nfi, out);
         };
         switch (q.type) {
             case SASS_STEP_CENTER:
@@ -415,7 +442,7 @@ extern "C" int sass_stage_frames_prepass(sass_plan* p, const float* frames, size
                 break;
             case SASS_STEP_FITTRANS:
                 com_ref(va);
-                pp_com_kernel<<<gf, kPerFrameThreads, 0, st>>>(W, nsys * 3, L(o.sel), D(o.smass), nsel, nfi, vb);
+                pp_com_kernel<<<gw, kWarpFrameThreads, 0, st>>>(W, nsys * 3, L(o.sel), D(o.smass), nsel, nfi, vb);
                 pp_combine_kernel<<<gf, kPerFrameThreads, 0, st>>>(va, ref_one, vb, 0, 1, nfi, vt);
                 if (nsel) pp_translate_kernel<<<grid_for(nf * nsel, 256), 256, 0, st>>>(W, nsys, L(o.sel), nsel, nfi, vt);
                 break;
@@ -428,17 +455,17 @@ extern "C" int sass_stage_frames_prepass(sass_plan* p, const float* frames, size
             default: {  // FITROTTRANS, FITROT
                 const bool rot_only = q.type == SASS_STEP_FITROT;
                 if (rot_only)  // centre of mass of the moved atoms before the fit
-                    pp_com_kernel<<<gf, kPerFrameThreads, 0, st>>>(W, nsys * 3, L(o.sel), D(o.smass), nsel, nfi, vc);
+                    pp_com_kernel<<<gw, kWarpFrameThreads, 0, st>>>(W, nsys * 3, L(o.sel), D(o.smass), nsel, nfi, vc);
                 if (nref) {
                     pp_gather_kernel<<<grid_for(nf * nref * 3, 256), 256, 0, st>>>(W, nsys, L(o.ref), nref, nfi, C);
                     // pos: the copy's centre; ref: the reference structure's (the copy itself when instant)
-                    pp_com_kernel<<<gf, kPerFrameThreads, 0, st>>>(C, nref * 3, nullptr, D(o.rmass), nref, nfi, vb);
+                    pp_com_kernel<<<gw, kWarpFrameThreads, 0, st>>>(C, nref * 3, nullptr, D(o.rmass), nref, nfi, vb);
                     if (ref_one)
-                        pp_com_kernel<<<1, kPerFrameThreads, 0, st>>>(D(o.refxyz), 0, nullptr, D(o.rmass), nref, 1, va);
+                        pp_com_kernel<<<1, 32, 0, st>>>(D(o.refxyz), 0, nullptr, D(o.rmass), nref, 1, va);
                     else
-                        pp_com_kernel<<<gf, kPerFrameThreads, 0, st>>>(C, nref * 3, nullptr, D(o.rmass), nref, nfi, va);
-                    pp_kmat_kernel<<<gf, kPerFrameThreads, 0, st>>>(C, ref_one ? D(o.refxyz) : nullptr, D(o.rmass), nref,
-                                                                    nfi, vb, va, ref_one, vK);
+                        pp_com_kernel<<<gw, kWarpFrameThreads, 0, st>>>(C, nref * 3, nullptr, D(o.rmass), nref, nfi, va);
+                    pp_kmat_kernel<<<gw, kWarpFrameThreads, 0, st>>>(C, ref_one ? D(o.refxyz) : nullptr, D(o.rmass),
+                                                                     nref, nfi, vb, va, ref_one, vK);
                     PCK(cudaGetLastError());
                     PCK(cudaMemcpyAsync(hK.data(), vK, nf * 9 * sizeof(double), cudaMemcpyDeviceToHost, st));
                     PCK(cudaStreamSynchronize(st));
