@@ -33,7 +33,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-ffp-contract=off", "-I" + 
 
 CUDA_SOURCES = [
     "capi.cu", "engine.cu", "phase_sum.cu", "phase_rec.cu", "correlate.cu", "peaks.cu", "noalloc.cu", "mlp.cu",
-    "cv.cu", "multipole.cu", "align.cu",
+    "cv.cu", "multipole.cu", "align.cu", "corr_long.cu",
 ]
 HOST_SOURCES = []  # filled when the host layer exists (see host_sources())
 
