@@ -169,10 +169,12 @@ def make_workload(name, nq=0, nf=0):
 
 
 def cpu_sample(w, seconds, nthreads):
-    """Time the oracle on one shell x m directions (m grown until ~`seconds`)."""
+    """Time the oracle on one shell x m directions (m grown until ~`seconds`). The oracle
+    runs one direction per worker thread, so m stays a multiple of the thread count (or all
+    of the shell's directions): a partial last round would understate the CPU's rate."""
     import oracle
     s = w.nq // 2
-    m = 1
+    m = min(w.nm, nthreads)
     fac = w.factors()[s:s + 1]
     while True:
         sv = w.shells[s] * w.directions[:m]
@@ -188,7 +190,8 @@ def cpu_sample(w, seconds, nthreads):
                     "sample": "oracle (FP64 restatement) on shell %d/%d x %d of %d directions, "
                               "all %d atoms x %d frames (%.3g terms, %.1f s)"
                               % (s, w.nq, m, w.nm, w.na, w.nf, terms, dt)}
-        m = min(w.nm, max(m * 2, int(m * seconds * 0.6 / max(dt, 1e-3))))
+        m = max(m * 2, int(m * seconds * 0.6 / max(dt, 1e-3)))
+        m = min(w.nm, (m + nthreads - 1) // nthreads * nthreads)
 
 
 MP_WORKLOADS = ("multipole_sphere", "multipole_cylinder")
@@ -234,7 +237,8 @@ def cpu_sample_mp(w, qv, kind, moments, seconds, nthreads):
                     "sample": "oracle multipole %s (FP64 restatement) on q-vector %d/%d, all %d "
                               "atoms x %d moments x %d of %d frames (%.3g terms, %.1f s)"
                               % (kind, s, w.nq, w.na, len(moments), nf, w.nf, terms, dt)}
-        nf = min(w.nf, max(nf * 2, int(nf * seconds * 0.6 / max(dt, 1e-3))))
+        nf = max(nf * 2, int(nf * seconds * 0.6 / max(dt, 1e-3)))
+        nf = min(w.nf, (nf + nthreads - 1) // nthreads * nthreads)  # whole rounds of frames per thread
 
 
 def run_reference(args, dist):
