@@ -34,3 +34,7 @@ def test_plan_create_rejects_bad_descriptors_without_gpu():
     d = abi.PlanDesc(7, 0, 0, 0, 10, 10, 1, 0, None, 0)  # unknown scattering type
     assert lib.sass_plan_create(ctypes.byref(d), ctypes.byref(h)) == 1
     assert lib.sass_plan_create(None, ctypes.byref(h)) == 1
+    # beyond the long-series transform: padded length above 2^20 (NF > 524,288)
+    for scattering in (0, 1):
+        d = abi.PlanDesc(scattering, 0, 0, 0, 10, 600000, 1, 0, None, 0)
+        assert lib.sass_plan_create(ctypes.byref(d), ctypes.byref(h)) == 3
