@@ -205,3 +205,17 @@ def test_coherent_fp32_error_at_length(native_lib, nf):
     rng = np.random.default_rng(nf)
     w = synth.coherent_sqt(seed=21, na=500, nf=nf, nq=3, nm=8, box=20.0)
     check(w, "fp32", "fftw")
+
+
+def test_out_of_memory_is_a_status(native_lib):
+    # a trajectory far beyond HBM (16.7M atoms x 131,072 frames = 35 TB staged): the device
+    # allocation fails first, staging returns SASS_ERR_OOM with a message, nothing is read
+    # from the host buffer, and the process keeps working
+    import ctypes
+    with abi.Plan(1 << 24, 1 << 17, 1, "all", "autocorrelate", "fftw", "fp32") as p:
+        dummy = np.zeros(3, dtype=np.float32)
+        rc = p.lib.sass_stage_frames(p._h, dummy.ctypes.data_as(ctypes.c_void_p), 0)
+        assert rc == 2, rc
+        assert p.lib.sass_plan_error(p._h)
+    w = synth.small("all", "autocorrelate", seed=18, na=20, nf=9, nq=2, nm=3)
+    check(w, "fp64", "fftw")
