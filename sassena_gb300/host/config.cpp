@@ -175,6 +175,16 @@ void Params::read_xml(const std::string& path) {
 
     // ---- stager (parameters.cpp:340-369) ---------------------------------------------------
     if (x.exists("//stager/target")) target = x.get_string("//stager/target");
+    stager_filepath = get_filepath(stager_file);
+    if (x.exists("//stager/dump")) stager_dump = x.get_bool("//stager/dump");
+    if (x.exists("//stager/file")) {
+        stager_file = x.get_string("//stager/file");
+        stager_filepath = get_filepath(stager_file);
+    }
+    if (x.exists("//stager/format")) stager_format = x.get_string("//stager/format");
+    if (x.exists("//stager/mode")) stager_mode = x.get_string("//stager/mode");
+    if (stager_mode != "frames" && stager_mode != "atoms")  // both map to the device's own layout
+        throw std::runtime_error("stager.mode not understood: " + stager_mode);
 
     // ---- scattering (parameters.cpp:372-607) -------------------------------------------------
     if (x.exists("//scattering")) {
@@ -294,6 +304,13 @@ void Params::overwrite(const std::string& key, const std::string& value) {
         structure_format = value;
     } else if (key == "stager.target") {
         target = value;
+    } else if (key == "stager.dump") {
+        stager_dump = value == "true" || value == "1" || value == "yes";
+    } else if (key == "stager.file") {
+        stager_file = value;
+        stager_filepath = get_filepath(value);
+    } else if (key == "stager.format") {
+        stager_format = value;
     } else if (key == "scattering.signal.file") {
         signal_file = value;
         signal_filepath = get_filepath(value);

@@ -66,8 +66,10 @@ struct Params {
     std::vector<FramesetParams> framesets;
     std::vector<MotionParams> motions;
     std::vector<AlignmentParams> alignments;
-    // stager
+    // stager (parameters.cpp:340-369): target selection; dump of the staged coordinates
     std::string target = "system";
+    bool stager_dump = false;
+    std::string stager_file = "dump.dcd", stager_filepath, stager_format = "dcd", stager_mode = "frames";
     // database
     std::string db_file = "db.xml", db_filepath;
     // scattering

@@ -209,9 +209,15 @@ bool run_scatter_device(const Params& p, Database& db, const Sample& s, RunStats
             float* q;
             ~Free() { sass_host_free(q); }
         } release{pinned};
+        if (p.stager_dump && p.stager_format != "dcd")
+            throw std::runtime_error("Format for coordinate dumping not known: " + p.stager_format);
         if (!prepass) {
             s.stage_into(p.target, pinned);
             check(plan, sass_stage_frames(plan, pinned, 0), "sass_stage_frames");
+            if (p.stager_dump) {
+                info("Dumping coordinates to file: " + p.stager_filepath);
+                write_dcd(p.stager_filepath, pinned, nf, na);
+            }
         } else {
             s.stage_into("system", pinned);
             Prepass pp = build_prepass(p, db, s, pinned);
@@ -233,9 +239,14 @@ bool run_scatter_device(const Params& p, Database& db, const Sample& s, RunStats
                 info("Staging pre-pass step: " + q.label);
             }
             const std::vector<size_t>& target = s.selection(p.target);
+            std::vector<float> staged(p.stager_dump ? nf * na * 3 : 0);
             check(plan, sass_stage_frames_prepass(plan, pinned, nsys, pp.masses.data(), steps.data(), steps.size(),
-                                                  target.data(), nullptr),
+                                                  target.data(), p.stager_dump ? staged.data() : nullptr),
                   "sass_stage_frames_prepass");
+            if (p.stager_dump) {
+                info("Dumping coordinates to file: " + p.stager_filepath);
+                write_dcd(p.stager_filepath, staged.data(), nf, na);
+            }
         }
     }
     check(plan, sass_set_atom_classes(plan, cls.atom_class.data(), 0), "sass_set_atom_classes");

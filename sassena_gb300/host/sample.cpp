@@ -95,6 +95,47 @@ void DcdFile::read_frame(size_t i, float* x, float* y, float* z) const {
     }
 }
 
+void write_dcd(const std::string& path, const float* frames, size_t nf, size_t na) {
+    std::ofstream out(path, std::ios::binary | std::ios::trunc);
+    if (!out) throw std::runtime_error("Couldn't open dump file: " + path);
+    auto i32 = [&](int32_t v) { out.write(reinterpret_cast<const char*>(&v), 4); };
+    // header record: "CORD", frames, start 0, interval 1, 6 zeros, timestep 1.0f, unit-cell
+    // block on, fourth-dimension block off, 7 zeros, CHARMM version 24
+    i32(84);
+    out.write("CORD", 4);
+    i32((int32_t)nf);
+    i32(0);
+    i32(1);
+    for (int k = 0; k < 6; ++k) i32(0);
+    const float dt = 1.0f;
+    out.write(reinterpret_cast<const char*>(&dt), 4);
+    i32(1);
+    i32(0);
+    for (int k = 0; k < 7; ++k) i32(0);
+    i32(24);
+    i32(84);
+    i32(4);  // title record with no title lines
+    i32(0);
+    i32(4);
+    i32(4);  // atom count record
+    i32((int32_t)na);
+    i32(4);
+    std::vector<float> col(na);
+    const double cell[6] = {0, 0, 0, 0, 0, 0};
+    for (size_t f = 0; f < nf; ++f) {
+        i32(48);
+        out.write(reinterpret_cast<const char*>(cell), 48);
+        i32(48);
+        for (int k = 0; k < 3; ++k) {
+            for (size_t j = 0; j < na; ++j) col[j] = frames[(f * na + j) * 3 + k];
+            i32((int32_t)(4 * na));
+            out.write(reinterpret_cast<const char*>(col.data()), (std::streamsize)(4 * na));
+            i32((int32_t)(4 * na));
+        }
+    }
+    if (!out) throw std::runtime_error("write error on dump file: " + path);
+}
+
 void Sample::init(const Params& p, Database& db) {
     if (p.structure_format != "pdb") throw std::runtime_error("structure format not supported: " + p.structure_format);
     std::ifstream in(p.structure_filepath);

@@ -34,6 +34,12 @@ struct DcdFile {
     void read_frame(size_t i, float* x, float* y, float* z) const;
 };
 
+// Staged coordinates [nf][na][3] written as a CHARMM DCD in the layout of the reference's
+// DCDCoordinateWriter (src/stager/coordinate_writer.cpp:27-137): 84-byte header with the
+// unit-cell flag set, an empty title, the atom count, then per frame a zero unit cell and the
+// X, Y, Z records (stager.dump, data_stager.cpp:91-94, 131-162).
+void write_dcd(const std::string& path, const float* frames, size_t nf, size_t na);
+
 class Sample {
 public:
     std::vector<size_t> atom_ids;                          // database ID per atom (structure order)

@@ -64,6 +64,9 @@ void dry_run(const Params& p, Database& db, const Sample& s, const std::string& 
         o << "]";
     }
     std::vector<float> coords = s.stage(p.target);
+    // without alignments or motions the staged frames are the host's: the dry run dumps them
+    if (p.stager_dump && p.alignments.empty() && p.motions.empty())
+        write_dcd(p.stager_filepath, coords.data(), s.nframes, s.selection(p.target).size());
     double sum = 0;
     for (float v : coords) sum += v;
     char b[64];

@@ -96,3 +96,36 @@ def test_driver_with_alignments_matches_oracle(native_lib, tmp_path, name):
     rfqt = ref[0][..., 0] + 1j * ref[0][..., 1]
     err = (np.abs(fqt - rfqt).max(axis=1) / np.abs(rfqt[:, 0])).max()
     assert err <= 1e-12, err
+
+
+def read_dcd(path, nf, na):
+    """Frames [nf, na, 3] of a DCD in the reference writer's layout (unit-cell block on)."""
+    raw = open(path, "rb").read()
+    off = 4 + 84 + 4 + 12 + 12  # header record, title record, atom-count record
+    out = np.zeros((nf, na, 3), dtype=np.float32)
+    for f in range(nf):
+        off += 4 + 48 + 4
+        for k in range(3):
+            out[f, :, k] = np.frombuffer(raw, dtype=np.float32, count=na, offset=off + 4)
+            off += 8 + 4 * na
+    return out
+
+
+@pytest.mark.parametrize("name", ["motions", "pre_post"])
+def test_driver_dumps_the_aligned_frames(native_lib, tmp_path, name):
+    # stager.dump after the device pre-pass: the file holds the oracle's aligned frames
+    d = str(tmp_path / "run")
+    w, cfg, o = pc.build(name, d)
+    with open(cfg) as f:
+        xml = f.read()
+    with open(cfg, "w") as f:
+        f.write(xml.replace("<stager>", "<stager><dump>true</dump>") if "<stager>" in xml
+                else xml.replace("</root>", "<stager><dump>true</dump></stager></root>"))
+    r = subprocess.run([abi.DRIVER_PATH, "--config", cfg], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    want = al.load(w.coords, o["masses"], o["alignments"], o["motions"], o["target"])
+    got = read_dcd(os.path.join(d, "dump.dcd"), want.shape[0], want.shape[1])
+    if name in FITS:
+        assert (np.abs(got - want) <= np.spacing(np.abs(want).astype(np.float32))).all()
+    else:
+        np.testing.assert_array_equal(got, want)

@@ -275,3 +275,28 @@ def test_multipole_moment_checks(small_files, tmp_path, kind, lines, needle):
         f.write(lines)
     r = run_driver("--config", cfg, "--dry-run", str(tmp_path / "x.json"))
     assert r.returncode != 0 and needle in r.stderr, r.stderr
+
+
+def test_stager_dump_writes_the_reference_dcd_layout(small_files, tmp_path):
+    # stager.dump (data_stager.cpp:91-94): the staged frames as a DCD laid out like the
+    # reference's DCDCoordinateWriter; without alignments the dry run stages on the host
+    w, _ = small_files
+    d = str(tmp_path / "dump")
+    cfg = synth.write_files(d, w, extra="<stager><dump>true</dump><file>out.dcd</file></stager>")
+    dry(cfg, tmp_path)
+    ref = str(tmp_path / "ref.dcd")
+    synth.write_dcd(ref, w.coords)
+    assert open(os.path.join(d, "out.dcd"), "rb").read() == open(ref, "rb").read()
+    # and the driver reads it back as a trajectory
+    cfg2 = synth.write_files(str(tmp_path / "again"), w)
+    import shutil
+    shutil.copy(os.path.join(d, "out.dcd"), str(tmp_path / "again" / "sample.dcd"))
+    j = dry(cfg2, tmp_path)
+    assert j["coord_sum"] == pytest.approx(float(np.sum(w.coords, dtype=np.float64)), rel=0, abs=1e-6)
+
+
+def test_stager_dump_unknown_format(small_files, tmp_path):
+    w, _ = small_files
+    cfg = synth.write_files(str(tmp_path / "x"), w, extra="<stager><mode>columns</mode></stager>")
+    r = run_driver("--config", cfg, "--dry-run", str(tmp_path / "x.json"))
+    assert r.returncode != 0 and "stager.mode" in r.stderr
