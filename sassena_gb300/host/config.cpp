@@ -92,6 +92,22 @@ void Params::read_xml(const std::string& path) {
                 if (x.exists("./to", s)) sp.to = x.get_size("./to", s);
             } else if (sp.type == "lexical") {
                 if (x.exists("./expression", s)) sp.expression = x.get_string("./expression", s);
+            } else if (sp.type == "file") {
+                // defaults as the reference sets them; for ndx it switches selector and expression
+                // (its default file name stays selection.pdb: the ndx branch assigns another variable)
+                sp.file = "selection.pdb";
+                sp.format = "pdb";
+                sp.selector = "beta";
+                sp.expression = "1|1\\.0|1\\.00";
+                if (x.exists("./format", s)) sp.format = x.get_string("./format", s);
+                if (sp.format == "ndx") {
+                    sp.selector = "name";
+                    sp.expression = ".*";
+                }
+                if (x.exists("./file", s)) sp.file = x.get_string("./file", s);
+                sp.filepath = get_filepath(sp.file);
+                if (x.exists("./selector", s)) sp.selector = x.get_string("./selector", s);
+                if (x.exists("./expression", s)) sp.expression = x.get_string("./expression", s);
             } else {
                 throw std::runtime_error("Selection type not supported by this build: " + sp.type);
             }

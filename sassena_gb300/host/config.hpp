@@ -29,6 +29,8 @@ struct SelectionParams {
     std::vector<size_t> ids;
     size_t from = 0, to = 0;
     std::string expression;
+    // type "file" (parameters.cpp:148-176): a PDB (beta or segid column) or an ndx index file
+    std::string file, filepath, format, selector;
 };
 
 // sample.alignments.alignment (parameters.cpp:298-340)

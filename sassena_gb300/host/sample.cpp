@@ -4,6 +4,7 @@
 #include <cstring>
 #include <fstream>
 #include <regex>
+#include <sstream>
 #include <stdexcept>
 
 namespace sassgpu {
@@ -95,6 +96,60 @@ void DcdFile::read_frame(size_t i, float* x, float* y, float* z) const {
     }
 }
 
+std::map<std::string, std::vector<size_t>> read_ndx_groups(const std::string& path, const std::string& selector,
+                                                          const std::string& expression) {
+    // AtomselectionReader::read_ndx, atomselection_reader.cpp:33-80: "[ name ]" opens a group
+    // (the name is the first token after "[", the closing bracket included when no space
+    // separates it); following lines hold 1-based indices, kept for groups whose name matches
+    if (selector != "name") throw std::runtime_error("NDX Atomselection only supports selection by 'name' at the moment");
+    std::ifstream in(path);
+    if (!in) throw std::runtime_error("Couldn't open selection file: " + path);
+    std::regex expr(expression);
+    std::map<std::string, std::vector<size_t>> groups;
+    std::string line, name;
+    while (std::getline(in, line)) {
+        const size_t pos = line.find('[');
+        if (pos != std::string::npos) {
+            const size_t pos2 = line.find(']');
+            if (pos2 == std::string::npos) throw std::runtime_error("ndx file is missing closing bracket");
+            std::istringstream cs(line.substr(pos + 1, pos2 - pos));
+            std::string token;
+            cs >> token;
+            name = trim(token);
+        } else if (!name.empty() && std::regex_match(name, expr)) {
+            std::istringstream ls(line);
+            long long v;
+            while (ls >> v) {
+                if (v < 1) break;  // the reference reads size_t: zero or negatives stop the line
+                groups[name].push_back((size_t)v - 1);
+            }
+        }
+    }
+    return groups;
+}
+
+std::vector<size_t> read_pdb_selection(const std::string& path, const std::string& selector,
+                                       const std::string& expression) {
+    // AtomselectionReader::read_pdb, atomselection_reader.cpp:82-120: ATOM records whose beta
+    // (columns 61-66) or segid (73-76) field, trimmed, matches the expression
+    if (selector != "beta" && selector != "segid")
+        throw std::runtime_error("PDB Atomselection only supports beta and segid at the moment");
+    std::ifstream in(path);
+    if (!in) throw std::runtime_error("Couldn't open selection file: " + path);
+    std::regex expr(expression);
+    std::vector<size_t> ids;
+    std::string line;
+    size_t n = 0;
+    while (std::getline(in, line)) {
+        if (line.compare(0, 6, "ATOM  ") != 0) continue;
+        const size_t pos = selector == "beta" ? 60 : 72, len = selector == "beta" ? 6 : 4;
+        const std::string v = trim(line.size() > pos ? line.substr(pos, len) : std::string());
+        if (std::regex_match(v, expr)) ids.push_back(n);
+        ++n;
+    }
+    return ids;
+}
+
 void write_dcd(const std::string& path, const float* frames, size_t nf, size_t na) {
     std::ofstream out(path, std::ios::binary | std::ios::trunc);
     if (!out) throw std::runtime_error("Couldn't open dump file: " + path);
@@ -164,6 +219,19 @@ void Sample::init(const Params& p, Database& db) {
             std::regex e(s.expression);
             for (size_t i = 0; i < na; ++i)
                 if (std::regex_match(db.labels[atom_ids[i]], e)) idx.push_back(i);
+        } else if (s.type == "file") {
+            if (s.format == "ndx") {  // every matching group becomes a selection of its own name
+                for (auto& g : read_ndx_groups(s.filepath, s.selector, s.expression)) {
+                    for (size_t i : g.second)
+                        if (i >= na) throw std::runtime_error("ndx group " + g.first + " refers to atom " + std::to_string(i));
+                    selections[g.first == "system" ? "system_RENAMED_BY_SASSENA" : g.first] = g.second;
+                }
+                continue;
+            } else if (s.format == "pdb") {
+                idx = read_pdb_selection(s.filepath, s.selector, s.expression);
+            } else {
+                throw std::runtime_error("Selection file format not understood");
+            }
         }
         for (size_t i : idx)
             if (i >= na) throw std::runtime_error("selection " + s.name + " refers to atom " + std::to_string(i));

@@ -40,6 +40,13 @@ struct DcdFile {
 // X, Y, Z records (stager.dump, data_stager.cpp:91-94, 131-162).
 void write_dcd(const std::string& path, const float* frames, size_t nf, size_t na);
 
+// File selections (selection type "file"): the groups of an ndx index file whose names match
+// `expression`, and the ATOM records of a PDB whose beta or segid field matches it.
+std::map<std::string, std::vector<size_t>> read_ndx_groups(const std::string& path, const std::string& selector,
+                                                          const std::string& expression);
+std::vector<size_t> read_pdb_selection(const std::string& path, const std::string& selector,
+                                       const std::string& expression);
+
 class Sample {
 public:
     std::vector<size_t> atom_ids;                          // database ID per atom (structure order)

@@ -300,3 +300,36 @@ def test_stager_dump_unknown_format(small_files, tmp_path):
     cfg = synth.write_files(str(tmp_path / "x"), w, extra="<stager><mode>columns</mode></stager>")
     r = run_driver("--config", cfg, "--dry-run", str(tmp_path / "x.json"))
     assert r.returncode != 0 and "stager.mode" in r.stderr
+
+
+def test_file_selections_ndx_and_pdb(small_files, tmp_path):
+    # selection type "file" (parameters.cpp:148-176, atomselection_reader.cpp:33-120)
+    w, _ = small_files
+    d = str(tmp_path / "sel")
+    os.makedirs(d, exist_ok=True)
+    with open(os.path.join(d, "index.ndx"), "w") as f:
+        f.write("[ System ]\n" + " ".join(str(i + 1) for i in range(w.na)) + "\n")
+        f.write("[ Core ]\n3 1 5\n7\n[Tail]\n2 4\n")
+    beta = [1.0 if i % 3 == 0 else 0.0 for i in range(w.na)]
+    with open(os.path.join(d, "flags.pdb"), "w") as f:
+        for i in range(w.na):
+            f.write("ATOM  %5d C1   MOL A   1    %8.3f%8.3f%8.3f  1.00%6.2f      SEG%d\n"
+                    % (i + 1, 0, 0, 0, beta[i], i % 2))
+    sels = ("<selections>"
+            "<selection><type>file</type><format>ndx</format><file>index.ndx</file>"
+            "<expression>Core|Tail\\]</expression></selection>"
+            "<selection><type>file</type><name>flagged</name><file>flags.pdb</file></selection>"
+            "<selection><type>file</type><name>seg1</name><file>flags.pdb</file><selector>segid</selector>"
+            "<expression>SEG1</expression></selection>"
+            "</selections>")
+    for target, want in (("Core", [2, 0, 4, 6]), ("Tail]", [1, 3]),
+                         ("flagged", [i for i in range(w.na) if i % 3 == 0]),
+                         ("seg1", [i for i in range(w.na) if i % 2 == 1])):
+        cfg = synth.write_files(d, w, sample_extra=sels, extra="<stager><target>%s</target></stager>" % target)
+        j = dry(cfg, tmp_path)
+        assert j["na"] == len(want), target
+        assert j["coord_sum"] == pytest.approx(float(w.coords[:, want].astype(np.float64).sum()), abs=1e-6)
+    # the System group does not match the expression, so it is not a selection
+    cfg = synth.write_files(d, w, sample_extra=sels, extra="<stager><target>System</target></stager>")
+    r = run_driver("--config", cfg, "--dry-run", str(tmp_path / "x.json"))
+    assert r.returncode != 0 and "unknown selection" in r.stderr
