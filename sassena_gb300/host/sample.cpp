@@ -242,18 +242,34 @@ void Sample::init(const Params& p, Database& db) {
     for (size_t i = 0; i < na; ++i) all[i] = i;
     selections["system"] = all;
 
-    for (const FramesetParams& fs : p.framesets) {
-        if (fs.format != "dcd") throw std::runtime_error("frameset format not supported by this build: " + fs.format);
-        if (fs.clones == 0) continue;
+    auto add_dcd = [&](const std::string& path, const FramesetParams& fs, size_t clones) {
         DcdFile d;
-        d.open(fs.filepath);
+        d.open(path);
         if (d.natoms != na)  // coordinate_sets.cpp:250-255
             throw std::runtime_error("Atom number mismatch (dcd) " + std::to_string(d.natoms) + " vs. (pdb) " +
                                      std::to_string(na));
         d.select(fs.first, fs.last, fs.last_set, fs.stride);
-        for (size_t c = 0; c < fs.clones; ++c) {
+        for (size_t c = 0; c < clones; ++c) {
             framesets.push_back(d);
             nframes += d.frame_pos.size();
+        }
+    };
+    for (const FramesetParams& fs : p.framesets) {
+        if (fs.clones == 0) continue;
+        if (fs.format == "dcd") {
+            add_dcd(fs.filepath, fs, fs.clones);
+        } else if (fs.format == "dcdlist") {
+            // Frames::add_frameset "dcdlist" (frames.cpp:71-85): whitespace-separated DCD paths,
+            // taken as written; tokens starting with '#' are skipped; each file `clones` times
+            std::ifstream list(fs.filepath);
+            if (!list) throw std::runtime_error("Couldn't open frameset list: " + fs.filepath);
+            std::string tok;
+            while (list >> tok) {
+                if (!tok.empty() && tok[0] == '#') continue;
+                for (size_t c = 0; c < fs.clones; ++c) add_dcd(tok, fs, 1);
+            }
+        } else {
+            throw std::runtime_error("frameset format not supported by this build: " + fs.format);
         }
     }
     if (nframes == 0) throw std::runtime_error("Number of frames must not be negative or zero!");

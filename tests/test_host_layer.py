@@ -333,3 +333,24 @@ def test_file_selections_ndx_and_pdb(small_files, tmp_path):
     cfg = synth.write_files(d, w, sample_extra=sels, extra="<stager><target>System</target></stager>")
     r = run_driver("--config", cfg, "--dry-run", str(tmp_path / "x.json"))
     assert r.returncode != 0 and "unknown selection" in r.stderr
+
+
+def test_dcdlist_frameset(small_files, tmp_path):
+    # frameset format dcdlist (frames.cpp:71-85): the listed files, each `clones` times
+    w, _ = small_files
+    d = str(tmp_path / "list")
+    cfg = synth.write_files(d, w)
+    a, b = os.path.join(d, "a.dcd"), os.path.join(d, "b.dcd")
+    synth.write_dcd(a, w.coords[:4])
+    synth.write_dcd(b, w.coords[4:])
+    with open(os.path.join(d, "frames.list"), "w") as f:
+        f.write("%s\n#%s\n%s\n" % (a, b, b))
+    xml = open(cfg).read().replace(
+        "<framesets><frameset><file>sample.dcd</file><format>dcd</format></frameset></framesets>",
+        "<framesets><frameset><file>frames.list</file><format>dcdlist</format><clones>2</clones>"
+        "</frameset></framesets>")
+    open(cfg, "w").write(xml)
+    j = dry(cfg, tmp_path)
+    want = np.concatenate([w.coords[:4], w.coords[:4], w.coords[4:], w.coords[4:]])
+    assert j["nf"] == len(want)
+    assert j["coord_sum"] == pytest.approx(float(want.astype(np.float64).sum()), abs=1e-6)
