@@ -73,7 +73,8 @@ __global__ void __launch_bounds__(NT) corr_fft_kernel(CorrLaunch a) {
         }
         __syncthreads();
         dif_tail<T2, NT>(buf, tw, lg, tws);
-        double2 av = block_sum<NT>(absorb_power<T, NT, MAXR>(buf, L, kbr, acc), red);
+        const T2 pv = absorb_power_t<T, NT, MAXR>(buf, L, kbr, acc);
+        double2 av = block_sum_t<T, NT>(pv.x, pv.y, red);
         if (threadIdx.x == 0) {
             asum.x += av.x;
             asum.y += av.y;
@@ -126,7 +127,8 @@ __global__ void __launch_bounds__(NT) self_fft_kernel(CorrLaunch a) {
             }
             __syncthreads();
             dif_tail<T2, NT>(buf, tw, lg, tws);
-            double2 av = block_sum<NT>(absorb_power<T, NT, MAXR>(buf, L, kbr, acc), red);
+            const T2 pv = absorb_power_t<T, NT, MAXR>(buf, L, kbr, acc);
+            double2 av = block_sum_t<T, NT>(pv.x, pv.y, red);
             if (threadIdx.x == 0) {
                 asum.x += av.x;
                 asum.y += av.y;

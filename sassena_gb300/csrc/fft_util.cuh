@@ -145,6 +145,55 @@ __device__ __forceinline__ void load_q(const double* q, T& qx, T& qy, T& qz) {
     }
 }
 
+// Sum of (x, y) over the CTA; valid in thread 0. The warp stage runs in T (FP32 in the FP32
+// form: GB300's FP64 pipe is a narrow fraction of its FP32 pipe), the sum of the warp totals in
+// FP64. Ends with a barrier so the caller may reuse shared memory afterwards.
+template <class T, int NT>
+__device__ double2 block_sum_t(T x, T y, double2* red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        x += __shfl_xor_sync(0xffffffffu, x, o);
+        y += __shfl_xor_sync(0xffffffffu, y, o);
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) red[warp] = make_double2((double)x, (double)y);
+    __syncthreads();
+    double2 s = make_double2(0.0, 0.0);
+    if (threadIdx.x == 0)
+        for (int w = 0; w < NT / 32; ++w) {
+            s.x += red[w].x;
+            s.y += red[w].y;
+        }
+    __syncthreads();
+    return s;
+}
+
+// Power spectrum of the series in buf (bit-reversed order): accumulate P and return this
+// thread's part of sum_w P(w) K(w) in T (reduce it with block_sum_t).
+template <class T, int NT, int MAXR>
+__device__ __forceinline__ typename cplx<T>::type absorb_power_t(const typename cplx<T>::type* buf, int L,
+                                                                  const typename cplx<T>::type* __restrict__ kbr,
+                                                                  PowerAcc<T, MAXR>& acc) {
+    typedef typename cplx<T>::type T2;
+    T ax = 0, ay = 0;
+#pragma unroll
+    for (int r = 0; r < MAXR; ++r) {
+        const int i = threadIdx.x + r * NT;
+        if (i < L) {
+            T2 X = buf[i];
+            T P = X.x * X.x + X.y * X.y;
+            acc.add(r, P);
+            T2 k = kbr[i];
+            ax += P * k.x;
+            ay += P * k.y;
+        }
+    }
+    T2 v;
+    v.x = ax;
+    v.y = ay;
+    return v;
+}
+
 // Power spectrum of the series in buf (bit-reversed order): accumulate P and return
 // this thread's part of sum_w P(w) K(w).
 template <class T, int NT, int MAXR>
