@@ -81,7 +81,8 @@ __global__ void __launch_bounds__(NT) corr_fft_kernel(CorrLaunch a) {
             a2sum += av.x * av.x + av.y * av.y;
         }
     }
-    write_power<T, NT, MAXR>(acc, L, a.ppart + c.part_off);
+    if constexpr (sizeof(T) == 4) write_power_pair<NT, MAXR>(acc, L, a.ppart + c.part_off);
+    else write_power<T, NT, MAXR>(acc, L, a.ppart + c.part_off);
     if (threadIdx.x == 0) {
         a.apart[c.slot] = asum;
         a.a2part[c.slot] = a2sum;
@@ -136,7 +137,8 @@ __global__ void __launch_bounds__(NT) self_fft_kernel(CorrLaunch a) {
             }
         }
     }
-    write_power<T, NT, MAXR>(acc, L, a.ppart + c.part_off);
+    if constexpr (sizeof(T) == 4) write_power_pair<NT, MAXR>(acc, L, a.ppart + c.part_off);
+    else write_power<T, NT, MAXR>(acc, L, a.ppart + c.part_off);
     if (threadIdx.x == 0) {
         a.apart[c.slot] = asum;
         a.a2part[c.slot] = a2sum;
@@ -502,8 +504,15 @@ __global__ void __launch_bounds__(NT) finalize_kernel(FinalLaunch a) {
         double2* buf = reinterpret_cast<double2*>(smem);
         for (int i = threadIdx.x; i < L; i += NT) {
             double p = 0.0;
-            for (int k = e.slot_begin; k < e.slot_end; ++k)
-                p += a.ppart[e.part_off + (size_t)(k - e.slot_begin) * e.part_len + i];
+            for (int k = e.slot_begin; k < e.slot_end; ++k) {
+                const double* src = a.ppart + e.part_off + (size_t)(k - e.slot_begin) * e.part_len + i;
+                if (e.f32pair) {
+                    const float2 sc = *reinterpret_cast<const float2*>(src);
+                    p += (double)sc.x - (double)sc.y;
+                } else {
+                    p += *src;
+                }
+            }
             buf[i] = make_double2(p, 0.0);
         }
         __syncthreads();
@@ -825,8 +834,13 @@ cudaError_t launch_accumulate(const CorrLaunch& a, bool self, cudaStream_t st) {
             return a.precision == PREC_FP32 ? launch_reg_fft<float>(a, self, st) : launch_reg_fft<double>(a, self, st);
         if (a.lg_max <= kWarpFftMaxLg)
             return a.precision == PREC_FP32 ? launch_warp_fft<float>(a, self, st) : launch_warp_fft<double>(a, self, st);
-        if (a.precision == PREC_FP32) return launch_fft<float, 256, 32>(a, self, st);
-        return launch_fft<double, 256, 32>(a, self, st);
+        // per-thread spectrum bins sized to the longest series of the launch (registers)
+        switch (a.lg_max) {
+            case 10: return a.precision == PREC_FP32 ? launch_fft<float, 256, 4>(a, self, st) : launch_fft<double, 256, 4>(a, self, st);
+            case 11: return a.precision == PREC_FP32 ? launch_fft<float, 256, 8>(a, self, st) : launch_fft<double, 256, 8>(a, self, st);
+            case 12: return a.precision == PREC_FP32 ? launch_fft<float, 256, 16>(a, self, st) : launch_fft<double, 256, 16>(a, self, st);
+            default: return a.precision == PREC_FP32 ? launch_fft<float, 256, 32>(a, self, st) : launch_fft<double, 256, 32>(a, self, st);
+        }
     }
     if (self) {
         if (a.precision == PREC_FP32) self_direct_kernel<float, 256, 16><<<a.nchunks, 256, 0, st>>>(a);
@@ -839,6 +853,11 @@ cudaError_t launch_accumulate(const CorrLaunch& a, bool self, cudaStream_t st) {
 }
 
 }  // namespace
+
+bool corr_writes_f32_pairs(int precision, int dsp, int lg_max) {
+    // the CTA-per-series kernels (padded length above the warp forms') in the FP32 form
+    return precision == PREC_FP32 && dsp == DSP_AUTOCORRELATE && lg_max > kWarpFftMaxLg;
+}
 
 size_t fft_smem_bytes(int precision, int lg, int nf, bool self) {
     if (lg <= kWarpFftMaxLg)

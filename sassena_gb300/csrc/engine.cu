@@ -636,13 +636,14 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
             FinalEntry e{};
             e.slot_begin = slot;
             e.part_off = poff;
-            e.part_len = plen;
+            e.part_len = (int)plen;
             e.nf = (int)s.nf;
             e.lg = s.lg;
             e.inv_nm = it.norm > 0 ? it.norm : 1.0 / (double)(it.offs[sh + 1] - it.offs[sh]);
             e.fqt = it.d_fqt + sh * s.nf;
             e.fq = it.d_fq + sh;
             e.fq2 = it.d_fq2 + sh;
+            e.f32pair = corr_writes_f32_pairs(cfg.precision, cfg.dsp, lg_max_) ? 1 : 0;
             const size_t units = coherent ? it.offs[sh + 1] - it.offs[sh] : s.na;
             const size_t g = std::min(per_shell, units);
             const size_t len = (units + g - 1) / g;
@@ -698,7 +699,7 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
             FinalEntry e{};
             e.slot_begin = slot;
             e.part_off = poff;
-            e.part_len = L;
+            e.part_len = (int)L;
             e.nf = (int)s.nf;
             e.lg = s.lg;
             e.inv_nm = it.norm > 0 ? it.norm : 1.0 / (double)(it.offs[sh + 1] - it.offs[sh]);

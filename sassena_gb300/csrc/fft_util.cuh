@@ -226,6 +226,18 @@ __device__ __forceinline__ void write_power(const PowerAcc<T, MAXR>& acc, int L,
     }
 }
 
+// FP32 Kahan partials stored as (sum, compensation) float pairs in the double slot: the FP64
+// finalisation combines them, so the kernels spend no FP64 conversions at the end.
+template <int NT, int MAXR>
+__device__ __forceinline__ void write_power_pair(const PowerAcc<float, MAXR>& acc, int L, double* dst) {
+    float2* d2 = reinterpret_cast<float2*>(dst);
+#pragma unroll
+    for (int r = 0; r < MAXR; ++r) {
+        const int i = threadIdx.x + r * NT;
+        if (i < L) d2[i] = make_float2(acc.s[r], acc.c[r]);
+    }
+}
+
 // Shared twiddle table of the launch: FP32 copies into shared memory, FP64 reads L1.
 template <class T, int NT>
 __device__ __forceinline__ const typename cplx<T>::type* stage_twiddles(

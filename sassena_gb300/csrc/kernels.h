@@ -182,7 +182,8 @@ cudaError_t launch_self_accumulate(const CorrLaunch& a, cudaStream_t st);  // in
 struct FinalEntry {
     int slot_begin, slot_end;  // partial slots of this shell (consecutive)
     size_t part_off;           // offset of slot_begin's partial; slots are `part_len` apart
-    size_t part_len;           // L (autocorrelate) or 2*nf (square/plain) doubles per slot
+    int part_len;              // L (autocorrelate) or 2*nf (square/plain) doubles per slot
+    int f32pair;               // partials are FP32 (Kahan sum, compensation) pairs, not doubles
     int nf, lg;
     double inv_nm;
     double2* fqt;              // [nf]
@@ -204,6 +205,9 @@ cudaError_t launch_finalize(const FinalLaunch& a, cudaStream_t st);
 
 // Shared memory of the FFT accumulate kernels for padded length 2^lg.
 size_t fft_smem_bytes(int precision, int lg, int nf, bool self);
+// Whether the autocorrelation kernels of a launch write their power partials as FP32
+// (sum, compensation) pairs (FinalEntry::f32pair): the FP32 form's CTA-per-series kernels.
+bool corr_writes_f32_pairs(int precision, int dsp, int lg_max);
 
 // ---------------------------------------------------------------------------------------
 // Long series (autocorrelation with padded length 2^14 .. 2^20): four-step FFT through HBM,

@@ -128,6 +128,7 @@ __global__ void noalloc_schedule(const unsigned long long* __restrict__ offs, in
         e.slot_end = (s + 1) * g;
         e.part_off = (size_t)s * g * L;
         e.part_len = L;
+        e.f32pair = 0;  // FP64 partials
         e.nf = nf;
         e.lg = lg;
         e.inv_nm = nm > 0 ? 1.0 / (double)nm : __longlong_as_double(0x7ff8000000000000LL);
