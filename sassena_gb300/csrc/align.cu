@@ -31,8 +31,7 @@
 namespace sassgpu {
 namespace {
 
-constexpr int kPerFrameThreads = 32;   // one thread per frame (small per-frame kernels)
-constexpr int kWarpFrameThreads = 128; // one warp per frame (sums over atom lists)
+constexpr int kPerFrameThreads = 32;  // one thread per frame (small per-frame kernels)
 
 __global__ void pp_promote_kernel(const float* __restrict__ in, size_t n, double* __restrict__ out) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -40,42 +39,55 @@ __global__ void pp_promote_kernel(const float* __restrict__ in, size_t n, double
 }
 
 // com[f] = sum_i m_i r_i / sum_i m_i over the list, r_i = base[f * stride + 3 idx[i]]
-// (idx NULL: i), summed in list order without fused multiply-adds. One warp per frame: the
-// lanes load 32 list entries at a time (coalesced) and form the products m_i r_i; the sums
-// then run through the entries in order (broadcast by shuffles), so every partial sum is the
-// reference's.
-__global__ void pp_com_kernel(const double* __restrict__ base, size_t stride, const size_t* __restrict__ idx,
-                              const double* __restrict__ mass, size_t n, int nf, double* __restrict__ com) {
-    const int f = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-    if (f >= nf) return;
-    const double* fr = base + (size_t)f * stride;
-    double m = 0.0, x = 0.0, y = 0.0, z = 0.0;
-    for (size_t i0 = 0; i0 < n; i0 += 32) {
-        const size_t i = i0 + lane;
-        double mi = 0.0, px = 0.0, py = 0.0, pz = 0.0;
-        if (i < n) {
-            const size_t j = idx ? idx[i] : i;
-            mi = mass[i];
-            px = __dmul_rn(fr[3 * j], mi);
-            py = __dmul_rn(fr[3 * j + 1], mi);
-            pz = __dmul_rn(fr[3 * j + 2], mi);
+// (idx NULL: i), summed in list order without fused multiply-adds, as the reference's loop
+// (center_of_mass.cpp:160-264). One CTA per 32 frames, one frame per lane: tiles of 32 list
+// entries x 32 frames are loaded cooperatively (consecutive threads read consecutive atoms of a
+// frame) and turned into the products m_i r_i in shared memory; then warp w runs accumulator w
+// (m, x, y, z) with lane = frame through the tile in list order.
+constexpr int kComFrames = 32, kComTile = 32, kComThreads = 128;
+
+__global__ void __launch_bounds__(kComThreads) pp_com_kernel(const double* __restrict__ base, size_t stride,
+                                                             const size_t* __restrict__ idx,
+                                                             const double* __restrict__ mass, size_t n, int nf,
+                                                             double* __restrict__ com) {
+    __shared__ double S[4][kComTile][kComFrames + 1];
+    const int f0 = blockIdx.x * kComFrames, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double acc = 0.0;
+    for (size_t i0 = 0; i0 < n; i0 += kComTile) {
+        for (int t = threadIdx.x; t < kComTile * kComFrames; t += kComThreads) {
+            const int e = t % kComTile, fl = t / kComTile;
+            const size_t i = i0 + e;
+            double mi = 0.0, px = 0.0, py = 0.0, pz = 0.0;
+            if (i < n && f0 + fl < nf) {
+                const size_t j = idx ? idx[i] : i;
+                const double* r = base + (size_t)(f0 + fl) * stride + 3 * j;
+                mi = mass[i];
+                px = __dmul_rn(r[0], mi);
+                py = __dmul_rn(r[1], mi);
+                pz = __dmul_rn(r[2], mi);
+            }
+            S[0][e][fl] = mi;
+            S[1][e][fl] = px;
+            S[2][e][fl] = py;
+            S[3][e][fl] = pz;
         }
-        const int cnt = (int)min((size_t)32, n - i0);
-        for (int k = 0; k < cnt; ++k) {
-            m = __dadd_rn(m, __shfl_sync(0xffffffffu, mi, k));
-            x = __dadd_rn(x, __shfl_sync(0xffffffffu, px, k));
-            y = __dadd_rn(y, __shfl_sync(0xffffffffu, py, k));
-            z = __dadd_rn(z, __shfl_sync(0xffffffffu, pz, k));
-        }
+        __syncthreads();
+        const int cnt = (int)min((size_t)kComTile, n - i0);
+        for (int e = 0; e < cnt; ++e) acc = __dadd_rn(acc, S[warp][e][lane]);
+        __syncthreads();
     }
-    if (lane == 0) {
+    S[warp][0][lane] = acc;  // totals: m, x, y, z of frame f0 + lane
+    __syncthreads();
+    const int f = f0 + lane;
+    if (warp == 0 && f < nf) {
         double* o = com + 3 * (size_t)f;
+        const double m = S[0][0][lane];
         if (n == 0) {
             o[0] = o[1] = o[2] = 0.0;
         } else {
-            o[0] = __ddiv_rn(x, m);
-            o[1] = __ddiv_rn(y, m);
-            o[2] = __ddiv_rn(z, m);
+            o[0] = __ddiv_rn(S[1][0][lane], m);
+            o[1] = __ddiv_rn(S[2][0][lane], m);
+            o[2] = __ddiv_rn(S[3][0][lane], m);
         }
     }
 }
@@ -132,38 +144,58 @@ __global__ void pp_gather_kernel(const double* __restrict__ W, size_t nsys, cons
 }
 
 // K[f] = sum_i m_i (u_i v_i^T), u_i = R_i - ref, v_i = C[f][i] - pos[f] (center_of_mass.cpp:79-98),
-// R_i = reference[i] or (NULL) C[f][i]; each element m_i * (u_r * v_c), summed in order. One warp
-// per frame as in pp_com_kernel: lanes form the nine products of 32 entries, the sums run in order.
-__global__ void pp_kmat_kernel(const double* __restrict__ C, const double* __restrict__ ref_xyz,
-                               const double* __restrict__ mass, size_t n, int nf, const double* __restrict__ pos,
-                               const double* __restrict__ ref, int ref_one, double* __restrict__ K) {
-    const int f = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-    if (f >= nf) return;
-    const double* cf = C + (size_t)f * n * 3;
-    const double* rr = ref_xyz ? ref_xyz : cf;
-    const double* pf = pos + 3 * f;
-    const double* qf = ref + 3 * (ref_one ? 0 : f);
-    double k[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (size_t i0 = 0; i0 < n; i0 += 32) {
-        const size_t i = i0 + lane;
-        double t[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-        if (i < n) {
-            const double mi = mass[i];
-            double u[3], v[3];
-            for (int d = 0; d < 3; ++d) {
-                v[d] = __dsub_rn(cf[3 * i + d], pf[d]);
-                u[d] = __dsub_rn(rr[3 * i + d], qf[d]);
+// R_i = reference[i] or (NULL) C[f][i]; each element m_i * (u_r * v_c), summed in order. Layout as
+// pp_com_kernel: tiles of 16 entries x 32 frames of the nine products in shared memory, then warp w
+// runs elements w, w + 4, w + 8 of K with lane = frame.
+constexpr int kKmatTile = 16;
+
+__global__ void __launch_bounds__(kComThreads) pp_kmat_kernel(const double* __restrict__ C, const double* __restrict__ ref_xyz,
+                                                              const double* __restrict__ mass, size_t n, int nf,
+                                                              const double* __restrict__ pos, const double* __restrict__ ref,
+                                                              int ref_one, double* __restrict__ K) {
+    __shared__ double S[9][kKmatTile][kComFrames + 1];
+    const int f0 = blockIdx.x * kComFrames, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (size_t i0 = 0; i0 < n; i0 += kKmatTile) {
+        for (int t = threadIdx.x; t < kKmatTile * kComFrames; t += kComThreads) {
+            const int e = t % kKmatTile, fl = t / kKmatTile;
+            const size_t i = i0 + e;
+            const int f = f0 + fl;
+            double tv[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+            if (i < n && f < nf) {
+                const double* cf = C + ((size_t)f * n + i) * 3;
+                const double* rr = ref_xyz ? ref_xyz + 3 * i : cf;
+                const double* pf = pos + 3 * (size_t)f;
+                const double* qf = ref + 3 * (size_t)(ref_one ? 0 : f);
+                const double mi = mass[i];
+                double u[3], v[3];
+                for (int d = 0; d < 3; ++d) {
+                    v[d] = __dsub_rn(cf[d], pf[d]);
+                    u[d] = __dsub_rn(rr[d], qf[d]);
+                }
+                for (int r = 0; r < 3; ++r)
+                    for (int c = 0; c < 3; ++c) tv[3 * r + c] = __dmul_rn(mi, __dmul_rn(u[r], v[c]));
             }
-            for (int r = 0; r < 3; ++r)
-                for (int c = 0; c < 3; ++c) t[3 * r + c] = __dmul_rn(mi, __dmul_rn(u[r], v[c]));
-        }
-        const int cnt = (int)min((size_t)32, n - i0);
-        for (int s = 0; s < cnt; ++s)
 #pragma unroll
-            for (int e = 0; e < 9; ++e) k[e] = __dadd_rn(k[e], __shfl_sync(0xffffffffu, t[e], s));
+            for (int q = 0; q < 9; ++q) S[q][e][fl] = tv[q];
+        }
+        __syncthreads();
+        const int cnt = (int)min((size_t)kKmatTile, n - i0);
+        for (int e = 0; e < cnt; ++e)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const int q = warp + 4 * k;
+                if (q < 9) acc[k] = __dadd_rn(acc[k], S[q][e][lane]);
+            }
+        __syncthreads();
     }
-    if (lane == 0)
-        for (int e = 0; e < 9; ++e) K[9 * (size_t)f + e] = k[e];
+    const int f = f0 + lane;
+    if (f < nf)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int q = warp + 4 * k;
+            if (q < 9) K[9 * (size_t)f + q] = acc[k];
+        }
 }
 
 // C[f][i] = R[f] (C[f][i] - pos[f]) + ref (center_of_mass.cpp:114-128; ublas prod order).
@@ -417,7 +449,7 @@ extern "C" int sass_stage_frames_prepass(sass_plan* p, const float* frames, size
     double* C = p->pp_C.as<double>();
     const int nfi = (int)nf;
     const unsigned gf = (unsigned)((nf + kPerFrameThreads - 1) / kPerFrameThreads);
-    const unsigned gw = (unsigned)((nf * 32 + kWarpFrameThreads - 1) / kWarpFrameThreads);  // warp per frame
+    const unsigned gw = (unsigned)((nf + 31) / 32);  // the ordered sums: one CTA per 32 frames
     auto L = [&](size_t off) { return reinterpret_cast<const size_t*>(dl + off); };
     auto D = [&](size_t off) { return reinterpret_cast<const double*>(dl + off); };
     std::vector<double> hK(nf * 9), hR(nf * 9);
@@ -430,9 +462,9 @@ extern "C" int sass_stage_frames_prepass(sass_plan* p, const float* frames, size
         const bool ref_one = q.reference != nullptr;
         auto com_ref = [&](double* out) {
             if (ref_one)
-                pp_com_kernel<<<1, 32, 0, st>>>(D(o.refxyz), 0, nullptr, D(o.rmass), nref, 1, out);
+                pp_com_kernel<<<1, kComThreads, 0, st>>>(D(o.refxyz), 0, nullptr, D(o.rmass), nref, 1, out);
             else
-                pp_com_kernel<<<gw, kWarpFrameThreads, 0, st>>>(W, nsys * 3, L(o.ref), D(o.rmass), nref, nfi, out);
+                pp_com_kernel<<<gw, kComThreads, 0, st>>>(W, nsys * 3, L(o.ref), D(o.rmass), nref, nfi, out);
         };
         switch (q.type) {
             case SASS_STEP_CENTER:
@@ -442,7 +474,7 @@ extern "C" int sass_stage_frames_prepass(sass_plan* p, const float* frames, size
                 break;
             case SASS_STEP_FITTRANS:
                 com_ref(va);
-                pp_com_kernel<<<gw, kWarpFrameThreads, 0, st>>>(W, nsys * 3, L(o.sel), D(o.smass), nsel, nfi, vb);
+                pp_com_kernel<<<gw, kComThreads, 0, st>>>(W, nsys * 3, L(o.sel), D(o.smass), nsel, nfi, vb);
                 pp_combine_kernel<<<gf, kPerFrameThreads, 0, st>>>(va, ref_one, vb, 0, 1, nfi, vt);
                 if (nsel) pp_translate_kernel<<<grid_for(nf * nsel, 256), 256, 0, st>>>(W, nsys, L(o.sel), nsel, nfi, vt);
                 break;
@@ -455,16 +487,16 @@ extern "C" int sass_stage_frames_prepass(sass_plan* p, const float* frames, size
             default: {  // FITROTTRANS, FITROT
                 const bool rot_only = q.type == SASS_STEP_FITROT;
                 if (rot_only)  // centre of mass of the moved atoms before the fit
-                    pp_com_kernel<<<gw, kWarpFrameThreads, 0, st>>>(W, nsys * 3, L(o.sel), D(o.smass), nsel, nfi, vc);
+                    pp_com_kernel<<<gw, kComThreads, 0, st>>>(W, nsys * 3, L(o.sel), D(o.smass), nsel, nfi, vc);
                 if (nref) {
                     pp_gather_kernel<<<grid_for(nf * nref * 3, 256), 256, 0, st>>>(W, nsys, L(o.ref), nref, nfi, C);
                     // pos: the copy's centre; ref: the reference structure's (the copy itself when instant)
-                    pp_com_kernel<<<gw, kWarpFrameThreads, 0, st>>>(C, nref * 3, nullptr, D(o.rmass), nref, nfi, vb);
+                    pp_com_kernel<<<gw, kComThreads, 0, st>>>(C, nref * 3, nullptr, D(o.rmass), nref, nfi, vb);
                     if (ref_one)
-                        pp_com_kernel<<<1, 32, 0, st>>>(D(o.refxyz), 0, nullptr, D(o.rmass), nref, 1, va);
+                        pp_com_kernel<<<1, kComThreads, 0, st>>>(D(o.refxyz), 0, nullptr, D(o.rmass), nref, 1, va);
                     else
-                        pp_com_kernel<<<gw, kWarpFrameThreads, 0, st>>>(C, nref * 3, nullptr, D(o.rmass), nref, nfi, va);
-                    pp_kmat_kernel<<<gw, kWarpFrameThreads, 0, st>>>(C, ref_one ? D(o.refxyz) : nullptr, D(o.rmass),
+                        pp_com_kernel<<<gw, kComThreads, 0, st>>>(C, nref * 3, nullptr, D(o.rmass), nref, nfi, va);
+                    pp_kmat_kernel<<<gw, kComThreads, 0, st>>>(C, ref_one ? D(o.refxyz) : nullptr, D(o.rmass),
                                                                      nref, nfi, vb, va, ref_one, vK);
                     PCK(cudaGetLastError());
                     PCK(cudaMemcpyAsync(hK.data(), vK, nf * 9 * sizeof(double), cudaMemcpyDeviceToHost, st));
