@@ -6,9 +6,10 @@
 // The reference works on each frame in FP64 (coor2_t, include/common.hpp:36-39) and stores
 // float32 at the end. Here the whole trajectory is promoted once to an FP64 array
 // W[nf][nsys][3] in HBM and every step runs over all frames at once:
-//   * centres of mass: one thread per frame sums its list sequentially in list order with
-//     separately rounded multiplies and adds (m += m_i; x += x_i * m_i), the reference's
-//     loop in center_of_mass.cpp:160-264, so the centres are the reference's bit for bit;
+//   * centres of mass: each frame's list is summed in list order with separately rounded
+//     multiplies and adds (m += m_i; x += x_i * m_i), the reference's loop in
+//     center_of_mass.cpp:160-264, so the centres are the reference's bit for bit (one lane
+//     per frame over tiles of products staged in shared memory);
 //   * translations and the fit's apply step: one thread per (frame, atom), again with
 //     explicitly rounded operations in the reference's order;
 //   * the fit's 3x3 correlation matrices (center_of_mass.cpp:79-98) are summed per frame on
