@@ -60,8 +60,7 @@ __global__ void __launch_bounds__(NT) corr_fft_kernel(CorrLaunch a) {
     const T2* kbr = reinterpret_cast<const T2*>(sys.kbr);
     PowerAcc<T, MAXR> acc;
     acc.clear();
-    double2 asum = make_double2(0.0, 0.0);
-    double a2sum = 0.0;
+    SeriesAcc<T> sacc;
     __syncthreads();
     for (int v = c.v_begin; v < c.v_end; ++v) {
         const T2* src = reinterpret_cast<const T2*>(sys.A) + (size_t)v * sys.nf;
@@ -74,18 +73,14 @@ __global__ void __launch_bounds__(NT) corr_fft_kernel(CorrLaunch a) {
         __syncthreads();
         dif_tail<T2, NT>(buf, tw, lg, tws);
         const T2 pv = absorb_power_t<T, NT, MAXR>(buf, L, kbr, acc);
-        double2 av = block_sum_t<T, NT>(pv.x, pv.y, red);
-        if (threadIdx.x == 0) {
-            asum.x += av.x;
-            asum.y += av.y;
-            a2sum += av.x * av.x + av.y * av.y;
-        }
+        const T2 av = block_sum_t<T, NT>(pv.x, pv.y, reinterpret_cast<T2*>(red));
+        if (threadIdx.x == 0) sacc.add(av.x, av.y);
     }
     if constexpr (sizeof(T) == 4) write_power_pair<NT, MAXR>(acc, L, a.ppart + c.part_off);
     else write_power<T, NT, MAXR>(acc, L, a.ppart + c.part_off);
     if (threadIdx.x == 0) {
-        a.apart[c.slot] = asum;
-        a.a2part[c.slot] = a2sum;
+        a.apart[c.slot] = sacc.mean_sum();
+        a.a2part[c.slot] = sacc.sq_sum();
     }
 }
 
@@ -110,8 +105,7 @@ __global__ void __launch_bounds__(NT) self_fft_kernel(CorrLaunch a) {
     const int v0 = sys.shell_v[c.shell], v1 = sys.shell_v[c.shell + 1];
     PowerAcc<T, MAXR> acc;
     acc.clear();
-    double2 asum = make_double2(0.0, 0.0);
-    double a2sum = 0.0;
+    SeriesAcc<T> sacc;
     for (int j = c.v_begin; j < c.v_end; ++j) {
         __syncthreads();  // previous atom's series fully consumed
         for (int t = threadIdx.x; t < nf; t += NT) rj[t] = sys.xyz[(size_t)t * sys.na_pad + j];
@@ -129,19 +123,15 @@ __global__ void __launch_bounds__(NT) self_fft_kernel(CorrLaunch a) {
             __syncthreads();
             dif_tail<T2, NT>(buf, tw, lg, tws);
             const T2 pv = absorb_power_t<T, NT, MAXR>(buf, L, kbr, acc);
-            double2 av = block_sum_t<T, NT>(pv.x, pv.y, red);
-            if (threadIdx.x == 0) {
-                asum.x += av.x;
-                asum.y += av.y;
-                a2sum += av.x * av.x + av.y * av.y;
-            }
+            const T2 av = block_sum_t<T, NT>(pv.x, pv.y, reinterpret_cast<T2*>(red));
+            if (threadIdx.x == 0) sacc.add(av.x, av.y);
         }
     }
     if constexpr (sizeof(T) == 4) write_power_pair<NT, MAXR>(acc, L, a.ppart + c.part_off);
     else write_power<T, NT, MAXR>(acc, L, a.ppart + c.part_off);
     if (threadIdx.x == 0) {
-        a.apart[c.slot] = asum;
-        a.a2part[c.slot] = a2sum;
+        a.apart[c.slot] = sacc.mean_sum();
+        a.a2part[c.slot] = sacc.sq_sum();
     }
 }
 
@@ -165,18 +155,6 @@ size_t warp_fft_smem(int lg_max, int nf, bool self) {
     return b;
 }
 
-// Sum over the warp in the form's own precision (a float shuffle moves one word, a
-// double shuffle two), returned in FP64 for the cross-series accumulation.
-template <class T>
-__device__ __forceinline__ double2 warp_sum2(T x, T y) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        x += __shfl_xor_sync(0xffffffffu, x, o);
-        y += __shfl_xor_sync(0xffffffffu, y, o);
-    }
-    return make_double2((double)x, (double)y);
-}
-
 template <class T, bool SELF>
 __global__ void __launch_bounds__(kWarpFftWarps * 32) warp_fft_kernel(CorrLaunch a) {
     typedef typename cplx<T>::type T2;
@@ -198,8 +176,7 @@ __global__ void __launch_bounds__(kWarpFftWarps * 32) warp_fft_kernel(CorrLaunch
     const T2* kbr = reinterpret_cast<const T2*>(sys.kbr);
     PowerAcc<T, MAXR> acc;
     acc.clear();
-    double2 asum = make_double2(0.0, 0.0);
-    double a2sum = 0.0;
+    SeriesAcc<T> sacc;
     __syncthreads();
 
     // one series: folded first DIF stage on load, the other stages, power + K-weighted sum
@@ -235,12 +212,8 @@ __global__ void __launch_bounds__(kWarpFftWarps * 32) warp_fft_kernel(CorrLaunch
                 ay += P * k.y;
             }
         }
-        const double2 av = warp_sum2<T>(ax, ay);
-        if (lane == 0) {
-            asum.x += av.x;
-            asum.y += av.y;
-            a2sum += av.x * av.x + av.y * av.y;
-        }
+        const T2 av = warp_sum_t<T>(ax, ay);
+        if (lane == 0) sacc.add(av.x, av.y);
         __syncwarp();  // the buffer is free for the next series
     };
 
@@ -274,8 +247,8 @@ __global__ void __launch_bounds__(kWarpFftWarps * 32) warp_fft_kernel(CorrLaunch
         if (i < L) pw[(size_t)warp * L + i] = acc.get(r);
     }
     if (lane == 0) {
-        red[warp] = asum;
-        red2[warp] = a2sum;
+        red[warp] = sacc.mean_sum();
+        red2[warp] = sacc.sq_sum();
     }
     __syncthreads();
     double* dst = a.ppart + c.part_off;
@@ -675,8 +648,7 @@ __global__ void __launch_bounds__(kWarpFftWarps * 32, (LG <= 8 && sizeof(T) == 4
     const T2* kbr = reinterpret_cast<const T2*>(sys.kbr);
     PowerAcc<T, E> acc;
     acc.clear();
-    double2 asum = make_double2(0.0, 0.0);
-    double a2sum = 0.0;
+    SeriesAcc<T> sacc;
     __syncthreads();
 
     auto transform = [&](auto gen) {
@@ -728,12 +700,8 @@ __global__ void __launch_bounds__(kWarpFftWarps * 32, (LG <= 8 && sizeof(T) == 4
             ax += P * kv.x;
             ay += P * kv.y;
         }
-        const double2 av = warp_sum2<T>(ax, ay);
-        if (lane == 0) {
-            asum.x += av.x;
-            asum.y += av.y;
-            a2sum += av.x * av.x + av.y * av.y;
-        }
+        const T2 av = warp_sum_t<T>(ax, ay);
+        if (lane == 0) sacc.add(av.x, av.y);
     };
 
     if (SELF) {
@@ -772,8 +740,8 @@ __global__ void __launch_bounds__(kWarpFftWarps * 32, (LG <= 8 && sizeof(T) == 4
 #pragma unroll
     for (int m = 0; m < E; ++m) pw[(size_t)warp * L + lane + 32 * m] = acc.get(m);
     if (lane == 0) {
-        red[warp] = asum;
-        red2[warp] = a2sum;
+        red[warp] = sacc.mean_sum();
+        red2[warp] = sacc.sq_sum();
     }
     __syncthreads();
     double* dst = a.ppart + c.part_off;

@@ -145,20 +145,29 @@ __device__ __forceinline__ void load_q(const double* q, T& qx, T& qy, T& qz) {
     }
 }
 
-// Sum of (x, y) over the CTA; valid in thread 0. The warp stage runs in T (FP32 in the FP32
-// form: GB300's FP64 pipe is a narrow fraction of its FP32 pipe), the sum of the warp totals in
-// FP64. Ends with a barrier so the caller may reuse shared memory afterwards.
+// Sum of (x, y) over the CTA in T, valid in thread 0 (FP32 in the FP32 form: GB300's FP64 pipe
+// is a narrow fraction of its FP32 pipe, and a warp instruction occupies it whole even with one
+// active lane). `red` holds NT / 32 pairs of T. Ends with a barrier so the caller may reuse
+// shared memory afterwards.
 template <class T, int NT>
-__device__ double2 block_sum_t(T x, T y, double2* red) {
+__device__ typename cplx<T>::type block_sum_t(T x, T y, typename cplx<T>::type* red) {
+    typedef typename cplx<T>::type T2;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         x += __shfl_xor_sync(0xffffffffu, x, o);
         y += __shfl_xor_sync(0xffffffffu, y, o);
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) red[warp] = make_double2((double)x, (double)y);
+    if (lane == 0) {
+        T2 v;
+        v.x = x;
+        v.y = y;
+        red[warp] = v;
+    }
     __syncthreads();
-    double2 s = make_double2(0.0, 0.0);
+    T2 s;
+    s.x = 0;
+    s.y = 0;
     if (threadIdx.x == 0)
         for (int w = 0; w < NT / 32; ++w) {
             s.x += red[w].x;
@@ -167,6 +176,55 @@ __device__ double2 block_sum_t(T x, T y, double2* red) {
     __syncthreads();
     return s;
 }
+
+// Sum of (x, y) over the warp in T, valid in every lane.
+template <class T>
+__device__ __forceinline__ typename cplx<T>::type warp_sum_t(T x, T y) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        x += __shfl_xor_sync(0xffffffffu, x, o);
+        y += __shfl_xor_sync(0xffffffffu, y, o);
+    }
+    typename cplx<T>::type v;
+    v.x = x;
+    v.y = y;
+    return v;
+}
+
+// Per-series bookkeeping of the afinal / a2final partials: the sum of the series means and of
+// their squared moduli. FP32 form: Kahan-compensated FP32, converted once at the end; FP64
+// form: plain FP64.
+template <class T>
+struct SeriesAcc;
+
+template <>
+struct SeriesAcc<float> {
+    float sx = 0.f, sy = 0.f, s2 = 0.f, cx = 0.f, cy = 0.f, c2 = 0.f;
+    __device__ static void kahan(float& s, float& c, float v) {
+        const float y = __fsub_rn(v, c), t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    }
+    __device__ void add(float x, float y) {
+        kahan(sx, cx, x);
+        kahan(sy, cy, y);
+        kahan(s2, c2, fmaf(x, x, y * y));
+    }
+    __device__ double2 mean_sum() const { return make_double2((double)sx - (double)cx, (double)sy - (double)cy); }
+    __device__ double sq_sum() const { return (double)s2 - (double)c2; }
+};
+
+template <>
+struct SeriesAcc<double> {
+    double sx = 0.0, sy = 0.0, s2 = 0.0;
+    __device__ void add(double x, double y) {
+        sx += x;
+        sy += y;
+        s2 += x * x + y * y;
+    }
+    __device__ double2 mean_sum() const { return make_double2(sx, sy); }
+    __device__ double sq_sum() const { return s2; }
+};
 
 // Power spectrum of the series in buf (bit-reversed order): accumulate P and return this
 // thread's part of sum_w P(w) K(w) in T (reduce it with block_sum_t).
