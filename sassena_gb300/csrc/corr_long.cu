@@ -236,7 +236,7 @@ __global__ void long_self_series_kernel(LongSelfArgs a) {
         const int s = (int)(idx / a.nf), t = (int)(idx - (size_t)s * a.nf);
         const int p = a.p0 + s, j = p / a.nm, m = p - j * a.nm;
         T qx, qy, qz;
-        load_q(a.qv + 3 * (size_t)m, qx, qy, qz);
+        load_qv(a.qv, a.qrev, (size_t)m, qx, qy, qz);
         G[idx] = self_term(b[j], a.xyz[(size_t)t * a.na_pad + j], qx, qy, qz);
     }
 }

@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(NT) self_fft_kernel(CorrLaunch a) {
         __syncthreads();
         for (int v = v0; v < v1; ++v) {
             T qx, qy, qz;
-            load_q(sys.qv + 3 * (size_t)v, qx, qy, qz);
+            load_qv(sys.qv, sys.qrev, (size_t)v, qx, qy, qz);
             for (int p = threadIdx.x; p < half; p += NT) {
                 T2 x = zero2<T2>();
                 if (p < nf) x = self_term(b, rj[p], qx, qy, qz);
@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(kWarpFftWarps * 32) warp_fft_kernel(CorrLaunch
             __syncthreads();
             for (int v = v0 + warp; v < v1; v += NW) {
                 T qx, qy, qz;
-                load_q(sys.qv + 3 * (size_t)v, qx, qy, qz);
+                load_qv(sys.qv, sys.qrev, (size_t)v, qx, qy, qz);
                 transform([&](int p) { return self_term(b, rj[p], qx, qy, qz); });
             }
         }
@@ -385,7 +385,7 @@ __global__ void __launch_bounds__(NT) self_direct_kernel(CorrLaunch a) {
                 double2 ph = make_double2(1.0, 0.0);
                 if (!square && a.restore_phase) sincos(q[0] * sys.cx + q[1] * sys.cy + q[2] * sys.cz, &ph.y, &ph.x);
                 T qx, qy, qz;
-                load_q(q, qx, qy, qz);
+                load_qv(sys.qv, sys.qrev, (size_t)v, qx, qy, qz);
                 double2 part = make_double2(0.0, 0.0);
                 for (int t = threadIdx.x; t < nf; t += NT) {
                     T2 x = self_term(b, sys.xyz[(size_t)t * sys.na_pad + j], qx, qy, qz);
@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(NT) self_direct_kernel(CorrLaunch a) {
             double2 ph = make_double2(1.0, 0.0);
             if (!square && a.restore_phase) sincos(q[0] * sys.cx + q[1] * sys.cy + q[2] * sys.cz, &ph.y, &ph.x);
             T qx, qy, qz;
-            load_q(q, qx, qy, qz);
+            load_qv(sys.qv, sys.qrev, (size_t)v, qx, qy, qz);
             double2 part = make_double2(0.0, 0.0);
 #pragma unroll
             for (int r = 0; r < MAXT; ++r) {
@@ -723,7 +723,7 @@ __global__ void __launch_bounds__(kWarpFftWarps * 32, (LG <= 8 && sizeof(T) == 4
             for (int pr = warp; pr < na * nd; pr += NW) {
                 const int at = pr / nd, v = v0 + (pr - at * nd);
                 T qx, qy, qz;
-                load_q(sys.qv + 3 * (size_t)v, qx, qy, qz);
+                load_qv(sys.qv, sys.qrev, (size_t)v, qx, qy, qz);
                 const T b = bsm[at];
                 const float4* ra = rj + (size_t)at * nf;
                 transform([&](int p) { return self_term(b, ra[p], qx, qy, qz); });
@@ -825,6 +825,19 @@ cudaError_t launch_accumulate(const CorrLaunch& a, bool self, cudaStream_t st) {
 bool corr_writes_f32_pairs(int precision, int dsp, int lg_max) {
     // the CTA-per-series kernels (padded length above the warp forms') in the FP32 form
     return precision == PREC_FP32 && dsp == DSP_AUTOCORRELATE && lg_max > kWarpFftMaxLg;
+}
+
+__global__ void q_revolutions_kernel(const double* __restrict__ qv, size_t nv, float4* __restrict__ out) {
+    const double inv2pi = 0.15915494309189533577;
+    for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < nv; v += (size_t)gridDim.x * blockDim.x)
+        out[v] = make_float4((float)(qv[3 * v] * inv2pi), (float)(qv[3 * v + 1] * inv2pi), (float)(qv[3 * v + 2] * inv2pi),
+                             0.f);
+}
+
+cudaError_t launch_q_revolutions(const double* qv, size_t nv, float4* out, cudaStream_t st) {
+    if (nv == 0) return cudaSuccess;
+    q_revolutions_kernel<<<grid_for(nv, 256), 256, 0, st>>>(qv, nv, out);
+    return cudaGetLastError();
 }
 
 size_t fft_smem_bytes(int precision, int lg, int nf, bool self) {

@@ -463,6 +463,15 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
     if (coherent) ECK(amp_.ensure(amp_bytes));
     if (part_bytes) ECK(part_.ensure(part_bytes));
 
+    // FP32 form: sub-vectors in revolutions, one table per call (filled in enqueue)
+    qrev_off_.assign(items.size(), 0);
+    size_t qrev_total = 0;
+    for (size_t i = 0; i < items.size(); ++i) {
+        qrev_off_[i] = qrev_total;
+        qrev_total += items[i].offs.back();
+    }
+    if (f32) ECK(qrev_.ensure(std::max<size_t>(1, qrev_total) * sizeof(float4)));
+
     // ---- phase-sum descriptors -------------------------------------------------------------
     std::vector<PhaseSystem> psys(items.size());
     std::vector<PhaseTileDesc> tiles;
@@ -544,6 +553,7 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
         c.qv = it.d_qv;
         c.shell_v = nullptr;  // patched after upload
         c.kbr = f32 ? (const void*)s.k32.p : (const void*)s.k64.p;
+        c.qrev = f32 ? qrev_.as<float4>() + qrev_off_[i] : nullptr;
         c.cx = s.center[0];
         c.cy = s.center[1];
         c.cz = s.center[2];
@@ -868,6 +878,12 @@ int Engine::enqueue(cudaStream_t st, std::string& err, cudaEvent_t* ev) {
         }
     }
     if (ev) ECK(cudaEventRecord(ev[1], st));
+    if (f32)
+        for (int i = 0; i < nitems_; ++i)
+            if (item_qv_[i]) {
+                ECK(launch_q_revolutions(item_qv_[i], item_offs_[i].back(), qrev_.as<float4>() + qrev_off_[i], st));
+                ++launches;
+            }
     CorrLaunch cl{};
     cl.precision = cfg_.precision;
     cl.dsp = cfg_.dsp;
@@ -910,6 +926,7 @@ int Engine::enqueue(cudaStream_t st, std::string& err, cudaEvent_t* ev) {
                 g.xyz = s.xyz.as<float4>();
                 g.bfac = bfac_.as<unsigned char>() + bfac_off_[li.item] + (size_t)lb.shell * s.na_pad * (f32 ? 4 : 8);
                 g.qv = item_qv_[li.item] + 3 * item_offs_[li.item][lb.shell];
+                g.qrev = f32 ? qrev_.as<float4>() + qrev_off_[li.item] + item_offs_[li.item][lb.shell] : nullptr;
                 g.G = long_G_.p;
                 ECK(launch_long_self_series(g, st));
                 ++launches;

@@ -176,7 +176,8 @@ private:
     std::vector<const double*> item_qv_;
     CorrChunk* d_long_chunks_ = nullptr;
     FinalEntry* d_long_entries_ = nullptr;
-    DevBuf long_Y_, long_mpart_, long_Z_, long_G_;
+    DevBuf long_Y_, long_mpart_, long_Z_, long_G_, qrev_;
+    std::vector<size_t> qrev_off_;
 };
 
 // HBM scratch for the column-pass output of one batch of long series.

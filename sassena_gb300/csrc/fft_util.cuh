@@ -131,6 +131,23 @@ __device__ __forceinline__ float2 self_term(float b, float4 r, float qx, float q
     return make_float2(b * c, b * s);
 }
 
+// The sub-vector v of a system in the form's units: FP32 from the per-call table in
+// revolutions, FP64 as given.
+__device__ __forceinline__ void load_qv(const double* qv, const float4* qrev, size_t v, float& qx, float& qy,
+                                        float& qz) {
+    const float4 r = qrev[v];
+    qx = r.x;
+    qy = r.y;
+    qz = r.z;
+}
+__device__ __forceinline__ void load_qv(const double* qv, const float4* qrev, size_t v, double& qx, double& qy,
+                                        double& qz) {
+    const double* q = qv + 3 * v;
+    qx = q[0];
+    qy = q[1];
+    qz = q[2];
+}
+
 template <class T>
 __device__ __forceinline__ void load_q(const double* q, T& qx, T& qy, T& qz) {
     if (sizeof(T) == 4) {  // FP32 form: revolutions per Angstrom

@@ -146,9 +146,14 @@ struct CorrSystem {
     const double* qv;       // sub-vectors [nv][3]
     const int* shell_v;     // [nshell+1] sub-vector offsets of each shell
     const void* kbr;        // [L] bit-reversed store kernel: float2 (FP32) or double2 (FP64)
+    const float4* qrev;     // FP32 form: sub-vectors in revolutions (q / 2 pi) [nv]
     double cx, cy, cz;      // frame centre (FP32 form) for the plain-dsp phase restore
     int nf, lg, na_pad;
 };
+
+// FP32 form: out[v] = (float)(q[v] / 2 pi) once per call, so that the series kernels read the
+// sub-vectors they need per (atom, direction) pair without FP64 conversions.
+cudaError_t launch_q_revolutions(const double* qv, size_t nv, float4* out, cudaStream_t st);
 
 // Work unit: series [v_begin, v_end) (coherent) or atoms [v_begin, v_end) with all the
 // shell's directions (incoherent) of one shell of one system, into one partial slot.
@@ -243,6 +248,7 @@ struct LongSelfArgs {
     const float4* xyz;         // [nf][na_pad]
     const void* bfac;          // the shell's factor row [na_pad] (T)
     const double* qv;          // the shell's q-vectors [nm][3]
+    const float4* qrev;        // FP32 form: the same in revolutions [nm]
     void* G;                   // [nseries][nf] T2
 };
 cudaError_t launch_long_self_series(const LongSelfArgs& a, cudaStream_t st);

@@ -145,6 +145,7 @@ __global__ void noalloc_schedule(const unsigned long long* __restrict__ offs, in
         y.qv = nullptr;
         y.shell_v = nullptr;
         y.kbr = kbr;
+        y.qrev = nullptr;  // FP64 only
         y.cx = y.cy = y.cz = 0.0;
         y.nf = nf;
         y.lg = lg;
