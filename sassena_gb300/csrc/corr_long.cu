@@ -280,6 +280,7 @@ cudaError_t launch_long_columns(const LongArgs& a, cudaStream_t st) {
 cudaError_t launch_long_rows(const LongArgs& a, cudaStream_t st) {
     if (!long_ok(a.lg)) return cudaErrorInvalidValue;
     if (a.nchunks == 0) return cudaSuccess;
+    if (a.nchunks > 65535) return cudaErrorInvalidValue;  // grid y: the engine's batches hold fewer
     const size_t sm = long_row_smem(a.precision);
     dim3 grid((unsigned)(1 << (a.lg - kLongRowLg)), (unsigned)a.nchunks);
     if (a.precision == PREC_FP32) {
@@ -327,15 +328,21 @@ cudaError_t launch_long_finalize(const LongFinal& a, cudaStream_t st) {
     if (!long_ok(a.lg)) return cudaErrorInvalidValue;
     const int R = 1 << (a.lg - kLongRowLg);
     const size_t sm_rows = (size_t)kLongC * sizeof(double2);
+    const size_t sm_cols = long_col_smem(PREC_FP64, a.lg);
     cudaError_t e = set_smem(long_final_rows_kernel, sm_rows);
     if (e != cudaSuccess) return e;
-    long_final_rows_kernel<<<dim3((unsigned)R, (unsigned)a.nentries), kLongNT, sm_rows, st>>>(a);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    const size_t sm_cols = long_col_smem(PREC_FP64, a.lg);
-    e = set_smem(long_final_cols_kernel, sm_cols);
-    if (e != cudaSuccess) return e;
-    long_final_cols_kernel<<<dim3(kLongC / kLongTile, (unsigned)a.nentries), kLongNT, sm_cols, st>>>(a);
-    return cudaGetLastError();
+    if ((e = set_smem(long_final_cols_kernel, sm_cols)) != cudaSuccess) return e;
+    for (int e0 = 0; e0 < a.nentries; e0 += 65535) {  // entries in grid y, at most 65,535 per launch
+        LongFinal b = a;
+        b.entries = a.entries + e0;
+        b.nentries = std::min(65535, a.nentries - e0);
+        b.Z = a.Z + (size_t)e0 * ((size_t)1 << a.lg);
+        long_final_rows_kernel<<<dim3((unsigned)R, (unsigned)b.nentries), kLongNT, sm_rows, st>>>(b);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        long_final_cols_kernel<<<dim3(kLongC / kLongTile, (unsigned)b.nentries), kLongNT, sm_cols, st>>>(b);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_long_store_kernel(const double2* tw64, int lg, int nf, double2* scratch, double2* k64,

@@ -745,7 +745,7 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
         for (size_t sh = 0; sh < nq; ++sh) shell_first[sh + 1] = shell_first[sh] + s.na * (it.offs[sh + 1] - it.offs[sh]);
         for (size_t cb = 0; cb < ic.size();) {
             size_t ce = cb + 1;
-            while (ce < ic.size() && (size_t)(ic[ce].v_end - ic[cb].v_begin) <= S &&
+            while (ce < ic.size() && (size_t)(ic[ce].v_end - ic[cb].v_begin) <= S && ce - cb < 65535 &&
                    (coherent || ic[ce].shell == ic[cb].shell))
                 ++ce;
             LongBatch b{(int)i, ic[cb].v_begin, ic[ce - 1].v_end, li.chunk_begin + (int)cb, li.chunk_begin + (int)ce,

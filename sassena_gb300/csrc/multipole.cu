@@ -443,6 +443,7 @@ struct MpCylinder {
     const int* mom;      // [nmom][2]
     double2* A;          // [nq][nmom][nf]
     int na_pad, na, nclass, nq, N, nmom, nf;
+    int f0;              // first frame of the launch (blockIdx.y counts from it)
 };
 
 // One CTA per (frame, block of kCylQB q-vectors), kCylThreads threads, tiles of kCylTA atoms.
@@ -454,7 +455,7 @@ static_assert(kCylQB * kCylTA + kCylTA <= kCylThreads, "tile roles exceed the CT
 
 __global__ void __launch_bounds__(kCylThreads) mp_cylinder_kernel(MpCylinder a) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const int f = blockIdx.y, q0 = blockIdx.x * kCylQB, nqb = min(kCylQB, a.nq - q0);
+    const int f = a.f0 + blockIdx.y, q0 = blockIdx.x * kCylQB, nqb = min(kCylQB, a.nq - q0);
     const int N = a.N, W = N + 1, ntask = nqb * 2 * W;
     double* Jn = reinterpret_cast<double*>(smem);                         // [QB][W][TA]
     double* cn = Jn + (size_t)kCylQB * W * kCylTA;                          // [W][TA]
@@ -722,7 +723,7 @@ extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const d
         MCK(cudaMemGetInfo(&free_b, &total_b));
         const size_t budget = std::max<size_t>((size_t)1 << 28, std::min<size_t>((size_t)16 << 30, free_b / 4));
         const size_t per_frame = na_pad * (nq * (L + 1) * sizeof(double) + nmom * sizeof(double2));
-        const size_t nfb = std::max<size_t>(1, std::min<size_t>(nf, budget / per_frame));
+        const size_t nfb = std::max<size_t>(1, std::min<size_t>({nf, budget / per_frame, (size_t)65535}));  // grid y
         const int ncf = (L + 1) * (L + 2) / 2;
         MCK(p->mp_ycf.ensure((size_t)(ncf + L + 1) * sizeof(double2)));
         ylm_coeff_kernel<<<(ncf + 127) / 128, 128, 0, st>>>(L, p->mp_ycf.as<double2>(), p->mp_ycf.as<double2>() + ncf);
@@ -800,9 +801,13 @@ extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const d
         ca.nf = (int)nf;
         const size_t sm = cylinder_smem(2 * L);
         if (sm > 48 * 1024) MCK(cudaFuncSetAttribute(mp_cylinder_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        mp_cylinder_kernel<<<dim3((unsigned)((nq + kCylQB - 1) / kCylQB), (unsigned)nf), kCylThreads, sm, st>>>(ca);
-        MCK(cudaGetLastError());
-        ++launches;
+        for (size_t f0 = 0; f0 < nf; f0 += 65535) {  // frames in grid y, at most 65,535 per launch
+            ca.f0 = (int)f0;
+            const unsigned nfl = (unsigned)std::min<size_t>(65535, nf - f0);
+            mp_cylinder_kernel<<<dim3((unsigned)((nq + kCylQB - 1) / kCylQB), nfl), kCylThreads, sm, st>>>(ca);
+            MCK(cudaGetLastError());
+            ++launches;
+        }
     }
     const size_t phase_launches = launches;
     // correlation and average of the amplitudes: moments play the sub-vectors

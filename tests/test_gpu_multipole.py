@@ -88,3 +88,12 @@ def test_errors(native_lib):
             with pytest.raises(abi.SassError) as e:
                 p.multipole(kind, q, w.class_factors, mom)
             assert e.value.code == 1  # SASS_ERR_ARG
+
+
+@pytest.mark.parametrize("kind", ["sphere", "cylinder"])
+def test_more_frames_than_one_grid_dimension(native_lib, kind):
+    # 70,000 frames: the cylinder launches frames in chunks of 65,535 (grid y), the sphere
+    # batches at most 65,535 frames per basis, and the correlation takes the long path
+    w, q = case(56, na=5, nf=70000, nq=1, box=6.0)
+    moments = oracle.sphere_moments(1) if kind == "sphere" else oracle.cylinder_moments(1)
+    check(w, q, kind, moments, axis=(0.2, 0.1, 1.0))
