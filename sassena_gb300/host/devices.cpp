@@ -292,6 +292,18 @@ bool run_scatter_device(const Params& p, Database& db, const Sample& s, RunStats
             check(plan, sass_compute(plan, nq, offs.data(), sv.data(), cf.data(), fqt.data(), fq.data(), fq2.data(), 0),
                   "sass_compute");
         st.compute_s += now_s() - tc;
+        if (!multipole) {  // which phase kernel ran (sd:compute schedule)
+            sass_schedule sch{};
+            if (sass_plan_schedule(plan, &sch) == SASS_OK) {
+                if (sch.rec_shells_per_lane > 0)
+                    info("Phase sum: shell recurrence on " + std::to_string(sch.rec_shells) + " q-vectors (" +
+                         std::to_string(sch.rec_shells_per_lane) + " shells per lane), direct kernel on " +
+                         std::to_string(sch.direct_tiles) + " tiles");
+                else
+                    info("Phase sum: direct kernel, " + std::to_string(sch.direct_tiles) + " tiles of " +
+                         std::to_string(sch.q_per_lane) + " q-vectors per lane");
+            }
+        }
         st.nsub += offs.back();
         st.terms += (double)offs.back() * (double)na * (double)nf;
         // rows in completion order (HDF5WriterClient::write, file_writer_service.cpp:504-531)

@@ -143,3 +143,26 @@ def test_driver_multipole_matches_oracle(native_lib, tmp_path, kind, resolution,
     assert err <= 1e-12, err
     assert np.array_equal(fq0, fqt[:, 0])
     assert np.allclose(fq, (ref[1][:, 0] + 1j * ref[1][:, 1])[order], rtol=1e-12, atol=1e-14)
+
+
+def test_driver_fp32_linear_scan(native_lib, tmp_path):
+    # a linear scan with a file orientation set: every |q| shares the direction set, so the
+    # FP32 form takes the shell-recurrence kernel through the driver (no caller-side change)
+    w = small("all", "autocorrelate", seed=55, na=120, nf=24, nq=1, nm=12)
+    d = str(tmp_path / "run")
+    cfg = synth.write_files(d, w, precision="fp32")
+    txt = open(cfg).read().replace(
+        "<vectors><type>file</type><file>qvectors.txt</file></vectors>",
+        "<vectors><type>scans</type><scans><scan><base><x>1</x><y>0</y><z>0</z></base>"
+        "<from>0.2</from><to>2.2</to><points>9</points></scan></scans></vectors>")
+    open(cfg, "w").write(txt)
+    r = run(cfg)
+    q, fqt, *_ = read_rows(os.path.join(d, "signal.h5"))
+    lengths = np.linalg.norm(q, axis=1)
+    sv = (lengths[:, None, None] * w.directions[None]).reshape(-1, 3)
+    offs = np.arange(len(q) + 1, dtype=np.uintp) * w.nm
+    fac = np.repeat(w.factors()[:1], len(q), axis=0)
+    ref = oracle.all_vectors(w.coords, offs, sv, fac, 0, 0, nthreads=8)
+    rfqt = ref[0][..., 0] + 1j * ref[0][..., 1]
+    assert (np.abs(fqt - rfqt).max(axis=1) / np.abs(rfqt[:, 0])).max() <= 1e-3
+    assert "recurrence" in r.stderr
