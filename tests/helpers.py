@@ -1,4 +1,6 @@
 """Shared helpers for the parity tests."""
+import os
+
 import numpy as np
 
 
@@ -23,3 +25,46 @@ def rel_err_vec(x, ref):
     ref = np.asarray(ref)
     scale = max(np.max(np.abs(ref)), 1e-300)
     return np.max(np.abs(x - ref)) / scale
+
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+class Fixture:
+    """One case of a golden .npz (arrays named "<case>.<field>"), with the workload rebuilt."""
+
+    def __init__(self, z, name):
+        self.name = name
+        g = lambda k: z[name + "." + k]  # noqa: E731
+        self.scattering, self.dsp, self.method = str(g("kind")).split("/")
+        self.coords = g("coords")
+        self.atom_class = g("atom_class")
+        self.class_factors = g("class_factors")
+        self.shells = g("shells")
+        self.directions = g("directions")
+        self.fqt, self.fq, self.fq2 = g("fqt"), g("fq"), g("fq2")
+        self.extra = {k.split(".", 1)[1]: z[k] for k in z.files if k.startswith(name + ".")}
+
+    @property
+    def na(self):
+        return self.coords.shape[1]
+
+    @property
+    def nf(self):
+        return self.coords.shape[0]
+
+    def sub_offsets(self):
+        return np.arange(len(self.shells) + 1, dtype=np.uintp) * len(self.directions)
+
+    def subvectors(self):
+        return (self.shells[:, None, None] * self.directions[None]).reshape(-1, 3)
+
+    def factors(self):
+        return self.class_factors[:, self.atom_class]
+
+
+def golden(family):
+    """{case: Fixture} of tests/golden/<family>.npz."""
+    z = np.load(os.path.join(GOLDEN, family + ".npz"))
+    names = sorted({k.split(".", 1)[0] for k in z.files if k.endswith(".fqt")})
+    return {n: Fixture(z, n) for n in names}

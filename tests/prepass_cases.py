@@ -5,11 +5,13 @@ Each case writes a small system (40 atoms, 7 frames of a random walk that also r
 drifts, so fits have work to do) with the driver's files, and describes the same steps in
 the terms of oracle.alignment.load (selections as index lists, references as full frames).
 """
+import json
 import os
+import subprocess
 
 import numpy as np
 
-from sassena_gb300 import synth
+from sassena_gb300 import abi, synth
 
 NA, NF = 40, 7
 MASSES = [1.008, 12.011, 14.007, 15.999]  # per class H, C, N, O
@@ -147,3 +149,25 @@ def build(name, directory):
     masses = np.array(MASSES)[w.atom_class]
     return w, cfg, dict(alignments=o_al, motions=o_mo, target=sel[target] if target else None,
                         masses=masses)
+
+
+STEP_TYPES = {0: "center", 1: "fittrans", 2: "fitrottrans", 3: "fitrot", 4: "motion"}
+
+
+def host_steps(cfg, out_json):
+    """The pre-pass steps and masses sassena-gpu builds for `cfg` (its --dry-run JSON), in the
+    terms of abi.Plan.stage_prepass."""
+    r = subprocess.run([abi.DRIVER_PATH, "--config", cfg, "--dry-run", out_json], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    j = json.load(open(out_json))
+    steps = []
+    for s in j["prepass"]:
+        d = {"type": STEP_TYPES[s["type"]], "selection": s["selection"],
+             "reference_selection": s["reference_selection"], "fit_target": s["fit_target"],
+             "fit_source": s["fit_source"]}
+        if s["reference"]:
+            d["reference"] = np.reshape(s["reference"], (-1, 3))
+        if s["translations"]:
+            d["translations"] = np.reshape(s["translations"], (-1, 3))
+        steps.append(d)
+    return steps, np.array(j["masses"])

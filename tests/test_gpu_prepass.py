@@ -5,7 +5,6 @@ translations and motions are summed in the reference's order, so those frames ar
 bit for bit; fits go through an SVD (LAPACK in the oracle, Jacobi here), so they may differ
 by one float32 ulp. End to end, the driver's S(q,t) for aligned configurations matches the
 FP64 oracle run on the oracle's aligned frames (bar 1e-12)."""
-import json
 import os
 import subprocess
 
@@ -25,21 +24,7 @@ FITS = {"fitrottrans", "fitrot_file", "fit_instant", "pre_post"}
 
 
 def host_steps(cfg, tmp_path):
-    out = str(tmp_path / "dry.json")
-    r = subprocess.run([abi.DRIVER_PATH, "--config", cfg, "--dry-run", out], capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr
-    j = json.load(open(out))
-    types = {0: "center", 1: "fittrans", 2: "fitrottrans", 3: "fitrot", 4: "motion"}
-    steps = []
-    for s in j["prepass"]:
-        d = {"type": types[s["type"]], "selection": s["selection"], "reference_selection": s["reference_selection"],
-             "fit_target": s["fit_target"], "fit_source": s["fit_source"]}
-        if s["reference"]:
-            d["reference"] = np.reshape(s["reference"], (-1, 3))
-        if s["translations"]:
-            d["translations"] = np.reshape(s["translations"], (-1, 3))
-        steps.append(d)
-    return steps, np.array(j["masses"])
+    return pc.host_steps(cfg, str(tmp_path / "dry.json"))
 
 
 @pytest.mark.parametrize("name", pc.CASES)
