@@ -553,7 +553,8 @@ __global__ void store_kernel_kernel(const double2* __restrict__ tw, int lg_tw, d
 }
 
 __global__ void stage_kernel(const float* __restrict__ raw, int nf, int na, int na_pad, double cx,
-                             double cy, double cz, int center, float4* __restrict__ xyz) {
+                             double cy, double cz, int center, float4* __restrict__ xyz,
+                             const int* __restrict__ rec_inv, int na_rec, float4* __restrict__ xyz_rec) {
     const size_t n = (size_t)nf * na_pad;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
          idx += (size_t)gridDim.x * blockDim.x) {
@@ -571,6 +572,7 @@ __global__ void stage_kernel(const float* __restrict__ raw, int nf, int na, int 
                 r.y = p[1];
                 r.z = p[2];
             }
+            if (xyz_rec) xyz_rec[f * na_rec + rec_inv[j]] = make_float4(r.x, r.y, r.z, 1.f);
         }
         xyz[idx] = r;
     }
@@ -874,9 +876,11 @@ cudaError_t launch_store_kernel(const double2* tw64, int lg_tw, double2* k64, fl
 }
 
 cudaError_t launch_stage(const float* raw, int nf, int na, int na_pad, double cx, double cy,
-                         double cz, int center, float4* xyz, cudaStream_t st) {
+                         double cz, int center, float4* xyz, const int* rec_inv, int na_rec,
+                         float4* xyz_rec, cudaStream_t st) {
     size_t n = (size_t)nf * na_pad;
-    stage_kernel<<<grid_for(n, 256), 256, 0, st>>>(raw, nf, na, na_pad, cx, cy, cz, center, xyz);
+    stage_kernel<<<grid_for(n, 256), 256, 0, st>>>(raw, nf, na, na_pad, cx, cy, cz, center, xyz, rec_inv,
+                                                   na_rec, xyz_rec);
     return cudaGetLastError();
 }
 

@@ -107,6 +107,29 @@ int build_system_tables(SystemState& s, cudaStream_t st, std::string& err) {
     return kOk;
 }
 
+// The address under which the device reads host memory `h` in place, or nullptr: the
+// device alias of pinned or registered memory, managed memory as is, and any other host
+// pointer where the device reads pageable memory through the host's page tables (Grace
+// with address translation over NVLink-C2C). Reading in place fuses the transfer with
+// the conversion; the link bounds both equally (about 209 GB/s measured on a GB300,
+// copy engine and SM loads alike).
+static const float* device_view(const float* h, int device) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost) return reinterpret_cast<const float*>(a.devicePointer);
+    if (a.type == cudaMemoryTypeManaged) return h;
+    if (a.type == cudaMemoryTypeDevice) return nullptr;
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return pageable ? h : nullptr;
+}
+
 int stage_system(SystemState& s, const float* coords, bool on_device, int precision, cudaStream_t st,
                  std::string& err) {
     if (!coords) {
@@ -114,12 +137,19 @@ int stage_system(SystemState& s, const float* coords, bool on_device, int precis
         return kErrArg;
     }
     const size_t n = s.nf * s.na * 3;
+    // device memory first: a plan that does not fit reads nothing of the caller's buffer
+    ECK(s.xyz.ensure(s.nf * s.na_pad * sizeof(float4)));
     const float* src = coords;
     std::vector<float> f0(s.na * 3);
     if (!on_device) {
-        ECK(s.raw.ensure(n * sizeof(float)));
-        ECK(cudaMemcpyAsync(s.raw.p, coords, n * sizeof(float), cudaMemcpyHostToDevice, st));
-        src = s.raw.as<float>();
+        int device = 0;
+        ECK(cudaGetDevice(&device));
+        src = device_view(coords, device);
+        if (!src) {
+            ECK(s.raw.ensure(n * sizeof(float)));
+            ECK(cudaMemcpyAsync(s.raw.p, coords, n * sizeof(float), cudaMemcpyHostToDevice, st));
+            src = s.raw.as<float>();
+        }
         memcpy(f0.data(), coords, f0.size() * sizeof(float));
     } else {
         ECK(cudaMemcpyAsync(f0.data(), coords, f0.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
@@ -142,12 +172,14 @@ int stage_system(SystemState& s, const float* coords, bool on_device, int precis
         }
     }
     memcpy(s.center, c, sizeof(c));
-    ECK(s.xyz.ensure(s.nf * s.na_pad * sizeof(float4)));
+    // the class-sorted copy, once it exists for the current classes, is filled in the same pass
+    const bool rec = s.rec_ready && s.rec_map_ok;
     ECK(launch_stage(src, (int)s.nf, (int)s.na, (int)s.na_pad, c[0], c[1], c[2], precision == PREC_FP32,
-                     s.xyz.as<float4>(), st));
+                     s.xyz.as<float4>(), rec ? s.rec_inv.as<int>() : nullptr, (int)s.na_rec,
+                     rec ? s.xyz_rec.as<float4>() : nullptr, st));
     ECK(cudaStreamSynchronize(st));
     s.staged = true;
-    s.rec_valid = false;
+    s.rec_valid = rec;
     s.mp_valid = false;
     return kOk;
 }
@@ -171,7 +203,7 @@ int set_system_classes(SystemState& s, const int32_t* cls, bool on_device, cudaS
     ECK(cudaStreamSynchronize(st));
     s.h_cls.assign(h.begin(), h.begin() + s.na);
     s.classes_set = true;
-    s.rec_valid = false;
+    s.rec_map_ok = s.rec_ready = s.rec_valid = false;
     return kOk;
 }
 
@@ -263,10 +295,10 @@ int choose_rec_k(const std::vector<std::vector<std::pair<int, int>>>& runs) {
     return best;
 }
 
-// Class-sorted coordinates for the recurrence kernel: class segments padded to 32 atoms,
-// w = 1 / 0 in float4.w, rows padded to the 128-atom stage.
-int ensure_rec_layout(SystemState& s, std::string& err) {
-    if (s.rec_valid) return kOk;
+// Class-sorted layout for the recurrence kernel: class segments padded to 32 atoms, w = 1
+// / 0 in float4.w, rows padded to the 128-atom stage. The slot map follows the classes;
+// the coordinates follow each staging (filled by the staging kernel once the copy exists).
+int build_rec_map(SystemState& s, std::string& err) {
     if (s.h_cls.size() != s.na) {
         err = "atom classes missing";
         return kErrArg;
@@ -290,17 +322,32 @@ int ensure_rec_layout(SystemState& s, std::string& err) {
         for (int j = 0; j < 32; ++j) npad += map[32 * b + j] < 0;
         bcls[b] |= npad << 16;
     }
+    std::vector<int> inv(s.na);
+    for (size_t i = 0; i < map.size(); ++i)
+        if (map[i] >= 0) inv[map[i]] = (int)i;
+    if (s.na_rec != map.size()) s.rec_ready = false;
     s.na_rec = map.size();
-    DevBuf d_map;
-    ECK(d_map.ensure(map.size() * sizeof(int)));
-    ECK(cudaMemcpy(d_map.p, map.data(), map.size() * sizeof(int), cudaMemcpyHostToDevice));
+    ECK(s.rec_map.ensure(map.size() * sizeof(int)));
+    ECK(cudaMemcpy(s.rec_map.p, map.data(), map.size() * sizeof(int), cudaMemcpyHostToDevice));
+    ECK(s.rec_inv.ensure(inv.size() * sizeof(int)));
+    ECK(cudaMemcpy(s.rec_inv.p, inv.data(), inv.size() * sizeof(int), cudaMemcpyHostToDevice));
     ECK(s.block_class.ensure(bcls.size() * sizeof(int)));
     ECK(cudaMemcpy(s.block_class.p, bcls.data(), bcls.size() * sizeof(int), cudaMemcpyHostToDevice));
+    s.rec_map_ok = true;
+    return kOk;
+}
+
+int ensure_rec_layout(SystemState& s, std::string& err) {
+    if (s.rec_valid && s.rec_map_ok) return kOk;
+    if (!s.rec_map_ok) {
+        int rc = build_rec_map(s, err);
+        if (rc) return rc;
+    }
     ECK(s.xyz_rec.ensure(s.nf * s.na_rec * sizeof(float4)));
-    ECK(launch_permute_stage(s.xyz.as<float4>(), (int)s.na_pad, d_map.as<int>(), (int)s.na_rec, (int)s.nf,
+    ECK(launch_permute_stage(s.xyz.as<float4>(), (int)s.na_pad, s.rec_map.as<int>(), (int)s.na_rec, (int)s.nf,
                              s.xyz_rec.as<float4>(), 0));
     ECK(cudaDeviceSynchronize());
-    s.rec_valid = true;
+    s.rec_valid = s.rec_ready = true;
     return kOk;
 }
 

@@ -50,8 +50,11 @@ struct SystemState {
     // class-sorted copy for the shell-recurrence kernel (built on first use)
     std::vector<int32_t> h_cls;   // [na] classes (host copy)
     DevBuf xyz_rec, block_class;  // [nf][na_rec] float4 with w; [na_rec / 32] int
+    DevBuf rec_map, rec_inv;      // [na_rec] atom of each slot (-1: padding); [na] slot of each atom
     size_t na_rec = 0;
-    bool rec_valid = false;
+    bool rec_map_ok = false;      // rec_map, rec_inv, block_class and na_rec follow the classes
+    bool rec_ready = false;       // xyz_rec exists with this map's padding slots zeroed: staging fills it
+    bool rec_valid = false;       // xyz_rec holds the staged frames
     // multipole devices: coordinates in the spherical or cylindrical representation
     DevBuf mp_xyz;  // [nf][na_pad] float4
     int mp_type = -1;

@@ -277,9 +277,12 @@ cudaError_t launch_twiddles(double2* tw64, float2* tw32, int lg, cudaStream_t st
 cudaError_t launch_store_kernel(const double2* tw64, int lg_tw, double2* k64, float2* k32, int nf,
                                 int lg, cudaStream_t st);
 
-// Staging: raw frame-major float [nf][na][3] -> float4 [nf][na_pad] (minus centre).
+// Staging: raw frame-major float [nf][na][3] -> float4 [nf][na_pad] (minus centre); with
+// xyz_rec, also the class-sorted copy xyz_rec[f][rec_inv[j]] = (x, y, z, 1). `raw` may be
+// host memory the device reads in place.
 cudaError_t launch_stage(const float* raw, int nf, int na, int na_pad, double cx, double cy,
-                         double cz, int center, float4* xyz, cudaStream_t st);
+                         double cz, int center, float4* xyz, const int* rec_inv, int na_rec,
+                         float4* xyz_rec, cudaStream_t st);
 // b[s][j] = class_factors[s][cls[j]] (0 for padding atoms), float or double output.
 cudaError_t launch_expand_factors(const double* class_factors, int nclass, int nshell,
                                   const int* cls, int na_pad, int precision, void* b,

@@ -217,3 +217,44 @@ def test_split_slices_never_empty(native_lib, precision):
     assert sch["atom_splits"] > 1
     ref = reference(w)
     assert_close(got, ref, 1e-12 if precision == "fp64" else TOL)
+
+
+def test_restaging_refreshes_the_class_sorted_copy(native_lib):
+    # Once the class-sorted copy exists, each staging fills it in the same pass as the padded
+    # frames, from host memory read in place (pageable or pinned) or from device memory; new
+    # classes rebuild it. Every staging form gives the same bits, and each result matches
+    # the oracle on the frames and classes of that moment.
+    import torch
+
+    w1 = synth.small("all", "autocorrelate", seed=47, na=300, nf=40, nq=6, nm=24)
+    w2 = dataclasses.replace(synth.small("all", "autocorrelate", seed=48, na=300, nf=40, nq=6, nm=24),
+                             shells=w1.shells, directions=w1.directions, class_factors=w1.class_factors)
+    w2b = dataclasses.replace(w2, atom_class=w1.atom_class)
+    args = (w1.sub_offsets(), w1.subvectors(), w1.class_factors)
+    lib = abi.load()
+    with abi.Plan(w1.na, w1.nf, len(w1.class_names), precision="fp32") as p:
+        p.stage(w1.coords)
+        p.set_classes(w1.atom_class)
+        assert_close(p.compute(*args), reference(w1))
+        assert p.schedule()["rec_tiles"] > 0
+        p.stage(w2.coords)  # pageable numpy memory; classes of w1
+        pageable = p.compute(*args)
+        assert_close(pageable, reference(w2b))
+        hp = lib.sass_host_alloc(w2.coords.nbytes)
+        try:
+            pinned = np.ctypeslib.as_array((np.ctypeslib.ctypes.c_float * w2.coords.size).from_address(hp))
+            pinned[:] = w2.coords.reshape(-1)
+            p.stage(pinned.reshape(w2.coords.shape))
+            for a, b in zip(p.compute(*args), pageable):
+                np.testing.assert_array_equal(a, b)
+        finally:
+            lib.sass_host_free(hp)
+        d = torch.from_numpy(w2.coords).cuda()
+        p.stage(d.data_ptr(), on_device=True)
+        for a, b in zip(p.compute(*args), pageable):
+            np.testing.assert_array_equal(a, b)
+        p.set_classes(w2.atom_class)  # new classes: a new slot map
+        assert_close(p.compute(*args), reference(w2))
+        p.stage(w1.coords)
+        p.set_classes(w1.atom_class)
+        assert_close(p.compute(*args), reference(w1))
