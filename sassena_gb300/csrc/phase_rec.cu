@@ -15,7 +15,7 @@
 // Layout: atoms are sorted by scattering class into segments padded to 32 atoms, so every
 // 32-atom block has one class; padding atoms sit at the origin, where every shell's term
 // is exactly 1, and are subtracted by count. The lane keeps plain FP32 block sums per
-// shell in registers and, where the class changes or a pipeline stage ends, folds them
+// shell in registers and, where the class changes or every few pipeline stages, folds them
 // times the class factor into Kahan-compensated FP32 running sums held in shared memory
 // (so registers grow by 2 per shell, allowing groups of up to 32 shells). Lanes run over
 // (group, direction) pairs of a system, so ragged direction counts leave no idle lanes
@@ -31,6 +31,9 @@ namespace sassgpu {
 namespace {
 
 constexpr int kRecWarps = 8, kRecAtoms = 128, kRecStages = 2, kRecBlock = 32;
+// Block sums are folded into the Kahan state where the class changes and at least every
+// kRecFoldStages stages (512 atoms of plain FP32 sums: relative rounding about 1e-5).
+constexpr int kRecFoldStages = 4;
 
 // Shared memory: per warp a ring of coordinate stages, the stage barriers, the tile
 // slot and the Kahan state (sum re, sum im, compensation re, compensation im) of every
@@ -140,13 +143,13 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 20 ? 2 : 1) phase_rec_ker
                     issue_coords(sx + slot * T, &bars[slot], row + k * T);
                 }
             int t = 0;
+            int info = __ldg(binfo);
+            float npad = 0.f;
             for (; t < nst; ++t) {
                 const unsigned slot = (used + t) % S;
                 const bool ok = mbar_wait_parity(&bars[slot], ((used + t) / S) & 1u);
                 if (!__all_sync(0xffffffffu, ok)) break;
                 const float4* cx = sx + slot * T;
-                int info = __ldg(binfo + t * NB);
-                float npad = 0.f;
 #pragma unroll 1
                 for (int b = 0; b < NB; ++b) {
 #pragma unroll 4
@@ -182,9 +185,12 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 20 ? 2 : 1) phase_rec_ker
                         }
                     }
                     npad += (float)(info >> 16);
-                    const int next = (b + 1 < NB) ? __ldg(binfo + t * NB + b + 1) : -1;
-                    // warp-uniform: every lane reads the same block information
-                    if (b + 1 == NB || (next & 0xffff) != (info & 0xffff)) {
+                    const int nb = t * NB + b + 1;  // the tile's next 32-atom block
+                    const int next = nb < nst * NB ? __ldg(binfo + nb) : -1;
+                    const bool fold_stage = b + 1 == NB && (t + 1) % kRecFoldStages == 0;
+                    // warp-uniform: every lane reads the same block information; the
+                    // tile's last block always folds (next = -1 is no class)
+                    if (fold_stage || (next & 0xffff) != (info & 0xffff)) {
                         kahan_fold<K>(ks, acc, npad, bf + (info & 0xffff) * K);
                         npad = 0.f;
                     }
