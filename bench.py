@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="coherent_sqt")
-    ap.add_argument("--plain-shells", type=int, default=2,
+    ap.add_argument("--plain-shells", type=int, default=3,
                     help="shells of the plain FP64 comparison run (time scaled by terms)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
@@ -484,7 +484,13 @@ def run_ours(args, dist):
             t64 = p64.timing()
         # error of the measured FP32 path itself: its full-workload output at those shells
         full = plan.compute(offs, w.subvectors(), np.ascontiguousarray(w.class_factors))
-        err = (np.abs(full[0][idx] - ref[0]).max(axis=1) / np.abs(ref[0][:, 0])).max()
+        # per compared shell: S(q,t) as max_t |S - S_ref| / |S_ref(q,0)|; I(q) as fq (the
+        # time-averaged correlation), fq0 = S(q,0) and fq2, each relative to its FP64 value
+        e_sqt = np.abs(full[0][idx] - ref[0]).max(axis=1) / np.abs(ref[0][:, 0])
+        e_fq = np.abs(full[1][idx] - ref[1]) / np.abs(ref[1])
+        e_fq0 = np.abs(full[0][idx, 0] - ref[0][:, 0]) / np.abs(ref[0][:, 0])
+        e_fq2 = np.abs(full[2][idx] - ref[2]) / np.abs(ref[2])
+        err = e_sqt.max()
         plan.compute(sub_offs, sub_sv, sub_cf)
         t32 = plan.timing()
         sub_terms = w.na * w.nf * w.nm * ns
@@ -492,6 +498,11 @@ def run_ours(args, dist):
         out["plain_fp64"] = {"value": plain_tps, "unit": UNIT, "shells_run": ns,
                              "ms_full_workload_extrapolated": terms / plain_tps * 1e3,
                              "fp32_max_rel_err_vs_fp64": float(err),
+                             "fp32_rel_err_per_shell": {
+                                 "q": [float(w.shells[i]) for i in idx],
+                                 "sqt": [float(v) for v in e_sqt], "sqt_median": float(np.median(e_sqt)),
+                                 "iq_fq": [float(v) for v in e_fq], "fq0": [float(v) for v in e_fq0],
+                                 "fq2": [float(v) for v in e_fq2]},
                              "speedup_same_gpu": (terms / plain_tps * 1e3) / ms,
                              "fp32_ms_same_shells": t32["total_ms"]}
 
