@@ -466,28 +466,60 @@ __global__ void __launch_bounds__(NT) self_direct_kernel(CorrLaunch a) {
 // Per-shell finalisation in FP64: sum partial slots, inverse FFT (autocorrelate),
 // normalise by 1/(L (NF - tau)) and 1/NM, conjugate for dsp.method = direct.
 // ---------------------------------------------------------------------------------------
+// Sums over a shell's partial slots, in slot order. The slots' loads are issued eight at a
+// time ahead of their additions, so a thread waits on memory once per eight slots instead
+// of once per slot (the finalisation runs one CTA per shell, too few to hide latency with
+// warps). FP64 slots are added in FP64 in the order of a plain loop.
+constexpr int kSlotBatch = 8;
+
+__device__ __forceinline__ double slot_sum(const double* __restrict__ src, size_t stride, int n, int f32pair) {
+    if (f32pair) {
+        // FP32 Kahan pairs (sum s_k, compensation c_k) with value s_k - c_k, added in
+        // float-float arithmetic on the FP32 pipe (Knuth's TwoSum for the sums, the
+        // compensations and rounding errors in the low word), converted to FP64 once:
+        // on GB300 an FP64 conversion and two FP64 adds per slot made this loop the
+        // bound of the finalisation. Relative rounding ~n * 2^-48, far below the FP32
+        // form's partials' own.
+        float hi = 0.f, lo = 0.f;
+        for (int k0 = 0; k0 < n; k0 += kSlotBatch) {
+            float2 v[kSlotBatch];
+#pragma unroll
+            for (int u = 0; u < kSlotBatch; ++u)
+                v[u] = k0 + u < n ? __ldg(reinterpret_cast<const float2*>(src + (size_t)(k0 + u) * stride))
+                                  : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int u = 0; u < kSlotBatch; ++u) {
+                const float s = __fadd_rn(hi, v[u].x), bb = __fsub_rn(s, hi);
+                const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(v[u].x, bb));
+                hi = s;
+                lo = __fadd_rn(lo, __fsub_rn(e, v[u].y));
+            }
+        }
+        return (double)hi + (double)lo;
+    }
+    double p = 0.0;
+    for (int k0 = 0; k0 < n; k0 += kSlotBatch) {
+        double v[kSlotBatch];
+#pragma unroll
+        for (int u = 0; u < kSlotBatch; ++u) v[u] = k0 + u < n ? __ldg(src + (size_t)(k0 + u) * stride) : 0.0;
+#pragma unroll
+        for (int u = 0; u < kSlotBatch; ++u)
+            if (k0 + u < n) p += v[u];
+    }
+    return p;
+}
+
 template <int NT>
 __global__ void __launch_bounds__(NT) finalize_kernel(FinalLaunch a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const FinalEntry e = a.entries[blockIdx.x];
-    const int nf = e.nf;
+    const int nf = e.nf, ns = e.slot_end - e.slot_begin;
     const double sgn = a.conj_out ? -1.0 : 1.0;
+    const double* part = a.ppart + e.part_off;
     if (a.dsp == DSP_AUTOCORRELATE) {
         const int L = 1 << e.lg;
         double2* buf = reinterpret_cast<double2*>(smem);
-        for (int i = threadIdx.x; i < L; i += NT) {
-            double p = 0.0;
-            for (int k = e.slot_begin; k < e.slot_end; ++k) {
-                const double* src = a.ppart + e.part_off + (size_t)(k - e.slot_begin) * e.part_len + i;
-                if (e.f32pair) {
-                    const float2 sc = *reinterpret_cast<const float2*>(src);
-                    p += (double)sc.x - (double)sc.y;
-                } else {
-                    p += *src;
-                }
-            }
-            buf[i] = make_double2(p, 0.0);
-        }
+        for (int i = threadIdx.x; i < L; i += NT) buf[i] = make_double2(slot_sum(part + i, e.part_len, ns, e.f32pair), 0.0);
         __syncthreads();
         dit_inverse<NT>(buf, a.tw, e.lg, a.lg_max - e.lg);
         for (int t = threadIdx.x; t < nf; t += NT) {
@@ -496,22 +528,30 @@ __global__ void __launch_bounds__(NT) finalize_kernel(FinalLaunch a) {
         }
     } else {
         for (int t = threadIdx.x; t < nf; t += NT) {
-            double2 v = make_double2(0.0, 0.0);
-            for (int k = e.slot_begin; k < e.slot_end; ++k) {
-                const double* x = a.ppart + e.part_off + (size_t)(k - e.slot_begin) * e.part_len + 2 * t;
-                v.x += x[0];
-                v.y += x[1];
-            }
-            e.fqt[t] = make_double2(v.x * e.inv_nm, sgn * v.y * e.inv_nm);
+            const double vx = slot_sum(part + 2 * t, e.part_len, ns, 0);
+            const double vy = slot_sum(part + 2 * t + 1, e.part_len, ns, 0);
+            e.fqt[t] = make_double2(vx * e.inv_nm, sgn * vy * e.inv_nm);
         }
     }
     if (threadIdx.x == 0) {
         double2 as = make_double2(0.0, 0.0);
         double a2 = 0.0;
-        for (int k = e.slot_begin; k < e.slot_end; ++k) {
-            as.x += a.apart[k].x;
-            as.y += a.apart[k].y;
-            a2 += a.a2part[k];
+        for (int k0 = e.slot_begin; k0 < e.slot_end; k0 += kSlotBatch) {
+            double2 va[kSlotBatch];
+            double v2[kSlotBatch];
+#pragma unroll
+            for (int u = 0; u < kSlotBatch; ++u) {
+                const bool in = k0 + u < e.slot_end;
+                va[u] = in ? a.apart[k0 + u] : make_double2(0.0, 0.0);
+                v2[u] = in ? a.a2part[k0 + u] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < kSlotBatch; ++u)
+                if (k0 + u < e.slot_end) {
+                    as.x += va[u].x;
+                    as.y += va[u].y;
+                    a2 += v2[u];
+                }
         }
         *e.fq = make_double2(as.x * e.inv_nm, sgn * as.y * e.inv_nm);
         *e.fq2 = make_double2(a2 * e.inv_nm, 0.0);
@@ -855,10 +895,11 @@ cudaError_t launch_self_accumulate(const CorrLaunch& a, cudaStream_t st) { retur
 cudaError_t launch_finalize(const FinalLaunch& a, cudaStream_t st) {
     if (a.nentries == 0) return cudaSuccess;
     const size_t sm = a.dsp == DSP_AUTOCORRELATE ? ((size_t)1 << a.lg_max) * sizeof(double2) : 0;
-    auto k = finalize_kernel<256>;
+    constexpr int NT = 1024;  // one CTA per shell: as many threads as a CTA takes
+    auto k = finalize_kernel<NT>;
     cudaError_t e = set_smem(k, sm);
     if (e != cudaSuccess) return e;
-    k<<<a.nentries, 256, sm, st>>>(a);
+    k<<<a.nentries, NT, sm, st>>>(a);
     return cudaGetLastError();
 }
 
