@@ -805,6 +805,195 @@ __global__ void __launch_bounds__(kWarpFftWarps * 32, (LG <= 8 && sizeof(T) == 4
     }
 }
 
+// ---------------------------------------------------------------------------------------
+// Block-register FFT for coherent series of one padded length L = 512 B (B = 2, 4, 8: 1,024
+// .. 4,096 points). The first log2 B DIF stages are folded into the load: after them,
+// position 512 b + j of the DIF array holds
+//     v_b[j] = W_L^{j br(b)} sum_{u < B/2} x[j + 512 u] W_B^{u br(b)}
+// (br: reversal of the log2 B bits of b; the upper half of x is the zero padding), and the
+// remaining stages are the 512-point DIF of each block on its own. So a warp transforms one
+// block of one series straight from the amplitudes in global memory, with no exchange
+// between warps: lane l holds positions 512 b + l + 32 m (m < 16), runs the in-lane stages
+// of span 256 .. 32 and the shuffle stages of span 16 .. 1 of the register warp FFT, and
+// accumulates the power of exactly those (bit-reversed) bins. Warps b, b + B, ... take block
+// b of consecutive series; each round's series sums add their blocks' partial means in
+// block order. Replaces 11 barrier-separated radix-2 stages in shared memory per series.
+// ---------------------------------------------------------------------------------------
+constexpr int kBlkFftWarps = 8, kBlkFftMinLg = 10, kBlkFftMaxLg = 12;
+
+// W_L^m for 0 <= m < L from the half table of the launch's largest length (W^m = -W^{m-L/2}).
+template <class T2>
+__device__ __forceinline__ T2 tw_full(const T2* tw, int m, int lg, int tws) {
+    const int h = 1 << (lg - 1);
+    if (m < h) return tw[m << tws];
+    T2 v = tw[(m - h) << tws];
+    v.x = -v.x;
+    v.y = -v.y;
+    return v;
+}
+
+template <class T>
+size_t blk_fft_smem(int lg_max) {
+    typedef typename cplx<T>::type T2;
+    size_t b = (sizeof(T) == 4 ? ((size_t)1 << lg_max) / 2 : 0) * sizeof(T2);  // FP32 twiddles
+    b += 2 * kBlkFftWarps * sizeof(T2);                                        // partial means
+    b += (size_t)kBlkFftWarps * 512 * (sizeof(T) == 4 ? sizeof(float2) : sizeof(double));  // bins
+    return b;
+}
+
+template <class T, int LG>
+__global__ void __launch_bounds__(kBlkFftWarps * 32, sizeof(T) == 4 ? 2 : 1) blk_fft_kernel(CorrLaunch a) {
+    typedef typename cplx<T>::type T2;
+    constexpr int NW = kBlkFftWarps, NT = NW * 32, L = 1 << LG, B = L / 512, E = 16, G = NW / B;
+    static_assert(B >= 2 && B <= NW && NW % B == 0, "block FFT lengths 1,024 .. 4,096");
+    extern __shared__ __align__(16) unsigned char smem[];
+    const CorrChunk c = a.chunks[blockIdx.x];
+    const CorrSystem sys = a.systems[c.system];
+    const int nf = sys.nf, tws = a.lg_max - LG;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int b = warp % B, g = warp / B;
+    const int br = (int)(__brev((unsigned)b) >> (32 - ilog2c(B)));
+    T2* twsm = reinterpret_cast<T2*>(smem);
+    unsigned char* region = smem + (sizeof(T) == 4 ? (size_t)(L / 2) * sizeof(T2) : 0);
+    T2* pm = reinterpret_cast<T2*>(region);  // [2][NW]: round parity x warp
+    unsigned char* pwb = region + 2 * NW * sizeof(T2);
+    const T2* tw = stage_twiddles<T, NT>(twsm, a.tw, a.lg_max);
+    const T2* kbr = reinterpret_cast<const T2*>(sys.kbr) + 512 * b;
+    __syncthreads();
+    T2 cu[B / 2];  // W_B^{u br(b)} of the folded stages
+#pragma unroll
+    for (int u = 0; u < B / 2; ++u) cu[u] = tw_full(tw, (512 * u * br) & (L - 1), LG, tws);
+    PowerAcc<T, E> acc;
+    acc.clear();
+    SeriesAcc<T> sacc;
+    const int nser = c.v_end - c.v_begin, rounds = (nser + G - 1) / G;
+    for (int r = 0; r < rounds; ++r) {
+        const int sl = r * G + g;  // warp-uniform
+        T2 pv = zero2<T2>();
+        if (sl < nser) {
+            const T2* src = reinterpret_cast<const T2*>(sys.A) + (size_t)(c.v_begin + sl) * nf;
+            T2 x[E];
+#pragma unroll
+            for (int m = 0; m < E; ++m) {
+                const int j = lane + 32 * m;
+                T2 sv = j < nf ? src[j] : zero2<T2>();
+#pragma unroll
+                for (int u = 1; u < B / 2; ++u) {
+                    const int n = j + 512 * u;
+                    if (n < nf) sv = cadd(sv, cmul(src[n], cu[u]));
+                }
+                x[m] = br == 0 ? sv : cmul(sv, tw_full(tw, j * br, LG, tws));
+            }
+#pragma unroll
+            for (int hm = E / 2; hm >= 1; hm >>= 1) {  // spans 32 hm inside the lane
+                const int sh = LG - 6 - ilog2c(hm) + tws;
+#pragma unroll
+                for (int m = 0; m < E; ++m) {
+                    if ((m & hm) == 0) {
+                        const T2 u = x[m], w = x[m + hm];
+                        x[m] = cadd(u, w);
+                        x[m + hm] = cmul(csub(u, w), tw[(lane + 32 * (m & (hm - 1))) << sh]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int lh = 4; lh >= 0; --lh) {  // spans 16 .. 1 across lanes
+                const int h = 1 << lh, sh = LG - 1 - lh + tws;
+                const bool upper = (lane & h) != 0;
+                const T sg = upper ? T(-1) : T(1);
+                T2 tv = tw[(lane & (h - 1)) << sh];
+                if (!upper) {
+                    tv.x = T(1);
+                    tv.y = T(0);
+                }
+#pragma unroll
+                for (int m = 0; m < E; ++m) {
+                    const T2 o = shfl_xor2(x[m], h);
+                    T2 d;
+                    d.x = fma(sg, x[m].x, o.x);
+                    d.y = fma(sg, x[m].y, o.y);
+                    x[m] = cmul(d, tv);
+                }
+            }
+            T ax = 0, ay = 0;
+#pragma unroll
+            for (int m = 0; m < E; ++m) {
+                const T P = x[m].x * x[m].x + x[m].y * x[m].y;
+                acc.add(m, P);
+                const T2 kv = __ldg(kbr + lane + 32 * m);
+                ax += P * kv.x;
+                ay += P * kv.y;
+            }
+            pv = warp_sum_t<T>(ax, ay);
+        }
+        if (lane == 0) pm[(r & 1) * NW + warp] = pv;
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (int gg = 0; gg < G && r * G + gg < nser; ++gg) {
+                T2 tot = pm[(r & 1) * NW + gg * B];
+#pragma unroll
+                for (int bb = 1; bb < B; ++bb) tot = cadd(tot, pm[(r & 1) * NW + gg * B + bb]);
+                sacc.add(tot.x, tot.y);
+            }
+    }
+    // bins: warps b, b + B, ... hold block b; combined in warp order
+    if constexpr (sizeof(T) == 4) {
+        float2* pw = reinterpret_cast<float2*>(pwb);
+#pragma unroll
+        for (int m = 0; m < E; ++m) pw[warp * 512 + lane + 32 * m] = make_float2(acc.s[m], acc.c[m]);
+        __syncthreads();
+        float2* dst = reinterpret_cast<float2*>(a.ppart + c.part_off);
+        for (int i = threadIdx.x; i < L; i += NT) {
+            const int bb = i >> 9, loc = i & 511;
+            float hi = 0.f, lo = 0.f;  // float-float sum of the warps' (sum - compensation)
+            for (int w = bb; w < NW; w += B) {
+                const float2 p = pw[w * 512 + loc];
+                const float s = __fadd_rn(hi, p.x), bv = __fsub_rn(s, hi);
+                const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bv)), __fsub_rn(p.x, bv));
+                hi = s;
+                lo = __fadd_rn(lo, __fsub_rn(e, p.y));
+            }
+            dst[i] = make_float2(hi, -lo);  // read back as (sum, compensation): hi + lo
+        }
+    } else {
+        double* pw = reinterpret_cast<double*>(pwb);
+#pragma unroll
+        for (int m = 0; m < E; ++m) pw[warp * 512 + lane + 32 * m] = acc.get(m);
+        __syncthreads();
+        double* dst = a.ppart + c.part_off;
+        for (int i = threadIdx.x; i < L; i += NT) {
+            const int bb = i >> 9, loc = i & 511;
+            double s = 0.0;
+            for (int w = bb; w < NW; w += B) s += pw[w * 512 + loc];
+            dst[i] = s;
+        }
+    }
+    if (threadIdx.x == 0) {
+        a.apart[c.slot] = sacc.mean_sum();
+        a.a2part[c.slot] = sacc.sq_sum();
+    }
+}
+
+template <class T, int LG>
+cudaError_t launch_blk_fft_lg(const CorrLaunch& a, cudaStream_t st) {
+    const size_t sm = blk_fft_smem<T>(a.lg_max);
+    auto k = blk_fft_kernel<T, LG>;
+    cudaError_t e = set_smem(k, sm);
+    if (e != cudaSuccess) return e;
+    k<<<a.nchunks, kBlkFftWarps * 32, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_blk_fft(const CorrLaunch& a, cudaStream_t st) {
+    switch (a.lg_max) {
+        case 10: return launch_blk_fft_lg<T, 10>(a, st);
+        case 11: return launch_blk_fft_lg<T, 11>(a, st);
+        case 12: return launch_blk_fft_lg<T, 12>(a, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
 template <class T, int LG>
 cudaError_t launch_reg_fft_lg(const CorrLaunch& a, bool self, cudaStream_t st) {
     const size_t sm = reg_fft_smem<T>(LG, a.nf_max, self);
@@ -844,6 +1033,8 @@ cudaError_t launch_accumulate(const CorrLaunch& a, bool self, cudaStream_t st) {
             return a.precision == PREC_FP32 ? launch_reg_fft<float>(a, self, st) : launch_reg_fft<double>(a, self, st);
         if (a.lg_max <= kWarpFftMaxLg)
             return a.precision == PREC_FP32 ? launch_warp_fft<float>(a, self, st) : launch_warp_fft<double>(a, self, st);
+        if (!self && a.lg_min == a.lg_max && a.lg_max >= kBlkFftMinLg && a.lg_max <= kBlkFftMaxLg)
+            return a.precision == PREC_FP32 ? launch_blk_fft<float>(a, st) : launch_blk_fft<double>(a, st);
         // per-thread spectrum bins sized to the longest series of the launch (registers)
         switch (a.lg_max) {
             case 10: return a.precision == PREC_FP32 ? launch_fft<float, 256, 4>(a, self, st) : launch_fft<double, 256, 4>(a, self, st);

@@ -207,6 +207,23 @@ def test_coherent_fp32_error_at_length(native_lib, nf):
     check(w, "fp32", "fftw")
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("nf", [300, 600, 1500])
+def test_coherent_block_fft_lengths(native_lib, precision, nf):
+    # padded lengths 1,024, 2,048 and 4,096: the block-register FFT with 2, 4 and 8 blocks
+    # of 512 points; 7 directions per shell leave warps without a series in a chunk's last round
+    w = synth.small("all", "autocorrelate", seed=23, na=19, nf=nf, nq=3, nm=7)
+    check(w, precision, "fftw")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_coherent_block_fft_direct_method_and_many_series(native_lib, precision):
+    # the conjugate convention of the direct method, and enough series per shell for
+    # several chunks and rounds
+    w = synth.small("all", "autocorrelate", seed=24, na=11, nf=700, nq=2, nm=150)
+    check(w, precision, "direct")
+
+
 def test_out_of_memory_is_a_status(native_lib):
     # a trajectory far beyond HBM (16.7M atoms x 131,072 frames = 35 TB staged): the device
     # allocation fails first, staging returns SASS_ERR_OOM with a message, nothing is read
