@@ -341,7 +341,7 @@ def phase_roofline(w, sch, phase_ms, corr_ms, sfu, fma):
         L = 1 << max(2, int(np.ceil(np.log2(2 * w.nf))))
         flops_per_term = 5.0 * L * np.log2(L) / w.nf
         peak = min(2.0 * fma / flops_per_term, sfu / 2.0)
-        kernel = "self_fft_kernel"
+        kernel = "reg_fft_kernel" if L <= 512 else "self_fft_kernel"
         achieved = terms / (corr_ms * 1e-3)
         return {"bound": "fp32" if 2.0 * fma / flops_per_term < sfu / 2.0 else "sfu",
                 "achieved": achieved, "peak": peak, "unit": "terms/s", "frac": achieved / peak,
@@ -453,9 +453,23 @@ def run_ours(args, dist):
     sfu, fma = abi.probe_pipes(dev)
     roof = phase_roofline(w, sch, statistics.median(phase_ms), statistics.median(corr_ms), sfu, fma)
     corr = statistics.median(corr_ms)
-    corr_bytes = (w.nq * w.nm * w.nf * 16) + (w.nq * w.nf * 16)
-    roof_corr = {"bound": "hbm", "kernel": "corr_fft_kernel+finalize", "ms": corr,
+    # algorithmic bytes: the FP32 amplitudes read once (float2, 8 B) and the FP64 row written
+    # per shell
+    corr_bytes = (w.nq * w.nm * w.nf * 8) + (w.nq * w.nf * 16)
+    lg = max(2, int(np.ceil(np.log2(2 * w.nf))))
+    if w.dsp != "autocorrelate":
+        corr_kernel = "corr_direct_kernel" if w.scattering == "all" else "self_direct_kernel"
+    elif lg <= 9:
+        corr_kernel = "reg_fft_kernel"
+    elif lg <= 12 and w.scattering == "all":
+        corr_kernel = "blk_fft_kernel"
+    else:
+        corr_kernel = "corr_fft_kernel" if w.scattering == "all" else "self_fft_kernel"
+    roof_corr = {"bound": "hbm", "kernel": corr_kernel + "+finalize_kernel", "ms": corr,
                  "achieved": corr_bytes / (corr * 1e-3) / 1e9, "unit": "GB/s"}
+    if w.scattering == "self":  # series generated inside the FFT kernel: no amplitudes in HBM
+        roof_corr = {"kernel": roof["kernel"] + "+finalize_kernel", "ms": corr,
+                     "note": "fused with the series generation; its roofline is `roofline`"}
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
