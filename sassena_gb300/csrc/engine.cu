@@ -479,8 +479,34 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
         int max_split = (int)(items[i].sys->na_pad / shape.atoms);
         if (item_ng[i]) max_split = std::min(max_split, (int)(items[i].sys->na_rec / 128));
         int ns = 1;
-        if (cfg.split_atoms > 0) ns = (int)((items[i].sys->na_pad + cfg.split_atoms - 1) / cfg.split_atoms);
-        else if (base_tiles < target) ns = (int)((target + base_tiles - 1) / std::max<size_t>(base_tiles, 1));
+        if (cfg.split_atoms > 0) {
+            ns = (int)((items[i].sys->na_pad + cfg.split_atoms - 1) / cfg.split_atoms);
+        } else if (base_tiles < target) {
+            ns = (int)((target + base_tiles - 1) / std::max<size_t>(base_tiles, 1));
+        } else if (items.size() == 1) {
+            // Enough tiles, but the last round of the persistent grid can leave SMs idle:
+            // an SM runs about tiles * s / SMs tiles of ceil(stages / s) atom stages each.
+            // Take the split count that minimises ceil(tiles * s / SMs) * ceil(stages / s),
+            // charging each extra split 0.4 % of the unsplit time for its FP64 partials and
+            // their reduction. (coherent S(q,t) workload on GB300, 2,048 tiles of 79 stages:
+            // s = 2 gives 26.95 tiles per SM and a 2.4 % shorter step than s = 1.)
+            const long long nst = item_ng[i] ? (long long)(items[i].sys->na_rec / 128)
+                                              : (long long)(items[i].sys->na_pad / shape.atoms);
+            const double t1 = (double)base_tiles;
+            auto cost = [&](int sp) {
+                const double per_sm = std::ceil(t1 * sp / (double)sms - 1e-9);
+                return per_sm * (double)((nst + sp - 1) / sp);
+            };
+            const double c1 = cost(1);
+            double best = c1;
+            for (int sp = 2; sp <= std::min(8, max_split); ++sp) {
+                const double c = cost(sp) + 0.004 * c1 * (sp - 1);
+                if (c < best) {
+                    best = c;
+                    ns = sp;
+                }
+            }
+        }
         nsplit_[i] = items[i].d_amp_given ? 1 : std::max(1, std::min(ns, max_split));
         stats_.max_split = std::max(stats_.max_split, nsplit_[i]);
     }
