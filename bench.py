@@ -341,7 +341,7 @@ def phase_roofline(w, sch, phase_ms, corr_ms, sfu, fma):
         L = 1 << max(2, int(np.ceil(np.log2(2 * w.nf))))
         flops_per_term = 5.0 * L * np.log2(L) / w.nf
         peak = min(2.0 * fma / flops_per_term, sfu / 2.0)
-        kernel = "reg_fft_kernel" if L <= 512 else "self_fft_kernel"
+        kernel = "reg_fft_kernel" if L <= 512 else ("self_blk_fft_kernel" if L <= 4096 else "self_fft_kernel")
         achieved = terms / (corr_ms * 1e-3)
         return {"bound": "fp32" if 2.0 * fma / flops_per_term < sfu / 2.0 else "sfu",
                 "achieved": achieved, "peak": peak, "unit": "terms/s", "frac": achieved / peak,

@@ -806,18 +806,20 @@ __global__ void __launch_bounds__(kWarpFftWarps * 32, (LG <= 8 && sizeof(T) == 4
 }
 
 // ---------------------------------------------------------------------------------------
-// Block-register FFT for coherent series of one padded length L = 512 B (B = 2, 4, 8: 1,024
-// .. 4,096 points). The first log2 B DIF stages are folded into the load: after them,
-// position 512 b + j of the DIF array holds
+// Block-register FFT for series of one padded length L = 512 B (B = 2, 4, 8: 1,024 .. 4,096
+// points). The first log2 B DIF stages are folded into the load: after them, position
+// 512 b + j of the DIF array holds
 //     v_b[j] = W_L^{j br(b)} sum_{u < B/2} x[j + 512 u] W_B^{u br(b)}
 // (br: reversal of the log2 B bits of b; the upper half of x is the zero padding), and the
 // remaining stages are the 512-point DIF of each block on its own. So a warp transforms one
-// block of one series straight from the amplitudes in global memory, with no exchange
-// between warps: lane l holds positions 512 b + l + 32 m (m < 16), runs the in-lane stages
-// of span 256 .. 32 and the shuffle stages of span 16 .. 1 of the register warp FFT, and
-// accumulates the power of exactly those (bit-reversed) bins. Warps b, b + B, ... take block
-// b of consecutive series; each round's series sums add their blocks' partial means in
-// block order. Replaces 11 barrier-separated radix-2 stages in shared memory per series.
+// block of one series with no exchange between warps: lane l holds positions 512 b + l + 32 m
+// (m < 16), runs the in-lane stages of span 256 .. 32 and the shuffle stages of span 16 .. 1
+// of the register warp FFT, and accumulates the power of exactly those (bit-reversed) bins.
+// Warps b, b + B, ... take block b of G = 8 / B series per round; each round's series sums
+// add their blocks' partial means in block order. Coherent series load straight from the
+// amplitudes in global memory; incoherent series are generated once per round into shared
+// memory from the atom's staged trajectory. Replaces 11 barrier-separated radix-2 stages in
+// shared memory per series.
 // ---------------------------------------------------------------------------------------
 constexpr int kBlkFftWarps = 8, kBlkFftMinLg = 10, kBlkFftMaxLg = 12;
 
@@ -832,37 +834,170 @@ __device__ __forceinline__ T2 tw_full(const T2* tw, int m, int lg, int tws) {
     return v;
 }
 
-template <class T>
-size_t blk_fft_smem(int lg_max) {
+template <class T, int LG>
+struct BlkFft {
     typedef typename cplx<T>::type T2;
-    size_t b = (sizeof(T) == 4 ? ((size_t)1 << lg_max) / 2 : 0) * sizeof(T2);  // FP32 twiddles
-    b += 2 * kBlkFftWarps * sizeof(T2);                                        // partial means
+    static constexpr int NW = kBlkFftWarps, NT = NW * 32, L = 1 << LG, B = L / 512, E = 16, G = NW / B;
+    static_assert(B >= 2 && B <= NW && NW % B == 0, "block FFT lengths 1,024 .. 4,096");
+    const T2* tw;
+    int tws, lane, b, br;
+    T2 cu[B / 2];  // W_B^{u br(b)} of the folded stages
+
+    __device__ void init(const T2* tw_, int tws_) {
+        tw = tw_;
+        tws = tws_;
+        lane = threadIdx.x & 31;
+        b = (threadIdx.x >> 5) % B;
+        br = (int)(__brev((unsigned)b) >> (32 - ilog2c(B)));
+#pragma unroll
+        for (int u = 0; u < B / 2; ++u) cu[u] = tw_full(tw, (512 * u * br) & (L - 1), LG, tws);
+    }
+
+    // x[m] = v_b[lane + 32 m] from get(n), the series' first L / 2 points (0 beyond NF)
+    template <class Get>
+    __device__ __forceinline__ void load(T2 (&x)[E], Get get) const {
+#pragma unroll
+        for (int m = 0; m < E; ++m) {
+            const int j = lane + 32 * m;
+            T2 sv = get(j);
+#pragma unroll
+            for (int u = 1; u < B / 2; ++u) sv = cadd(sv, cmul(get(j + 512 * u), cu[u]));
+            x[m] = br == 0 ? sv : cmul(sv, tw_full(tw, j * br, LG, tws));
+        }
+    }
+
+    // the 512-point DIF of the block: bit-reversed order at the same positions
+    __device__ __forceinline__ void stages(T2 (&x)[E]) const {
+#pragma unroll
+        for (int hm = E / 2; hm >= 1; hm >>= 1) {  // spans 32 hm inside the lane
+            const int sh = LG - 6 - ilog2c(hm) + tws;
+#pragma unroll
+            for (int m = 0; m < E; ++m) {
+                if ((m & hm) == 0) {
+                    const T2 u = x[m], w = x[m + hm];
+                    x[m] = cadd(u, w);
+                    x[m + hm] = cmul(csub(u, w), tw[(lane + 32 * (m & (hm - 1))) << sh]);
+                }
+            }
+        }
+#pragma unroll
+        for (int lh = 4; lh >= 0; --lh) {  // spans 16 .. 1 across lanes
+            const int h = 1 << lh, sh = LG - 1 - lh + tws;
+            const bool upper = (lane & h) != 0;
+            const T sg = upper ? T(-1) : T(1);
+            T2 tv = tw[(lane & (h - 1)) << sh];
+            if (!upper) {
+                tv.x = T(1);
+                tv.y = T(0);
+            }
+#pragma unroll
+            for (int m = 0; m < E; ++m) {
+                const T2 o = shfl_xor2(x[m], h);
+                T2 d;
+                d.x = fma(sg, x[m].x, o.x);
+                d.y = fma(sg, x[m].y, o.y);
+                x[m] = cmul(d, tv);
+            }
+        }
+    }
+
+    // accumulate |X|^2 of the lane's bins; the warp's part of sum_w P(w) K(w)
+    __device__ __forceinline__ T2 power(const T2 (&x)[E], const T2* __restrict__ kbr, PowerAcc<T, E>& acc) const {
+        T ax = 0, ay = 0;
+#pragma unroll
+        for (int m = 0; m < E; ++m) {
+            const T P = x[m].x * x[m].x + x[m].y * x[m].y;
+            acc.add(m, P);
+            const T2 kv = __ldg(kbr + 512 * b + lane + 32 * m);
+            ax += P * kv.x;
+            ay += P * kv.y;
+        }
+        return warp_sum_t<T>(ax, ay);
+    }
+
+    // end of a chunk: the bins of warps b, b + B, ... combined in warp order into the
+    // chunk's partial slot (FP32: float-float sum of (sum - compensation), stored as a
+    // (sum, compensation) pair; FP64: plain sums), and the series sums. `pwb`: NW x 512 bins.
+    __device__ void finish(const PowerAcc<T, E>& acc, const SeriesAcc<T>& sacc, unsigned char* pwb,
+                           const CorrLaunch& a, const CorrChunk& c) const {
+        const int warp = threadIdx.x >> 5;
+        if constexpr (sizeof(T) == 4) {
+            float2* pw = reinterpret_cast<float2*>(pwb);
+#pragma unroll
+            for (int m = 0; m < E; ++m) pw[warp * 512 + lane + 32 * m] = make_float2(acc.s[m], acc.c[m]);
+            __syncthreads();
+            float2* dst = reinterpret_cast<float2*>(a.ppart + c.part_off);
+            for (int i = threadIdx.x; i < L; i += NT) {
+                const int bb = i >> 9, loc = i & 511;
+                float hi = 0.f, lo = 0.f;
+                for (int w = bb; w < NW; w += B) {
+                    const float2 p = pw[w * 512 + loc];
+                    const float s = __fadd_rn(hi, p.x), bv = __fsub_rn(s, hi);
+                    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bv)), __fsub_rn(p.x, bv));
+                    hi = s;
+                    lo = __fadd_rn(lo, __fsub_rn(e, p.y));
+                }
+                dst[i] = make_float2(hi, -lo);  // read back as (sum, compensation): hi + lo
+            }
+        } else {
+            double* pw = reinterpret_cast<double*>(pwb);
+#pragma unroll
+            for (int m = 0; m < E; ++m) pw[warp * 512 + lane + 32 * m] = acc.get(m);
+            __syncthreads();
+            double* dst = a.ppart + c.part_off;
+            for (int i = threadIdx.x; i < L; i += NT) {
+                const int bb = i >> 9, loc = i & 511;
+                double s = 0.0;
+                for (int w = bb; w < NW; w += B) s += pw[w * 512 + loc];
+                dst[i] = s;
+            }
+        }
+        if (threadIdx.x == 0) {
+            a.apart[c.slot] = sacc.mean_sum();
+            a.a2part[c.slot] = sacc.sq_sum();
+        }
+    }
+
+    // after a round's barrier: thread 0 adds the round's series (block partials in block order)
+    __device__ __forceinline__ static void add_round(const T2* pmr, int nser_round, SeriesAcc<T>& sacc) {
+        for (int gg = 0; gg < nser_round; ++gg) {
+            T2 tot = pmr[gg * B];
+#pragma unroll
+            for (int bb = 1; bb < B; ++bb) tot = cadd(tot, pmr[gg * B + bb]);
+            sacc.add(tot.x, tot.y);
+        }
+    }
+};
+
+template <class T>
+size_t blk_fft_smem(int lg_max, int nf, bool self) {
+    typedef typename cplx<T>::type T2;
+    const size_t H = ((size_t)1 << lg_max) / 2;
+    size_t b = (sizeof(T) == 4 ? H : 0) * sizeof(T2);  // FP32 twiddles
+    if (self) b += (size_t)kBlkFftWarps * 256 * sizeof(T2) + (size_t)nf * sizeof(float4);  // G series, trajectory
+    b += 2 * kBlkFftWarps * sizeof(T2);                                                     // partial means
     b += (size_t)kBlkFftWarps * 512 * (sizeof(T) == 4 ? sizeof(float2) : sizeof(double));  // bins
     return b;
 }
 
 template <class T, int LG>
 __global__ void __launch_bounds__(kBlkFftWarps * 32, sizeof(T) == 4 ? 2 : 1) blk_fft_kernel(CorrLaunch a) {
-    typedef typename cplx<T>::type T2;
-    constexpr int NW = kBlkFftWarps, NT = NW * 32, L = 1 << LG, B = L / 512, E = 16, G = NW / B;
-    static_assert(B >= 2 && B <= NW && NW % B == 0, "block FFT lengths 1,024 .. 4,096");
+    typedef BlkFft<T, LG> F;
+    typedef typename F::T2 T2;
+    constexpr int NW = F::NW, NT = F::NT, L = F::L, E = F::E, G = F::G;
     extern __shared__ __align__(16) unsigned char smem[];
     const CorrChunk c = a.chunks[blockIdx.x];
     const CorrSystem sys = a.systems[c.system];
-    const int nf = sys.nf, tws = a.lg_max - LG;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int b = warp % B, g = warp / B;
-    const int br = (int)(__brev((unsigned)b) >> (32 - ilog2c(B)));
+    const int nf = sys.nf, warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = warp / F::B;
     T2* twsm = reinterpret_cast<T2*>(smem);
     unsigned char* region = smem + (sizeof(T) == 4 ? (size_t)(L / 2) * sizeof(T2) : 0);
     T2* pm = reinterpret_cast<T2*>(region);  // [2][NW]: round parity x warp
     unsigned char* pwb = region + 2 * NW * sizeof(T2);
     const T2* tw = stage_twiddles<T, NT>(twsm, a.tw, a.lg_max);
-    const T2* kbr = reinterpret_cast<const T2*>(sys.kbr) + 512 * b;
+    const T2* kbr = reinterpret_cast<const T2*>(sys.kbr);
     __syncthreads();
-    T2 cu[B / 2];  // W_B^{u br(b)} of the folded stages
-#pragma unroll
-    for (int u = 0; u < B / 2; ++u) cu[u] = tw_full(tw, (512 * u * br) & (L - 1), LG, tws);
+    F f;
+    f.init(tw, a.lg_max - LG);
     PowerAcc<T, E> acc;
     acc.clear();
     SeriesAcc<T> sacc;
@@ -873,111 +1008,84 @@ __global__ void __launch_bounds__(kBlkFftWarps * 32, sizeof(T) == 4 ? 2 : 1) blk
         if (sl < nser) {
             const T2* src = reinterpret_cast<const T2*>(sys.A) + (size_t)(c.v_begin + sl) * nf;
             T2 x[E];
-#pragma unroll
-            for (int m = 0; m < E; ++m) {
-                const int j = lane + 32 * m;
-                T2 sv = j < nf ? src[j] : zero2<T2>();
-#pragma unroll
-                for (int u = 1; u < B / 2; ++u) {
-                    const int n = j + 512 * u;
-                    if (n < nf) sv = cadd(sv, cmul(src[n], cu[u]));
-                }
-                x[m] = br == 0 ? sv : cmul(sv, tw_full(tw, j * br, LG, tws));
-            }
-#pragma unroll
-            for (int hm = E / 2; hm >= 1; hm >>= 1) {  // spans 32 hm inside the lane
-                const int sh = LG - 6 - ilog2c(hm) + tws;
-#pragma unroll
-                for (int m = 0; m < E; ++m) {
-                    if ((m & hm) == 0) {
-                        const T2 u = x[m], w = x[m + hm];
-                        x[m] = cadd(u, w);
-                        x[m + hm] = cmul(csub(u, w), tw[(lane + 32 * (m & (hm - 1))) << sh]);
-                    }
-                }
-            }
-#pragma unroll
-            for (int lh = 4; lh >= 0; --lh) {  // spans 16 .. 1 across lanes
-                const int h = 1 << lh, sh = LG - 1 - lh + tws;
-                const bool upper = (lane & h) != 0;
-                const T sg = upper ? T(-1) : T(1);
-                T2 tv = tw[(lane & (h - 1)) << sh];
-                if (!upper) {
-                    tv.x = T(1);
-                    tv.y = T(0);
-                }
-#pragma unroll
-                for (int m = 0; m < E; ++m) {
-                    const T2 o = shfl_xor2(x[m], h);
-                    T2 d;
-                    d.x = fma(sg, x[m].x, o.x);
-                    d.y = fma(sg, x[m].y, o.y);
-                    x[m] = cmul(d, tv);
-                }
-            }
-            T ax = 0, ay = 0;
-#pragma unroll
-            for (int m = 0; m < E; ++m) {
-                const T P = x[m].x * x[m].x + x[m].y * x[m].y;
-                acc.add(m, P);
-                const T2 kv = __ldg(kbr + lane + 32 * m);
-                ax += P * kv.x;
-                ay += P * kv.y;
-            }
-            pv = warp_sum_t<T>(ax, ay);
+            f.load(x, [&](int n) { return n < nf ? src[n] : zero2<T2>(); });
+            f.stages(x);
+            pv = f.power(x, kbr, acc);
         }
         if (lane == 0) pm[(r & 1) * NW + warp] = pv;
         __syncthreads();
-        if (threadIdx.x == 0)
-            for (int gg = 0; gg < G && r * G + gg < nser; ++gg) {
-                T2 tot = pm[(r & 1) * NW + gg * B];
-#pragma unroll
-                for (int bb = 1; bb < B; ++bb) tot = cadd(tot, pm[(r & 1) * NW + gg * B + bb]);
-                sacc.add(tot.x, tot.y);
-            }
+        if (threadIdx.x == 0) F::add_round(pm + (r & 1) * NW, min(G, nser - r * G), sacc);
     }
-    // bins: warps b, b + B, ... hold block b; combined in warp order
-    if constexpr (sizeof(T) == 4) {
-        float2* pw = reinterpret_cast<float2*>(pwb);
-#pragma unroll
-        for (int m = 0; m < E; ++m) pw[warp * 512 + lane + 32 * m] = make_float2(acc.s[m], acc.c[m]);
+    f.finish(acc, sacc, pwb, a, c);
+}
+
+// Incoherent series of one padded length L (1,024 .. 4,096): CTA per chunk of atoms of one
+// shell. Per atom its trajectory is staged; per round the G series (atom, direction d0 .. d0
+// + G - 1) are generated into shared memory, then transformed block-wise as above.
+template <class T, int LG>
+__global__ void __launch_bounds__(kBlkFftWarps * 32, sizeof(T) == 4 ? 2 : 1) self_blk_fft_kernel(CorrLaunch a) {
+    typedef BlkFft<T, LG> F;
+    typedef typename F::T2 T2;
+    constexpr int NW = F::NW, NT = F::NT, L = F::L, E = F::E, G = F::G, H = L / 2;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const CorrChunk c = a.chunks[blockIdx.x];
+    const CorrSystem sys = a.systems[c.system];
+    const int nf = sys.nf, warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = warp / F::B;
+    T2* twsm = reinterpret_cast<T2*>(smem);
+    unsigned char* region = smem + (sizeof(T) == 4 ? (size_t)H * sizeof(T2) : 0);
+    T2* xs = reinterpret_cast<T2*>(region);  // [G][H] the round's series
+    T2* pm = xs + G * H;                     // [2][NW]
+    float4* rj = reinterpret_cast<float4*>(pm + 2 * NW);  // [nf] the atom's trajectory
+    unsigned char* pwb = reinterpret_cast<unsigned char*>(rj + nf);
+    const T2* tw = stage_twiddles<T, NT>(twsm, a.tw, a.lg_max);
+    const T2* kbr = reinterpret_cast<const T2*>(sys.kbr);
+    const T* bfac = reinterpret_cast<const T*>(sys.bfac);
+    const int v0 = sys.shell_v[c.shell], nd = sys.shell_v[c.shell + 1] - v0;
+    __syncthreads();
+    F f;
+    f.init(tw, a.lg_max - LG);
+    PowerAcc<T, E> acc;
+    acc.clear();
+    SeriesAcc<T> sacc;
+    int r = 0;
+    for (int j = c.v_begin; j < c.v_end; ++j) {
+        __syncthreads();  // the previous atom's series are consumed
+        for (int t = threadIdx.x; t < nf; t += NT) rj[t] = sys.xyz[(size_t)t * sys.na_pad + j];
+        const T bj = bfac[(size_t)c.shell * sys.na_pad + j];
         __syncthreads();
-        float2* dst = reinterpret_cast<float2*>(a.ppart + c.part_off);
-        for (int i = threadIdx.x; i < L; i += NT) {
-            const int bb = i >> 9, loc = i & 511;
-            float hi = 0.f, lo = 0.f;  // float-float sum of the warps' (sum - compensation)
-            for (int w = bb; w < NW; w += B) {
-                const float2 p = pw[w * 512 + loc];
-                const float s = __fadd_rn(hi, p.x), bv = __fsub_rn(s, hi);
-                const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bv)), __fsub_rn(p.x, bv));
-                hi = s;
-                lo = __fadd_rn(lo, __fsub_rn(e, p.y));
+        for (int d0 = 0; d0 < nd; d0 += G, ++r) {
+            for (int i = threadIdx.x; i < G * H; i += NT) {
+                const int gg = i / H, n = i - gg * H, d = d0 + gg;
+                T2 v = zero2<T2>();
+                if (d < nd && n < nf) {
+                    T qx, qy, qz;
+                    load_qv(sys.qv, sys.qrev, (size_t)(v0 + d), qx, qy, qz);
+                    v = self_term(bj, rj[n], qx, qy, qz);
+                }
+                xs[i] = v;
             }
-            dst[i] = make_float2(hi, -lo);  // read back as (sum, compensation): hi + lo
-        }
-    } else {
-        double* pw = reinterpret_cast<double*>(pwb);
-#pragma unroll
-        for (int m = 0; m < E; ++m) pw[warp * 512 + lane + 32 * m] = acc.get(m);
-        __syncthreads();
-        double* dst = a.ppart + c.part_off;
-        for (int i = threadIdx.x; i < L; i += NT) {
-            const int bb = i >> 9, loc = i & 511;
-            double s = 0.0;
-            for (int w = bb; w < NW; w += B) s += pw[w * 512 + loc];
-            dst[i] = s;
+            __syncthreads();
+            T2 pv = zero2<T2>();
+            if (d0 + g < nd) {  // warp-uniform
+                const T2* xg = xs + g * H;
+                T2 x[E];
+                f.load(x, [&](int n) { return xg[n]; });
+                f.stages(x);
+                pv = f.power(x, kbr, acc);
+            }
+            if (lane == 0) pm[(r & 1) * NW + warp] = pv;
+            __syncthreads();
+            if (threadIdx.x == 0) F::add_round(pm + (r & 1) * NW, min(G, nd - d0), sacc);
         }
     }
-    if (threadIdx.x == 0) {
-        a.apart[c.slot] = sacc.mean_sum();
-        a.a2part[c.slot] = sacc.sq_sum();
-    }
+    __syncthreads();
+    f.finish(acc, sacc, pwb, a, c);
 }
 
 template <class T, int LG>
-cudaError_t launch_blk_fft_lg(const CorrLaunch& a, cudaStream_t st) {
-    const size_t sm = blk_fft_smem<T>(a.lg_max);
-    auto k = blk_fft_kernel<T, LG>;
+cudaError_t launch_blk_fft_lg(const CorrLaunch& a, bool self, cudaStream_t st) {
+    const size_t sm = blk_fft_smem<T>(a.lg_max, a.nf_max, self);
+    auto k = self ? self_blk_fft_kernel<T, LG> : blk_fft_kernel<T, LG>;
     cudaError_t e = set_smem(k, sm);
     if (e != cudaSuccess) return e;
     k<<<a.nchunks, kBlkFftWarps * 32, sm, st>>>(a);
@@ -985,11 +1093,11 @@ cudaError_t launch_blk_fft_lg(const CorrLaunch& a, cudaStream_t st) {
 }
 
 template <class T>
-cudaError_t launch_blk_fft(const CorrLaunch& a, cudaStream_t st) {
+cudaError_t launch_blk_fft(const CorrLaunch& a, bool self, cudaStream_t st) {
     switch (a.lg_max) {
-        case 10: return launch_blk_fft_lg<T, 10>(a, st);
-        case 11: return launch_blk_fft_lg<T, 11>(a, st);
-        case 12: return launch_blk_fft_lg<T, 12>(a, st);
+        case 10: return launch_blk_fft_lg<T, 10>(a, self, st);
+        case 11: return launch_blk_fft_lg<T, 11>(a, self, st);
+        case 12: return launch_blk_fft_lg<T, 12>(a, self, st);
     }
     return cudaErrorInvalidValue;
 }
@@ -1033,8 +1141,8 @@ cudaError_t launch_accumulate(const CorrLaunch& a, bool self, cudaStream_t st) {
             return a.precision == PREC_FP32 ? launch_reg_fft<float>(a, self, st) : launch_reg_fft<double>(a, self, st);
         if (a.lg_max <= kWarpFftMaxLg)
             return a.precision == PREC_FP32 ? launch_warp_fft<float>(a, self, st) : launch_warp_fft<double>(a, self, st);
-        if (!self && a.lg_min == a.lg_max && a.lg_max >= kBlkFftMinLg && a.lg_max <= kBlkFftMaxLg)
-            return a.precision == PREC_FP32 ? launch_blk_fft<float>(a, st) : launch_blk_fft<double>(a, st);
+        if (a.lg_min == a.lg_max && a.lg_max >= kBlkFftMinLg && a.lg_max <= kBlkFftMaxLg)
+            return a.precision == PREC_FP32 ? launch_blk_fft<float>(a, self, st) : launch_blk_fft<double>(a, self, st);
         // per-thread spectrum bins sized to the longest series of the launch (registers)
         switch (a.lg_max) {
             case 10: return a.precision == PREC_FP32 ? launch_fft<float, 256, 4>(a, self, st) : launch_fft<double, 256, 4>(a, self, st);

@@ -224,6 +224,22 @@ def test_coherent_block_fft_direct_method_and_many_series(native_lib, precision)
     check(w, precision, "direct")
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("nf", [300, 600, 1500])
+def test_incoherent_block_fft_lengths(native_lib, precision, nf):
+    # the incoherent block-register FFT at padded lengths 1,024, 2,048 and 4,096; 5 directions
+    # per shell leave warps without a series in each atom's last round
+    w = synth.small("self", "autocorrelate", seed=25, na=9, nf=nf, nq=2, nm=5)
+    check(w, precision, "fftw")
+
+
+def test_incoherent_block_fft_direct_method_and_chunks(native_lib):
+    # the direct method's conjugate, and enough atoms for several chunks per shell
+    w = synth.small("self", "autocorrelate", seed=26, na=150, nf=520, nq=2, nm=3)
+    check(w, "fp64", "direct")
+    check(w, "fp32", "direct")
+
+
 def test_out_of_memory_is_a_status(native_lib):
     # a trajectory far beyond HBM (16.7M atoms x 131,072 frames = 35 TB staged): the device
     # allocation fails first, staging returns SASS_ERR_OOM with a message, nothing is read
