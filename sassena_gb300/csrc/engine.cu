@@ -204,6 +204,7 @@ int set_system_classes(SystemState& s, const int32_t* cls, bool on_device, cudaS
     s.h_cls.assign(h.begin(), h.begin() + s.na);
     s.classes_set = true;
     s.rec_map_ok = s.rec_ready = s.rec_valid = false;
+    s.mp_valid = false;  // the cylinder representation carries the classes
     return kOk;
 }
 

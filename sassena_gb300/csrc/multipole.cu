@@ -90,13 +90,16 @@ struct MpBase {
     double e[9];  // e_r, e_phi, e_z of CartesianVectorBase(axis), coor3d.cpp:278-295
 };
 
+// Spherical (r, phi, theta) of every atom in place; or cylindrical (r, phi, z, class) of
+// atom j at slot[j] of its frame row (padding slots: class -1).
 __global__ void mp_convert_kernel(const float4* __restrict__ xyz, int na_pad, int na, int nf, int cylinder,
-                                  MpBase b, float4* __restrict__ out) {
+                                  MpBase b, const int* __restrict__ slot, const int* __restrict__ cls,
+                                  float4* __restrict__ out) {
     const size_t n = (size_t)nf * na_pad;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const int j = (int)(i % na_pad);
         if (j >= na) {
-            out[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            out[i] = make_float4(0.f, 0.f, 0.f, cylinder ? -1.f : 0.f);
             continue;
         }
         const float4 c = xyz[i];
@@ -109,7 +112,7 @@ __global__ void mp_convert_kernel(const float4* __restrict__ xyz, int na_pad, in
             const double pz = x * b.e[6] + y * b.e[7] + z * b.e[8];
             double r, phi, zz;
             to_cylinder(px, py, pz, r, phi, zz);
-            out[i] = make_float4((float)r, (float)phi, (float)zz, 0.f);
+            out[(i - j) + slot[j]] = make_float4((float)r, (float)phi, (float)zz, (float)cls[j]);
         }
     }
 }
@@ -436,7 +439,7 @@ __global__ void __launch_bounds__(kContractThreads) mp_sphere_contract_kernel(Mp
 // cylinder
 // ---------------------------------------------------------------------------------------
 struct MpCylinder {
-    const float4* cyl;   // [nf][na_pad] (r, phi, z)
+    const float4* cyl;   // [nf][na_pad] (r, phi, z, class), atoms in order of frame-0 radius
     const int* cls;
     const double* cf;    // [nq][nclass]
     const double* qcyl;  // [nq][3] (q_r, phi_q, q_z)
@@ -477,7 +480,7 @@ __global__ void __launch_bounds__(kCylThreads) mp_cylinder_kernel(MpCylinder a) 
                 const double qr = a.qcyl[3 * q], qz = a.qcyl[3 * q + 2];
                 const float4 c = row[j];
                 const double r = c.x, z = c.z;
-                const int cl = a.cls[j];
+                const int cl = (int)c.w;  // atoms sit in radius order; w carries the class
                 const double b = cl >= 0 ? a.cf[(size_t)q * a.nclass + cl] : 0.0;
                 double sgn = 1.0;  // parallel_sign, multipole_scatter_device.cpp:944-948
                 if (z != 0 && qz != 0) sgn = (z * qz) / (fabs(z) * fabs(qz));
@@ -705,10 +708,35 @@ extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const d
     // representation cache (rebuilt after staging or for another device type / axis)
     if (s.mp_type != type || !s.mp_valid || (cyl && memcmp(s.mp_axis, axis, sizeof(s.mp_axis)) != 0)) {
         MCK(s.mp_xyz.ensure(nf * na_pad * sizeof(float4)));
+        const int* slot = nullptr;
+        if (cyl) {
+            // Atoms sorted by their frame-0 distance from the axis: the cylinder kernel's
+            // 32-atom tiles then hold similar Bessel arguments q_r r, so a warp's rows take one
+            // branch (Miller's recurrence or Hankel's expansion) with similar trip counts. A
+            // warp-wide FP64 instruction holds the narrow FP64 pipe whatever its active lanes.
+            std::vector<float4> f0(na_pad);
+            MCK(cudaMemcpyAsync(f0.data(), s.xyz.p, na_pad * sizeof(float4), cudaMemcpyDeviceToHost, st));
+            MCK(cudaStreamSynchronize(st));
+            std::vector<double> r2(s.na);
+            for (size_t j = 0; j < s.na; ++j) {
+                const double x = f0[j].x, y = f0[j].y, z = f0[j].z;
+                const double px = x * base.e[0] + y * base.e[1] + z * base.e[2];
+                const double py = x * base.e[3] + y * base.e[4] + z * base.e[5];
+                r2[j] = px * px + py * py;
+            }
+            std::vector<int> order(s.na), pos(s.na);
+            for (size_t j = 0; j < s.na; ++j) order[j] = (int)j;
+            std::stable_sort(order.begin(), order.end(), [&](int u, int v) { return r2[u] < r2[v]; });
+            for (size_t k = 0; k < s.na; ++k) pos[order[k]] = (int)k;
+            MCK(p->mp_slot.ensure(s.na * sizeof(int)));
+            MCK(cudaMemcpyAsync(p->mp_slot.p, pos.data(), s.na * sizeof(int), cudaMemcpyHostToDevice, st));
+            MCK(cudaStreamSynchronize(st));
+            slot = p->mp_slot.as<int>();
+        }
         const size_t n = nf * na_pad;
         const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
         mp_convert_kernel<<<std::max(blocks, 1), 256, 0, st>>>(s.xyz.as<float4>(), (int)na_pad, (int)s.na, (int)nf, cyl,
-                                                                base, s.mp_xyz.as<float4>());
+                                                                base, slot, s.cls.as<int>(), s.mp_xyz.as<float4>());
         MCK(cudaGetLastError());
         ++launches;
         s.mp_type = type;

@@ -24,7 +24,7 @@ struct sass_plan {
     int rec_k = 0;  // shell recurrence: 0 automatic, -1 off, else shells per lane
     sassgpu::DevBuf qv, cf, fqt, fq, fq2, amp_tmp;
     // multipole devices: packed per-call inputs, basis batch, amplitudes, results
-    sassgpu::DevBuf mp_in, mp_Jb, mp_Yc, mp_amp, mp_out, mp_ycf;
+    sassgpu::DevBuf mp_in, mp_Jb, mp_Yc, mp_amp, mp_out, mp_ycf, mp_slot;
     // staging pre-pass: packed lists, FP64 system frames, float upload, fit copy, vectors
     sassgpu::DevBuf pp_lists, pp_W, pp_F, pp_C, pp_vec;
 };
