@@ -90,8 +90,8 @@ struct MpBase {
     double e[9];  // e_r, e_phi, e_z of CartesianVectorBase(axis), coor3d.cpp:278-295
 };
 
-// Spherical (r, phi, theta) of every atom in place; or cylindrical (r, phi, z, class) of
-// atom j at slot[j] of its frame row (padding slots: class -1).
+// Spherical (r, phi, theta, class) or cylindrical (r, phi, z, class) of atom j at slot[j] of
+// its frame row (padding slots: class -1).
 __global__ void mp_convert_kernel(const float4* __restrict__ xyz, int na_pad, int na, int nf, int cylinder,
                                   MpBase b, const int* __restrict__ slot, const int* __restrict__ cls,
                                   float4* __restrict__ out) {
@@ -99,12 +99,14 @@ __global__ void mp_convert_kernel(const float4* __restrict__ xyz, int na_pad, in
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const int j = (int)(i % na_pad);
         if (j >= na) {
-            out[i] = make_float4(0.f, 0.f, 0.f, cylinder ? -1.f : 0.f);
+            out[i] = make_float4(0.f, 0.f, 0.f, -1.f);
             continue;
         }
         const float4 c = xyz[i];
         if (!cylinder) {
-            out[i] = to_spherical(c.x, c.y, c.z);
+            float4 v = to_spherical(c.x, c.y, c.z);
+            v.w = (float)cls[j];
+            out[(i - j) + slot[j]] = v;
         } else {
             const double x = c.x, y = c.y, z = c.z;
             const double px = x * b.e[0] + y * b.e[1] + z * b.e[2];
@@ -318,7 +320,7 @@ __device__ void cyl_bessel_row(int N, double x, double* out, int stride) {
 // sphere: basis and contraction
 // ---------------------------------------------------------------------------------------
 struct MpSphereBasis {
-    const float4* sph;  // [nf][na_pad] (r, phi, theta)
+    const float4* sph;  // [nf][na_pad] (r, phi, theta, class), atoms in order of frame-0 radius
     const int* cls;     // [na_pad] (-1 padding)
     const double* cf;   // [nq][nclass]
     const double* qlen; // [nq]
@@ -355,7 +357,7 @@ __global__ void __launch_bounds__(128) mp_jl_kernel(MpSphereBasis a) {
         const size_t fq = i / a.na_pad;
         const int j = (int)(i - fq * a.na_pad), fl = (int)(fq / a.nq), q = (int)(fq - (size_t)fl * a.nq);
         const float4 c = a.sph[(size_t)(a.f0 + fl) * a.na_pad + j];
-        const int cl = a.cls[j];
+        const int cl = (int)c.w;  // atoms sit in radius order; w carries the class (-1: padding)
         const double b = cl >= 0 ? a.cf[(size_t)q * a.nclass + cl] : 0.0;
         sph_bessel_row(a.L, a.qlen[q] * (double)c.x, b, a.Jb + (fq * (a.L + 1)) * a.na_pad + j, a.na_pad);
     }
@@ -708,31 +710,33 @@ extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const d
     // representation cache (rebuilt after staging or for another device type / axis)
     if (s.mp_type != type || !s.mp_valid || (cyl && memcmp(s.mp_axis, axis, sizeof(s.mp_axis)) != 0)) {
         MCK(s.mp_xyz.ensure(nf * na_pad * sizeof(float4)));
-        const int* slot = nullptr;
-        if (cyl) {
-            // Atoms sorted by their frame-0 distance from the axis: the cylinder kernel's
-            // 32-atom tiles then hold similar Bessel arguments q_r r, so a warp's rows take one
-            // branch (Miller's recurrence or Hankel's expansion) with similar trip counts. A
-            // warp-wide FP64 instruction holds the narrow FP64 pipe whatever its active lanes.
-            std::vector<float4> f0(na_pad);
-            MCK(cudaMemcpyAsync(f0.data(), s.xyz.p, na_pad * sizeof(float4), cudaMemcpyDeviceToHost, st));
-            MCK(cudaStreamSynchronize(st));
-            std::vector<double> r2(s.na);
-            for (size_t j = 0; j < s.na; ++j) {
-                const double x = f0[j].x, y = f0[j].y, z = f0[j].z;
+        // Atoms sorted by their frame-0 distance from the axis (cylinder) or the origin
+        // (sphere): consecutive atoms then have similar Bessel arguments, so a warp's 32
+        // Bessel rows take one branch (Miller's recurrence, Hankel's expansion, the power
+        // series, the upward recurrence) with similar trip counts. A warp-wide FP64
+        // instruction holds the narrow FP64 pipe whatever its active lanes.
+        std::vector<float4> f0(na_pad);
+        MCK(cudaMemcpyAsync(f0.data(), s.xyz.p, na_pad * sizeof(float4), cudaMemcpyDeviceToHost, st));
+        MCK(cudaStreamSynchronize(st));
+        std::vector<double> r2(s.na);
+        for (size_t j = 0; j < s.na; ++j) {
+            const double x = f0[j].x, y = f0[j].y, z = f0[j].z;
+            if (cyl) {
                 const double px = x * base.e[0] + y * base.e[1] + z * base.e[2];
                 const double py = x * base.e[3] + y * base.e[4] + z * base.e[5];
                 r2[j] = px * px + py * py;
+            } else {
+                r2[j] = x * x + y * y + z * z;
             }
-            std::vector<int> order(s.na), pos(s.na);
-            for (size_t j = 0; j < s.na; ++j) order[j] = (int)j;
-            std::stable_sort(order.begin(), order.end(), [&](int u, int v) { return r2[u] < r2[v]; });
-            for (size_t k = 0; k < s.na; ++k) pos[order[k]] = (int)k;
-            MCK(p->mp_slot.ensure(s.na * sizeof(int)));
-            MCK(cudaMemcpyAsync(p->mp_slot.p, pos.data(), s.na * sizeof(int), cudaMemcpyHostToDevice, st));
-            MCK(cudaStreamSynchronize(st));
-            slot = p->mp_slot.as<int>();
         }
+        std::vector<int> order(s.na), pos(s.na);
+        for (size_t j = 0; j < s.na; ++j) order[j] = (int)j;
+        std::stable_sort(order.begin(), order.end(), [&](int u, int v) { return r2[u] < r2[v]; });
+        for (size_t k = 0; k < s.na; ++k) pos[order[k]] = (int)k;
+        MCK(p->mp_slot.ensure(s.na * sizeof(int)));
+        MCK(cudaMemcpyAsync(p->mp_slot.p, pos.data(), s.na * sizeof(int), cudaMemcpyHostToDevice, st));
+        MCK(cudaStreamSynchronize(st));
+        const int* slot = p->mp_slot.as<int>();
         const size_t n = nf * na_pad;
         const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
         mp_convert_kernel<<<std::max(blocks, 1), 256, 0, st>>>(s.xyz.as<float4>(), (int)na_pad, (int)s.na, (int)nf, cyl,

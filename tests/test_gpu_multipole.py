@@ -67,6 +67,26 @@ def test_large_arguments(native_lib):
     check(w, q, "cylinder", oracle.cylinder_moments(20), axis=(0.2, -0.5, 1.0))
 
 
+def test_sphere_cached_representation_follows_classes_and_frames(native_lib):
+    # the sphere's representation (atoms in radius order, classes carried along) is cached
+    # between calls: new classes or a new staging rebuild it
+    w, q = case(59, na=70, nf=10, nq=2, box=30.0)
+    mom = oracle.sphere_moments(6)
+    cls2 = w.atom_class[::-1].copy()
+    w2 = synth.small("all", "autocorrelate", seed=60, na=70, nf=10, nq=2, nm=3, box=30.0)
+    with abi.Plan(w.na, w.nf, len(w.class_names), "all", "autocorrelate", "fftw", "fp64") as p:
+        p.stage(w.coords)
+        p.set_classes(w.atom_class)
+        for coords, cls in ((w.coords, w.atom_class), (w.coords, cls2), (w2.coords, cls2)):
+            if coords is not w.coords:
+                p.stage(coords)
+            p.set_classes(cls)
+            fqt, fq, fq2 = p.multipole("sphere", q, w.class_factors, mom)
+            ref = oracle.mp_sphere(coords, q, w.class_factors[:, cls], mom)
+            assert rel_err_sqt(fqt, ref[0]).max() <= 1e-12
+            assert rel_err_vec(fq, cplx(ref[1])) <= 1e-12
+
+
 def test_cylinder_cached_representation_follows_classes_and_frames(native_lib):
     # the cylinder representation (atoms in radius order, classes carried along) is cached
     # between calls: new classes or a new staging rebuild it, another axis too
