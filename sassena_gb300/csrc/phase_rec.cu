@@ -128,7 +128,6 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 20 ? 2 : 1) phase_rec_ker
 #pragma unroll
         for (int k = 0; k < K; ++k) acc[k] = make_float2(0.f, 0.f);
         const float2 qd = make_float2(q0, dq);
-        const float2 kM = make_float2(12582912.0f, 12582912.0f), kNeg = make_float2(-1.f, -1.f);
         const float2 k2pi = make_float2(6.28318530717958647692f, 6.28318530717958647692f);
         const float2 kTwo = make_float2(2.f, -2.f);
         const int f = td.f0 + warp;
@@ -157,10 +156,12 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 20 ? 2 : 1) phase_rec_ker
                         const float4 r = cx[b * kRecBlock + jj];
                         const float du = fmaf(r.z, uz, fmaf(r.y, uy, __fmul_rn(r.x, ux)));
                         const float2 dd = make_float2(du, du);
-                        // (lam0, dlam) x u.r in revolutions, reduced to [-1/2, 1/2]: the sum with
-                        // 1.5 * 2^23 rounds to the nearest integer n, then f = lam u.r - n by FMA
-                        const float2 nm = __ffma2_rn(qd, dd, kM);
-                        const float2 nn = __ffma2_rn(nm, kNeg, kM);  // -n, exact
+                        // (lam0, dlam) x u.r in revolutions, reduced to [-1/2, 1/2]: n is the
+                        // nearest integer of the rounded product, then f = lam u.r - n by FMA
+                        // (rint runs beside the FMA pipe, which bounds this kernel; magic-number
+                        // rounding cost two FMA-pipe operations per pair, 1.7 % of the kernel)
+                        const float2 pr = __fmul2_rn(qd, dd);
+                        const float2 nn = make_float2(-rintf(pr.x), -rintf(pr.y));
                         const float2 x = __fmul2_rn(__ffma2_rn(qd, dd, nn), k2pi);
                         float s0, c0, s1, c1;
                         __sincosf(x.x, &s0, &c0);
