@@ -158,8 +158,8 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 20 ? 2 : 1) phase_rec_ker
                         const float2 dd = make_float2(du, du);
                         // (lam0, dlam) x u.r in revolutions, reduced to [-1/2, 1/2]: n is the
                         // nearest integer of the rounded product, then f = lam u.r - n by FMA
-                        // (rint runs beside the FMA pipe, which bounds this kernel; magic-number
-                        // rounding cost two FMA-pipe operations per pair, 1.7 % of the kernel)
+                        // (magic-number rounding took two more operations per pair on the FMA
+                        // pipe, which bounds this kernel: 1.7 % slower on the GB300)
                         const float2 pr = __fmul2_rn(qd, dd);
                         const float2 nn = make_float2(-rintf(pr.x), -rintf(pr.y));
                         const float2 x = __fmul2_rn(__ffma2_rn(qd, dd, nn), k2pi);
