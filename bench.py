@@ -458,7 +458,10 @@ def run_ours(args, dist):
     corr_bytes = (w.nq * w.nm * w.nf * 8) + (w.nq * w.nf * 16)
     lg = max(2, int(np.ceil(np.log2(2 * w.nf))))
     if w.dsp != "autocorrelate":
-        corr_kernel = "corr_direct_kernel" if w.scattering == "all" else "self_direct_kernel"
+        if w.scattering == "all":
+            corr_kernel = "corr_sq_warp_kernel" if w.nf <= 512 else "corr_direct_kernel"
+        else:
+            corr_kernel = "self_direct_kernel"
     elif lg <= 9:
         corr_kernel = "reg_fft_kernel"
     elif lg <= 12 and w.scattering == "all":

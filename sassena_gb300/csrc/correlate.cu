@@ -631,6 +631,144 @@ __global__ void expand_factors_kernel(const double* __restrict__ cf, int nclass,
     }
 }
 
+// ---------------------------------------------------------------------------------------
+// dsp = square / plain, coherent, series of at most 32 K frames: warp per series. Lane l holds
+// frames l + 32 k (k < K) of the chunk's per-frame sums in registers (Kahan FP32 in the FP32
+// form, FP64 in the FP64 form); each series' mean is one warp reduction; the warps' frame
+// sums and series sums are combined in warp order at the end of the chunk. Replaces a CTA per
+// series with two CTA-wide FP64 reductions each (short series left most of its threads idle).
+// ---------------------------------------------------------------------------------------
+constexpr int kSqWarps = 8;
+
+template <class T>
+struct FrameAcc;  // per-frame complex sums of one lane
+
+template <>
+struct FrameAcc<float> {
+    float sx, sy, cx, cy;
+    __device__ void clear() { sx = sy = cx = cy = 0.f; }
+    __device__ __forceinline__ void add(float x, float y) {
+        SeriesAcc<float>::kahan(sx, cx, x);
+        SeriesAcc<float>::kahan(sy, cy, y);
+    }
+    __device__ double2 get() const { return make_double2((double)sx - (double)cx, (double)sy - (double)cy); }
+};
+
+template <>
+struct FrameAcc<double> {
+    double sx, sy;
+    __device__ void clear() { sx = sy = 0.0; }
+    __device__ __forceinline__ void add(double x, double y) {
+        sx += x;
+        sy += y;
+    }
+    __device__ double2 get() const { return make_double2(sx, sy); }
+};
+
+template <class T, int K>
+__global__ void __launch_bounds__(kSqWarps * 32) corr_sq_warp_kernel(CorrLaunch a) {
+    typedef typename cplx<T>::type T2;
+    constexpr int NW = kSqWarps, NT = NW * 32;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const CorrChunk c = a.chunks[blockIdx.x];
+    const CorrSystem sys = a.systems[c.system];
+    const int nf = sys.nf, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool square = a.dsp == DSP_SQUARE;
+    const T2* A = reinterpret_cast<const T2*>(sys.A);
+    double2* pw = reinterpret_cast<double2*>(smem);  // [NW][nf] frame sums, then [NW] series sums
+    FrameAcc<T> acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k].clear();
+    SeriesAcc<T> sacc;
+    const T inv_nf = T(1) / T(nf);
+    for (int v = c.v_begin + warp; v < c.v_end; v += NW) {
+        T2 ph;
+        ph.x = T(1);
+        ph.y = T(0);
+        if (!square && a.restore_phase) {
+            const double* q = sys.qv + 3 * (size_t)v;
+            double s, co;
+            sincos(q[0] * sys.cx + q[1] * sys.cy + q[2] * sys.cz, &s, &co);
+            ph.x = (T)co;
+            ph.y = (T)s;
+        }
+        T px = 0, py = 0;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int t = lane + 32 * k;
+            if (t < nf) {
+                const T2 x = A[(size_t)v * nf + t];
+                T2 cv;
+                if (square) {
+                    cv.x = x.x * x.x + x.y * x.y;
+                    cv.y = T(0);
+                } else {
+                    cv = cmul(x, ph);
+                }
+                acc[k].add(cv.x, cv.y);
+                px += cv.x;
+                py += cv.y;
+            }
+        }
+        const T2 sv = warp_sum_t<T>(px, py);
+        if (lane == 0) sacc.add(sv.x * inv_nf, sv.y * inv_nf);
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int t = lane + 32 * k;
+        if (t < nf) pw[(size_t)warp * nf + t] = acc[k].get();
+    }
+    double2* red = pw + (size_t)NW * nf;
+    double* red2 = reinterpret_cast<double*>(red + NW);
+    if (lane == 0) {
+        red[warp] = sacc.mean_sum();
+        red2[warp] = sacc.sq_sum();
+    }
+    __syncthreads();
+    double* dst = a.ppart + c.part_off;
+    for (int t = threadIdx.x; t < nf; t += NT) {
+        double2 s = make_double2(0.0, 0.0);
+        for (int w = 0; w < NW; ++w) {
+            s.x += pw[(size_t)w * nf + t].x;
+            s.y += pw[(size_t)w * nf + t].y;
+        }
+        dst[2 * t] = s.x;
+        dst[2 * t + 1] = s.y;
+    }
+    if (threadIdx.x == 0) {
+        double2 as = make_double2(0.0, 0.0);
+        double a2 = 0.0;
+        for (int w = 0; w < NW; ++w) {
+            as.x += red[w].x;
+            as.y += red[w].y;
+            a2 += red2[w];
+        }
+        a.apart[c.slot] = as;
+        a.a2part[c.slot] = a2;
+    }
+}
+
+template <class T, int K>
+cudaError_t launch_sq_warp_k(const CorrLaunch& a, cudaStream_t st) {
+    const size_t sm = (size_t)kSqWarps * a.nf_max * sizeof(double2) + kSqWarps * (sizeof(double2) + sizeof(double));
+    auto k = corr_sq_warp_kernel<T, K>;
+    cudaError_t e = set_smem(k, sm);
+    if (e != cudaSuccess) return e;
+    k<<<a.nchunks, kSqWarps * 32, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_sq_warp(const CorrLaunch& a, cudaStream_t st) {
+    const int k = (a.nf_max + 31) / 32;
+    if (k <= 2) return launch_sq_warp_k<T, 2>(a, st);
+    if (k <= 4) return launch_sq_warp_k<T, 4>(a, st);
+    if (k <= 8) return launch_sq_warp_k<T, 8>(a, st);
+    return launch_sq_warp_k<T, 16>(a, st);
+}
+
+constexpr int kSqWarpMaxNf = 512;
+
 template <class T, int NT, int MAXR>
 cudaError_t launch_fft(const CorrLaunch& a, bool self, cudaStream_t st) {
     const size_t sm = fft_smem<T>(a.lg_max, NT, a.nf_max, self);
@@ -1154,6 +1292,8 @@ cudaError_t launch_accumulate(const CorrLaunch& a, bool self, cudaStream_t st) {
     if (self) {
         if (a.precision == PREC_FP32) self_direct_kernel<float, 256, 16><<<a.nchunks, 256, 0, st>>>(a);
         else self_direct_kernel<double, 256, 16><<<a.nchunks, 256, 0, st>>>(a);
+    } else if (a.dsp != DSP_AUTOCORRELATE && a.nf_max <= kSqWarpMaxNf) {
+        return a.precision == PREC_FP32 ? launch_sq_warp<float>(a, st) : launch_sq_warp<double>(a, st);
     } else {
         if (a.precision == PREC_FP32) corr_direct_kernel<float2, 256, 16><<<a.nchunks, 256, 0, st>>>(a);
         else corr_direct_kernel<double2, 256, 16><<<a.nchunks, 256, 0, st>>>(a);

@@ -240,6 +240,16 @@ def test_incoherent_block_fft_direct_method_and_chunks(native_lib):
     check(w, "fp32", "direct")
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("dsp", ["square", "plain"])
+@pytest.mark.parametrize("nf", [50, 100, 230, 500])
+def test_coherent_square_plain_warp_kernel(native_lib, precision, dsp, nf):
+    # warp per series with 2, 4, 8 and 16 frames per lane; 45 directions per shell give every
+    # warp of a chunk a different number of series
+    w = synth.small("all", dsp, seed=27, na=13, nf=nf, nq=3, nm=45)
+    check(w, precision, "fftw")
+
+
 def test_out_of_memory_is_a_status(native_lib):
     # a trajectory far beyond HBM (16.7M atoms x 131,072 frames = 35 TB staged): the device
     # allocation fails first, staging returns SASS_ERR_OOM with a message, nothing is read
