@@ -757,8 +757,7 @@ def run_batched(args, dist):
     ms = dist.max(e0.elapsed_time(e1) / steps)
     info = b.info()
     sched = b.schedule()
-    bt = b.timing()
-    launches = bt["kernel_launches"] * steps
+    launches = b.timing()["kernel_launches"] * steps
     # end to end: stage every system from host memory, one run, copy all results back
     e2e = []
     for i in range(0 if args.no_e2e else 2):
@@ -784,7 +783,6 @@ def run_batched(args, dist):
                       "terms_per_step": terms, "phase_tiles": info["phase_tiles"],
                       "schedule": sched,
                       "tile": tuned, "autotune_s": tune_s, "create_s": create_s,
-                      "last_run_ms": {k: bt[k] for k in ("phase_ms", "corr_ms", "finalize_ms")},
                       "l2": "inputs larger than L2"},
            "e2e": {"value": terms / (min(e2e) * 1e-3) if e2e else None, "unit": UNIT,
                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
