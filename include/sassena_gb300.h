@@ -41,7 +41,7 @@ extern "C" {
 #define SASS_OK 0
 #define SASS_ERR_ARG 1          /* invalid argument or shape */
 #define SASS_ERR_OOM 2          /* device or host allocation failed */
-#define SASS_ERR_UNSUPPORTED 3  /* configuration outside this build (e.g. NF > 4096 with FFT) */
+#define SASS_ERR_UNSUPPORTED 3  /* configuration outside this build (e.g. NF > 524,288 with FFT) */
 #define SASS_ERR_CUDA 4         /* CUDA runtime error */
 #define SASS_ERR_TIMEOUT 5      /* a bounded device-side wait gave up */
 #define SASS_ERR_STATE 6        /* call out of order (e.g. compute before staging) */
