@@ -665,6 +665,23 @@ struct FrameAcc<double> {
     __device__ double2 get() const { return make_double2(sx, sy); }
 };
 
+// exp(i q_v . c), the centring phase restored for dsp = plain in the FP32 form: in
+// revolutions with the nearest integer removed, then the SFU (phase error about 1e-5 rad
+// for |q . c| up to 25 revolutions, far inside the FP32 form's 1e-3). FP64 form: FP64.
+__device__ __forceinline__ float2 restore_phase(const CorrSystem& sys, size_t v, float) {
+    const float4 q = sys.qrev[v];
+    const float u = fmaf(q.z, (float)sys.cz, fmaf(q.y, (float)sys.cy, q.x * (float)sys.cx));
+    float s, c;
+    __sincosf(__fsub_rn(u, rintf(u)) * 6.28318530717958647692f, &s, &c);
+    return make_float2(c, s);
+}
+__device__ __forceinline__ double2 restore_phase(const CorrSystem& sys, size_t v, double) {
+    const double* q = sys.qv + 3 * v;
+    double s, c;
+    sincos(q[0] * sys.cx + q[1] * sys.cy + q[2] * sys.cz, &s, &c);
+    return make_double2(c, s);
+}
+
 template <class T, int K>
 __global__ void __launch_bounds__(kSqWarps * 32) corr_sq_warp_kernel(CorrLaunch a) {
     typedef typename cplx<T>::type T2;
@@ -685,13 +702,7 @@ __global__ void __launch_bounds__(kSqWarps * 32) corr_sq_warp_kernel(CorrLaunch 
         T2 ph;
         ph.x = T(1);
         ph.y = T(0);
-        if (!square && a.restore_phase) {
-            const double* q = sys.qv + 3 * (size_t)v;
-            double s, co;
-            sincos(q[0] * sys.cx + q[1] * sys.cy + q[2] * sys.cz, &s, &co);
-            ph.x = (T)co;
-            ph.y = (T)s;
-        }
+        if (!square && a.restore_phase) ph = restore_phase(sys, (size_t)v, T());
         T px = 0, py = 0;
 #pragma unroll
         for (int k = 0; k < K; ++k) {
@@ -768,6 +779,126 @@ cudaError_t launch_sq_warp(const CorrLaunch& a, cudaStream_t st) {
 }
 
 constexpr int kSqWarpMaxNf = 512;
+
+// The same for the incoherent device: trajectories of kSqAtoms atoms of the chunk are staged
+// per barrier (coalesced over atoms), and the warps share out their (atom, direction) series,
+// generated in registers.
+constexpr int kSqAtoms = 4;
+
+template <class T, int K>
+__global__ void __launch_bounds__(kSqWarps * 32) self_sq_warp_kernel(CorrLaunch a) {
+    typedef typename cplx<T>::type T2;
+    constexpr int NW = kSqWarps, NT = NW * 32, NAS = kSqAtoms;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const CorrChunk c = a.chunks[blockIdx.x];
+    const CorrSystem sys = a.systems[c.system];
+    const int nf = sys.nf, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool square = a.dsp == DSP_SQUARE;
+    const T* bfac = reinterpret_cast<const T*>(sys.bfac);
+    const int v0 = sys.shell_v[c.shell], nd = sys.shell_v[c.shell + 1] - v0;
+    float4* rj = reinterpret_cast<float4*>(smem);                          // [NAS][nf]
+    double2* pw = reinterpret_cast<double2*>(rj + (size_t)NAS * a.nf_max);  // [NW][nf], then series sums
+    T* bsm = reinterpret_cast<T*>(pw + (size_t)NW * a.nf_max + 2 * NW);     // [NAS]
+    FrameAcc<T> acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k].clear();
+    SeriesAcc<T> sacc;
+    const T inv_nf = T(1) / T(nf);
+    for (int j0 = c.v_begin; j0 < c.v_end; j0 += NAS) {
+        const int na = min(NAS, c.v_end - j0);
+        __syncthreads();  // every warp is done with the previous atoms' trajectories
+        for (int i = threadIdx.x; i < na * nf; i += NT) {
+            const int t = i / na, at = i - t * na;
+            rj[at * nf + t] = sys.xyz[(size_t)t * sys.na_pad + j0 + at];
+        }
+        if (threadIdx.x < na) bsm[threadIdx.x] = bfac[(size_t)c.shell * sys.na_pad + j0 + threadIdx.x];
+        __syncthreads();
+        for (int pr = warp; pr < na * nd; pr += NW) {
+            const int at = pr / nd, v = v0 + (pr - at * nd);
+            T qx, qy, qz;
+            load_qv(sys.qv, sys.qrev, (size_t)v, qx, qy, qz);
+            const T b = bsm[at];
+            const float4* ra = rj + (size_t)at * nf;
+            T2 ph;
+            ph.x = T(1);
+            ph.y = T(0);
+            if (!square && a.restore_phase) ph = restore_phase(sys, (size_t)v, T());
+            T px = 0, py = 0;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const int t = lane + 32 * k;
+                if (t < nf) {
+                    const T2 x = self_term(b, ra[t], qx, qy, qz);
+                    T2 cv;
+                    if (square) {
+                        cv.x = x.x * x.x + x.y * x.y;
+                        cv.y = T(0);
+                    } else {
+                        cv = cmul(x, ph);
+                    }
+                    acc[k].add(cv.x, cv.y);
+                    px += cv.x;
+                    py += cv.y;
+                }
+            }
+            const T2 sv = warp_sum_t<T>(px, py);
+            if (lane == 0) sacc.add(sv.x * inv_nf, sv.y * inv_nf);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int t = lane + 32 * k;
+        if (t < nf) pw[(size_t)warp * nf + t] = acc[k].get();
+    }
+    double2* red = pw + (size_t)NW * nf;
+    double* red2 = reinterpret_cast<double*>(red + NW);
+    if (lane == 0) {
+        red[warp] = sacc.mean_sum();
+        red2[warp] = sacc.sq_sum();
+    }
+    __syncthreads();
+    double* dst = a.ppart + c.part_off;
+    for (int t = threadIdx.x; t < nf; t += NT) {
+        double2 s = make_double2(0.0, 0.0);
+        for (int w = 0; w < NW; ++w) {
+            s.x += pw[(size_t)w * nf + t].x;
+            s.y += pw[(size_t)w * nf + t].y;
+        }
+        dst[2 * t] = s.x;
+        dst[2 * t + 1] = s.y;
+    }
+    if (threadIdx.x == 0) {
+        double2 as = make_double2(0.0, 0.0);
+        double a2 = 0.0;
+        for (int w = 0; w < NW; ++w) {
+            as.x += red[w].x;
+            as.y += red[w].y;
+            a2 += red2[w];
+        }
+        a.apart[c.slot] = as;
+        a.a2part[c.slot] = a2;
+    }
+}
+
+template <class T, int K>
+cudaError_t launch_self_sq_warp_k(const CorrLaunch& a, cudaStream_t st) {
+    const size_t sm = (size_t)kSqAtoms * a.nf_max * sizeof(float4) + (size_t)kSqWarps * a.nf_max * sizeof(double2) +
+                      2 * kSqWarps * sizeof(double2) + kSqAtoms * sizeof(double);
+    auto k = self_sq_warp_kernel<T, K>;
+    cudaError_t e = set_smem(k, sm);
+    if (e != cudaSuccess) return e;
+    k<<<a.nchunks, kSqWarps * 32, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_self_sq_warp(const CorrLaunch& a, cudaStream_t st) {
+    const int k = (a.nf_max + 31) / 32;
+    if (k <= 2) return launch_self_sq_warp_k<T, 2>(a, st);
+    if (k <= 4) return launch_self_sq_warp_k<T, 4>(a, st);
+    if (k <= 8) return launch_self_sq_warp_k<T, 8>(a, st);
+    return launch_self_sq_warp_k<T, 16>(a, st);
+}
 
 template <class T, int NT, int MAXR>
 cudaError_t launch_fft(const CorrLaunch& a, bool self, cudaStream_t st) {
@@ -1289,7 +1420,9 @@ cudaError_t launch_accumulate(const CorrLaunch& a, bool self, cudaStream_t st) {
             default: return a.precision == PREC_FP32 ? launch_fft<float, 256, 32>(a, self, st) : launch_fft<double, 256, 32>(a, self, st);
         }
     }
-    if (self) {
+    if (self && a.dsp != DSP_AUTOCORRELATE && a.nf_max <= kSqWarpMaxNf) {
+        return a.precision == PREC_FP32 ? launch_self_sq_warp<float>(a, st) : launch_self_sq_warp<double>(a, st);
+    } else if (self) {
         if (a.precision == PREC_FP32) self_direct_kernel<float, 256, 16><<<a.nchunks, 256, 0, st>>>(a);
         else self_direct_kernel<double, 256, 16><<<a.nchunks, 256, 0, st>>>(a);
     } else if (a.dsp != DSP_AUTOCORRELATE && a.nf_max <= kSqWarpMaxNf) {

@@ -250,6 +250,16 @@ def test_coherent_square_plain_warp_kernel(native_lib, precision, dsp, nf):
     check(w, precision, "fftw")
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("dsp", ["square", "plain"])
+@pytest.mark.parametrize("nf", [40, 100, 300, 500])
+def test_incoherent_square_plain_warp_kernel(native_lib, precision, dsp, nf):
+    # the incoherent warp-per-series form: 4 atoms staged per barrier, 150 atoms give several
+    # chunks per shell and a last group of fewer atoms; 7 directions leave warps idle
+    w = synth.small("self", dsp, seed=28, na=150, nf=nf, nq=2, nm=7)
+    check(w, precision, "fftw")
+
+
 def test_out_of_memory_is_a_status(native_lib):
     # a trajectory far beyond HBM (16.7M atoms x 131,072 frames = 35 TB staged): the device
     # allocation fails first, staging returns SASS_ERR_OOM with a message, nothing is read
