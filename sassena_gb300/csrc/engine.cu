@@ -508,7 +508,13 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
                 }
             }
         }
-        nsplit_[i] = items[i].d_amp_given ? 1 : std::max(1, std::min(ns, max_split));
+        // each split writes FP64 partials of the item's whole amplitude array: at most 4 GiB
+        // of them (items that large have tiles enough without splits, and allocating and
+        // freeing tens of GB, as small split sizes on large systems would, slows every later
+        // allocation of the process)
+        const size_t per_split = (size_t)items[i].offs.back() * items[i].sys->nf * 16;
+        const int budget = (int)std::max<size_t>(1, ((size_t)1 << 32) / std::max<size_t>(per_split, 1));
+        nsplit_[i] = items[i].d_amp_given ? 1 : std::max(1, std::min(std::min(ns, max_split), budget));
         stats_.max_split = std::max(stats_.max_split, nsplit_[i]);
     }
     stats_.split_atoms = cfg.split_atoms;
