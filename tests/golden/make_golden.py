@@ -11,7 +11,8 @@ on the random streams of numpy staying the same across versions.
 Families (one .npz each, arrays prefixed by the case name):
   scatter_*   coherent / incoherent devices, every dsp type and method, the three benchmark
               workload shapes shrunk (incoherent F(q,t) at 128 frames, coherent S(q,t) at 1,024
-              frames, the static X-ray square with sfactor type-2 factors) and one long series;
+              frames, the static X-ray square with sfactor type-2 factors), an incoherent series
+              of 600 frames and one long series;
   multipole   the sphere and cylinder multipole devices;
   prepass     the staged frames after the alignments and motions of tests/prepass_cases.py.
 """
@@ -49,6 +50,8 @@ def scatter_cases():
                                                   nq=3, qmin=0.05, qmax=0.5, nm=6), "fftw")
     out["long_series"] = (synth.small("all", "autocorrelate", seed=106, na=3, nf=4200, nq=1, nm=2,
                                       box=10.0), "fftw")
+    out["incoherent_blocks"] = (synth.small("self", "autocorrelate", seed=107, na=5, nf=600, nq=2, nm=3,
+                                            box=10.0), "fftw")  # padded length 2,048: 4 blocks of 512
     return out
 
 

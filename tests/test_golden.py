@@ -28,13 +28,14 @@ def errors(fx, out):
 
 def test_fixture_inventory():
     # every dsp type and method on both devices, the three workload shapes and a long series
-    assert len(SCATTER) == 12 and set(MULTIPOLE) == {"mp_sphere", "mp_cylinder"}
+    assert len(SCATTER) == 13 and set(MULTIPOLE) == {"mp_sphere", "mp_cylinder"}
     kinds = {(f.scattering, f.dsp, f.method) for f in SCATTER.values()}
     for s in ("all", "self"):
         for d, m in (("autocorrelate", "fftw"), ("autocorrelate", "direct"), ("square", "fftw"),
                      ("plain", "fftw")):
             assert (s, d, m) in kinds
     assert SCATTER["long_series"].nf > 4096 and SCATTER["coherent_sqt_shape"].nf == 1024
+    assert SCATTER["incoherent_blocks"].nf == 600 and SCATTER["incoherent_blocks"].scattering == "self"
 
 
 @pytest.mark.parametrize("name", sorted(SCATTER))
