@@ -15,14 +15,25 @@
 // until the process exits.
 //
 // Sharing: every call uses the same array and the array keeps the previous call's
-// contents. The partial sums are fully rewritten by each call before they are read
-// (no state carries over), but two calls that overlap on the GPU (different
+// contents. The partial sums are fully rewritten by each call before they are read.
+// The FFT twiddles and the store-kernel table depend only on NF; the array records,
+// in a tag word written by the device, which NF its tables were built for. Every
+// call enqueues the table kernels, and they return at once when the tag already
+// names this call's NF, so the decision is taken on the GPU in stream order and no
+// host-side cache can go stale. Two calls that overlap on the GPU (different
 // streams, or different host threads) race on the array and corrupt each other's
 // results. Serialise calls, e.g. by issuing them on one stream.
 //
 // First call per device: the device address of the array is looked up with
 // cudaGetSymbolAddress (with that device current) on the first call that uses the
-// device. Make that first call before capturing work into a CUDA graph.
+// device. Make that first call before capturing work into a CUDA graph. A device
+// reset (cudaDeviceReset) while the library is loaded is not supported: the
+// address looked up before the reset is kept.
+//
+// Sub-vector offsets are 64-bit in the interface but the correlation descriptors
+// index sub-vectors with 32-bit integers: the total number of sub-vectors must stay
+// below 2^31. A q whose offsets are not increasing, or lie beyond that limit, gets
+// NaN outputs instead of reading outside the amplitudes.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -45,6 +56,7 @@ constexpr int kMaxDevices = 64;
 constexpr size_t kOffPart = 0;                                             // double [slots][L]
 constexpr size_t kOffApart = kOffPart + (size_t)kMaxSlots * kMaxL * 8;     // double2 [slots]
 constexpr size_t kOffA2 = kOffApart + kMaxSlots * 16;                      // double [slots]
+constexpr size_t kOffTag = kOffA2 + kMaxSlots * 8;                         // int: NF of the tables
 constexpr size_t kOffTw = kOffA2 + kMaxSlots * 8 + 1024;                   // double2 [L/2]
 constexpr size_t kOffK = kOffTw + (size_t)(kMaxL / 2) * 16;                // double2 [L]
 constexpr size_t kOffChunks = kOffK + (size_t)kMaxL * 16;                  // CorrChunk [slots]
@@ -60,13 +72,15 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 struct DeviceState {
     bool ready = false;
     unsigned char* base = nullptr;  // device address of g_noalloc_scratch
-    int table_nf = -1;              // NF whose FFT tables are in the array
 };
 std::mutex g_lock;
 DeviceState g_dev[kMaxDevices];
 
-// tw[k] = exp(-2 pi i k / L), k < L/2 (FP64 sincospi).
-__global__ void noalloc_twiddles(double2* tw, int L) {
+// tw[k] = exp(-2 pi i k / L), k < L/2 (FP64 sincospi). Skipped when the tag says the
+// tables already belong to this NF (the tag is written by noalloc_schedule, which runs
+// after both table kernels on the stream).
+__global__ void noalloc_twiddles(double2* tw, int L, const int* tag, int nf) {
+    if (*tag == nf) return;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < L / 2; k += gridDim.x * blockDim.x) {
         double s, c;
         sincospi(-2.0 * (double)k / (double)L, &s, &c);
@@ -77,7 +91,8 @@ __global__ void noalloc_twiddles(double2* tw, int L) {
 // K at bit-reversed position i: K(w) = sum_{tau<NF} exp(+2 pi i w tau / L) / (NF L (NF-tau)),
 // the weights that turn a power spectrum into the tau-mean of the normalised correlation.
 __global__ void noalloc_store_kernel_table(const double2* __restrict__ tw, double2* kbr, int nf,
-                                           int lg) {
+                                           int lg, const int* tag) {
+    if (*tag == nf) return;
     const int L = 1 << lg;
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < L; w += gridDim.x * blockDim.x) {
         double re = 0.0, im = 0.0;
@@ -97,15 +112,31 @@ __global__ void noalloc_store_kernel_table(const double2* __restrict__ tw, doubl
     }
 }
 
+// Offsets of q s, or an empty range when they are not increasing or exceed the
+// 32-bit sub-vector index of the correlation descriptors.
+__device__ __forceinline__ bool noalloc_range(const unsigned long long* offs, int s, long long& b,
+                                              long long& e) {
+    const unsigned long long ub = offs[s], ue = offs[s + 1];
+    if (ue < ub || ue > 0x7fffffffull) {
+        b = e = 0;
+        return false;
+    }
+    b = (long long)ub;
+    e = (long long)ue;
+    return true;
+}
+
 // Descriptors of one call, written on the device from the device-side offsets: g chunks
-// per q (some possibly empty), one finalisation entry per q, the system record.
+// per q (some possibly empty), one finalisation entry per q, the system record. Last,
+// the tag records that the tables now hold this call's NF.
 __global__ void noalloc_schedule(const unsigned long long* __restrict__ offs, int nq, int g, int nf, int lg,
                                  const double2* A, const double2* kbr, double2* fqt, double2* fq, double2* fq2,
-                                 CorrChunk* chunks, FinalEntry* entries, CorrSystem* sys) {
+                                 CorrChunk* chunks, FinalEntry* entries, CorrSystem* sys, int* tag) {
     const size_t L = (size_t)1 << lg;
     for (int c = threadIdx.x; c < nq * g; c += blockDim.x) {
         const int s = c / g, k = c - s * g;
-        const long long b = (long long)offs[s], e = (long long)offs[s + 1];
+        long long b, e;
+        noalloc_range(offs, s, b, e);
         const long long nm = e - b;
         const long long len = nm > 0 ? (nm + g - 1) / g : 0;
         long long vb = b + k * len, ve = vb + len;
@@ -122,7 +153,9 @@ __global__ void noalloc_schedule(const unsigned long long* __restrict__ offs, in
         chunks[c] = ch;
     }
     for (int s = threadIdx.x; s < nq; s += blockDim.x) {
-        const long long nm = (long long)offs[s + 1] - (long long)offs[s];
+        long long b, en;
+        const bool valid = noalloc_range(offs, s, b, en);
+        const long long nm = en - b;
         FinalEntry e;
         e.slot_begin = s * g;
         e.slot_end = (s + 1) * g;
@@ -131,7 +164,7 @@ __global__ void noalloc_schedule(const unsigned long long* __restrict__ offs, in
         e.f32pair = 0;  // FP64 partials
         e.nf = nf;
         e.lg = lg;
-        e.inv_nm = nm > 0 ? 1.0 / (double)nm : __longlong_as_double(0x7ff8000000000000LL);
+        e.inv_nm = valid && nm > 0 ? 1.0 / (double)nm : __longlong_as_double(0x7ff8000000000000LL);
         e.fqt = fqt + (size_t)s * nf;
         e.fq = fq + s;
         e.fq2 = fq2 + s;
@@ -151,6 +184,7 @@ __global__ void noalloc_schedule(const unsigned long long* __restrict__ offs, in
         y.lg = lg;
         y.na_pad = 0;
         *sys = y;
+        *tag = nf;
     }
 }
 
@@ -184,12 +218,12 @@ extern "C" int sass_correlate_noalloc(int device, void* stream, const double* am
     unsigned char* b = ds.base;
     double2* tw = reinterpret_cast<double2*>(b + kOffTw);
     double2* kbr = reinterpret_cast<double2*>(b + kOffK);
-    if (ds.table_nf != (int)nf) {
+    int* tag = reinterpret_cast<int*>(b + kOffTag);
+    {
         const int L = 1 << lg;
-        noalloc_twiddles<<<(L / 2 + 255) / 256, 256, 0, st>>>(tw, L);
-        noalloc_store_kernel_table<<<(L + 127) / 128, 128, 0, st>>>(tw, kbr, (int)nf, lg);
+        noalloc_twiddles<<<(L / 2 + 255) / 256, 256, 0, st>>>(tw, L, tag, (int)nf);
+        noalloc_store_kernel_table<<<(L + 127) / 128, 128, 0, st>>>(tw, kbr, (int)nf, lg, tag);
         if (cudaGetLastError() != cudaSuccess) return SASS_ERR_CUDA;
-        ds.table_nf = (int)nf;
     }
     const int g = kMaxSlots / (int)nq;  // chunks per q (>= 1)
     CorrChunk* chunks = reinterpret_cast<CorrChunk*>(b + kOffChunks);
@@ -198,7 +232,7 @@ extern "C" int sass_correlate_noalloc(int device, void* stream, const double* am
     noalloc_schedule<<<1, 256, 0, st>>>(reinterpret_cast<const unsigned long long*>(sub_offsets), (int)nq, g,
                                         (int)nf, lg, reinterpret_cast<const double2*>(amplitudes), kbr,
                                         reinterpret_cast<double2*>(fqt), reinterpret_cast<double2*>(fq),
-                                        reinterpret_cast<double2*>(fq2), chunks, entries, sys);
+                                        reinterpret_cast<double2*>(fq2), chunks, entries, sys, tag);
     if (cudaGetLastError() != cudaSuccess) return SASS_ERR_CUDA;
 
     CorrLaunch ca{};
