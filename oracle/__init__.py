@@ -4,10 +4,16 @@ Only tests/, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
 import this package, and only as the checker. The product package
 ``sassena_gb300`` never imports it.
 
-Parity status: parity unpinned. The reference has no golden vectors for this
-path and cannot be built in this environment, so the C++ restatement
-(``cpu_oracle.cpp``) is pinned by analytic known answers and by the independent
-numpy restatement in ``numpy_oracle.py``.
+Parity status: pinned to the reference's own code. The reference has no golden
+vectors for this path and cannot be built whole here (MPI, Boost, FFTW3, HDF5 and
+libxml2 are absent), but its hot path compiles from its own sources against small
+stand-in headers (``ref_build/``, output in ``_ref/``): the coherent and incoherent
+vectors devices, smath, scatter factors, database getters and q-vector scans.
+``tests/golden/reference.npz`` holds that code's outputs, and the C++ restatement
+(``cpu_oracle.cpp``) reproduces them (bit for bit where the sums are sequential,
+within FFT rounding where FFTW is involved; ``tests/test_reference_pin.py``). The
+analytic known answers and the independent numpy restatement (``numpy_oracle.py``)
+remain as further checks.
 """
 from __future__ import annotations
 
@@ -30,8 +36,10 @@ _sp = ctypes.POINTER(ctypes.c_size_t)
 
 
 def build() -> str:
-    """Compile the oracle library with its Makefile (idempotent)."""
+    """Compile the oracle library with its Makefile (idempotent), and the reference's own
+    compiled hot path (oracle/_ref) where the reference tree is present."""
     subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    subprocess.run(["make", "-s", "-C", os.path.join(_HERE, "ref_build")], check=True)
     return _LIB_PATH
 
 

@@ -579,7 +579,9 @@ double oracle_volume(int type, const double* v, size_t nv) {
     if (nv < 1) return NAN;
     if (type == 0) return v[0];
     if (type == 1) return (4.0 / 3.0) * M_PI * powf((float)v[0], 3);
-    if (type == 2) return sqrt(powf((float)M_PI, 3)) * powf((float)v[0], 3);
+    // the reference's sqrt takes the float overload (std::sqrt after "using namespace std"), so the
+    // whole product is a float
+    if (type == 2) return (double)(std::sqrt(powf((float)M_PI, 3)) * powf((float)v[0], 3));
     return NAN;
 }
 

@@ -68,3 +68,57 @@ def golden(family):
     z = np.load(os.path.join(GOLDEN, family + ".npz"))
     names = sorted({k.split(".", 1)[0] for k in z.files if k.endswith(".fqt")})
     return {n: Fixture(z, n) for n in names}
+
+
+class ReferenceCase:
+    """One device run of tests/golden/reference.npz (outputs of the reference's own compiled
+    scatter devices, made by make_reference_golden.py), with the q-vectors expanded into
+    sub-vectors the way the reference does it: file orientations normalised by 1/|v|
+    (parameters.cpp:936-941) and scaled by |q| (abstract_vectors_scatter_device.cpp:116-122);
+    no orientations means the q-vector itself (:172)."""
+
+    def __init__(self, z, name):
+        g = lambda k: z[name + "." + k]  # noqa: E731
+        self.name = name
+        self.scattering, self.dsp, self.method = str(g("kind")).split("/")
+        self.coords = g("coords")
+        self.atom_class = g("atom_type")
+        self.class_factors = g("class_factors")
+        self.qvectors, self.orient = g("qvectors"), g("orient")
+        self.fqt, self.fq, self.fq2 = g("fqt"), g("fq"), g("fq2")
+        self.q_out = g("q_out")
+
+    @property
+    def na(self):
+        return self.coords.shape[1]
+
+    @property
+    def nf(self):
+        return self.coords.shape[0]
+
+    def sub_offsets(self):
+        per = max(len(self.orient), 1)
+        return np.arange(len(self.qvectors) + 1, dtype=np.uintp) * per
+
+    def subvectors(self):
+        q = self.qvectors
+        if len(self.orient) == 0:
+            return q.copy()
+        ql = np.sqrt(q[:, 0] ** 2 + q[:, 1] ** 2 + q[:, 2] ** 2)
+        ol = np.sqrt(self.orient[:, 0] ** 2 + self.orient[:, 1] ** 2 + self.orient[:, 2] ** 2)
+        u = (1.0 / ol)[:, None] * self.orient
+        return (ql[:, None, None] * u[None]).reshape(-1, 3)
+
+    def factors(self):
+        return self.class_factors[:, self.atom_class]
+
+
+def reference_cases():
+    """{case: ReferenceCase} of the device runs in tests/golden/reference.npz."""
+    z = np.load(os.path.join(GOLDEN, "reference.npz"))
+    names = sorted({k.split(".", 1)[0] for k in z.files if k.endswith(".fqt")})
+    return {n: ReferenceCase(z, n) for n in names}
+
+
+def reference_fixture():
+    return np.load(os.path.join(GOLDEN, "reference.npz"))
