@@ -1,5 +1,7 @@
 #include "config.hpp"
 
+#include <random>
+
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
@@ -36,21 +38,71 @@ Vec3 read_vec(const XmlDoc& x, const std::string& base, const XmlNode* ctx, Vec3
 
 double length(const Vec3& v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
 
-// splitmix64: the project's own seeded generator for sphere/cylinder draws.
-struct SplitMix {
-    uint64_t s;
-    explicit SplitMix(uint64_t seed) : s(seed) {}
-    uint64_t next() {
-        uint64_t z = (s += 0x9E3779B97F4A7C15ull);
-        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-        return z ^ (z >> 31);
+// Orientation draws of vectors.type = sphere / cylinder with algorithm
+// boost_uniform_on_sphere (parameters.cpp:945-959 and :1001-1012): a boost::mt19937 seeded
+// with the configured seed, copied into a variate_generator with uniform_on_sphere<double>(3)
+// or (2), one call per orientation. Restated from Boost.Random's published algorithms:
+// - boost::mt19937 is the standard 32-bit Mersenne Twister (std::mt19937 gives the same
+//   stream for the same seed, truncated to 32 bits as mt19937::seed truncates it);
+// - uniform_01<double> maps a draw x to x * 2^-32 (exact);
+// - Boost 1.56 and later (BoostRandom::Marsaglia, the default): uniform_on_sphere takes
+//   Marsaglia's method for two and three dimensions: x, y = 2u - 1 until x^2 + y^2 <= 1
+//   (and > 0 in two dimensions); three dimensions give (2x sqrt(1-s), 2y sqrt(1-s), 2s - 1),
+//   two give (x, y) / sqrt(s);
+// - Boost 1.47 to 1.55 (BoostRandom::BoxMuller, gpu/boost_random = 1.47): the distribution
+//   holds a normal_distribution that draws Box-Muller pairs (rho = sqrt(-2 log(1 - u2)),
+//   cos(2 pi u1) first, sin(2 pi u1) kept for the next variate, across orientations) and
+//   divides the normal vector by its length.
+// The host build has no FP contraction, so x*x + y*y rounds as on an x86-64 build.
+struct BoostSphere {
+    std::mt19937 eng;
+    bool legacy;
+    bool valid = false;  // Box-Muller: a cached second variate exists
+    double r1 = 0, cached_rho = 0;
+    BoostSphere(unsigned long seed, bool legacy_box_muller)
+        : eng((std::mt19937::result_type)(uint32_t)seed), legacy(legacy_box_muller) {}
+    double uniform01() { return (double)eng() * (1.0 / 4294967296.0); }
+    double normal() {
+        if (!valid) {
+            r1 = uniform01();
+            const double r2 = uniform01();
+            cached_rho = std::sqrt(-2.0 * std::log(1.0 - r2));
+            valid = true;
+        } else {
+            valid = false;
+        }
+        const double pi = 3.14159265358979323846;
+        return cached_rho * (valid ? std::cos(2.0 * pi * r1) : std::sin(2.0 * pi * r1)) * 1.0 + 0.0;
     }
-    double uniform() { return ((next() >> 11) + 0.5) * (1.0 / 9007199254740992.0); }  // (0,1)
-    void normal2(double& a, double& b) {  // Box-Muller
-        double r = std::sqrt(-2.0 * std::log(uniform())), t = 6.283185307179586 * uniform();
-        a = r * std::cos(t);
-        b = r * std::sin(t);
+    std::vector<double> draw(int dim) {
+        std::vector<double> v(dim);
+        if (legacy) {
+            double sq = 0;
+            for (int k = 0; k < dim; ++k) {
+                v[k] = normal();
+                sq += v[k] * v[k];
+            }
+            const double l = std::sqrt(sq);
+            for (int k = 0; k < dim; ++k) v[k] = v[k] / l;
+            return v;
+        }
+        double x, y, sq;
+        do {
+            x = uniform01() * 2 - 1;
+            y = uniform01() * 2 - 1;
+            sq = x * x + y * y;
+        } while ((dim == 2 && sq == 0) || sq > 1);
+        if (dim == 3) {
+            const double mult = 2 * std::sqrt(1 - sq);
+            v[0] = x * mult;
+            v[1] = y * mult;
+            v[2] = 2 * sq - 1;
+        } else {
+            const double mult = 1 / std::sqrt(sq);
+            v[0] = x * mult;
+            v[1] = y * mult;
+        }
+        return v;
     }
 };
 
@@ -262,6 +314,11 @@ void Params::read_xml(const std::string& path) {
             if (x.exists(b + "seed")) seed = (unsigned long)x.get_long(b + "seed");
             if (x.exists(b + "file")) vectors_file = x.get_string(b + "file");
             vectors_filepath = get_filepath(vectors_file);
+            // the Boost.Random release whose draws are reproduced (an option of this build)
+            if (x.exists("//gpu/boost_random")) boost_random = x.get_string("//gpu/boost_random");
+            if (boost_random != "1.56" && boost_random != "1.47")
+                throw std::runtime_error("gpu.boost_random must be 1.56 (Boost 1.56 and later) or 1.47 (1.47 to "
+                                         "1.55): " + boost_random);
             orientations = create_orientations(*this);
         } else if (orientation_type == "multipole") {
             const std::string b = "//scattering/average/orientation/multipole/";
@@ -434,29 +491,17 @@ std::vector<Vec3> create_orientations(const Params& p) {
     } else if (p.vectors_type == "sphere") {
         if (p.vectors_algorithm != "boost_uniform_on_sphere")
             throw std::runtime_error("Vectors algorithm not understood: " + p.vectors_algorithm);
-        SplitMix rng(p.seed);
+        BoostSphere sphere(p.seed, p.boost_random == "1.47");
         for (long i = 0; i < p.resolution; ++i) {
-            double a, b, c, d;
-            Vec3 v;
-            double l;
-            do {
-                rng.normal2(a, b);
-                rng.normal2(c, d);
-                v = Vec3{a, b, c};
-                l = length(v);
-            } while (l == 0.0);
-            out.push_back(Vec3{v[0] / l, v[1] / l, v[2] / l});
+            std::vector<double> r = sphere.draw(3);
+            out.push_back(Vec3{r[0], r[1], r[2]});
         }
     } else if (p.vectors_type == "cylinder") {
         if (p.vectors_algorithm == "boost_uniform_on_sphere") {
-            SplitMix rng(p.seed);
+            BoostSphere circle(p.seed, p.boost_random == "1.47");
             for (long i = 0; i < p.resolution; ++i) {
-                double a, b, l;
-                do {
-                    rng.normal2(a, b);
-                    l = std::sqrt(a * a + b * b);
-                } while (l == 0.0);
-                out.push_back(Vec3{a / l, b / l, 0.0});
+                std::vector<double> r = circle.draw(2);
+                out.push_back(Vec3{r[0], r[1], 0.0});
             }
         } else if (p.vectors_algorithm == "raster_linear") {
             const double two_pi = 2 * M_PI;
@@ -552,7 +597,7 @@ double Database::volume(size_t id) const {
     switch (it->second.type) {
         case 0: return v[0];
         case 1: return (4.0 / 3.0) * M_PI * powf((float)v[0], 3);
-        case 2: return std::sqrt(powf((float)M_PI, 3)) * powf((float)v[0], 3);
+        case 2: return (double)(std::sqrt(powf((float)M_PI, 3)) * powf((float)v[0], 3));  // float, as the reference
     }
     throw std::runtime_error("Size-type not implemented: type=" + std::to_string(it->second.type));
 }

@@ -100,6 +100,7 @@ struct Params {
     size_t serverflush_s = 600;
     // gpu (new)
     std::string precision = "fp64";
+    std::string boost_random = "1.56";  // Boost.Random release whose sphere draws are reproduced
     int device = 0;
     size_t batch_q = 0;            // q-vectors per sass_compute call (0 = all)
     size_t amplitude_budget = 0;   // bytes (0 = library default)
