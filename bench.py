@@ -55,11 +55,19 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="coherent_sqt")
-    ap.add_argument("--plain-shells", type=int, default=3,
-                    help="shells of the plain FP64 comparison run (time scaled by terms)")
+    ap.add_argument("--plain-shells", type=int, default=0,
+                    help="shells of the plain FP64 comparison run (0: every shell when the whole "
+                         "workload takes at most --plain-budget seconds, else 3, time scaled by terms)")
+    ap.add_argument("--plain-budget", type=float, default=30.0)
+    ap.add_argument("--oracle-terms", type=float, default=6e8,
+                    help="atom*q*frame terms of the oracle sample of the FP64/FP32 accuracy check")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=5.0,
+                    help="CPU time of each timed step of --impl reference (a bounded sample)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"],
+                    help="form timed by the scatter workloads (fp64: the plain FP64 path itself)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--nq", type=int, default=0, help="override the number of shells (profiling)")
     ap.add_argument("--nf", type=int, default=0, help="override the number of frames (profiling)")
@@ -169,29 +177,42 @@ def make_workload(name, nq=0, nf=0):
 
 
 def cpu_sample(w, seconds, nthreads):
-    """Time the oracle on one shell x m directions (m grown until ~`seconds`). The oracle
-    runs one direction per worker thread, so m stays a multiple of the thread count (or all
-    of the shell's directions): a partial last round would understate the CPU's rate."""
+    """Time the oracle's CPU-baseline build (-O3, tuned for the host CPU) on one shell x m
+    directions, m grown until the sample takes about `seconds`. The oracle runs one direction
+    per worker thread, so m stays a multiple of the thread count (or all of the shell's
+    directions): a partial last round would understate the CPU's rate. Also reports the
+    share of the CPU time spent in the correlation (dsp) rather than the phase sum."""
     import oracle
     s = w.nq // 2
     m = min(w.nm, nthreads)
     fac = w.factors()[s:s + 1]
+    dsp = {"autocorrelate": 0, "square": 1, "plain": 2}[w.dsp]
+    fn = oracle.all_vectors if w.scattering == "all" else oracle.self_vectors
     while True:
         sv = w.shells[s] * w.directions[:m]
         offs = np.array([0, m], dtype=np.uintp)
         t0 = time.perf_counter()
-        dsp = {"autocorrelate": 0, "square": 1, "plain": 2}[w.dsp]
-        oracle.all_vectors(w.coords, offs, sv, fac, dsp, 0, nthreads) if w.scattering == "all" \
-            else oracle.self_vectors(w.coords, offs, sv, fac, dsp, 0, nthreads)
+        fn(w.coords, offs, sv, fac, dsp, 0, nthreads, timing=True)
         dt = time.perf_counter() - t0
         terms = w.na * m * w.nf
-        if dt >= seconds * 0.4 or m >= w.nm:
+        if dt >= seconds * 0.6 or m >= w.nm:
+            sc, ds = oracle.last_split(timing=True)
             return {"value": terms / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
-                    "sample": "oracle (FP64 restatement) on shell %d/%d x %d of %d directions, "
-                              "all %d atoms x %d frames (%.3g terms, %.1f s)"
-                              % (s, w.nq, m, w.nm, w.na, w.nf, terms, dt)}
-        m = max(m * 2, int(m * seconds * 0.6 / max(dt, 1e-3)))
+                    "seconds": dt, "terms": terms, "correlation_share": ds / max(sc + ds, 1e-12),
+                    "sample": "oracle (FP64 restatement, pinned to the reference's compiled devices; "
+                              "-O3 CPU-baseline build) on shell %d/%d x %d of %d directions, all %d atoms "
+                              "x %d frames (%.3g terms, %.1f s)" % (s, w.nq, m, w.nm, w.na, w.nf, terms, dt)}
+        m = max(m * 2, int(m * seconds * 0.8 / max(dt, 1e-3)))
         m = min(w.nm, (m + nthreads - 1) // nthreads * nthreads)
+
+
+def workload_config(w, world):
+    """The config object both arms print for a scatter workload."""
+    return {"workload": w.name, "na": w.na, "nf": w.nf, "nq": w.nq, "nm": w.nm,
+            "terms_per_step": w.terms(), "dsp": w.dsp, "scattering": w.scattering,
+            "fft_length": 1 << max(2, int(np.ceil(np.log2(2 * w.nf)))),
+            "l2": "inputs larger than L2 (coordinates %.0f MB)" % (w.na * w.nf * 16 / 1e6),
+            "parallelism": "replicas x%d" % world}
 
 
 MP_WORKLOADS = ("multipole_sphere", "multipole_cylinder")
@@ -309,25 +330,32 @@ def run_reference(args, dist):
     else:
         w = make_workload(args.workload, args.nq, args.nf)
     nthreads = os.cpu_count() or 1
-    vals = []
+    vals, secs, shares = [], [], []
     for i in range(args.warmup + args.steps):
-        r = cpu_sample(w, args.cpu_seconds / max(1, args.steps), nthreads)
+        # each step is a bounded sample of the workload: one shell x as many directions as
+        # take about --ref-step-seconds on every host thread (warm-up samples are shorter)
+        r = cpu_sample(w, args.ref_step_seconds if i >= args.warmup else 1.0, nthreads)
         if i >= args.warmup:
             vals.append(r["value"])
+            secs.append(r["seconds"])
+            shares.append(r["correlation_share"])
     v = statistics.median(vals)
-    cfg = {"workload": args.workload, "na": w.na, "nf": w.nf, "nq": w.nq, "nm": w.nm,
-           "terms_per_step": w.terms(), "dsp": w.dsp, "scattering": w.scattering}
+    cfg = workload_config(w, dist.world)
     print(json.dumps({"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT,
                       "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-                      "ms_per_step": w.terms() / v * 1e3, "higher_is_better": True,
+                      "ms_per_step": statistics.median(secs) * 1e3,
+                      "ms_per_full_step_extrapolated": w.terms() / v * 1e3, "higher_is_better": True,
                       "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                       "data": "synthetic (seeded)", "config": cfg,
-                      "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads,
-                                       "kind": "port", "sample": r["sample"]},
+                      "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+                                       "sample": r["sample"],
+                                       "correlation_share": statistics.median(shares)},
                       "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
                               "d2h_bytes_per_step": 0},
-                      "note": "reference unbuildable here (MPI/Boost/FFTW3/HDF5/libxml2 absent);"
-                              " timed its CPU restatement, ms_per_step extrapolated by terms"}))
+                      "note": "the reference's whole program cannot be built here (MPI/Boost/FFTW3/HDF5/"
+                              "libxml2 absent); timed the CPU oracle, which reproduces the reference's "
+                              "compiled scatter devices (tests/test_reference_pin.py). A step is a bounded "
+                              "sample of the workload; ms_per_full_step_extrapolated scales it by terms"}))
 
 
 def phase_roofline(w, sch, phase_ms, corr_ms, sfu, fma):
@@ -375,6 +403,115 @@ def phase_roofline(w, sch, phase_ms, corr_ms, sfu, fma):
     return roof
 
 
+def shell_errors(got, ref):
+    """Per shell: S(q,t) as max_t |S - S_ref| / |S_ref(q,0)|; I(q) as fq (the time-averaged
+    correlation), fq0 = S(q,0) and fq2, each relative to its reference value."""
+    (f, a, a2), (rf, ra, ra2) = got, ref
+    den = np.abs(rf[:, 0])
+    return {"sqt": np.abs(f - rf).max(axis=1) / den, "fq": np.abs(a - ra) / np.abs(ra),
+            "fq0": np.abs(f[:, 0] - rf[:, 0]) / den, "fq2": np.abs(a2 - ra2) / np.abs(ra2)}
+
+
+def _cplx(a):
+    return a[..., 0] + 1j * a[..., 1]
+
+
+def fp64_roofline(w, t64, terms, dev):
+    """The plain FP64 form's phase-sum kernel against the FP64 pipe rate measured live
+    (sass_probe_fp64). Its FP64 pipe instructions per term (products, sums and the
+    software sin/cos) come from the ncu capture in profiles/phase_sum_kernel_fp64_<workload>.json."""
+    from sassena_gb300 import abi
+    fma = abi.probe_fp64(dev)
+    prof = os.path.join(ROOT, "profiles", "phase_sum_kernel_fp64_%s.json" % w.name)
+    per_term = None
+    if os.path.exists(prof):
+        with open(prof) as f:
+            per_term = json.load(f).get("fp64_pipe_inst_per_term")
+    achieved = terms / (t64["phase_ms"] * 1e-3)
+    roof = {"bound": "fp64", "kernel": "phase_sum_kernel<double>", "kernel_ms": t64["phase_ms"],
+            "fp64_fma_per_s": fma, "achieved": achieved, "unit": "terms/s"}
+    if per_term:
+        roof.update({"fp64_pipe_inst_per_term": per_term, "peak": fma / per_term,
+                     "frac": achieved * per_term / fma,
+                     "peak_source": "measured live: sass_probe_fp64 %.4g FP64 FMA/s / %.1f FP64-pipe "
+                                    "instructions per term (ncu)" % (fma, per_term)})
+    return roof
+
+
+def plain_fp64_audit(args, w, plan, ms, dev):
+    """The plain FP64 form on the same GPU: its time on the whole workload (a subset of
+    shells, scaled by terms, only where the whole would exceed --plain-budget seconds), the
+    FP32 path's error against it for every shell it ran, and both forms against the CPU
+    oracle on a seeded sample of directions per shell (all atoms and frames)."""
+    import oracle
+    from sassena_gb300 import abi
+
+    terms = w.terms()
+    nclass = len(w.class_names)
+    cf_all = np.ascontiguousarray(w.class_factors)
+    full32 = plan.compute(w.sub_offsets(), w.subvectors(), cf_all)  # the measured FP32 output
+
+    def subset(idx, dirs):
+        offs = np.arange(len(idx) + 1, dtype=np.uintp) * len(dirs)
+        return offs, (w.shells[idx, None, None] * dirs[None]).reshape(-1, 3), cf_all[idx]
+
+    with abi.Plan(w.na, w.nf, nclass, w.scattering, w.dsp, "fftw", "fp64", device=dev) as p64:
+        p64.stage(w.coords)
+        p64.set_classes(w.atom_class)
+        mid = np.array([w.nq // 2])
+        p64.compute(*subset(mid, w.directions))
+        est_ms = p64.timing()["total_ms"] * w.nq
+        if args.plain_shells == 0 and est_ms <= args.plain_budget * 1e3:
+            idx = np.arange(w.nq)
+        else:
+            ns = max(1, min(args.plain_shells or 3, w.nq))
+            idx = np.linspace(0, w.nq - 1, ns).round().astype(int)
+        ref = p64.compute(*subset(idx, w.directions))
+        t64 = p64.timing()
+        sch64 = p64.schedule()
+        # the oracle sample: D seeded directions per shell, all atoms and frames
+        d = max(1, min(w.nm, int(args.oracle_terms // (w.nq * w.na * w.nf))))
+        step_q = max(1, int(np.ceil(w.nq * w.na * w.nf * d / args.oracle_terms)))
+        oidx = np.arange(0, w.nq, step_q)
+        rng = np.random.default_rng(2026)
+        odirs = w.directions[np.sort(rng.choice(w.nm, d, replace=False))]
+        o_offs, o_sv, o_cf = subset(oidx, odirs)
+        g64 = p64.compute(o_offs, o_sv, o_cf)
+    g32 = plan.compute(o_offs, o_sv, o_cf)
+    dsp = {"autocorrelate": 0, "square": 1, "plain": 2}[w.dsp]
+    fn = oracle.all_vectors if w.scattering == "all" else oracle.self_vectors
+    t0 = time.perf_counter()
+    orc = [_cplx(a) for a in fn(w.coords, o_offs, o_sv, o_cf[:, w.atom_class], dsp, 0, os.cpu_count())]
+    oracle_s = time.perf_counter() - t0
+
+    e32 = shell_errors([x[idx] for x in full32], ref)
+    eo32 = shell_errors(g32, orc)
+    eo64 = shell_errors(g64, orc)
+    run_terms = w.na * w.nf * w.nm * len(idx)
+    plain_tps = run_terms / (t64["total_ms"] * 1e-3)
+    full_ms = terms / plain_tps * 1e3
+    lst = lambda v: [float(x) for x in v]  # noqa: E731
+    res = {"value": plain_tps, "unit": UNIT, "shells_run": int(len(idx)),
+           "whole_workload": bool(len(idx) == w.nq),
+           ("ms_full_workload" if len(idx) == w.nq else "ms_full_workload_extrapolated"): full_ms,
+           "speedup_same_gpu": full_ms / ms,
+           "roofline": fp64_roofline(w, t64, run_terms, dev), "schedule": sch64,
+           "fp32_max_rel_err_vs_fp64": float(e32["sqt"].max()),
+           "fp32_rel_err_per_shell": {"q": lst(w.shells[idx]), "sqt": lst(e32["sqt"]),
+                                      "sqt_median": float(np.median(e32["sqt"])), "iq_fq": lst(e32["fq"]),
+                                      "fq0": lst(e32["fq0"]), "fq2": lst(e32["fq2"])},
+           "vs_oracle": {"directions_per_shell": int(d), "shells": int(len(oidx)),
+                         "sample": "oracle FP64 on %d shells x %d seeded directions, all %d atoms x %d "
+                                   "frames (%.1f s on %d threads)" % (len(oidx), d, w.na, w.nf, oracle_s,
+                                                                       os.cpu_count()),
+                         "fp32_sqt_per_shell": lst(eo32["sqt"]), "fp32_sqt_max": float(eo32["sqt"].max()),
+                         "fp32_fq_max": float(eo32["fq"].max()), "fp32_fq0_max": float(eo32["fq0"].max()),
+                         "fp32_fq2_max": float(eo32["fq2"].max()),
+                         "fp64_sqt_max": float(eo64["sqt"].max()), "fp64_fq_max": float(eo64["fq"].max()),
+                         "fp64_fq2_max": float(eo64["fq2"].max())}}
+    return res
+
+
 def run_ours(args, dist):
     import torch
 
@@ -388,7 +525,7 @@ def run_ours(args, dist):
     torch.cuda.set_stream(stream)
     nclass = len(w.class_names)
     terms = w.terms()
-    plan = abi.Plan(w.na, w.nf, nclass, w.scattering, w.dsp, "fftw", "fp32", device=dev,
+    plan = abi.Plan(w.na, w.nf, nclass, w.scattering, w.dsp, "fftw", args.precision, device=dev,
                     stream=stream.cuda_stream)
     plan.stage(w.coords)
     plan.set_classes(w.atom_class)
@@ -451,7 +588,11 @@ def run_ours(args, dist):
     # ---- roofline of the dominant kernel ---------------------------------------------------
     sch = plan.schedule()
     sfu, fma = abi.probe_pipes(dev)
-    roof = phase_roofline(w, sch, statistics.median(phase_ms), statistics.median(corr_ms), sfu, fma)
+    if args.precision == "fp64":
+        roof = fp64_roofline(w, {"phase_ms": statistics.median(phase_ms)}, terms, dev)
+        roof["schedule"] = sch
+    else:
+        roof = phase_roofline(w, sch, statistics.median(phase_ms), statistics.median(corr_ms), sfu, fma)
     corr = statistics.median(corr_ms)
     # algorithmic bytes: the FP32 amplitudes read once (float2, 8 B) and the FP64 row written
     # per shell
@@ -475,53 +616,18 @@ def run_ours(args, dist):
                      "note": "fused with the series generation; its roofline is `roofline`"}
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms,
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32" if args.precision == "fp32" else "f64",
            "data": "synthetic (seeded random walk, %s)" % w.name,
-           "config": {"workload": w.name, "na": w.na, "nf": w.nf, "nq": w.nq, "nm": w.nm,
-                      "terms_per_step": terms, "dsp": w.dsp, "scattering": w.scattering,
-                      "fft_length": 1 << max(2, int(np.ceil(np.log2(2 * w.nf)))),
-                      "l2": "inputs larger than L2 (coordinates %.0f MB)" % (w.na * w.nf * 16 / 1e6),
-                      "parallelism": "replicas x%d" % dist.world},
+           "config": workload_config(w, dist.world),
            "e2e": {"value": terms * dist.world / (e2e_step * 1e-3), "unit": UNIT,
                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_step},
            "roofline": roof, "roofline_correlation": roof_corr,
            "gpu_launches": int(launches), "clocks": clk}
 
     # ---- plain FP64 path on the same GPU, and the FP32 error against it -------------------
-    if not args.no_plain:
-        ns = max(1, min(args.plain_shells, w.nq))
-        idx = np.linspace(0, w.nq - 1, ns).round().astype(int)
-        sub_offs = np.arange(ns + 1, dtype=np.uintp) * w.nm
-        sub_sv = (w.shells[idx, None, None] * w.directions[None]).reshape(-1, 3)
-        sub_cf = w.class_factors[idx]
-        with abi.Plan(w.na, w.nf, nclass, w.scattering, w.dsp, "fftw", "fp64", device=dev) as p64:
-            p64.stage(w.coords)
-            p64.set_classes(w.atom_class)
-            ref = p64.compute(sub_offs, sub_sv, sub_cf)
-            t64 = p64.timing()
-        # error of the measured FP32 path itself: its full-workload output at those shells
-        full = plan.compute(offs, w.subvectors(), np.ascontiguousarray(w.class_factors))
-        # per compared shell: S(q,t) as max_t |S - S_ref| / |S_ref(q,0)|; I(q) as fq (the
-        # time-averaged correlation), fq0 = S(q,0) and fq2, each relative to its FP64 value
-        e_sqt = np.abs(full[0][idx] - ref[0]).max(axis=1) / np.abs(ref[0][:, 0])
-        e_fq = np.abs(full[1][idx] - ref[1]) / np.abs(ref[1])
-        e_fq0 = np.abs(full[0][idx, 0] - ref[0][:, 0]) / np.abs(ref[0][:, 0])
-        e_fq2 = np.abs(full[2][idx] - ref[2]) / np.abs(ref[2])
-        err = e_sqt.max()
-        plan.compute(sub_offs, sub_sv, sub_cf)
-        t32 = plan.timing()
-        sub_terms = w.na * w.nf * w.nm * ns
-        plain_tps = sub_terms / (t64["total_ms"] * 1e-3)
-        out["plain_fp64"] = {"value": plain_tps, "unit": UNIT, "shells_run": ns,
-                             "ms_full_workload_extrapolated": terms / plain_tps * 1e3,
-                             "fp32_max_rel_err_vs_fp64": float(err),
-                             "fp32_rel_err_per_shell": {
-                                 "q": [float(w.shells[i]) for i in idx],
-                                 "sqt": [float(v) for v in e_sqt], "sqt_median": float(np.median(e_sqt)),
-                                 "iq_fq": [float(v) for v in e_fq], "fq0": [float(v) for v in e_fq0],
-                                 "fq2": [float(v) for v in e_fq2]},
-                             "speedup_same_gpu": (terms / plain_tps * 1e3) / ms,
-                             "fp32_ms_same_shells": t32["total_ms"]}
+    if not args.no_plain and args.precision == "fp32":
+        out["plain_fp64"] = plain_fp64_audit(args, w, plan, ms, dev)
 
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu:
         out["cpu_baseline"] = cpu_sample(w, args.cpu_seconds, os.cpu_count() or 1)
@@ -889,7 +995,8 @@ def run_cv(args, dist):
     last = rows[-1]
     out = {"metric": METRIC, "value": last["terms"] / (last["ms_mc"] * 1e-3), "unit": UNIT,
            "n_gpus": 1, "steps": len(budgets), "warmup": 0, "ms_per_step": last["ms_mc"],
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32" if args.precision == "fp32" else "f64",
            "data": "synthetic (seeded layered system, density 1 + %.1f cos(2 pi z / %.0f A))"
                    % (w.meta["amplitude"], w.meta["period"]),
            "config": {"workload": "layered_cv", "na": w.na, "nf": w.nf, "nq": w.nq,

@@ -25,7 +25,9 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_TIMING_PATH = os.path.join(_HERE, "_build", "liboracle_timing.so")
 _lib = None
+_timing = None
 
 DSP_AUTOCORRELATE, DSP_SQUARE, DSP_PLAIN = 0, 1, 2
 METHOD_FFTW, METHOD_DIRECT = 0, 1
@@ -43,57 +45,66 @@ def build() -> str:
     return _LIB_PATH
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(
-            os.path.join(_HERE, "cpu_oracle.cpp")
-        ):
-            build()
-        L = ctypes.CDLL(_LIB_PATH)
-        for name in ("oracle_all_vectors", "oracle_self_vectors"):
-            f = getattr(L, name)
-            f.restype = ctypes.c_int
-            f.argtypes = [_fp, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t, _sp, _dp, _dp,
-                          ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
-        L.oracle_amplitudes.restype = ctypes.c_int
-        L.oracle_amplitudes.argtypes = [_fp, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t,
-                                        _dp, _sp, _dp, ctypes.c_int, _dp]
-        L.oracle_dft.argtypes = [_dp, ctypes.c_size_t, ctypes.c_int]
-        L.oracle_autocorrelate_fftw.argtypes = [_dp, ctypes.c_size_t]
-        L.oracle_autocorrelate_direct.argtypes = [_dp, ctypes.c_size_t]
-        L.oracle_sfactor.restype = ctypes.c_double
-        L.oracle_sfactor.argtypes = [ctypes.c_int, _dp, ctypes.c_size_t, ctypes.c_double]
-        L.oracle_volume.restype = ctypes.c_double
-        L.oracle_volume.argtypes = [ctypes.c_int, _dp, ctypes.c_size_t]
-        L.oracle_exclusion.restype = ctypes.c_double
-        L.oracle_exclusion.argtypes = [ctypes.c_int, _dp, ctypes.c_size_t, ctypes.c_double,
-                                       ctypes.c_double]
-        _ip = ctypes.POINTER(ctypes.c_int)
-        L.oracle_mp_sphere.restype = ctypes.c_int
-        L.oracle_mp_sphere.argtypes = [_fp, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t, _dp,
-                                       _dp, ctypes.c_size_t, _ip, ctypes.c_int, ctypes.c_int,
-                                       ctypes.c_int, _dp, _dp, _dp]
-        L.oracle_mp_cylinder.restype = ctypes.c_int
-        L.oracle_mp_cylinder.argtypes = [_fp, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t,
-                                         _dp, _dp, ctypes.c_size_t, _ip, _dp, ctypes.c_int,
-                                         ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
-        L.oracle_sph_bessel.argtypes = [ctypes.c_int, ctypes.c_double, _dp]
-        L.oracle_cyl_bessel.argtypes = [ctypes.c_int, ctypes.c_double, _dp]
-        L.oracle_conj_ylm.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp]
-        L.oracle_to_spherical.argtypes = [_fp, ctypes.c_size_t, _fp]
-        L.oracle_scan.restype = ctypes.c_size_t
-        L.oracle_scan.argtypes = [_dp, ctypes.c_double, ctypes.c_double, ctypes.c_size_t,
-                                  ctypes.c_double, _dp]
+def lib(timing=False):
+    """The parity build of the oracle, or (timing=True) its CPU-baseline build."""
+    global _lib, _timing
+    if timing and _timing is not None:
+        return _timing
+    if not timing and _lib is not None:
+        return _lib
+    path = _TIMING_PATH if timing else _LIB_PATH
+    if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(
+        os.path.join(_HERE, "cpu_oracle.cpp")
+    ):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    L = ctypes.CDLL(path)
+    L.oracle_last_split.argtypes = [_dp, _dp]
+    for name in ("oracle_all_vectors", "oracle_self_vectors"):
+        f = getattr(L, name)
+        f.restype = ctypes.c_int
+        f.argtypes = [_fp, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t, _sp, _dp, _dp,
+                      ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
+    L.oracle_amplitudes.restype = ctypes.c_int
+    L.oracle_amplitudes.argtypes = [_fp, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t,
+                                    _dp, _sp, _dp, ctypes.c_int, _dp]
+    L.oracle_dft.argtypes = [_dp, ctypes.c_size_t, ctypes.c_int]
+    L.oracle_autocorrelate_fftw.argtypes = [_dp, ctypes.c_size_t]
+    L.oracle_autocorrelate_direct.argtypes = [_dp, ctypes.c_size_t]
+    L.oracle_sfactor.restype = ctypes.c_double
+    L.oracle_sfactor.argtypes = [ctypes.c_int, _dp, ctypes.c_size_t, ctypes.c_double]
+    L.oracle_volume.restype = ctypes.c_double
+    L.oracle_volume.argtypes = [ctypes.c_int, _dp, ctypes.c_size_t]
+    L.oracle_exclusion.restype = ctypes.c_double
+    L.oracle_exclusion.argtypes = [ctypes.c_int, _dp, ctypes.c_size_t, ctypes.c_double,
+                                   ctypes.c_double]
+    _ip = ctypes.POINTER(ctypes.c_int)
+    L.oracle_mp_sphere.restype = ctypes.c_int
+    L.oracle_mp_sphere.argtypes = [_fp, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t, _dp,
+                                   _dp, ctypes.c_size_t, _ip, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_int, _dp, _dp, _dp]
+    L.oracle_mp_cylinder.restype = ctypes.c_int
+    L.oracle_mp_cylinder.argtypes = [_fp, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t,
+                                     _dp, _dp, ctypes.c_size_t, _ip, _dp, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
+    L.oracle_sph_bessel.argtypes = [ctypes.c_int, ctypes.c_double, _dp]
+    L.oracle_cyl_bessel.argtypes = [ctypes.c_int, ctypes.c_double, _dp]
+    L.oracle_conj_ylm.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp]
+    L.oracle_to_spherical.argtypes = [_fp, ctypes.c_size_t, _fp]
+    L.oracle_scan.restype = ctypes.c_size_t
+    L.oracle_scan.argtypes = [_dp, ctypes.c_double, ctypes.c_double, ctypes.c_size_t,
+                              ctypes.c_double, _dp]
+    if timing:
+        _timing = L
+    else:
         _lib = L
-    return _lib
+    return L
 
 
 def _ptr(a, t):
     return a.ctypes.data_as(t)
 
 
-def _vectors(kind, coords, sub_offsets, subvectors, factors, dsp_type, dsp_method, nthreads):
+def _vectors(kind, coords, sub_offsets, subvectors, factors, dsp_type, dsp_method, nthreads, timing=False):
     coords = np.ascontiguousarray(coords, dtype=np.float32)
     nf, na = coords.shape[0], coords.shape[1]
     sub_offsets = np.ascontiguousarray(sub_offsets, dtype=np.uintp)
@@ -103,7 +114,7 @@ def _vectors(kind, coords, sub_offsets, subvectors, factors, dsp_type, dsp_metho
     fqt = np.zeros((nq, nf, 2))
     fq = np.zeros((nq, 2))
     fq2 = np.zeros((nq, 2))
-    fn = getattr(lib(), "oracle_%s_vectors" % kind)
+    fn = getattr(lib(timing), "oracle_%s_vectors" % kind)
     rc = fn(_ptr(coords, _fp), nf, na, nq, _ptr(sub_offsets, _sp), _ptr(subvectors, _dp),
             _ptr(factors, _dp), dsp_type, dsp_method, nthreads, _ptr(fqt, _dp), _ptr(fq, _dp),
             _ptr(fq2, _dp))
@@ -113,17 +124,26 @@ def _vectors(kind, coords, sub_offsets, subvectors, factors, dsp_type, dsp_metho
 
 
 def all_vectors(coords, sub_offsets, subvectors, factors, dsp_type=DSP_AUTOCORRELATE,
-                dsp_method=METHOD_FFTW, nthreads=None):
-    """Coherent S(q,t) per q: returns (fqt [nq,nf,2], fq [nq,2], fq2 [nq,2])."""
+                dsp_method=METHOD_FFTW, nthreads=None, timing=False):
+    """Coherent S(q,t) per q: returns (fqt [nq,nf,2], fq [nq,2], fq2 [nq,2]).
+    timing=True runs the CPU-baseline build (for timings only)."""
     return _vectors("all", coords, sub_offsets, subvectors, factors, dsp_type, dsp_method,
-                    nthreads or os.cpu_count())
+                    nthreads or os.cpu_count(), timing)
 
 
 def self_vectors(coords, sub_offsets, subvectors, factors, dsp_type=DSP_AUTOCORRELATE,
-                 dsp_method=METHOD_FFTW, nthreads=None):
+                 dsp_method=METHOD_FFTW, nthreads=None, timing=False):
     """Incoherent F(q,t) per q: returns (fqt [nq,nf,2], fq [nq,2], fq2 [nq,2])."""
     return _vectors("self", coords, sub_offsets, subvectors, factors, dsp_type, dsp_method,
-                    nthreads or os.cpu_count())
+                    nthreads or os.cpu_count(), timing)
+
+
+def last_split(timing=False):
+    """(scatter_s, dsp_s): thread-seconds of the last vectors call of that build spent in
+    the phase sum and in the correlation (dsp)."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    lib(timing).oracle_last_split(ctypes.byref(a), ctypes.byref(b))
+    return a.value, b.value
 
 
 def amplitudes(coords, subvectors, sub_shell, factors, nthreads=None):

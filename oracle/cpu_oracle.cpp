@@ -23,6 +23,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <complex>
 #include <cstddef>
@@ -172,6 +173,14 @@ struct Accum {
         fq2[0] = a2.real(); fq2[1] = a2.imag();
     }
 };
+
+// Seconds spent (summed over worker threads) in the phase sum and in dsp by the last
+// vectors call: the correlation share of the CPU time. Two clock reads per series.
+std::atomic<long long> g_scatter_ns(0), g_dsp_ns(0);
+inline long long now_ns() {
+    return std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
 
 template <class F>
 void parallel_for(size_t n, int nthreads, F&& fn) {
@@ -447,10 +456,19 @@ void oracle_autocorrelate_direct(double* data, size_t nf) {
 // single-partition branch :259-285) and ::scatter (:388-439). Sub-vectors are
 // scattered in parallel and then dsp+store run in sub-vector order, as the
 // reference's main thread does (:270-279).
+// Thread-seconds of the last oracle_all_vectors / oracle_self_vectors call spent in the
+// phase sum (scatter) and in dsp (correlation).
+void oracle_last_split(double* scatter_s, double* dsp_s) {
+    *scatter_s = g_scatter_ns.load() * 1e-9;
+    *dsp_s = g_dsp_ns.load() * 1e-9;
+}
+
 int oracle_all_vectors(const float* coords, size_t nf, size_t na, size_t nq,
                        const size_t* sub_offsets, const double* subvectors,
                        const double* factors, int dsp_type, int dsp_method,
                        int nthreads, double* fqt, double* fq, double* fq2) {
+    g_scatter_ns = 0;
+    g_dsp_ns = 0;
     if (nf == 0 || na == 0) return 1;
     Dft fwd(2 * nf, -1), bwd(2 * nf, +1);
     for (size_t iq = 0; iq < nq; ++iq) {
@@ -465,6 +483,7 @@ int oracle_all_vectors(const float* coords, size_t nf, size_t na, size_t nq,
             const double* q = subvectors + 3 * (m0 + m);
             double qx = q[0], qy = q[1], qz = q[2];
             cd* p_a = &at[m * 2 * nf];
+            const long long t0 = now_ns();
             for (size_t fi = 0; fi < nf; ++fi) {
                 const float* p_data = coords + fi * na * 3;
                 double Ar = 0, Ai = 0;
@@ -479,7 +498,10 @@ int oracle_all_vectors(const float* coords, size_t nf, size_t na, size_t nq,
             }
             // alignpad (:186-207) zero-fills [nf, 2nf); dsp is per sub-vector
             for (size_t fi = nf; fi < 2 * nf; ++fi) p_a[fi] = 0;
+            const long long t1 = now_ns();
             dsp(p_a, nf, dsp_type, dsp_method, fwd, bwd);
+            g_scatter_ns += t1 - t0;
+            g_dsp_ns += now_ns() - t1;
         });
         for (size_t m = 0; m < nm; ++m) acc.store(&at[m * 2 * nf], nf);
         acc.finish(nm, fqt + iq * nf * 2, fq + iq * 2, fq2 + iq * 2);
@@ -498,6 +520,8 @@ int oracle_self_vectors(const float* coords, size_t nf, size_t na, size_t nq,
                         const size_t* sub_offsets, const double* subvectors,
                         const double* factors, int dsp_type, int dsp_method,
                         int nthreads, double* fqt, double* fq, double* fq2) {
+    g_scatter_ns = 0;
+    g_dsp_ns = 0;
     if (nf == 0 || na == 0) return 1;
     Dft fwd(2 * nf, -1), bwd(2 * nf, +1);
     for (size_t iq = 0; iq < nq; ++iq) {
@@ -513,6 +537,7 @@ int oracle_self_vectors(const float* coords, size_t nf, size_t na, size_t nq,
                 const double* q = subvectors + 3 * (m0 + mi);
                 double qx = q[0], qy = q[1], qz = q[2];
                 cd* p = &at[mi * 2 * nf];
+                const long long t0 = now_ns();
                 for (size_t j = 0; j < nf; ++j) {
                     const float* r = coords + (j * na + ai) * 3;
                     float x1 = r[0], y1 = r[1], z1 = r[2];
@@ -522,7 +547,10 @@ int oracle_self_vectors(const float* coords, size_t nf, size_t na, size_t nq,
                     p[j] = cd(s * cp1, s * sp1);
                 }
                 for (size_t j = nf; j < 2 * nf; ++j) p[j] = 0;
+                const long long t1 = now_ns();
                 dsp(p, nf, dsp_type, dsp_method, fwd, bwd);
+                g_scatter_ns += t1 - t0;
+                g_dsp_ns += now_ns() - t1;
             });
             for (size_t mi = 0; mi < nm; ++mi) acc.store(&at[mi * 2 * nf], nf);
         }
