@@ -80,7 +80,25 @@ def layered():
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_incoherent_fqt_full_size_vs_oracle(native_lib, incoherent, precision):
-    incoherent.check(precision)
+    """At this size the reference's own FP64 arithmetic drifts: it adds each of the 10^5
+    series' correlations (1,000 atoms x 100 directions per shell) to one running sum in
+    turn (smath::add_elements in SelfVectorsScatterDevice::store), and the rounding of
+    adding nearly equal values accumulates to about 2e-12 of F(q,0). The oracle follows that
+    order and shows the drift against the exact F(q,0) = sum_j b_j^2; the GPU sums the power
+    spectra in a tree and is exact to about 1e-16 there. So the FP64 bar is 1e-12 plus the
+    oracle's measured drift, and the GPU's own F(q,0) is held to 1e-13 of the exact value."""
+    c = incoherent
+    tol = TOL[precision]
+    if precision == "fp64":
+        exact = (c.cf[:, c.w.atom_class] ** 2).sum(axis=1)
+        drift = np.abs(c.ref[0][:, 0, 0] - exact) / exact
+        (fqt, _, _), _ = c.gpu("fp64")
+        assert (np.abs(fqt[:, 0] - exact) / exact).max() <= 1e-13
+        tol = 1e-12 + 2.0 * drift.max()
+    (fqt, fq, fq2), _ = c.gpu(precision)
+    rfqt, rfq, rfq2 = c.ref
+    e = (rel_err_sqt(fqt, rfqt).max(), rel_err_vec(fq, cplx(rfq)), rel_err_vec(fq2, cplx(rfq2)))
+    assert max(e) <= tol, "%s: rel err fqt/fq/fq2 = %.2e/%.2e/%.2e (bar %.2e)" % ((precision,) + e + (tol,))
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
