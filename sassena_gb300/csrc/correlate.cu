@@ -1075,6 +1075,379 @@ __global__ void __launch_bounds__(kWarpFftWarps * 32, (LG <= 8 && sizeof(T) == 4
 }
 
 // ---------------------------------------------------------------------------------------
+// Transposed register FFT (FP32) for one padded length L = 16 C, C = 4, 8, 16 (64 .. 256
+// points), G = 32 / C series per warp. With n = a + C b (a < C, b < 16) and k = k_b + 16 k_a,
+//     X[k] = sum_a W_C^{a k_a} [ W_L^{a k_b} sum_b x[a + C b] W_16^{b k_b} ],
+// so lane (g, a) of pass 1 generates or loads its column b = 0 .. 7 of series g (the upper
+// half is the zero padding), runs the 16-point DFT over b in registers (the first stage
+// folded, constant twiddles), multiplies by W_L^{a k_b} and writes the 16 values into the
+// warp's shared-memory tile; after one __syncwarp, lane l of pass 2 reads the rows
+// (g = l / 16 + 2 j, k_b = l % 16), j < G / 2, and runs the C-point DFTs over a in
+// registers. One transpose through shared memory replaces the five shuffle stages of the
+// lane-strided form. Lane l then owns the bins k_b = l % 16 + 16 k_a of its series: their
+// power is summed in plain FP32 for a few rounds and folded into Kahan-compensated FP32
+// state in shared memory, and each series' sum_k P K (its mean over lags) is reduced over
+// the half warp. Tile rows are padded and the per-lane twiddle and store-kernel tables are
+// laid out lane-contiguous, so shared-memory accesses are free of bank conflicts. All
+// twiddle choices are resolved at compile time.
+// ---------------------------------------------------------------------------------------
+constexpr int kReg2Warps = 8, kReg2MinLg = 6, kReg2MaxLg = 8;
+
+// W_L^m for 0 <= m < L from the half table of the launch's largest length (W^m = -W^{m-L/2}).
+template <class T2>
+__device__ __forceinline__ T2 tw_full(const T2* tw, int m, int lg, int tws) {
+    const int h = 1 << (lg - 1);
+    if (m < h) return tw[m << tws];
+    T2 v = tw[(m - h) << tws];
+    v.x = -v.x;
+    v.y = -v.y;
+    return v;
+}
+
+template <int LG>
+struct Reg2Shape {
+    static constexpr int L = 1 << LG, C = L / 16, G = 32 / C, RPL = G / 2;
+    static constexpr int S = 2 * C + 4;          // words per tile row (C complex + 2 padding)
+    static constexpr int GS = 16 * S + 2 * C;    // words per series
+    static constexpr int WW = G * GS;            // words per warp
+    static constexpr int FOLD = 8;               // rounds of plain FP32 power sums between Kahan folds
+    static constexpr int NAS = LG >= 8 ? 4 : 8;  // atoms staged per barrier (three CTAs per SM fit)
+};
+
+__host__ __device__ constexpr int brev_bits(int v, int bits) {
+    return bits == 0 ? 0 : (((v & 1) << (bits - 1)) | brev_bits(v >> 1, bits - 1));
+}
+
+// cos / sin of -2 pi j / 16 (the forward transform's W_16^j)
+__host__ __device__ constexpr float w16_re(int j) {
+    return j == 0 ? 1.f : j == 1 ? 0.923879532511286756f : j == 2 ? 0.707106781186547524f
+         : j == 3 ? 0.382683432365089772f : j == 4 ? 0.f : j == 5 ? -0.382683432365089772f
+         : j == 6 ? -0.707106781186547524f : j == 7 ? -0.923879532511286756f : j == 8 ? -1.f
+         : j == 9 ? -0.923879532511286756f : j == 10 ? -0.707106781186547524f : j == 11 ? -0.382683432365089772f
+         : j == 12 ? 0.f : j == 13 ? 0.382683432365089772f : j == 14 ? 0.707106781186547524f
+         : 0.923879532511286756f;
+}
+__host__ __device__ constexpr float w16_im(int j) { return -w16_re((j + 12) & 15); }
+
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+
+// v * W_16^J: products in scalar FP32, so no register pairs need rebuilding; the factors
+// 1, -i, -1, +i cost no multiplications.
+template <int J>
+__device__ __forceinline__ float2 mul_w16c(float2 v) {
+    constexpr int j = J & 15;
+    if constexpr (j == 0) return v;
+    else if constexpr (j == 4) return make_float2(v.y, -v.x);
+    else if constexpr (j == 8) return make_float2(-v.x, -v.y);
+    else if constexpr (j == 12) return make_float2(-v.y, v.x);
+    else {
+        constexpr float c = w16_re(j), s = w16_im(j);
+        return make_float2(fmaf(v.x, c, -v.y * s), fmaf(v.x, s, v.y * c));
+    }
+}
+
+// DIF butterfly: a' = a + b (paired), b' = (a - b) W_16^J
+template <int J>
+__device__ __forceinline__ void bfly16c(float2& a, float2& b) {
+    constexpr int j = J & 15;
+    const float2 u = a, w = b;
+    a = __fadd2_rn(u, w);
+    if constexpr (j == 0) b = sub2(u, w);
+    else if constexpr (j == 4) b = make_float2(u.y - w.y, w.x - u.x);
+    else if constexpr (j == 8) b = sub2(w, u);
+    else if constexpr (j == 12) b = make_float2(w.y - u.y, u.x - w.x);
+    else b = mul_w16c<j>(sub2(u, w));
+}
+
+// Radix-2 DIF stages of span H .. 1 over x[OFF .. OFF + N) (N <= 16, natural order in,
+// bit-reversed order out), unrolled by template recursion.
+template <int N, int OFF, int H, int M, int TOT>
+__device__ __forceinline__ void dif_stage(float2 (&x)[TOT]) {
+    if constexpr (M < N) {
+        if constexpr ((M & H) == 0) bfly16c<(M & (H - 1)) * (8 / H)>(x[OFF + M], x[OFF + M + H]);
+        dif_stage<N, OFF, H, M + 1, TOT>(x);
+    }
+}
+template <int N, int OFF, int H, int TOT>
+__device__ __forceinline__ void dif_lane(float2 (&x)[TOT]) {
+    if constexpr (H >= 1) {
+        dif_stage<N, OFF, H, 0, TOT>(x);
+        dif_lane<N, OFF, H / 2, TOT>(x);
+    }
+}
+
+// the folded first stage of pass 1 (upper half zero): x[b + 8] = x[b] W_16^b
+template <int B = 0>
+__device__ __forceinline__ void fold_first(float2 (&x)[16]) {
+    if constexpr (B < 8) {
+        x[B + 8] = mul_w16c<B>(x[B]);
+        fold_first<B + 1>(x);
+    }
+}
+
+// pass-1 results into the tile: register p holds k_b = br16(p)
+template <int S, int P = 0>
+__device__ __forceinline__ void store_tile(float* base, const float2 (&x)[16]) {
+    if constexpr (P < 16) {
+        *reinterpret_cast<float2*>(base + brev_bits(P, 4) * S) = x[P];
+        store_tile<S, P + 1>(base, x);
+    }
+}
+
+// the RPL row transforms of pass 2: x[J C .. J C + C) for J < RPL
+template <int C, int RPL, int J = 0>
+__device__ __forceinline__ void dif_rows(float2 (&x)[16]) {
+    if constexpr (J < RPL) {
+        dif_lane<C, J * C, C / 2, 16>(x);
+        dif_rows<C, RPL, J + 1>(x);
+    }
+}
+
+// Shared memory of reg2_fft_kernel, in bytes from the start.
+template <int LG>
+struct Reg2Layout {
+    typedef Reg2Shape<LG> Sh;
+    static constexpr size_t kTiles = (size_t)kReg2Warps * Sh::WW * 4, kBins = (size_t)kReg2Warps * Sh::L * 8;
+    static constexpr size_t kTw = 0;                          // float4 [8][C]: W_L^{a br16(p)}, p = 2 pp, 2 pp + 1
+    static constexpr size_t kK = kTw + (size_t)Sh::L * 8;     // float4 [C / 2][16]: K of bins k_b + 16 br_C(q), q = 2 qq, 2 qq + 1
+    static constexpr size_t kKahan = kK + (size_t)Sh::L * 8;  // float2 [NW][C][16]: power (sum, compensation)
+    static constexpr size_t kTile = kKahan + (size_t)kReg2Warps * Sh::C * 16 * 8;
+    static constexpr size_t kRed = kTile + (kTiles > kBins ? kTiles : kBins);  // tiles, then partial bins
+    static constexpr size_t kTraj = kRed + kReg2Warps * (16 + 8);  // float4 [NAS][nf], then float [NAS]
+};
+
+template <int LG>
+size_t reg2_fft_smem(int nf, bool self) {
+    size_t b = Reg2Layout<LG>::kTraj;
+    if (self) b += (size_t)Reg2Shape<LG>::NAS * nf * sizeof(float4) + Reg2Shape<LG>::NAS * sizeof(float);
+    return b;
+}
+
+template <int LG, bool SELF>
+__global__ void __launch_bounds__(kReg2Warps * 32, 3) reg2_fft_kernel(CorrLaunch a) {
+    typedef Reg2Shape<LG> Sh;
+    typedef Reg2Layout<LG> Ly;
+    constexpr int NW = kReg2Warps, NT = NW * 32, L = Sh::L, C = Sh::C, G = Sh::G, RPL = Sh::RPL;
+    constexpr int BC = ilog2c(C);
+    extern __shared__ __align__(16) unsigned char smem[];
+    const CorrChunk c = a.chunks[blockIdx.x];
+    const CorrSystem sys = a.systems[c.system];
+    const int nf = sys.nf, tws = a.lg_max - LG;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float4* ttab = reinterpret_cast<float4*>(smem + Ly::kTw);
+    float4* ktab = reinterpret_cast<float4*>(smem + Ly::kK);
+    float2* kst = reinterpret_cast<float2*>(smem + Ly::kKahan) + (size_t)warp * C * 16;
+    float* tile = reinterpret_cast<float*>(smem + Ly::kTile) + (size_t)warp * Sh::WW;
+    double* pw = reinterpret_cast<double*>(smem + Ly::kTile);  // [NW][L] after the loop
+    double2* red = reinterpret_cast<double2*>(smem + Ly::kRed);
+    double* red2 = reinterpret_cast<double*>(red + NW);
+    float4* rj = reinterpret_cast<float4*>(smem + Ly::kTraj);
+    {
+        // lane-contiguous tables: entry (pp, col) and (qq, kb) are read by consecutive lanes
+        const float2* twg = reinterpret_cast<const float2*>(a.tw);
+        const float2* kbr = reinterpret_cast<const float2*>(sys.kbr);
+        for (int i = threadIdx.x; i < L / 2; i += NT) {
+            const int pp = i / C, col = i - pp * C;
+            const float2 t0 = tw_full(twg, col * brev_bits(2 * pp, 4), LG, tws);
+            const float2 t1 = tw_full(twg, col * brev_bits(2 * pp + 1, 4), LG, tws);
+            ttab[i] = make_float4(t0.x, t0.y, t1.x, t1.y);
+            const int qq = i >> 4, kb = i & 15;
+            const int k0 = kb + 16 * brev_bits(2 * qq, BC), k1 = kb + 16 * brev_bits(2 * qq + 1, BC);
+            const float2 a0 = kbr[__brev((unsigned)k0) >> (32 - LG)], a1 = kbr[__brev((unsigned)k1) >> (32 - LG)];
+            ktab[i] = make_float4(a0.x, a0.y, a1.x, a1.y);
+        }
+        for (int i = threadIdx.x; i < NW * C * 16; i += NT)
+            reinterpret_cast<float2*>(smem + Ly::kKahan)[i] = make_float2(0.f, 0.f);
+    }
+    // pass-1 role: series g1, column col; pass-2 role: row k_b of series half + 2 j
+    const int g1 = lane / C, col = lane - g1 * C, kb = lane & 15, half = lane >> 4;
+    float pacc[C];
+#pragma unroll
+    for (int q = 0; q < C; ++q) pacc[q] = 0.f;
+    SeriesAcc<float> sacc;
+    int rounds = 0;
+    __syncthreads();
+
+    // Kahan fold of the plain sums; lanes l and l + 16 hold the same bins
+    auto fold = [&]() {
+#pragma unroll
+        for (int q = 0; q < C; ++q) {
+            const float v = pacc[q] + __shfl_xor_sync(0xffffffffu, pacc[q], 16);
+            pacc[q] = 0.f;
+            if (half == 0) {
+                float2 st = kst[q * 16 + kb];
+                const float y = __fsub_rn(v, st.y), t = __fadd_rn(st.x, y);
+                st.y = __fsub_rn(__fsub_rn(t, st.x), y);
+                st.x = t;
+                kst[q * 16 + kb] = st;
+            }
+        }
+    };
+
+    // the warp's G series: get(n, m) is point n (< NF) of this lane's pass-1 series times
+    // m (0 for the zero padding), valid(g) whether series g exists this round
+    auto transform = [&](auto get, auto valid) {
+        float2 x[16];
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {  // points beyond NF read the last point, scaled by 0
+            const int n = col + C * b;
+            x[b] = get(min(n, nf - 1), n < nf ? 1.f : 0.f);
+        }
+        fold_first(x);  // first stage, upper half zero
+        dif_lane<16, 0, 4, 16>(x);
+#pragma unroll
+        for (int p = 0; p < 16; p += 2) {  // times W_L^{col k1}, k1 = br16(p) (p = 0: k1 = 0)
+            const float4 w = ttab[(p / 2) * C + col];
+            if (p > 0) x[p] = make_float2(fmaf(x[p].x, w.x, -x[p].y * w.y), fmaf(x[p].x, w.y, x[p].y * w.x));
+            x[p + 1] = make_float2(fmaf(x[p + 1].x, w.z, -x[p + 1].y * w.w), fmaf(x[p + 1].x, w.w, x[p + 1].y * w.z));
+        }
+        __syncwarp();  // the previous round's pass 2 has read the tile
+        store_tile<Sh::S>(tile + g1 * Sh::GS + 2 * col, x);
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < RPL; ++j) {
+            const float* row = tile + (half + 2 * j) * Sh::GS + kb * Sh::S;
+#pragma unroll
+            for (int q = 0; q < C; q += 2) {
+                const float4 v = *reinterpret_cast<const float4*>(row + 2 * q);
+                x[j * C + q] = make_float2(v.x, v.y);
+                x[j * C + q + 1] = make_float2(v.z, v.w);
+            }
+        }
+        dif_rows<C, RPL>(x);
+        // power of the lane's bins k = k_b + 16 br_C(q) and each series' sum_k P K
+        float sx[RPL], sy[RPL];
+#pragma unroll
+        for (int j = 0; j < RPL; ++j) sx[j] = sy[j] = 0.f;
+#pragma unroll
+        for (int q = 0; q < C; q += 2) {
+            const float4 kv = ktab[(q / 2) * 16 + kb];
+#pragma unroll
+            for (int j = 0; j < RPL; ++j) {
+                const float2 v0 = x[j * C + q], v1 = x[j * C + q + 1];
+                const float P0 = fmaf(v0.x, v0.x, v0.y * v0.y), P1 = fmaf(v1.x, v1.x, v1.y * v1.y);
+                pacc[q] += P0;
+                pacc[q + 1] += P1;
+                sx[j] = fmaf(P1, kv.z, fmaf(P0, kv.x, sx[j]));
+                sy[j] = fmaf(P1, kv.w, fmaf(P0, kv.y, sy[j]));
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < RPL; ++j) {
+            float tx = sx[j], ty = sy[j];
+#pragma unroll
+            for (int o = 8; o >= 1; o >>= 1) {  // within the half warp: the series' total
+                tx += __shfl_xor_sync(0xffffffffu, tx, o);
+                ty += __shfl_xor_sync(0xffffffffu, ty, o);
+            }
+            if (kb == 0 && valid(half + 2 * j)) sacc.add(tx, ty);
+        }
+        if (++rounds == Sh::FOLD) {
+            fold();
+            rounds = 0;
+        }
+    };
+
+    if (SELF) {
+        constexpr int NAS = Sh::NAS;
+        float* bsm = reinterpret_cast<float*>(rj + (size_t)NAS * nf);
+        const float* bfac = reinterpret_cast<const float*>(sys.bfac);
+        const int v0 = sys.shell_v[c.shell], nd = sys.shell_v[c.shell + 1] - v0;
+        for (int j0 = c.v_begin; nd > 0 && j0 < c.v_end; j0 += NAS) {  // (no directions: no series)
+            const int na = min(NAS, c.v_end - j0), npair = na * nd;
+            __syncthreads();  // every warp is done with the previous atoms' trajectories
+            for (int i = threadIdx.x; i < na * nf; i += NT) {
+                const int t = i / na, at = i - t * na;
+                rj[at * nf + t] = sys.xyz[(size_t)t * sys.na_pad + j0 + at];
+            }
+            if (threadIdx.x < na) bsm[threadIdx.x] = bfac[(size_t)c.shell * sys.na_pad + j0 + threadIdx.x];
+            __syncthreads();
+            // pair pr = atom * nd + direction (nd >= 1), walked without divisions
+            int at0 = 0, d0 = warp * G;
+            while (d0 >= nd) {
+                d0 -= nd;
+                ++at0;
+            }
+            for (int pr0 = warp * G; pr0 < npair; pr0 += NW * G) {
+                int at = at0, d = d0 + g1;
+                while (d >= nd) {
+                    d -= nd;
+                    ++at;
+                }
+                const bool ok = at < na;
+                if (!ok) {
+                    at = na - 1;
+                    d = 0;
+                }
+                float qx, qy, qz;
+                load_qv(sys.qv, sys.qrev, (size_t)(v0 + d), qx, qy, qz);
+                const float b = ok ? bsm[at] : 0.f;
+                const float4* ra = rj + (size_t)at * nf;
+                transform([&](int n, float m) { return self_term(b * m, ra[n], qx, qy, qz); },
+                          [&](int g) { return pr0 + g < npair; });
+                d0 += NW * G;
+                while (d0 >= nd) {
+                    d0 -= nd;
+                    ++at0;
+                }
+            }
+        }
+    } else {
+        const int nser = c.v_end - c.v_begin;
+        for (int s0 = warp * G; s0 < nser; s0 += NW * G) {
+            const bool mine = s0 + g1 < nser;
+            const float mm = mine ? 1.f : 0.f;
+            const float2* src = reinterpret_cast<const float2*>(sys.A) + (size_t)(c.v_begin + (mine ? s0 + g1 : 0)) * nf;
+            transform([&](int n, float m) {
+                const float2 v = src[n];
+                return make_float2(v.x * (m * mm), v.y * (m * mm));
+            },
+                      [&](int g) { return s0 + g < nser; });
+        }
+    }
+    fold();
+
+    // the warp's bins and series sums (lanes 0 and 16), then the chunk's partial slot in
+    // bit-reversed order
+    __syncthreads();  // every warp is done with its tile: the region now holds partial bins
+    if (half == 0) {
+#pragma unroll
+        for (int q = 0; q < C; ++q) {
+            const float2 st = kst[q * 16 + kb];
+            const int k = kb + 16 * brev_bits(q, BC);
+            pw[(size_t)warp * L + (__brev((unsigned)k) >> (32 - LG))] = (double)st.x - (double)st.y;
+        }
+    }
+    double2 ms = sacc.mean_sum();
+    double s2 = sacc.sq_sum();
+    ms.x += __shfl_xor_sync(0xffffffffu, ms.x, 16);
+    ms.y += __shfl_xor_sync(0xffffffffu, ms.y, 16);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, 16);
+    if (lane == 0) {
+        red[warp] = ms;
+        red2[warp] = s2;
+    }
+    __syncthreads();
+    double* dst = a.ppart + c.part_off;
+    for (int i = threadIdx.x; i < L; i += NT) {
+        double sum = 0.0;
+        for (int w = 0; w < NW; ++w) sum += pw[(size_t)w * L + i];
+        dst[i] = sum;
+    }
+    if (threadIdx.x == 0) {
+        double2 as = make_double2(0.0, 0.0);
+        double a2 = 0.0;
+        for (int w = 0; w < NW; ++w) {
+            as.x += red[w].x;
+            as.y += red[w].y;
+            a2 += red2[w];
+        }
+        a.apart[c.slot] = as;
+        a.a2part[c.slot] = a2;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
 // Block-register FFT for series of one padded length L = 512 B (B = 2, 4, 8: 1,024 .. 4,096
 // points). The first log2 B DIF stages are folded into the load: after them, position
 // 512 b + j of the DIF array holds
@@ -1091,17 +1464,6 @@ __global__ void __launch_bounds__(kWarpFftWarps * 32, (LG <= 8 && sizeof(T) == 4
 // shared memory per series.
 // ---------------------------------------------------------------------------------------
 constexpr int kBlkFftWarps = 8, kBlkFftMinLg = 10, kBlkFftMaxLg = 12;
-
-// W_L^m for 0 <= m < L from the half table of the launch's largest length (W^m = -W^{m-L/2}).
-template <class T2>
-__device__ __forceinline__ T2 tw_full(const T2* tw, int m, int lg, int tws) {
-    const int h = 1 << (lg - 1);
-    if (m < h) return tw[m << tws];
-    T2 v = tw[(m - h) << tws];
-    v.x = -v.x;
-    v.y = -v.y;
-    return v;
-}
 
 template <class T, int LG>
 struct BlkFft {
@@ -1371,8 +1733,19 @@ cudaError_t launch_blk_fft(const CorrLaunch& a, bool self, cudaStream_t st) {
     return cudaErrorInvalidValue;
 }
 
+template <int LG>
+cudaError_t launch_reg2_fft_lg(const CorrLaunch& a, bool self, cudaStream_t st) {
+    const size_t sm = reg2_fft_smem<LG>(a.nf_max, self);
+    auto k = self ? reg2_fft_kernel<LG, true> : reg2_fft_kernel<LG, false>;
+    cudaError_t e = set_smem(k, sm);
+    if (e != cudaSuccess) return e;
+    k<<<a.nchunks, kReg2Warps * 32, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
 template <class T, int LG>
 cudaError_t launch_reg_fft_lg(const CorrLaunch& a, bool self, cudaStream_t st) {
+    if constexpr (sizeof(T) == 4 && LG >= kReg2MinLg && LG <= kReg2MaxLg) return launch_reg2_fft_lg<LG>(a, self, st);
     const size_t sm = reg_fft_smem<T>(LG, a.nf_max, self);
     auto k = self ? reg_fft_kernel<T, LG, true> : reg_fft_kernel<T, LG, false>;
     cudaError_t e = set_smem(k, sm);
