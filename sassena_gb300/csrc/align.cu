@@ -244,7 +244,7 @@ __global__ void pp_target_kernel(const double* __restrict__ W, size_t nsys, cons
 }
 
 unsigned grid_for(size_t n, int threads) {
-    return (unsigned)std::max<size_t>(1, std::min<size_t>((n + threads - 1) / threads, 152 * 32));
+    return grid_blocks(n, threads, 32);
 }
 
 // ---------------------------------------------------------------------------------------

@@ -326,7 +326,8 @@ __device__ __forceinline__ const typename cplx<T>::type* stage_twiddles(
 
 inline int grid_for(size_t n, int threads) {
     size_t b = (n + threads - 1) / threads;
-    if (b > 152 * 32) b = 152 * 32;
+    const size_t cap = (size_t)current_sms() * 32;
+    if (b > cap) b = cap;
     if (b < 1) b = 1;
     return (int)b;
 }

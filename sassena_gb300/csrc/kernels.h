@@ -13,6 +13,28 @@
 
 namespace sassgpu {
 
+// SM count of the current device, queried once per device. Grids are sized from it, never
+// from a fixed count; 1 if the query fails, so grid-stride loops stay valid (only slower).
+inline int current_sms() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    static int cache[64] = {0};
+    if (dev >= 0 && dev < 64 && cache[dev] > 0) return cache[dev];
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+    if (dev >= 0 && dev < 64) cache[dev] = n;
+    return n;
+}
+
+// Blocks of `threads` for a grid-stride loop over n items: enough for every item, at most
+// per_sm CTAs per SM of the current device, at least one.
+inline unsigned grid_blocks(size_t n, int threads, int per_sm) {
+    size_t b = (n + (size_t)threads - 1) / (size_t)threads;
+    const size_t cap = (size_t)current_sms() * (size_t)per_sm;
+    if (b > cap) b = cap;
+    return b < 1 ? 1u : (unsigned)b;
+}
+
 enum Precision { PREC_FP64 = 0, PREC_FP32 = 1 };
 
 // Device-side error codes written to the plan's error word (first writer wins).

@@ -300,7 +300,7 @@ cudaError_t launch_mlp_sphere(const __nv_bfloat16* w, const double* qlen, int ns
 
 cudaError_t launch_scale_series(void* A, bool f32, const double* wsqrt, size_t nv, int nf, cudaStream_t st) {
     const size_t n = nv * (size_t)nf;
-    int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    int blocks = n ? (int)grid_blocks(n, 256, 16) : 0;
     if (blocks < 1) return cudaSuccess;
     if (f32) scale_series_kernel<float2><<<blocks, 256, 0, st>>>((float2*)A, wsqrt, nv, nf);
     else scale_series_kernel<double2><<<blocks, 256, 0, st>>>((double2*)A, wsqrt, nv, nf);

@@ -738,7 +738,7 @@ extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const d
         MCK(cudaStreamSynchronize(st));
         const int* slot = p->mp_slot.as<int>();
         const size_t n = nf * na_pad;
-        const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+        const int blocks = (int)grid_blocks(n, 256, 16);
         mp_convert_kernel<<<std::max(blocks, 1), 256, 0, st>>>(s.xyz.as<float4>(), (int)na_pad, (int)s.na, (int)nf, cyl,
                                                                 base, slot, s.cls.as<int>(), s.mp_xyz.as<float4>());
         MCK(cudaGetLastError());
@@ -791,9 +791,9 @@ extern "C" int sass_multipole_compute(sass_plan* p, int type, size_t nq, const d
             ba.f0 = (int)f0;
             ba.nfb = nb;
             const size_t ny = (size_t)nb * na_pad, nj = ny * nq;
-            mp_ylm_kernel<<<(unsigned)std::min<size_t>((ny + 127) / 128, 152 * 64), 128, ysm, st>>>(ba);
+            mp_ylm_kernel<<<grid_blocks(ny, 128, 64), 128, ysm, st>>>(ba);
             MCK(cudaGetLastError());
-            mp_jl_kernel<<<(unsigned)std::min<size_t>((nj + 127) / 128, 152 * 64), 128, 0, st>>>(ba);
+            mp_jl_kernel<<<grid_blocks(nj, 128, 64), 128, 0, st>>>(ba);
             MCK(cudaGetLastError());
             ++launches;
             MpSphereContract ca{};

@@ -329,7 +329,7 @@ __global__ void permute_stage_kernel(const float4* __restrict__ src, int na_pad_
 cudaError_t launch_permute_stage(const float4* src, int na_pad_src, const int* map, int na_dst, int nf, float4* dst,
                                  cudaStream_t st) {
     const size_t n = (size_t)nf * na_dst;
-    const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 32);
+    const int blocks = (int)grid_blocks(n, 256, 32);
     permute_stage_kernel<<<std::max(blocks, 1), 256, 0, st>>>(src, na_pad_src, map, na_dst, nf, dst);
     return cudaGetLastError();
 }

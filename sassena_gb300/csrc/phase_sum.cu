@@ -476,7 +476,7 @@ cudaError_t launch_phase_sum(const PhaseLaunch& a, cudaStream_t st) {
 cudaError_t launch_split_reduce(const double2* part, int nsplit, size_t n, double2* out,
                                 cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    int blocks = (int)grid_blocks(n, 256, 16);
     split_reduce_kernel<double2><<<blocks, 256, 0, st>>>(part, nsplit, n, out);
     return cudaGetLastError();
 }
@@ -484,7 +484,7 @@ cudaError_t launch_split_reduce(const double2* part, int nsplit, size_t n, doubl
 cudaError_t launch_split_reduce_f32(const double2* part, int nsplit, size_t n, float2* out,
                                     cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    int blocks = (int)grid_blocks(n, 256, 16);
     split_reduce_kernel<float2><<<blocks, 256, 0, st>>>(part, nsplit, n, out);
     return cudaGetLastError();
 }
