@@ -488,7 +488,7 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
             // Enough tiles, but the last round of the persistent grid can leave SMs idle:
             // an SM runs about tiles * s / SMs tiles of ceil(stages / s) atom stages each.
             // Take the split count that minimises ceil(tiles * s / SMs) * ceil(stages / s),
-            // charging each extra split 0.4 % of the unsplit time for its FP64 partials and
+            // charging each extra split 0.4 % of the unsplit time for its partials and
             // their reduction. (coherent S(q,t) workload on GB300, 2,048 tiles of 79 stages:
             // s = 2 gives 26.95 tiles per SM and a 2.4 % shorter step than s = 1.)
             const long long nst = item_ng[i] ? (long long)(items[i].sys->na_rec / 128)
@@ -508,11 +508,11 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
                 }
             }
         }
-        // each split writes FP64 partials of the item's whole amplitude array: at most 4 GiB
-        // of them (items that large have tiles enough without splits, and allocating and
-        // freeing tens of GB, as small split sizes on large systems would, slows every later
-        // allocation of the process)
-        const size_t per_split = (size_t)items[i].offs.back() * items[i].sys->nf * 16;
+        // each split writes partials of the item's whole amplitude array (FP32 pairs in the
+        // FP32 form, FP64 pairs in the FP64 form): at most 4 GiB of them (items that large have
+        // tiles enough without splits, and allocating and freeing tens of GB, as small split
+        // sizes on large systems would, slows every later allocation of the process)
+        const size_t per_split = (size_t)items[i].offs.back() * items[i].sys->nf * (f32 ? 8 : 16);
         const int budget = (int)std::max<size_t>(1, ((size_t)1 << 32) / std::max<size_t>(per_split, 1));
         nsplit_[i] = items[i].d_amp_given ? 1 : std::max(1, std::min(std::min(ns, max_split), budget));
         stats_.max_split = std::max(stats_.max_split, nsplit_[i]);
@@ -534,7 +534,7 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
             amp_bytes += ((nv * nf * (f32 ? 8 : 16) + 255) & ~(size_t)255);
             if (nsplit_[i] > 1) {
                 part_off_[i] = part_bytes;
-                part_bytes += (size_t)nsplit_[i] * nv * nf * 16;
+                part_bytes += (size_t)nsplit_[i] * nv * nf * (f32 ? 8 : 16);
             }
         }
         stats_.terms += (double)nv * (double)it.sys->na * (double)nf;
@@ -561,6 +561,7 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
     item_nf_.assign(items.size(), 0);
     split_part_.assign(items.size(), {nullptr, nullptr});
     split_out32_.assign(items.size(), nullptr);
+    split_part32_.assign(items.size(), nullptr);
     item_cf_.assign(items.size(), nullptr);
     item_sys_.assign(items.size(), nullptr);
     item_nq_.assign(items.size(), 0);
@@ -594,11 +595,17 @@ int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items,
         item_amp_[i] = amp;
         if (coherent && !it.d_amp_given) {
             if (nsplit_[i] > 1) {
-                double2* part = reinterpret_cast<double2*>(part_.as<unsigned char>() + part_off_[i]);
-                p.out = part;
-                p.out_f32 = nullptr;
-                split_part_[i] = {part, f32 ? nullptr : reinterpret_cast<double2*>(amp)};
-                if (f32) split_out32_[i] = reinterpret_cast<float2*>(amp);
+                unsigned char* part = part_.as<unsigned char>() + part_off_[i];
+                if (f32) {  // FP32 partials (8 bytes per frame), summed in FP64 by the reduction
+                    p.out = nullptr;
+                    p.out_f32 = reinterpret_cast<float2*>(part);
+                    split_part32_[i] = reinterpret_cast<float2*>(part);
+                    split_out32_[i] = reinterpret_cast<float2*>(amp);
+                } else {
+                    p.out = reinterpret_cast<double2*>(part);
+                    p.out_f32 = nullptr;
+                    split_part_[i] = {reinterpret_cast<double2*>(part), reinterpret_cast<double2*>(amp)};
+                }
             } else {
                 p.out = f32 ? nullptr : reinterpret_cast<double2*>(amp);
                 p.out_f32 = f32 ? reinterpret_cast<float2*>(amp) : nullptr;
@@ -952,7 +959,7 @@ int Engine::enqueue(cudaStream_t st, std::string& err, cudaEvent_t* ev) {
         for (int i = 0; i < nitems_; ++i) {
             if (nsplit_[i] <= 1) continue;
             const size_t n = item_nv_[i] * item_nf_[i];
-            if (f32) ECK(launch_split_reduce_f32(split_part_[i].first, nsplit_[i], n, split_out32_[i], st));
+            if (f32) ECK(launch_split_reduce_f32(split_part32_[i], nsplit_[i], n, split_out32_[i], st));
             else ECK(launch_split_reduce(split_part_[i].first, nsplit_[i], n, split_part_[i].second, st));
             ++launches;
         }

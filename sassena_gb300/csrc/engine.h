@@ -141,7 +141,8 @@ private:
     std::vector<int> nsplit_;
     std::vector<size_t> item_nv_, item_nf_;
     std::vector<std::pair<double2*, double2*>> split_part_;  // (partials, FP64 out) per item
-    std::vector<float2*> split_out32_;
+    std::vector<float2*> split_out32_;   // FP32 form: amplitudes the split partials reduce into
+    std::vector<float2*> split_part32_;  // FP32 form: the FP32 split partials
     std::vector<const double*> item_cf_;
     std::vector<SystemState*> item_sys_;
     std::vector<size_t> item_nq_;

@@ -66,8 +66,8 @@ struct PhaseSystem {
     const float4* xyz;     // [nf][na_pad] staged coordinates
     const void* bfac;      // [nshell][na_pad] factors: float (FP32) or double (FP64)
     const double* qv;      // [nv][3] sub-vectors of this system
-    double2* out;          // FP64 amplitudes [nv][nf], or FP64 split partials [nsplit][nv][nf]
-    float2* out_f32;       // FP32 amplitudes [nv][nf] when the system has one atom split
+    double2* out;          // FP64 form: amplitudes [nv][nf], or split partials [nsplit][nv][nf]
+    float2* out_f32;       // FP32 amplitudes [nv][nf] (one atom split), or FP32 split partials [nsplit][nv][nf]
     size_t split_stride;   // nv * nf
     int na_pad, nf;
 };
@@ -97,7 +97,7 @@ cudaError_t launch_phase_sum(const PhaseLaunch& a, cudaStream_t st);
 // out[i] = sum_s part[s][i] in split order (FP64), stored as double2 or float2.
 cudaError_t launch_split_reduce(const double2* part, int nsplit, size_t n, double2* out,
                                 cudaStream_t st);
-cudaError_t launch_split_reduce_f32(const double2* part, int nsplit, size_t n, float2* out,
+cudaError_t launch_split_reduce_f32(const float2* part, int nsplit, size_t n, float2* out,
                                     cudaStream_t st);
 
 // ---------------------------------------------------------------------------------------
@@ -118,8 +118,8 @@ struct RecSystem {
     const int* block_class;   // [na_rec / 32] class (low 16 bits) | padding atoms << 16 of every 32-atom block
     const double* cf;         // [nq][nclass] class factors
     const double* dirs;       // [nd][3] base vectors (FP64)
-    double2* out;             // FP64 split partials [nsplit][nv][nf] (when split)
-    float2* out_f32;          // FP32 amplitudes [nv][nf] (one split)
+    double2* out;             // unused by the FP32-only recurrence (kept for the descriptor layout)
+    float2* out_f32;          // FP32 amplitudes [nv][nf] (one split), or FP32 split partials [nsplit][nv][nf]
     size_t split_stride;      // nv * nf
     int na_rec, nf, nd, nclass;
     int g_begin;              // first group of this system in the launch's group list

@@ -230,8 +230,7 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 20 ? 2 : 1) phase_rec_ker
                 const size_t v = (size_t)(gr.s0 + k) * sys.nd + dw;
                 const size_t o = v * nf + td.f0 + w;
                 const double re = (double)st.x - (double)st.z, im = (double)st.y - (double)st.w;
-                if (sys.out_f32) sys.out_f32[o] = make_float2((float)re, (float)im);
-                else sys.out[(size_t)td.split * sys.split_stride + o] = make_double2(re, im);
+                sys.out_f32[(size_t)td.split * sys.split_stride + o] = make_float2((float)re, (float)im);
             }
         }
     }

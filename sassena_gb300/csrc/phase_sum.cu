@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(W * 32)
         for (int k = 0; k < Q; ++k) so[(lane + 32 * k) * W + warp] = acc.result(k);
         __syncthreads();
         if (F32 && sys.out_f32) {
-            float2* dst = sys.out_f32;
+            float2* dst = sys.out_f32 + (size_t)td.split * sys.split_stride;
             for (int idx = threadIdx.x; idx < td.nv * W; idx += W * 32) {
                 int vl = idx / W, w = idx - vl * W, ff = td.f0 + w;
                 if (ff < sys.nf) {
@@ -398,6 +398,22 @@ __global__ void split_reduce_kernel(const double2* __restrict__ part, int nsplit
             a.y += b.y;
         }
         out[i] = store_as<OUT>(a);
+    }
+}
+
+// FP32 form: the partials are FP32 pairs, summed in FP64 in split order.
+__global__ void split_reduce32_kernel(const float2* __restrict__ part, int nsplit, size_t n,
+                                     float2* __restrict__ out) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const float2 p0 = part[i];
+        double ax = p0.x, ay = p0.y;
+        for (int s = 1; s < nsplit; ++s) {
+            const float2 b = part[(size_t)s * n + i];
+            ax += b.x;
+            ay += b.y;
+        }
+        out[i] = make_float2((float)ax, (float)ay);
     }
 }
 
@@ -481,11 +497,11 @@ cudaError_t launch_split_reduce(const double2* part, int nsplit, size_t n, doubl
     return cudaGetLastError();
 }
 
-cudaError_t launch_split_reduce_f32(const double2* part, int nsplit, size_t n, float2* out,
+cudaError_t launch_split_reduce_f32(const float2* part, int nsplit, size_t n, float2* out,
                                     cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     int blocks = (int)grid_blocks(n, 256, 16);
-    split_reduce_kernel<float2><<<blocks, 256, 0, st>>>(part, nsplit, n, out);
+    split_reduce32_kernel<<<blocks, 256, 0, st>>>(part, nsplit, n, out);
     return cudaGetLastError();
 }
 
