@@ -25,6 +25,7 @@
 #include "log.hpp"
 #include "sample.hpp"
 #include "scatter_devices/all_vectors_scatter_device.hpp"
+#include "scatter_devices/gpu_vectors_scatter_device.hpp"
 #include "scatter_devices/self_vectors_scatter_device.hpp"
 #include "services.hpp"
 
@@ -61,29 +62,13 @@ size_t g_id_base = 0;  // fresh database IDs per run: sfactors caches values per
 
 }  // namespace
 
-extern "C" {
-
-/* One run of the reference's coherent (self = 0) or incoherent (self = 1) vectors device.
- *   dsp_type "autocorrelate" | "square" | "plain"; dsp_method "fftw" | "direct"
- *   coords      float32 [nf][na][3], the target selection's staged frames
- *   atom_type   [na] index into the per-type database tables below
- *   sf_type     [ntype] sfactor function type (0 constant, 2 four Gaussians + c)
- *   sf_const    [ntype][9] its constants (database.cpp:469-528)
- *   vol         [ntype] volume (volume function type 0, a constant)
- *   ex_type     [ntype] exclusion function type (0 constant, 1 linear, 2 Gaussian)
- *   ex_const    [ntype] its constant
- *   background  scattering.background.factor (kappa 1 for every atom)
- *   qvectors    [nq][3] scattering vectors, in the order the device writes them
- *   orient      [nm][3] orientations of vectors.type = file, normalised here as
- *               ScatteringAverageOrientationVectorsParameters::create does; nm = 0
- *               means no orientational averaging (the q-vectors themselves)
- * Outputs per written row r: q_out[r][3], fqt[r][nf][2], fq[r][2], fq2[r][2].
- * Returns the number of rows, or -1 with a message in ref_last_error(). */
-long ref_run_vectors(int self, const char* dsp_type, const char* dsp_method, size_t nthreads,
-                     const float* coords, size_t nf, size_t na, const int* atom_type, size_t ntype,
-                     const int* sf_type, const double* sf_const, const double* vol, const int* ex_type,
-                     const double* ex_const, double background, size_t nq, const double* qvectors,
-                     size_t nm, const double* orient, double* q_out, double* fqt, double* fq, double* fq2) {
+// One run of a vectors device (the reference's, or the binding's GpuVectorsScatterDevice)
+// on the case the arguments describe; see ref_run_vectors.
+static long run_device(bool binding, int self, const char* dsp_type, const char* dsp_method, size_t nthreads,
+                const float* coords, size_t nf, size_t na, const int* atom_type, size_t ntype, const int* sf_type,
+                const double* sf_const, const double* vol, const int* ex_type, const double* ex_const,
+                double background, size_t nq, const double* qvectors, size_t nm, const double* orient,
+                double* q_out, double* fqt, double* fq, double* fq2) {
     g_errors.clear();
     Params* P = Params::Inst();
     P->scattering.type = self ? "self" : "all";
@@ -151,7 +136,10 @@ long ref_run_vectors(int self, const char* dsp_type, const char* dsp_method, siz
     boost::mpi::communicator comm;
     boost::asio::ip::tcp::endpoint ep;
     try {
-        if (self) {
+        if (binding) {
+            GpuVectorsScatterDevice dev(comm, comm, sample, qs, self ? na : nf, ep, ep);
+            dev.run();
+        } else if (self) {
             RunSelf dev(comm, comm, sample, qs, na, ep, ep);  // NAF = NA (scatter_device_factory.cpp:60-65)
             dev.run();
         } else {
@@ -166,6 +154,48 @@ long ref_run_vectors(int self, const char* dsp_type, const char* dsp_method, siz
     signal_row_sink() = nullptr;
     return rows;
 }
+
+extern "C" {
+
+/* One run of the reference's coherent (self = 0) or incoherent (self = 1) vectors device.
+ *   dsp_type "autocorrelate" | "square" | "plain"; dsp_method "fftw" | "direct"
+ *   coords      float32 [nf][na][3], the target selection's staged frames
+ *   atom_type   [na] index into the per-type database tables below
+ *   sf_type     [ntype] sfactor function type (0 constant, 2 four Gaussians + c)
+ *   sf_const    [ntype][9] its constants (database.cpp:469-528)
+ *   vol         [ntype] volume (volume function type 0, a constant)
+ *   ex_type     [ntype] exclusion function type (0 constant, 1 linear, 2 Gaussian)
+ *   ex_const    [ntype] its constant
+ *   background  scattering.background.factor (kappa 1 for every atom)
+ *   qvectors    [nq][3] scattering vectors, in the order the device writes them
+ *   orient      [nm][3] orientations of vectors.type = file, normalised here as
+ *               ScatteringAverageOrientationVectorsParameters::create does; nm = 0
+ *               means no orientational averaging (the q-vectors themselves)
+ * Outputs per written row r: q_out[r][3], fqt[r][nf][2], fq[r][2], fq2[r][2].
+ * Returns the number of rows, or -1 with a message in ref_last_error(). */
+long ref_run_vectors(int self, const char* dsp_type, const char* dsp_method, size_t nthreads,
+                     const float* coords, size_t nf, size_t na, const int* atom_type, size_t ntype,
+                     const int* sf_type, const double* sf_const, const double* vol, const int* ex_type,
+                     const double* ex_const, double background, size_t nq, const double* qvectors,
+                     size_t nm, const double* orient, double* q_out, double* fqt, double* fq, double* fq2) {
+    return run_device(false, self, dsp_type, dsp_method, nthreads, coords, nf, na, atom_type, ntype, sf_type,
+                      sf_const, vol, ex_type, ex_const, background, nq, qvectors, nm, orient, q_out, fqt, fq, fq2);
+}
+
+/* The same run with this project's GpuVectorsScatterDevice (the binding a maintainer adds,
+ * sassena_gb300/integration) in place of the reference's device, driven by the reference's
+ * run(). The C ABI it calls is the recording stand-in of binding_abi.cpp: the rows it writes
+ * are zero, and bind_last_* return what it passed to the library. */
+long bind_run_vectors(int self, const char* dsp_type, const char* dsp_method, size_t nthreads,
+                      const float* coords, size_t nf, size_t na, const int* atom_type, size_t ntype,
+                      const int* sf_type, const double* sf_const, const double* vol, const int* ex_type,
+                      const double* ex_const, double background, size_t nq, const double* qvectors,
+                      size_t nm, const double* orient, double* q_out, double* fqt, double* fq, double* fq2) {
+    return run_device(true, self, dsp_type, dsp_method, nthreads, coords, nf, na, atom_type, ntype, sf_type,
+                      sf_const, vol, ex_type, ex_const, background, nq, qvectors, nm, orient, q_out, fqt, fq, fq2);
+}
+
+
 
 /* The reference's q-vector scans (ScatteringVectorsParameters::create_from_scans) for up to
  * three scans; base[s][3], from/to/exponent[s], points[s]. Writes at most cap vectors to

@@ -49,6 +49,10 @@ def load(ref_tree=None):
                                   ctypes.c_size_t, ctypes.c_size_t, _ip, ctypes.c_size_t, _ip, _dp, _dp, _ip,
                                   _dp, ctypes.c_double, ctypes.c_size_t, _dp, ctypes.c_size_t, _dp, _dp, _dp,
                                   _dp, _dp]
+    L.bind_run_vectors.restype = ctypes.c_long
+    L.bind_run_vectors.argtypes = L.ref_run_vectors.argtypes
+    L.bind_last_sizes.argtypes = [ctypes.POINTER(ctypes.c_long), _sp]
+    L.bind_last_calls.argtypes = [_sp, _dp, _dp, _ip, _fp]
     L.ref_scans.restype = ctypes.c_long
     L.ref_scans.argtypes = [ctypes.c_size_t, _dp, _dp, _sp, _dp, _dp, ctypes.c_size_t, _dp]
     L.ref_sfactor.restype = ctypes.c_double
@@ -102,7 +106,8 @@ def directions(rng, n):
     return v / np.linalg.norm(v, axis=1, keepdims=True) * rng.uniform(0.5, 2.0, (n, 1))  # unnormalised on purpose
 
 
-def run_case(L, self_, dsp, method, coords, atom_type, tables, background, qvectors, orient, nthreads=3):
+def run_case(L, self_, dsp, method, coords, atom_type, tables, background, qvectors, orient, nthreads=3,
+             binding=False):
     sf_type, sf_const, vol, ex_type, ex_const = tables
     nf, na = coords.shape[0], coords.shape[1]
     nq, nm = len(qvectors), len(orient)
@@ -111,7 +116,8 @@ def run_case(L, self_, dsp, method, coords, atom_type, tables, background, qvect
     fq = np.zeros((nq, 2))
     fq2 = np.zeros((nq, 2))
     orient_arr = np.ascontiguousarray(orient if nm else np.zeros((1, 3)))
-    rows = L.ref_run_vectors(int(self_), dsp.encode(), method.encode(), nthreads,
+    fn = L.bind_run_vectors if binding else L.ref_run_vectors
+    rows = fn(int(self_), dsp.encode(), method.encode(), nthreads,
                              _p(np.ascontiguousarray(coords), _fp), nf, na,
                              _p(np.ascontiguousarray(atom_type, dtype=np.int32), _ip), len(sf_type),
                              _p(sf_type, _ip), _p(sf_const, _dp), _p(vol, _dp), _p(ex_type, _ip), _p(ex_const, _dp),
@@ -120,6 +126,26 @@ def run_case(L, self_, dsp, method, coords, atom_type, tables, background, qvect
     if rows != nq:
         raise RuntimeError("reference run failed (%d rows): %s" % (rows, L.ref_last_error().decode()))
     return q_out, fqt, fq, fq2
+
+
+def binding_calls(L, coords):
+    """What GpuVectorsScatterDevice passed to the C ABI in the last bind_run_vectors."""
+    ints = (ctypes.c_long * 8)()
+    sizes = (ctypes.c_size_t * 4)()
+    L.bind_last_sizes(ints, sizes)
+    offs = np.zeros(sizes[0], dtype=np.uintp)
+    sv = np.zeros(sizes[1])
+    cf = np.zeros(sizes[2])
+    classes = np.zeros(ints[4], dtype=np.int32)
+    frames = np.zeros(sizes[3], dtype=np.float32)
+    L.bind_last_calls(_p(offs, _sp), _p(sv, _dp), _p(cf, _dp), _p(classes, _ip), _p(frames, _fp))
+    if not np.array_equal(frames.reshape(coords.shape), coords):
+        raise RuntimeError("the binding staged other frames than the stager's")
+    if ints[7] != 1:
+        raise RuntimeError("the binding made %d sass_compute calls, expected one" % ints[7])
+    return dict(bind_desc=np.array(list(ints)[:7], dtype=np.int64), bind_offs=offs.astype(np.int64),
+                bind_subvectors=sv.reshape(-1, 3), bind_class_factors=cf.reshape(len(offs) - 1, ints[6]),
+                bind_classes=classes)
 
 
 def class_factors(L, tables, background, qlen):
@@ -156,7 +182,14 @@ def vector_cases(L):
         q_out, fqt, fq, fq2 = run_case(L, self_, dsp, method, coords, atom_type, tables, background, qvectors,
                                        orient, nthreads)
         qref = np.sqrt(qvectors[:, 0] ** 2 + qvectors[:, 1] ** 2 + qvectors[:, 2] ** 2)
-        cases[name] = dict(kind=np.array("%s/%s/%s" % ("self" if self_ else "all", dsp, method)),
+        # the binding device on the same case: the rows it writes (zero: its C ABI only
+        # records) must come in the reference's order, and its recorded calls are kept
+        bq_out, _, _, _ = run_case(L, self_, dsp, method, coords, atom_type, tables, background, qvectors,
+                                   orient, nthreads, binding=True)
+        if not np.array_equal(bq_out, q_out):
+            raise RuntimeError("binding rows out of order in " + name)
+        calls = binding_calls(L, coords)
+        cases[name] = dict(**calls,kind=np.array("%s/%s/%s" % ("self" if self_ else "all", dsp, method)),
                            coords=coords, atom_type=atom_type, sf_type=tables[0], sf_const=tables[1],
                            vol=tables[2], ex_type=tables[3], ex_const=tables[4], background=np.array(background),
                            qvectors=qvectors, orient=orient, q_out=q_out, fqt=fqt, fq=fq, fq2=fq2,

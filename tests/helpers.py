@@ -87,6 +87,13 @@ class ReferenceCase:
         self.qvectors, self.orient = g("qvectors"), g("orient")
         self.fqt, self.fq, self.fq2 = g("fqt"), g("fq"), g("fq2")
         self.q_out = g("q_out")
+        # what GpuVectorsScatterDevice (sassena_gb300/integration), driven by the reference's
+        # own run(), passed to the C ABI on the same case (make_reference_golden.py)
+        self.bind_desc = g("bind_desc")  # scattering, dsp type, method, precision, na, nf, nclass
+        self.bind_offs = g("bind_offs").astype(np.uintp)
+        self.bind_subvectors = g("bind_subvectors")
+        self.bind_class_factors = g("bind_class_factors")
+        self.bind_classes = g("bind_classes")
 
     @property
     def na(self):
