@@ -32,6 +32,7 @@ struct sass_mlp {
     int device = 0;
     cudaStream_t st = nullptr;
     DevBuf master, w16, grad, m, v, loss, X, T, Y, qlen, gbar, wsqrt, outs;
+    DevBuf scratch;  // per-CTA partial gradients and quadrature parts (fixed-order sums)
     double q_mid = 1.0, q_half = 1.0, y_mean = 0.0, y_std = 1.0;
     int step = 0;
     std::string msg;
@@ -163,10 +164,10 @@ int sass_mlp_gradient(sass_mlp* n, const float* x, const float* t, size_t count,
     CK(n->msg, n->T.ensure(count * 4));
     CK(n->msg, cudaMemcpy(n->X.p, x, count * 16, cudaMemcpyHostToDevice));
     CK(n->msg, cudaMemcpy(n->T.p, t, count * 4, cudaMemcpyHostToDevice));
-    CK(n->msg, cudaMemsetAsync(n->grad.p, 0, kMlpParams * 4, n->st));
-    CK(n->msg, cudaMemsetAsync(n->loss.p, 0, 8, n->st));
+    CK(n->msg, n->scratch.ensure(mlp_train_scratch_bytes(sm_count(n->device))));
     CK(n->msg, launch_mlp_train(n->w16.as<__nv_bfloat16>(), n->X.as<float>(), n->T.as<float>(), (int)count,
-                                n->grad.as<float>(), n->loss.as<double>(), sm_count(n->device), n->st));
+                                n->grad.as<float>(), n->loss.as<double>(), n->scratch.p, sm_count(n->device),
+                                n->st));
     CK(n->msg, cudaMemcpyAsync(grad, n->grad.p, kMlpParams * 4, cudaMemcpyDeviceToHost, n->st));
     double l = 0;
     CK(n->msg, cudaMemcpyAsync(&l, n->loss.p, 8, cudaMemcpyDeviceToHost, n->st));
@@ -185,13 +186,14 @@ int sass_mlp_train(sass_mlp* n, const float* x, const float* t, size_t count, in
     CK(n->msg, cudaMemcpy(n->X.p, x, count * 16, cudaMemcpyHostToDevice));
     CK(n->msg, cudaMemcpy(n->T.p, t, count * 4, cudaMemcpyHostToDevice));
     const size_t b = std::min<size_t>((size_t)batch, count);
+    CK(n->msg, n->scratch.ensure(mlp_train_scratch_bytes(sm_count(n->device))));
+    CK(n->msg, cudaMemsetAsync(n->loss.p, 0, 8, n->st));
     size_t off = 0;
     for (int k = 0; k < steps; ++k) {
         if (off + b > count) off = 0;
-        CK(n->msg, cudaMemsetAsync(n->grad.p, 0, kMlpParams * 4, n->st));
-        CK(n->msg, cudaMemsetAsync(n->loss.p, 0, 8, n->st));
         CK(n->msg, launch_mlp_train(n->w16.as<__nv_bfloat16>(), n->X.as<float>() + off * 4, n->T.as<float>() + off,
-                                    (int)b, n->grad.as<float>(), n->loss.as<double>(), sm_count(n->device), n->st));
+                                    (int)b, n->grad.as<float>(), n->loss.as<double>(), n->scratch.p,
+                                    sm_count(n->device), n->st));
         CK(n->msg, launch_mlp_adam(n->master.as<float>(), n->w16.as<__nv_bfloat16>(), n->grad.as<float>(),
                                    n->m.as<float>(), n->v.as<float>(), (float)lr, ++n->step, n->st));
         off += b;
@@ -221,9 +223,11 @@ int sass_mlp_sphere_mean(sass_mlp* n, const double* qlen, size_t nshell, size_t 
     CK(n->msg, n->qlen.ensure(nshell * 8));
     CK(n->msg, n->gbar.ensure(nshell * 8));
     CK(n->msg, cudaMemcpy(n->qlen.p, qlen, nshell * 8, cudaMemcpyHostToDevice));
+    CK(n->msg, n->scratch.ensure(std::max(mlp_sphere_scratch_bytes((int)nshell, (int)npoints, sm_count(n->device)),
+                                          mlp_train_scratch_bytes(sm_count(n->device)))));
     CK(n->msg, launch_mlp_sphere(n->w16.as<__nv_bfloat16>(), n->qlen.as<double>(), (int)nshell, (int)npoints,
                                  (float)n->q_mid, (float)n->q_half, (float)n->y_mean, (float)n->y_std,
-                                 n->gbar.as<double>(), sm_count(n->device), n->st));
+                                 n->gbar.as<double>(), n->scratch.as<double>(), sm_count(n->device), n->st));
     CK(n->msg, cudaMemcpyAsync(gbar, n->gbar.p, nshell * 8, cudaMemcpyDeviceToHost, n->st));
     CK(n->msg, cudaStreamSynchronize(n->st));
     return SASS_OK;

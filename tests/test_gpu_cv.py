@@ -21,10 +21,35 @@ def test_mlp_gradient_matches_oracle(native_lib):
     assert abs(loss - lref) <= 1e-5 * abs(lref)
     err = np.abs(g - gref).max() / np.abs(gref).max()
     assert err <= 2e-5, err
-    # and the forward pass
+    # and the forward pass. The 128 x 128 layer's operand h1 is rounded to BF16 on both
+    # sides, but from the GPU's FP32 tanh and the oracle's FP64 tanh: where those straddle a
+    # BF16 rounding boundary (a few of the 10^5 values here), h1 differs by one BF16 step
+    # (2^-8 relative) and that sample's y by up to about 1e-3. All others agree to 1e-5.
     y = net.predict(x)
     yref, _ = mo.forward(bf, x)
-    assert np.abs(y - yref).max() <= 1e-5 * max(1.0, np.abs(yref).max())
+    dev = np.abs(y - yref) / max(1.0, np.abs(yref).max())
+    assert np.mean(dev <= 1e-5) >= 0.99 and dev.max() <= 2e-3, (np.mean(dev <= 1e-5), dev.max())
+
+
+def test_mlp_training_is_reproducible(native_lib):
+    """The gradient and the loss are summed over the CTAs in a fixed order (no floating-point
+    atomics): two evaluations give the same bits, and two trainings from the same seed on
+    the same data end with the same weights; so does the sphere quadrature."""
+    rng = np.random.default_rng(7)
+    x = rng.normal(size=(5000, 4)).astype(np.float32)
+    t = rng.normal(size=5000).astype(np.float32)
+    net = abi.MLP(seed=5)
+    g1, l1 = net.gradient(x, t)
+    g2, l2 = net.gradient(x, t)
+    assert np.array_equal(g1, g2) and l1 == l2
+    weights = []
+    for _ in range(2):
+        n = abi.MLP(seed=5)
+        n.train(x, t, steps=50, batch=1024, lr=1e-3)
+        weights.append(n.params()[0])
+        q = np.array([0.3, 0.9])
+        weights.append(n.sphere_mean(q, 50000))
+    assert np.array_equal(weights[0], weights[2]) and np.array_equal(weights[1], weights[3])
 
 
 def test_mlp_training_fits_a_smooth_function(native_lib):
