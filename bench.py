@@ -404,12 +404,13 @@ def phase_roofline(w, sch, phase_ms, corr_ms, sfu, fma):
 
 
 def shell_errors(got, ref):
-    """Per shell: S(q,t) as max_t |S - S_ref| / |S_ref(q,0)|; I(q) as fq (the time-averaged
-    correlation), fq0 = S(q,0) and fq2, each relative to its reference value."""
+    """Per shell: S(q,t) as max_t |S - S_ref| / max_t |S_ref(q,t)| (the shell's scale: S_ref(q,0)
+    for an autocorrelation, the largest frame intensity for dsp square); I(q) as fq (the
+    time-averaged correlation), fq0 = S(q,0) and fq2, each relative to its reference value."""
     (f, a, a2), (rf, ra, ra2) = got, ref
-    den = np.abs(rf[:, 0])
+    den = np.abs(rf).max(axis=1)
     return {"sqt": np.abs(f - rf).max(axis=1) / den, "fq": np.abs(a - ra) / np.abs(ra),
-            "fq0": np.abs(f[:, 0] - rf[:, 0]) / den, "fq2": np.abs(a2 - ra2) / np.abs(ra2)}
+            "fq0": np.abs(f[:, 0] - rf[:, 0]) / np.abs(rf[:, 0]), "fq2": np.abs(a2 - ra2) / np.abs(ra2)}
 
 
 def _cplx(a):
@@ -469,8 +470,10 @@ def plain_fp64_audit(args, w, plan, ms, dev):
         ref = p64.compute(*subset(idx, w.directions))
         t64 = p64.timing()
         sch64 = p64.schedule()
-        # the oracle sample: D seeded directions per shell, all atoms and frames
-        d = max(1, min(w.nm, int(args.oracle_terms // (w.nq * w.na * w.nf))))
+        # the oracle sample: D seeded directions per shell (at least 8, so that each shell's
+        # value is an orientational average and not one direction's intensity, which can sit
+        # in a deep minimum), all atoms and frames, on every step_q-th shell within the budget
+        d = min(w.nm, max(8, int(args.oracle_terms // (w.nq * w.na * w.nf))))
         step_q = max(1, int(np.ceil(w.nq * w.na * w.nf * d / args.oracle_terms)))
         oidx = np.arange(0, w.nq, step_q)
         rng = np.random.default_rng(2026)
@@ -495,7 +498,7 @@ def plain_fp64_audit(args, w, plan, ms, dev):
            "whole_workload": bool(len(idx) == w.nq),
            ("ms_full_workload" if len(idx) == w.nq else "ms_full_workload_extrapolated"): full_ms,
            "speedup_same_gpu": full_ms / ms,
-           "roofline": fp64_roofline(w, t64, run_terms, dev), "schedule": sch64,
+           "schedule": sch64,
            "fp32_max_rel_err_vs_fp64": float(e32["sqt"].max()),
            "fp32_rel_err_per_shell": {"q": lst(w.shells[idx]), "sqt": lst(e32["sqt"]),
                                       "sqt_median": float(np.median(e32["sqt"])), "iq_fq": lst(e32["fq"]),
@@ -509,6 +512,10 @@ def plain_fp64_audit(args, w, plan, ms, dev):
                          "fp32_fq2_max": float(eo32["fq2"].max()),
                          "fp64_sqt_max": float(eo64["sqt"].max()), "fp64_fq_max": float(eo64["fq"].max()),
                          "fp64_fq2_max": float(eo64["fq2"].max())}}
+    # the FP64 phase-sum kernel's roofline, where it ran (self scattering has no phase sum:
+    # its FP64 series go straight into the correlation)
+    if sch64.get("direct_tiles", 0) > 0:
+        res["roofline"] = fp64_roofline(w, t64, run_terms, dev)
     return res
 
 

@@ -351,10 +351,12 @@ int sass_probe_fp64(int device, double* fp64_fma_per_s);
  *   sub_offsets device uint64 [nq+1], sub-vectors of q i are [sub_offsets[i], sub_offsets[i+1])
  *   fqt, fq, fq2 device outputs as in sass_compute (dsp = autocorrelate, method fftw/direct)
  * Working memory is one fixed 8.2 MiB device array inside the library; nothing is
- * allocated. Limits: nq <= 128, nf <= 4096 (else SASS_ERR_UNSUPPORTED). Calls share
- * the array: calls that overlap on the GPU race, so issue them in order on one
- * stream. The first call on a device looks up the array's address; make it before
- * any stream capture. Asynchronous on `stream` (a cudaStream_t, NULL = default). */
+ * allocated. Limits: nq <= 128, nf <= 4096 (else SASS_ERR_UNSUPPORTED); sub_offsets
+ * must increase and stay below 2^31 (they are read on the device: a q whose range
+ * breaks this is treated as empty and its rows come back NaN). Calls share the
+ * array: calls that overlap on the GPU race, so issue them in order on one stream.
+ * A device reset loses the array's contents and is not supported between calls.
+ * Asynchronous on `stream` (a cudaStream_t, NULL = default). */
 int sass_correlate_noalloc(int device, void* stream, const double* amplitudes, size_t nf,
                            size_t nq, const uint64_t* sub_offsets, int dsp_method,
                            double* fqt, double* fq, double* fq2);
