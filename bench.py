@@ -960,6 +960,11 @@ def run_cv(args, dist):
     t0 = time.perf_counter()
     net, loss = cv.fit(x, t, sc, steps=args.cv_steps, batch=4096, lr=2e-3, seed=3, device=dev)
     train_s = time.perf_counter() - t0
+    # accuracy of the sphere quadrature the estimator subtracts (32,768 spherical-Fibonacci
+    # points, the default of sass_compute_cv) against a 16 times denser set
+    g_quad = net.sphere_mean(w.shells, 32768)
+    g_dense = net.sphere_mean(w.shells, 16 * 32768)
+    quad_dev = float(np.max(np.abs(g_quad / g_dense - 1.0)))
     run_mc(synth.sphere_directions(64, 1))  # warm-up of the plain path
     rows = []
     for m in budgets:
@@ -979,7 +984,11 @@ def run_cv(args, dist):
         se_mc = est_mc.std(axis=0, ddof=1).max(axis=1) / scale
         # paired difference at t = 0: unbiasedness of the control variate
         d0 = (est_cv[:, :, 0] - est_mc[:, :, 0]).real
-        z = np.abs(d0.mean(axis=0)) / np.maximum(d0.std(axis=0, ddof=1) / np.sqrt(args.draws), 1e-300)
+        d0_se = d0.std(axis=0, ddof=1) / np.sqrt(args.draws)
+        z = np.abs(d0.mean(axis=0)) / np.maximum(d0_se, 1e-300)
+        # the mean paired difference relative to S(q,0), with its standard error: a bound on
+        # any bias of the control variate (its quadrature mean G) at the scale of the target
+        bias = np.abs(d0.mean(axis=0)) / scale
         rows.append({"M": m, "draws": args.draws, "terms": w.na * w.nq * m * w.nf,
                      "ms_mc": ms_mc, "ms_cv": float(np.median(ms_cv)),
                      "se_mc_max": float(se_mc.max()), "se_mc_median": float(np.median(se_mc)),
@@ -987,6 +996,8 @@ def run_cv(args, dist):
                      "variance_ratio_median": float(np.median((se_mc / se_cv) ** 2)),
                      "variance_ratio_per_shell": [float(v) for v in (se_mc / se_cv) ** 2],
                      "unbiased_z_max": float(z.max()), "unbiased_z_over_3": int((z > 3).sum()),
+                     "paired_diff_rel_max": float(bias.max()),
+                     "paired_diff_rel_se_median": float(np.median(d0_se / scale)),
                      "m_star_mc": float(m * (se_mc.max() / 1e-3) ** 2),
                      "m_star_cv": float(m * (se_cv.max() / 1e-3) ** 2)})
     # plain FP64 path: time per term on two shells x 64 directions
@@ -1018,7 +1029,8 @@ def run_cv(args, dist):
                       "value_note": "value: FP32 plain path terms/s end to end (host in/out) at M=%d"
                                     % last["M"]},
            "control_variate": {"samples": args.cv_samples, "sample_s": samp_s, "train_s": train_s,
-                               "steps": args.cv_steps, "final_loss": loss},
+                               "steps": args.cv_steps, "final_loss": loss,
+                               "quadrature_rel_dev_vs_16x_denser": quad_dev},
            "budgets": rows,
            "time_to_1e-3": {"from_M": last["M"],
                             "fp32_cv": {"ms": t_cv, "M": last["m_star_cv"]},

@@ -102,13 +102,17 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 20 ? 2 : 1) phase_rec_ker
     unsigned used = 0;
     bool failed = false;
     const double inv2pi = 0.15915494309189533577;
+    // Thread 0 takes the next tile from the queue when the current one starts and publishes
+    // it at the next loop head, so the atomic's round trip overlaps the tile's work.
+    int next_tile = 0;
+    if (threadIdx.x == 0) next_tile = (int)atomicAdd(a.counter, 1u);
 
     for (;;) {
-        __syncthreads();
-        if (threadIdx.x == 0) *s_tile = (int)atomicAdd(a.counter, 1u);
-        __syncthreads();
+        if (threadIdx.x == 0) *s_tile = next_tile;
+        __syncthreads();  // also: the previous tile's results are read out of the Kahan state
         const int ti_ = *s_tile;
         if (ti_ >= a.ntiles) break;
+        if (threadIdx.x == 0) next_tile = (int)atomicAdd(a.counter, 1u);
         const RecTileDesc td = a.tiles[ti_];
         const RecSystem& sys = a.systems[td.system];
         const int nf = sys.nf;
@@ -167,7 +171,9 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 20 ? 2 : 1) phase_rec_ker
                         __sincosf(x.x, &s0, &c0);
                         __sincosf(x.y, &s1, &c1);
                         const float2 w0 = make_float2(c0, s0);
-                        // w1 = z1 = z0 exp(i theta)
+                        // w1 = z1 = z0 exp(i theta) by a complex product on the FMA pipe: a third
+                        // SFU pair for z1 instead (one more SFU result per atom) made the kernel
+                        // 5.5 % slower on the GB300, whose SFU pipe then limits
                         const float2 w1 = __ffma2_rn(make_float2(-s0, c0), make_float2(s1, s1),
                                                      __fmul2_rn(w0, make_float2(c1, c1)));
                         const float2 c2 = __fmul2_rn(make_float2(c1, c1), kTwo);  // (2c, -2c)
@@ -211,26 +217,30 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 20 ? 2 : 1) phase_rec_ker
             }
             used += nst;
         }
-        // Results from the Kahan state of all warps: 8 consecutive threads write one
-        // (shell, direction) row's frames [f0, f0 + 8) as one contiguous segment. Every
-        // (split, shell, direction, frame) slot is written, also for empty atom ranges.
+        // Results from the Kahan state of all warps: thread (l, w) = (tid / 8, tid % 8) writes
+        // frame f0 + w of lane l's (group, direction) pair for every shell of the group, so 8
+        // consecutive threads write one (shell, direction) row's frames [f0, f0 + 8) as one
+        // contiguous segment. Every (split, shell, direction, frame) slot is written, also for
+        // empty atom ranges.
         __syncthreads();
         {
-            const int nfr = min(kRecWarps, nf - td.f0);
-            const float4* ks_all = reinterpret_cast<const float4*>(smem + L::kKahanOffset);
-            for (int i = threadIdx.x; i < K * 32 * kRecWarps; i += kRecWarps * 32) {
-                const int w = i % kRecWarps, row = i / kRecWarps;
-                const int l = row & 31, k = row >> 5;
-                if (w >= nfr || l >= td.np) continue;
+            static_assert(kRecWarps == 8, "8 frames per tile: one per warp, 8 threads per output row");
+            const int w = threadIdx.x % kRecWarps, l = threadIdx.x / kRecWarps;
+            if (td.f0 + w < nf && l < td.np) {
                 const int pl = td.p0 + l;
                 const int gw = pl / sys.nd, dw = pl - gw * sys.nd;
                 const RecGroup gr = a.groups[sys.g_begin + gw];
-                if (k >= gr.ks) continue;
-                const float4 st = ks_all[(w * K + k) * 32 + l];
-                const size_t v = (size_t)(gr.s0 + k) * sys.nd + dw;
-                const size_t o = v * nf + td.f0 + w;
-                const double re = (double)st.x - (double)st.z, im = (double)st.y - (double)st.w;
-                sys.out_f32[(size_t)td.split * sys.split_stride + o] = make_float2((float)re, (float)im);
+                const size_t row_stride = (size_t)sys.nd * nf;
+                float2* dst = sys.out_f32 + (size_t)td.split * sys.split_stride +
+                              ((size_t)gr.s0 * sys.nd + dw) * nf + td.f0 + w;
+                const float4* ks_all = reinterpret_cast<const float4*>(smem + L::kKahanOffset) + w * K * 32 + l;
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    if (k >= gr.ks) break;
+                    const float4 st = ks_all[k * 32];
+                    const double re = (double)st.x - (double)st.z, im = (double)st.y - (double)st.w;
+                    dst[k * row_stride] = make_float2((float)re, (float)im);
+                }
             }
         }
     }
