@@ -105,11 +105,12 @@ const char* sass_status_name(int status);
 /* Stage the trajectory: frame-major float32 [nf][na][3] (the reference's coor_t
  * buffer; replaces DataStagerByFrame::stage, src/stager/data_stager.cpp:72-118).
  * coords_on_device != 0 means `coords` is a device pointer. Host memory is read in
- * place where the device can address it (pinned or registered memory, or any host
- * memory where the GPU reads pageable memory through the host's page tables), else
- * copied first. The call returns after staging: the caller may then free or reuse the
- * buffer. Device memory is reserved before the buffer is read, so SASS_ERR_OOM leaves
- * it unread. */
+ * place where the device can address it: pinned or registered memory through its device
+ * mapping; pageable memory, where the GPU can read it through the host's page tables,
+ * page-locked (cudaHostRegister) for the duration of the call and read the same way
+ * (read in place unlocked if locking fails); otherwise it is copied first. The call
+ * returns after staging: the caller may then free or reuse the buffer. Device memory is
+ * reserved before the buffer is read, so SASS_ERR_OOM leaves it unread. */
 int sass_stage_frames(sass_plan* plan, const float* coords, int coords_on_device);
 
 /* ---- Staging pre-pass: alignments and motions ------------------------------------

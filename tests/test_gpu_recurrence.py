@@ -258,3 +258,37 @@ def test_restaging_refreshes_the_class_sorted_copy(native_lib):
         p.stage(w1.coords)
         p.set_classes(w1.atom_class)
         assert_close(p.compute(*args), reference(w1))
+
+
+def test_staging_of_pageable_memory_locked_elsewhere(native_lib):
+    # Pageable host memory is page-locked for the staging call and read through its device
+    # mapping. Where part of the buffer is already locked by someone else, locking fails and
+    # the device reads the pages in place: the same bits either way, and the caller's own
+    # registration is left as it was.
+    import torch
+
+    import os
+
+    w = synth.small("all", "autocorrelate", seed=49, na=300, nf=400, nq=6, nm=24)
+    args = (w.sub_offsets(), w.subvectors(), w.class_factors)
+    cr = torch.cuda.cudart()
+    with abi.Plan(w.na, w.nf, len(w.class_names), precision="fp32") as p:
+        p.set_classes(w.atom_class)
+        p.stage(w.coords)
+        first = p.compute(*args)
+        assert_close(first, reference(w))
+        p.stage(w.coords)  # the same buffer again
+        for a, b in zip(p.compute(*args), first):
+            np.testing.assert_array_equal(a, b)
+        # whole pages inside the buffer's middle half (1.4 MB of coordinates)
+        page = os.sysconf("SC_PAGE_SIZE")
+        lo = -(-(w.coords.ctypes.data + w.coords.nbytes // 4) // page) * page
+        hi = (w.coords.ctypes.data + 3 * w.coords.nbytes // 4) // page * page
+        assert hi > lo
+        assert int(cr.cudaHostRegister(lo, hi - lo, 0)) == 0
+        try:
+            p.stage(w.coords)
+            for a, b in zip(p.compute(*args), first):
+                np.testing.assert_array_equal(a, b)
+        finally:
+            assert int(cr.cudaHostUnregister(lo)) == 0
