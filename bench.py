@@ -369,7 +369,9 @@ def phase_roofline(w, sch, phase_ms, corr_ms, sfu, fma):
         L = 1 << max(2, int(np.ceil(np.log2(2 * w.nf))))
         flops_per_term = 5.0 * L * np.log2(L) / w.nf
         peak = min(2.0 * fma / flops_per_term, sfu / 2.0)
-        kernel = "reg_fft_kernel" if L <= 512 else ("self_blk_fft_kernel" if L <= 4096 else "self_fft_kernel")
+        # FP32 form: the transposed register FFT at L = 64 .. 256, the lane-strided one to 512
+        kernel = ("reg2_fft_kernel" if 64 <= L <= 256 else "reg_fft_kernel") if L <= 512 else \
+            ("self_blk_fft_kernel" if L <= 4096 else "self_fft_kernel")
         achieved = terms / (corr_ms * 1e-3)
         return {"bound": "fp32" if 2.0 * fma / flops_per_term < sfu / 2.0 else "sfu",
                 "achieved": achieved, "peak": peak, "unit": "terms/s", "frac": achieved / peak,
@@ -611,7 +613,7 @@ def run_ours(args, dist):
         else:
             corr_kernel = "self_direct_kernel"
     elif lg <= 9:
-        corr_kernel = "reg_fft_kernel"
+        corr_kernel = "reg2_fft_kernel" if args.precision == "fp32" and 6 <= lg <= 8 else "reg_fft_kernel"
     elif lg <= 12 and w.scattering == "all":
         corr_kernel = "blk_fft_kernel"
     else:
