@@ -113,6 +113,17 @@ const char* sass_status_name(int status);
  * reserved before the buffer is read, so SASS_ERR_OOM leaves it unread. */
 int sass_stage_frames(sass_plan* plan, const float* coords, int coords_on_device);
 
+/* Request that the host frames of a later sass_stage_frames call be copied ahead: the
+ * plan's next sass_compute queues the copy on a copy stream of the plan, behind its own
+ * input copies, so that the transfer overlaps its kernels. The next sass_stage_frames of
+ * the same pointer then waits for the copy and converts from device memory; the buffer
+ * must not change until then. Staging another buffer, or another request, discards it; a
+ * request with no compute before the staging is staged as usual. Pageable buffers are
+ * page-locked from the request to that staging where the GPU reads pageable memory
+ * through the host's page tables. No reference counterpart: DataStagerByFrame::stage
+ * (data_stager.cpp:72-118) reads the frames serially before the device runs. */
+int sass_prefetch_frames(sass_plan* plan, const float* coords);
+
 /* ---- Staging pre-pass: alignments and motions ------------------------------------
  * Replaces the per-frame work of CoordinateSets::load (src/sample/coordinate_sets.cpp:
  * 244-368): pre-alignments, motions and post-alignments applied in FP64 to the whole

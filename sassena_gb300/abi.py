@@ -26,7 +26,7 @@ PRECISION = {"fp64": 0, "fp32": 1}
 # Every symbol the header declares (checked by the CPU tests).
 EXPORTS = [
     "sass_plan_create", "sass_plan_destroy", "sass_plan_error", "sass_status_name",
-    "sass_stage_frames", "sass_set_atom_classes", "sass_compute", "sass_amplitudes",
+    "sass_stage_frames", "sass_prefetch_frames", "sass_set_atom_classes", "sass_compute", "sass_amplitudes",
     "sass_last_timing", "sass_set_phase_tile", "sass_frame_center", "sass_host_alloc",
     "sass_host_free", "sass_probe_pipes", "sass_probe_fp64", "sass_correlate_noalloc", "sass_version",
     "sass_autotune", "sass_batch_create", "sass_batch_autotune", "sass_batch_run",
@@ -119,6 +119,7 @@ def load(path=LIB_PATH):
     L.sass_status_name.argtypes = [ctypes.c_int]
     L.sass_status_name.restype = ctypes.c_char_p
     L.sass_stage_frames.argtypes = [_vp, _vp, ctypes.c_int]
+    L.sass_prefetch_frames.argtypes = [_vp, _vp]
     L.sass_stage_frames_prepass.argtypes = [_vp, _vp, ctypes.c_size_t, _vp, ctypes.POINTER(PrepassStep),
                                             ctypes.c_size_t, _vp, _vp]
     L.sass_set_atom_classes.argtypes = [_vp, _vp, ctypes.c_int]
@@ -233,6 +234,16 @@ class Plan:
         if c.shape != (self.nf, self.na, 3):
             raise ValueError("coords must be [nf, na, 3]")
         self._check(self.lib.sass_stage_frames(self._h, _ptr(c), 0))
+
+    def prefetch(self, coords):
+        """Have the next compute() copy these host frames ahead for the next stage() of the same
+        array (sass_prefetch_frames). The array is kept alive here and must not change until
+        that stage()."""
+        c = np.ascontiguousarray(coords, dtype=np.float32)
+        if c.shape != (self.nf, self.na, 3):
+            raise ValueError("coords must be [nf, na, 3]")
+        self._prefetched = c
+        self._check(self.lib.sass_prefetch_frames(self._h, _ptr(c)))
 
     def stage_prepass(self, frames, masses, steps, target, return_staged=True):
         """Alignments / motions on the whole system, then staging of the target atoms.

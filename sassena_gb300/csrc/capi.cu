@@ -337,6 +337,9 @@ int sass_plan_create(const sass_plan_desc* desc, sass_plan** out) {
 void sass_plan_destroy(sass_plan* p) {
     if (!p) return;
     cudaSetDevice(p->d.device);
+    drop_prefetch(p->sys);
+    if (p->side) cudaStreamDestroy(p->side);
+    if (p->pf_done) cudaEventDestroy(p->pf_done);
     if (p->st) cudaStreamSynchronize(p->st);
     for (int i = 0; i < kEvents; ++i)
         if (p->ev[i]) cudaEventDestroy(p->ev[i]);
@@ -349,6 +352,18 @@ int sass_stage_frames(sass_plan* p, const float* coords, int on_device) {
     if (!p) return SASS_ERR_ARG;
     CK(p->msg, cudaSetDevice(p->d.device));
     int rc = stage_system(p->sys, coords, on_device != 0, p->d.precision, p->st, p->msg);
+    if (!rc) p->msg.clear();
+    return rc;
+}
+
+int sass_prefetch_frames(sass_plan* p, const float* coords) {
+    if (!p) return SASS_ERR_ARG;
+    CK(p->msg, cudaSetDevice(p->d.device));
+    if (!p->side) {
+        CK(p->msg, cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking));
+        CK(p->msg, cudaEventCreateWithFlags(&p->pf_done, cudaEventDisableTiming));
+    }
+    int rc = prefetch_system(p->sys, coords, p->msg);
     if (!rc) p->msg.clear();
     return rc;
 }
@@ -512,6 +527,12 @@ int sass_compute(sass_plan* p, size_t nq, const size_t* offs, const double* subv
         if (rc) return rc;
         rc = p->eng.enqueue(p->st, p->msg, p->ev);
         if (rc) return rc;
+        // a requested frame prefetch goes to the copy engine now, behind this call's own
+        // input copies, and overlaps the kernels just queued
+        if (p->side) {
+            rc = issue_prefetch(p->sys, p->side, p->pf_done, p->msg);
+            if (rc) return rc;
+        }
         CK(p->msg, cudaEventSynchronize(p->ev[3]));
         p->timing.phase_ms += ev_ms(p->ev[0], p->ev[1]);
         p->timing.corr_ms += ev_ms(p->ev[1], p->ev[2]);

@@ -132,14 +132,17 @@ static const float* device_view(const float* h, int device, bool& pageable) {
     return pageable ? h : nullptr;
 }
 
-// Page-locks a caller's pageable buffer for the duration of one staging call and unlocks
-// it (after the stream has drained) when it goes out of scope.
+// Unlocks a caller's buffer that this library page-locked, once the work that reads it is
+// done (the stream has drained and, for a prefetch copy, its completion event has fired),
+// when it goes out of scope.
 struct ScopedHostRegistration {
     void* p = nullptr;
     cudaStream_t st = nullptr;
+    cudaEvent_t done = nullptr;
     ~ScopedHostRegistration() {
         if (!p) return;
         (void)cudaStreamSynchronize(st);
+        if (done) (void)cudaEventSynchronize(done);
         if (cudaHostUnregister(p) != cudaSuccess) (void)cudaGetLastError();
     }
 };
@@ -155,8 +158,27 @@ int stage_system(SystemState& s, const float* coords, bool on_device, int precis
     ECK(s.xyz.ensure(s.nf * s.na_pad * sizeof(float4)));
     const float* src = coords;
     std::vector<float> f0(s.na * 3);
+    // A prefetch request: an issued copy may still be writing `raw`, so the stream waits for
+    // it, and a copy of this very buffer is the source. A buffer locked for the request is
+    // unlocked once the stream has drained (the guards run at return, after the final
+    // synchronize). A request never issued is dropped and the frames are staged as usual.
+    const bool from_prefetch = s.prefetch_done && !on_device && s.prefetch_src == coords;
+    ScopedHostRegistration prefetch_pin;
+    if (s.prefetch_src) {
+        prefetch_pin.p = s.prefetch_locked;
+        prefetch_pin.st = st;
+        prefetch_pin.done = s.prefetch_done;
+        const cudaEvent_t done = s.prefetch_done;
+        s.prefetch_src = nullptr;
+        s.prefetch_done = nullptr;
+        s.prefetch_locked = nullptr;
+        if (done) ECK(cudaStreamWaitEvent(st, done, 0));
+    }
     ScopedHostRegistration pin;
-    if (!on_device) {
+    if (from_prefetch) {
+        src = s.raw.as<float>();
+        memcpy(f0.data(), coords, f0.size() * sizeof(float));
+    } else if (!on_device) {
         int device = 0;
         ECK(cudaGetDevice(&device));
         bool pageable = false;
@@ -217,6 +239,55 @@ int stage_system(SystemState& s, const float* coords, bool on_device, int precis
     s.rec_valid = rec;
     s.mp_valid = false;
     return kOk;
+}
+
+int prefetch_system(SystemState& s, const float* coords, std::string& err) {
+    if (!coords) {
+        err = "coords is NULL";
+        return kErrArg;
+    }
+    drop_prefetch(s);  // one copy ahead at a time
+    const size_t bytes = s.nf * s.na * 3 * sizeof(float);
+    ECK(s.raw.ensure(bytes));
+    int device = 0;
+    ECK(cudaGetDevice(&device));
+    bool pageable = false;
+    (void)device_view(coords, device, pageable);
+    // pageable memory the device can map is locked until the staging that uses the copy, so
+    // that the copy engine reads it asynchronously (as the staging itself would lock it)
+    if (pageable) {
+        if (cudaHostRegister(const_cast<float*>(coords), bytes, cudaHostRegisterDefault) == cudaSuccess)
+            s.prefetch_locked = const_cast<float*>(coords);
+        else
+            (void)cudaGetLastError();
+    }
+    s.prefetch_src = coords;
+    return kOk;
+}
+
+int issue_prefetch(SystemState& s, cudaStream_t side, cudaEvent_t done, std::string& err) {
+    if (!s.prefetch_src || s.prefetch_done) return kOk;  // nothing requested, or already issued
+    // `raw` is free: every staging that reads it synchronises before it returns
+    const size_t bytes = s.nf * s.na * 3 * sizeof(float);
+    cudaError_t e = cudaMemcpyAsync(s.raw.p, s.prefetch_src, bytes, cudaMemcpyDefault, side);
+    if (e == cudaSuccess) e = cudaEventRecord(done, side);
+    if (e != cudaSuccess) {
+        (void)cudaStreamSynchronize(side);
+        if (s.prefetch_locked && cudaHostUnregister(s.prefetch_locked) != cudaSuccess) (void)cudaGetLastError();
+        s.prefetch_src = nullptr;
+        s.prefetch_locked = nullptr;
+        return fail_cuda(e, "prefetch copy", err);
+    }
+    s.prefetch_done = done;
+    return kOk;
+}
+
+void drop_prefetch(SystemState& s) {
+    if (s.prefetch_done && cudaEventSynchronize(s.prefetch_done) != cudaSuccess) (void)cudaGetLastError();
+    if (s.prefetch_locked && cudaHostUnregister(s.prefetch_locked) != cudaSuccess) (void)cudaGetLastError();
+    s.prefetch_src = nullptr;
+    s.prefetch_done = nullptr;
+    s.prefetch_locked = nullptr;
 }
 
 int set_system_classes(SystemState& s, const int32_t* cls, bool on_device, cudaStream_t st, std::string& err) {

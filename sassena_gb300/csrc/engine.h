@@ -47,6 +47,12 @@ struct SystemState {
     double center[3] = {0, 0, 0};
     DevBuf raw, xyz, cls, tw64, tw32, k64, k32;
     bool staged = false, classes_set = false;
+    // frames to copy ahead into `raw` (prefetch_system, issue_prefetch): the host buffer, the
+    // event that completes the copy once issued (null: not issued yet), and the buffer this
+    // library page-locked for it (null: none)
+    const float* prefetch_src = nullptr;
+    cudaEvent_t prefetch_done = nullptr;
+    void* prefetch_locked = nullptr;
     // class-sorted copy for the shell-recurrence kernel (built on first use)
     std::vector<int32_t> h_cls;   // [na] classes (host copy)
     DevBuf xyz_rec, block_class;  // [nf][na_rec] float4 with w; [na_rec / 32] int
@@ -111,6 +117,16 @@ int build_system_tables(SystemState& s, cudaStream_t st, std::string& err);
 int stage_system(SystemState& s, const float* coords, bool on_device, int precision, cudaStream_t st,
                  std::string& err);
 int set_system_classes(SystemState& s, const int32_t* cls, bool on_device, cudaStream_t st, std::string& err);
+// Request the copy of host frames `coords` into `s.raw` for the next stage_system of the same
+// buffer (page-locking pageable memory the device can map). issue_prefetch queues the copy
+// on stream `side`, with completion event `done`: the plan calls it once its next compute
+// has queued its own input copies, so that the copy engine takes those first and the frame
+// copy overlaps the kernels. stage_system of that buffer then waits for `done` and converts
+// from `raw`; a request never issued is staged as usual.
+int prefetch_system(SystemState& s, const float* coords, std::string& err);
+int issue_prefetch(SystemState& s, cudaStream_t side, cudaEvent_t done, std::string& err);
+// Wait for an issued prefetch copy (if any) on the host and release what the request holds.
+void drop_prefetch(SystemState& s);
 
 // Whether shells [0, nq) of host sub-vectors qv (offsets offs) are multiples of one base
 // set: equal counts per shell and qv[offs[s] + d] = lam[s] * qv[offs[base] + d] within

@@ -16,6 +16,9 @@ struct sass_plan {
     sassgpu::Engine eng;
     cudaStream_t st = nullptr;
     bool own_stream = false;
+    // sass_prefetch_frames: the copy stream and the copy's completion event (created lazily)
+    cudaStream_t side = nullptr;
+    cudaEvent_t pf_done = nullptr;
     std::string msg;
     sass_timing timing{};
     cudaEvent_t ev[sassgpu::kEvents] = {};

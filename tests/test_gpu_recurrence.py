@@ -292,3 +292,53 @@ def test_staging_of_pageable_memory_locked_elsewhere(native_lib):
                 np.testing.assert_array_equal(a, b)
         finally:
             assert int(cr.cudaHostUnregister(lo)) == 0
+
+
+def test_prefetched_frames_stage_the_same_bits(native_lib):
+    # sass_prefetch_frames has the next compute copy a buffer ahead on the plan's copy stream
+    # while its kernels run; the next staging of that buffer converts from the copy. Pageable
+    # and pinned buffers, a copy discarded by staging another buffer, and a request replaced
+    # by a second one (staged with no compute in between) all give the bits of a plain
+    # staging.
+    w1 = synth.small("all", "autocorrelate", seed=51, na=300, nf=40, nq=6, nm=24)
+    w2 = dataclasses.replace(synth.small("all", "autocorrelate", seed=52, na=300, nf=40, nq=6, nm=24),
+                             atom_class=w1.atom_class)
+    args = (w1.sub_offsets(), w1.subvectors(), w1.class_factors)
+    lib = abi.load()
+    with abi.Plan(w1.na, w1.nf, len(w1.class_names), precision="fp32") as p:
+        p.set_classes(w1.atom_class)
+        p.stage(w1.coords)
+        plain1 = p.compute(*args)
+        assert_close(plain1, reference(w1))
+        p.stage(w2.coords)
+        plain2 = p.compute(*args)
+
+        def same(got, want):
+            for a, b in zip(got, want):
+                np.testing.assert_array_equal(a, b)
+
+        p.prefetch(w1.coords)  # pageable numpy memory
+        p.compute(*args)  # work the copy overlaps (frames of w2)
+        p.stage(w1.coords)
+        same(p.compute(*args), plain1)
+        p.prefetch(w2.coords)  # copied during the compute, then discarded: another buffer is staged
+        p.compute(*args)
+        p.stage(w1.coords)
+        same(p.compute(*args), plain1)
+        p.prefetch(w1.coords)  # replaced by the second prefetch
+        p.prefetch(w2.coords)
+        p.stage(w2.coords)
+        same(p.compute(*args), plain2)
+        hp = lib.sass_host_alloc(w1.coords.nbytes)
+        try:
+            pinned = np.ctypeslib.as_array((np.ctypeslib.ctypes.c_float * w1.coords.size)
+                                           .from_address(hp)).reshape(w1.coords.shape)
+            pinned[...] = w1.coords
+            p.prefetch(pinned)
+            p.compute(*args)
+            p.stage(pinned)
+            same(p.compute(*args), plain1)
+            p.prefetch(pinned)  # pending when the plan is destroyed
+        finally:
+            p.close()
+            lib.sass_host_free(hp)
