@@ -1285,8 +1285,10 @@ __global__ void __launch_bounds__(kReg2Warps * 32, 3) reg2_fft_kernel(CorrLaunch
     };
 
     // the warp's G series: get(n, m) is point n (< NF) of this lane's pass-1 series times
-    // m (0 for the zero padding), valid(g) whether series g exists this round
-    auto transform = [&](auto get, auto valid) {
+    // m (0 for the zero padding), valid(g) whether series g exists this round, w2 this
+    // lane's pass-1 series' power weight (the incoherent series are generated with unit
+    // length and weighted by b^2 in the power sums: |b X|^2 = b^2 |X|^2)
+    auto transform = [&](auto get, auto valid, float w2) {
         float2 x[16];
 #pragma unroll
         for (int b = 0; b < 8; ++b) {  // points beyond NF read the last point, scaled by 0
@@ -1315,6 +1317,10 @@ __global__ void __launch_bounds__(kReg2Warps * 32, 3) reg2_fft_kernel(CorrLaunch
             }
         }
         dif_rows<C, RPL>(x);
+        // power weights of the pass-2 series half + 2 j, from a pass-1 lane of each
+        float wj[RPL];
+#pragma unroll
+        for (int j = 0; j < RPL; ++j) wj[j] = __shfl_sync(0xffffffffu, w2, (half + 2 * j) * C);
         // power of the lane's bins k = k_b + 16 br_C(q) and each series' sum_k P K
         float sx[RPL], sy[RPL];
 #pragma unroll
@@ -1326,15 +1332,15 @@ __global__ void __launch_bounds__(kReg2Warps * 32, 3) reg2_fft_kernel(CorrLaunch
             for (int j = 0; j < RPL; ++j) {
                 const float2 v0 = x[j * C + q], v1 = x[j * C + q + 1];
                 const float P0 = fmaf(v0.x, v0.x, v0.y * v0.y), P1 = fmaf(v1.x, v1.x, v1.y * v1.y);
-                pacc[q] += P0;
-                pacc[q + 1] += P1;
+                pacc[q] = fmaf(P0, wj[j], pacc[q]);
+                pacc[q + 1] = fmaf(P1, wj[j], pacc[q + 1]);
                 sx[j] = fmaf(P1, kv.z, fmaf(P0, kv.x, sx[j]));
                 sy[j] = fmaf(P1, kv.w, fmaf(P0, kv.y, sy[j]));
             }
         }
 #pragma unroll
         for (int j = 0; j < RPL; ++j) {
-            float tx = sx[j], ty = sy[j];
+            float tx = sx[j] * wj[j], ty = sy[j] * wj[j];
 #pragma unroll
             for (int o = 8; o >= 1; o >>= 1) {  // within the half warp: the series' total
                 tx += __shfl_xor_sync(0xffffffffu, tx, o);
@@ -1383,8 +1389,12 @@ __global__ void __launch_bounds__(kReg2Warps * 32, 3) reg2_fft_kernel(CorrLaunch
                 load_qv(sys.qv, sys.qrev, (size_t)(v0 + d), qx, qy, qz);
                 const float b = ok ? bsm[at] : 0.f;
                 const float4* ra = rj + (size_t)at * nf;
-                transform([&](int n, float m) { return self_term(b * m, ra[n], qx, qy, qz); },
-                          [&](int g) { return pr0 + g < npair; });
+                transform(
+                    [&](int n, float m) {  // unit length; the zero padding selected, not multiplied
+                        const float2 v = self_term(1.f, ra[n], qx, qy, qz);
+                        return m != 0.f ? v : make_float2(0.f, 0.f);
+                    },
+                    [&](int g) { return pr0 + g < npair; }, b * b);
                 d0 += NW * G;
                 while (d0 >= nd) {
                     d0 -= nd;
@@ -1402,7 +1412,7 @@ __global__ void __launch_bounds__(kReg2Warps * 32, 3) reg2_fft_kernel(CorrLaunch
                 const float2 v = src[n];
                 return make_float2(v.x * (m * mm), v.y * (m * mm));
             },
-                      [&](int g) { return s0 + g < nser; });
+                      [&](int g) { return s0 + g < nser; }, 1.f);
         }
     }
     fold();
