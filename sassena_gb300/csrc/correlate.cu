@@ -1224,7 +1224,7 @@ size_t reg2_fft_smem(int nf, bool self) {
 }
 
 template <int LG, bool SELF>
-__global__ void __launch_bounds__(kReg2Warps * 32, 3) reg2_fft_kernel(CorrLaunch a) {
+__global__ void __launch_bounds__(kReg2Warps * 32, SELF ? 2 : 3) reg2_fft_kernel(CorrLaunch a) {
     typedef Reg2Shape<LG> Sh;
     typedef Reg2Layout<LG> Ly;
     constexpr int NW = kReg2Warps, NT = NW * 32, L = Sh::L, C = Sh::C, G = Sh::G, RPL = Sh::RPL;
@@ -1284,8 +1284,8 @@ __global__ void __launch_bounds__(kReg2Warps * 32, 3) reg2_fft_kernel(CorrLaunch
         }
     };
 
-    // the warp's G series: get(n, m) is point n (< NF) of this lane's pass-1 series times
-    // m (0 for the zero padding), valid(g) whether series g exists this round, w2 this
+    // the warp's G series: get(b, n, m) is point n = col + C b (< NF) of this lane's pass-1
+    // series times m (0 for the zero padding), valid(g) whether series g exists this round, w2 this
     // lane's pass-1 series' power weight (the incoherent series are generated with unit
     // length and weighted by b^2 in the power sums: |b X|^2 = b^2 |X|^2)
     auto transform = [&](auto get, auto valid, float w2) {
@@ -1293,7 +1293,7 @@ __global__ void __launch_bounds__(kReg2Warps * 32, 3) reg2_fft_kernel(CorrLaunch
 #pragma unroll
         for (int b = 0; b < 8; ++b) {  // points beyond NF read the last point, scaled by 0
             const int n = col + C * b;
-            x[b] = get(min(n, nf - 1), n < nf ? 1.f : 0.f);
+            x[b] = get(b, min(n, nf - 1), n < nf ? 1.f : 0.f);
         }
         fold_first(x);  // first stage, upper half zero
         dif_lane<16, 0, 4, 16>(x);
@@ -1374,6 +1374,10 @@ __global__ void __launch_bounds__(kReg2Warps * 32, 3) reg2_fft_kernel(CorrLaunch
                 d0 -= nd;
                 ++at0;
             }
+            // the lane's 8 points of its atom's trajectory, kept in registers while the lane's
+            // pairs stay on that atom (consecutive rounds take the next directions)
+            float cx[8], cy[8], cz[8];
+            int cached = -1;
             for (int pr0 = warp * G; pr0 < npair; pr0 += NW * G) {
                 int at = at0, d = d0 + g1;
                 while (d >= nd) {
@@ -1388,10 +1392,20 @@ __global__ void __launch_bounds__(kReg2Warps * 32, 3) reg2_fft_kernel(CorrLaunch
                 float qx, qy, qz;
                 load_qv(sys.qv, sys.qrev, (size_t)(v0 + d), qx, qy, qz);
                 const float b = ok ? bsm[at] : 0.f;
-                const float4* ra = rj + (size_t)at * nf;
+                if (at != cached) {
+                    const float4* ra = rj + (size_t)at * nf;
+#pragma unroll
+                    for (int p = 0; p < 8; ++p) {
+                        const float4 r = ra[min(col + C * p, nf - 1)];
+                        cx[p] = r.x;
+                        cy[p] = r.y;
+                        cz[p] = r.z;
+                    }
+                    cached = at;
+                }
                 transform(
-                    [&](int n, float m) {  // unit length; the zero padding selected, not multiplied
-                        const float2 v = self_term(1.f, ra[n], qx, qy, qz);
+                    [&](int p, int, float m) {  // unit length; the zero padding selected, not multiplied
+                        const float2 v = self_term(1.f, make_float4(cx[p], cy[p], cz[p], 0.f), qx, qy, qz);
                         return m != 0.f ? v : make_float2(0.f, 0.f);
                     },
                     [&](int g) { return pr0 + g < npair; }, b * b);
@@ -1408,7 +1422,7 @@ __global__ void __launch_bounds__(kReg2Warps * 32, 3) reg2_fft_kernel(CorrLaunch
             const bool mine = s0 + g1 < nser;
             const float mm = mine ? 1.f : 0.f;
             const float2* src = reinterpret_cast<const float2*>(sys.A) + (size_t)(c.v_begin + (mine ? s0 + g1 : 0)) * nf;
-            transform([&](int n, float m) {
+            transform([&](int, int n, float m) {
                 const float2 v = src[n];
                 return make_float2(v.x * (m * mm), v.y * (m * mm));
             },
