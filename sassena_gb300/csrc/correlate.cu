@@ -519,7 +519,25 @@ __global__ void __launch_bounds__(NT) finalize_kernel(FinalLaunch a) {
     if (a.dsp == DSP_AUTOCORRELATE) {
         const int L = 1 << e.lg;
         double2* buf = reinterpret_cast<double2*>(smem);
-        for (int i = threadIdx.x; i < L; i += NT) buf[i] = make_double2(slot_sum(part + i, e.part_len, ns, e.f32pair), 0.0);
+        if (L < NT) {
+            // fewer bins than threads: G = NT / L threads per bin, each summing a contiguous
+            // range of the slots; the G partial sums are then added in range order (a short
+            // series' shell otherwise left most threads idle while a quarter of them walked
+            // every slot: 112 chunk slots of the 256-point incoherent spectra)
+            double* gp = reinterpret_cast<double*>(smem + ((size_t)1 << a.lg_max) * sizeof(double2));
+            const int G = NT / L, i = threadIdx.x % L, g = threadIdx.x / L;
+            const int s0 = (int)((long long)ns * g / G), s1 = (int)((long long)ns * (g + 1) / G);
+            gp[threadIdx.x] = slot_sum(part + (size_t)s0 * e.part_len + i, e.part_len, s1 - s0, e.f32pair);
+            __syncthreads();
+            if (threadIdx.x < L) {
+                double v = 0.0;
+                for (int k = 0; k < G; ++k) v += gp[k * L + threadIdx.x];
+                buf[threadIdx.x] = make_double2(v, 0.0);
+            }
+        } else {
+            for (int i = threadIdx.x; i < L; i += NT)
+                buf[i] = make_double2(slot_sum(part + i, e.part_len, ns, e.f32pair), 0.0);
+        }
         __syncthreads();
         dit_inverse<NT>(buf, a.tw, e.lg, a.lg_max - e.lg);
         for (int t = threadIdx.x; t < nf; t += NT) {
@@ -1863,8 +1881,9 @@ cudaError_t launch_self_accumulate(const CorrLaunch& a, cudaStream_t st) { retur
 
 cudaError_t launch_finalize(const FinalLaunch& a, cudaStream_t st) {
     if (a.nentries == 0) return cudaSuccess;
-    const size_t sm = a.dsp == DSP_AUTOCORRELATE ? ((size_t)1 << a.lg_max) * sizeof(double2) : 0;
     constexpr int NT = 1024;  // one CTA per shell: as many threads as a CTA takes
+    // the spectrum, then one FP64 partial sum per thread (short series)
+    const size_t sm = a.dsp == DSP_AUTOCORRELATE ? ((size_t)1 << a.lg_max) * sizeof(double2) + NT * sizeof(double) : 0;
     auto k = finalize_kernel<NT>;
     cudaError_t e = set_smem(k, sm);
     if (e != cudaSuccess) return e;
