@@ -309,6 +309,7 @@ int set_system_classes(SystemState& s, const int32_t* cls, bool on_device, cudaS
     ECK(cudaStreamSynchronize(st));
     s.h_cls.assign(h.begin(), h.begin() + s.na);
     s.classes_set = true;
+    ++s.class_gen;
     s.rec_map_ok = s.rec_ready = s.rec_valid = false;
     s.mp_valid = false;  // the cylinder representation carries the classes
     return kOk;
@@ -461,13 +462,79 @@ int ensure_rec_layout(SystemState& s, std::string& err) {
 }  // namespace
 
 void Engine::release() {
+    key_.clear();
     DevBuf* bufs[] = {&blob_,    &bfac_, &amp_, &part_,  &ppart_, &apart_,
                       &a2part_, &counter_, &err_, &tw64_, &tw32_, &rec_bfac_};
     for (DevBuf* b : bufs) b->release();
     hblob_.release();
 }
 
+// Everything the descriptors depend on: the configuration and, per item, the system (its
+// class assignment's generation, its staged buffers, the staging's centre and whether the
+// class-sorted copy holds the staged frames), the sub-vector offsets, the product structure
+// and every device pointer. The contents behind the device pointers (coordinates,
+// sub-vectors, factors, weights) are read by the kernels at enqueue, not here, so a new
+// staging of the same system with the same centre keeps the descriptors.
+static std::vector<uint64_t> prepare_key(const EngineConfig& c, const std::vector<WorkItem>& items) {
+    std::vector<uint64_t> k;
+    auto u = [&](uint64_t v) { k.push_back(v); };
+    auto p = [&](const void* v) { k.push_back((uint64_t)(uintptr_t)v); };
+    auto d = [&](double v) {
+        uint64_t b;
+        memcpy(&b, &v, sizeof(b));
+        k.push_back(b);
+    };
+    u((uint64_t)c.scattering);
+    u((uint64_t)c.dsp);
+    u((uint64_t)c.method);
+    u((uint64_t)c.precision);
+    u((uint64_t)(uint32_t)c.shape.q_per_lane);
+    u((uint64_t)(uint32_t)c.shape.warps);
+    u((uint64_t)(uint32_t)c.shape.atoms);
+    u((uint64_t)(uint32_t)c.shape.poly_pairs);
+    u((uint64_t)(uint32_t)c.split_atoms);
+    u((uint64_t)(uint32_t)c.rec_k);
+    u((uint64_t)(uint32_t)c.device);
+    u(items.size());
+    for (const WorkItem& it : items) {
+        p(it.sys);
+        if (it.sys) {
+            const SystemState& s = *it.sys;
+            u(s.class_gen);
+            u((uint64_t)s.staged | (uint64_t)s.classes_set << 1 | (uint64_t)s.rec_valid << 2 |
+              (uint64_t)s.rec_map_ok << 3 | (uint64_t)s.rec_ready << 4);
+            for (int c3 = 0; c3 < 3; ++c3) d(s.center[c3]);
+            p(s.xyz.p);
+            p(s.xyz_rec.p);
+            p(s.block_class.p);
+            p(s.cls.p);
+            u(s.na_rec);
+        }
+        u(it.offs.size());
+        for (size_t o : it.offs) u(o);
+        u(it.lam.size());
+        for (double l : it.lam) d(l);
+        u((uint64_t)(int64_t)it.lam_base);
+        for (const void* q : {(const void*)it.d_qv, (const void*)it.d_cf, (const void*)it.d_fqt,
+                              (const void*)it.d_fq, (const void*)it.d_fq2, (const void*)it.d_wsqrt,
+                              (const void*)it.d_fqt_w, (const void*)it.d_fq_w, (const void*)it.d_fq2_w,
+                              (const void*)it.d_amp_given})
+            p(q);
+        d(it.norm);
+    }
+    return k;
+}
+
 int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items, std::string& err) {
+    std::vector<uint64_t> key = prepare_key(cfg, items);
+    if (!key_.empty() && key == key_) return kOk;
+    key_.clear();
+    const int rc = prepare_full(cfg, items, err);
+    if (rc == kOk) key_ = std::move(key);
+    return rc;
+}
+
+int Engine::prepare_full(const EngineConfig& cfg, const std::vector<WorkItem>& items, std::string& err) {
     cfg_ = cfg;
     stats_ = EngineStats();
     const bool f32 = cfg.precision == PREC_FP32;

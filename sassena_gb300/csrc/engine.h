@@ -47,6 +47,7 @@ struct SystemState {
     double center[3] = {0, 0, 0};
     DevBuf raw, xyz, cls, tw64, tw32, k64, k32;
     bool staged = false, classes_set = false;
+    uint64_t class_gen = 0;  // counts class assignments (part of a prepared engine's key)
     // frames to copy ahead into `raw` (prefetch_system, issue_prefetch): the host buffer, the
     // event that completes the copy once issued (null: not issued yet), and the buffer this
     // library page-locked for it (null: none)
@@ -146,11 +147,15 @@ public:
     int enqueue(cudaStream_t st, std::string& err, cudaEvent_t* events = nullptr);
     const EngineStats& stats() const { return stats_; }
     unsigned int* err_word() const { return err_.as<unsigned int>(); }
+    // prepare() calls after the first with the same configuration and items (same inputs,
+    // outputs and system generations) keep the descriptors and skip the host work
     // the amplitudes of item i after enqueue() (coherent): float2 (FP32) or double2 [nv][nf]
     const void* amplitudes(int i) const { return amp_.as<unsigned char>() + amp_off_[i]; }
     void release();
 
 private:
+    int prepare_full(const EngineConfig& cfg, const std::vector<WorkItem>& items, std::string& err);
+    std::vector<uint64_t> key_;  // what the current descriptors were built for (empty: none)
     EngineConfig cfg_;
     EngineStats stats_;
     int lg_max_ = 2, lg_min_ = 2, nf_max_ = 1, nitems_ = 0;
