@@ -526,11 +526,11 @@ static std::vector<uint64_t> prepare_key(const EngineConfig& c, const std::vecto
 }
 
 int Engine::prepare(const EngineConfig& cfg, const std::vector<WorkItem>& items, std::string& err) {
-    std::vector<uint64_t> key = prepare_key(cfg, items);
-    if (!key_.empty() && key == key_) return kOk;
+    if (!key_.empty() && prepare_key(cfg, items) == key_) return kOk;
     key_.clear();
     const int rc = prepare_full(cfg, items, err);
-    if (rc == kOk) key_ = std::move(key);
+    // taken after the preparation, which may build the class-sorted copy of a system
+    if (rc == kOk) key_ = prepare_key(cfg, items);
     return rc;
 }
 

@@ -272,3 +272,36 @@ def test_out_of_memory_is_a_status(native_lib):
         assert p.lib.sass_plan_error(p._h)
     w = synth.small("all", "autocorrelate", seed=18, na=20, nf=9, nq=2, nm=3)
     check(w, "fp64", "fftw")
+
+
+@pytest.mark.parametrize("scattering", ["all", "self"])
+def test_repeated_calls_follow_new_inputs(native_lib, scattering):
+    # A call with the same q-vector layout as the previous one reuses the engine's
+    # descriptors; new class factors, new sub-vector values, a new staging or new classes
+    # must still reach the result. Each call is compared bit for bit with a fresh plan.
+    import dataclasses
+
+    w1 = synth.small(scattering, "autocorrelate", seed=61, na=200, nf=30, nq=4, nm=12)
+    w2 = dataclasses.replace(w1, class_factors=w1.class_factors * 1.5 + 0.25)
+    w3 = dataclasses.replace(w1, directions=synth.sphere_directions(w1.nm, 62))
+    w4 = dataclasses.replace(synth.small(scattering, "autocorrelate", seed=63, na=200, nf=30, nq=4, nm=12),
+                             shells=w1.shells, directions=w1.directions, class_factors=w1.class_factors,
+                             atom_class=w1.atom_class)
+    w5 = dataclasses.replace(w4, atom_class=np.roll(w4.atom_class, 7))
+
+    def fresh(w, precision):
+        return abi.compute_workload(w, precision)
+
+    for precision in ("fp64", "fp32"):
+        with abi.Plan(w1.na, w1.nf, len(w1.class_names), scattering, "autocorrelate", "fftw", precision) as p:
+            p.stage(w1.coords)
+            p.set_classes(w1.atom_class)
+            for w, restage, reclass in ((w1, False, False), (w1, False, False), (w2, False, False),
+                                        (w3, False, False), (w4, True, False), (w5, False, True)):
+                if restage:
+                    p.stage(w.coords)
+                if reclass:
+                    p.set_classes(w.atom_class)
+                got = p.compute(w.sub_offsets(), w.subvectors(), np.ascontiguousarray(w.class_factors))
+                for a, b in zip(got, fresh(w, precision)):
+                    np.testing.assert_array_equal(a, b)
