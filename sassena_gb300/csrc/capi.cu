@@ -533,14 +533,14 @@ int sass_compute(sass_plan* p, size_t nq, const size_t* offs, const double* subv
             rc = issue_prefetch(p->sys, p->side, p->pf_done, p->msg);
             if (rc) return rc;
         }
-        CK(p->msg, cudaEventSynchronize(p->ev[3]));
+        // one host synchronisation: the error word's copy drains the stream, events included
+        rc = read_err_word(p->msg, p->eng.err_word(), p->st);
+        if (rc) return rc;
         p->timing.phase_ms += ev_ms(p->ev[0], p->ev[1]);
         p->timing.corr_ms += ev_ms(p->ev[1], p->ev[2]);
         p->timing.finalize_ms += ev_ms(p->ev[2], p->ev[3]);
         p->timing.kernel_launches += p->eng.stats().launches;
         p->timing.phase_launches += p->eng.stats().phase_launches;
-        rc = read_err_word(p->msg, p->eng.err_word(), p->st);
-        if (rc) return rc;
         i = j;
     }
     CK(p->msg, cudaEventRecord(p->ev[6], p->st));
