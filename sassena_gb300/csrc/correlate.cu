@@ -1129,7 +1129,7 @@ struct Reg2Shape {
     static constexpr int GS = 16 * S + 2 * C;    // words per series
     static constexpr int WW = G * GS;            // words per warp
     static constexpr int FOLD = 8;               // rounds of plain FP32 power sums between Kahan folds
-    static constexpr int NAS = LG >= 8 ? 4 : 8;  // atoms staged per barrier (three CTAs per SM fit)
+    static constexpr int NAS = LG >= 8 ? 4 : 8;  // atoms staged per barrier (shared memory of three CTAs per SM)
 };
 
 __host__ __device__ constexpr int brev_bits(int v, int bits) {
