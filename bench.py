@@ -359,6 +359,16 @@ def run_reference(args, dist):
                               "sample of the workload; ms_per_full_step_extrapolated scales it by terms"}))
 
 
+def profile_traffic(kernel, workload):
+    """DRAM bytes per launch of `kernel` on `workload` from its ncu capture
+    (profiles/<kernel>_<workload>.json), or None where none was taken."""
+    prof = os.path.join(ROOT, "profiles", "%s_%s.json" % (kernel, workload))
+    if not os.path.exists(prof):
+        return None
+    with open(prof) as f:
+        return json.load(f).get("dram_bytes_per_launch")
+
+
 def phase_roofline(w, sch, phase_ms, corr_ms, sfu, fma):
     """Roofline of the step's dominant kernel against its live-measured ceiling.
 
@@ -376,18 +386,14 @@ def phase_roofline(w, sch, phase_ms, corr_ms, sfu, fma):
         achieved = terms / (corr_ms * 1e-3)
         return {"bound": "fp32" if 2.0 * fma / flops_per_term < sfu / 2.0 else "sfu",
                 "achieved": achieved, "peak": peak, "unit": "terms/s", "frac": achieved / peak,
-                "traffic": None, "kernel": kernel, "kernel_ms": corr_ms,
+                "traffic": profile_traffic(kernel, w.name), "kernel": kernel, "kernel_ms": corr_ms,
                 "peak_source": "measured live: sass_probe_pipes FP32 %.4g FMA/s x 2 / %.1f FFT "
                                "flops per term; SFU %.4g results/s / 2" % (fma, flops_per_term, sfu),
                 "schedule": sch}
     achieved = terms / (phase_ms * 1e-3)
     rec_only = sch["rec_tiles"] > 0 and sch["direct_tiles"] == 0
     kernel = "phase_rec_kernel" if rec_only else "phase_sum_kernel"
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "%s_%s.json" % (kernel, w.name))
-    if os.path.exists(prof):
-        with open(prof) as f:
-            traffic = json.load(f).get("dram_bytes_per_launch")
+    traffic = profile_traffic(kernel, w.name)
     if rec_only:
         # per term at least one FMA per component (recurrence) and one FADD per component
         # (accumulation) on the FP32 pipe: 4 lane operations
