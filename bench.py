@@ -359,6 +359,19 @@ def run_reference(args, dist):
                               "sample of the workload; ms_per_full_step_extrapolated scales it by terms"}))
 
 
+def hbm_peak():
+    """HBM GB/s for the correlation's roofline: the measured copy bandwidth in
+    MEASURED_PEAKS.json where the file is present, else 6,800 GB/s (an earlier GB300
+    measurement, reported as the fallback)."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            v = json.load(f).get("hbm_gbs")
+        if v:
+            return float(v), "of measured (MEASURED_PEAKS.json hbm_gbs, STREAM-style copy)"
+    return 6800.0, "of fallback (6.8 TB/s)"
+
+
 def profile_traffic(kernel, workload):
     """DRAM bytes per launch of `kernel` on `workload` from its ncu capture
     (profiles/<kernel>_<workload>.json), or None where none was taken."""
@@ -634,8 +647,11 @@ def run_ours(args, dist):
         corr_kernel = "blk_fft_kernel"
     else:
         corr_kernel = "corr_fft_kernel" if w.scattering == "all" else "self_fft_kernel"
+    hbm, hbm_src = hbm_peak()
     roof_corr = {"bound": "hbm", "kernel": corr_kernel + "+finalize_kernel", "ms": corr,
-                 "achieved": corr_bytes / (corr * 1e-3) / 1e9, "unit": "GB/s"}
+                 "achieved": corr_bytes / (corr * 1e-3) / 1e9, "unit": "GB/s", "peak": hbm,
+                 "frac": corr_bytes / (corr * 1e-3) / 1e9 / hbm, "peak_source": hbm_src,
+                 "algorithmic_bytes": corr_bytes}
     if w.scattering == "self":  # series generated inside the FFT kernel: no amplitudes in HBM
         roof_corr = {"kernel": roof["kernel"] + "+finalize_kernel", "ms": corr,
                      "note": "fused with the series generation; its roofline is `roofline`"}
