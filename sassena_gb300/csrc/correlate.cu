@@ -610,10 +610,22 @@ __global__ void store_kernel_kernel(const double2* __restrict__ tw, int lg_tw, d
     }
 }
 
+// x - (h + l) rounded to FP32: s + e = x - h exactly (TwoSum), then s + (e - l)
+__device__ __forceinline__ float centred(float x, float h, float l) {
+    const float s = __fsub_rn(x, h), bb = __fsub_rn(s, x);
+    const float e = __fadd_rn(__fsub_rn(x, __fsub_rn(s, bb)), __fsub_rn(-h, bb));
+    return __fadd_rn(s, __fsub_rn(e, l));
+}
+
 __global__ void stage_kernel(const float* __restrict__ raw, int nf, int na, int na_pad, double cx,
                              double cy, double cz, int center, float4* __restrict__ xyz,
                              const int* __restrict__ rec_inv, int na_rec, float4* __restrict__ xyz_rec) {
     const size_t n = (size_t)nf * na_pad;
+    // the centre as float pairs hi + lo: x - c is formed by TwoSum in FP32 and rounded once
+    // (per coordinate an FP64 subtraction and two conversions made this kernel bound by
+    // GB300's narrow FP64 pipe once its input came from device memory)
+    const float hx = (float)cx, hy = (float)cy, hz = (float)cz;
+    const float lx = (float)(cx - (double)hx), ly = (float)(cy - (double)hy), lz = (float)(cz - (double)hz);
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n;
          idx += (size_t)gridDim.x * blockDim.x) {
         const size_t f = idx / na_pad;
@@ -622,9 +634,9 @@ __global__ void stage_kernel(const float* __restrict__ raw, int nf, int na, int 
         if (j < na) {
             const float* p = raw + (f * na + j) * 3;
             if (center) {
-                r.x = (float)((double)p[0] - cx);
-                r.y = (float)((double)p[1] - cy);
-                r.z = (float)((double)p[2] - cz);
+                r.x = centred(p[0], hx, lx);
+                r.y = centred(p[1], hy, ly);
+                r.z = centred(p[2], hz, lz);
             } else {
                 r.x = p[0];
                 r.y = p[1];

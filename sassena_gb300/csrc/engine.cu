@@ -769,7 +769,7 @@ int Engine::prepare_full(const EngineConfig& cfg, const std::vector<WorkItem>& i
         if (coherent && !it.d_amp_given) {
             if (nsplit_[i] > 1) {
                 unsigned char* part = part_.as<unsigned char>() + part_off_[i];
-                if (f32) {  // FP32 partials (8 bytes per frame), summed in FP64 by the reduction
+                if (f32) {  // FP32 partials (8 bytes per frame), summed in float-float by the reduction
                     p.out = nullptr;
                     p.out_f32 = reinterpret_cast<float2*>(part);
                     split_part32_[i] = reinterpret_cast<float2*>(part);

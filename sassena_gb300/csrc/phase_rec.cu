@@ -238,8 +238,10 @@ __global__ void __launch_bounds__(kRecWarps * 32, K <= 20 ? 2 : 1) phase_rec_ker
                 for (int k = 0; k < K; ++k) {
                     if (k >= gr.ks) break;
                     const float4 st = ks_all[k * 32];
-                    const double re = (double)st.x - (double)st.z, im = (double)st.y - (double)st.w;
-                    dst[k * row_stride] = make_float2((float)re, (float)im);
+                    // sum minus compensation, rounded once in FP32 (through FP64 these two
+                    // subtractions and six conversions per value made every tile's epilogue
+                    // wait about 9 us on GB300's narrow FP64 pipe)
+                    dst[k * row_stride] = make_float2(__fsub_rn(st.x, st.z), __fsub_rn(st.y, st.w));
                 }
             }
         }

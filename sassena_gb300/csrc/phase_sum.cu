@@ -114,6 +114,8 @@ struct Fp32Acc {
     __device__ double2 result(int k) const {
         return make_double2((double)sr[k] - (double)cr[k], (double)si[k] - (double)ci[k]);
     }
+    // the FP32 output: sum minus compensation rounded once, on the FP32 pipe
+    __device__ float2 result_f32(int k) const { return make_float2(__fsub_rn(sr[k], cr[k]), __fsub_rn(si[k], ci[k])); }
 };
 
 // sin and cos of 2 pi f for a pair of reduced angles f in [-1/2, 1/2] revolutions on the
@@ -220,6 +222,12 @@ struct Fp32PairAcc {
         const float s_r = (k & 1) ? sr[j].y : sr[j].x, c_r = (k & 1) ? cr[j].y : cr[j].x;
         const float s_i = (k & 1) ? si[j].y : si[j].x, c_i = (k & 1) ? ci[j].y : ci[j].x;
         return make_double2((double)s_r - (double)c_r, (double)s_i - (double)c_i);
+    }
+    __device__ float2 result_f32(int k) const {
+        const int j = k >> 1;
+        const float s_r = (k & 1) ? sr[j].y : sr[j].x, c_r = (k & 1) ? cr[j].y : cr[j].x;
+        const float s_i = (k & 1) ? si[j].y : si[j].x, c_i = (k & 1) ? ci[j].y : ci[j].x;
+        return make_float2(__fsub_rn(s_r, c_r), __fsub_rn(s_i, c_i));
     }
 };
 
@@ -353,19 +361,22 @@ __global__ void __launch_bounds__(W * 32)
         }
 
         __syncthreads();  // every pipeline of this tile is drained: the ring becomes staging
+        if constexpr (F32) {
+            // FP32 amplitudes or FP32 split partials (the FP32 form always writes FP32):
+            // results formed and staged in FP32
+            float2* so32 = reinterpret_cast<float2*>(smem);
 #pragma unroll
-        for (int k = 0; k < Q; ++k) so[(lane + 32 * k) * W + warp] = acc.result(k);
-        __syncthreads();
-        if (F32 && sys.out_f32) {
+            for (int k = 0; k < Q; ++k) so32[(lane + 32 * k) * W + warp] = acc.result_f32(k);
+            __syncthreads();
             float2* dst = sys.out_f32 + (size_t)td.split * sys.split_stride;
             for (int idx = threadIdx.x; idx < td.nv * W; idx += W * 32) {
                 int vl = idx / W, w = idx - vl * W, ff = td.f0 + w;
-                if (ff < sys.nf) {
-                    double2 v = so[vl * W + w];
-                    dst[(size_t)(td.v0 + vl) * sys.nf + ff] = make_float2((float)v.x, (float)v.y);
-                }
+                if (ff < sys.nf) dst[(size_t)(td.v0 + vl) * sys.nf + ff] = so32[vl * W + w];
             }
         } else {
+#pragma unroll
+            for (int k = 0; k < Q; ++k) so[(lane + 32 * k) * W + warp] = acc.result(k);
+            __syncthreads();
             double2* dst = sys.out + (size_t)td.split * sys.split_stride;
             for (int idx = threadIdx.x; idx < td.nv * W; idx += W * 32) {
                 int vl = idx / W, w = idx - vl * W, ff = td.f0 + w;
@@ -401,19 +412,33 @@ __global__ void split_reduce_kernel(const double2* __restrict__ part, int nsplit
     }
 }
 
-// FP32 form: the partials are FP32 pairs, summed in FP64 in split order.
+// s + e = a + b exactly (Knuth's TwoSum), in FP32
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// FP32 form: the partials are FP32 pairs, summed in split order in float-float arithmetic
+// (TwoSum, the rounding errors gathered in a low word) and rounded once to FP32: the sum
+// of two partials is the correctly rounded FP32 sum. On GB300 the FP64 adds and
+// conversions this took before bounded the kernel on the narrow FP64 pipe (0.15 ms for the
+// coherent workload's 2 x 82 MB of partials, a quarter of HBM bandwidth).
 __global__ void split_reduce32_kernel(const float2* __restrict__ part, int nsplit, size_t n,
                                      float2* __restrict__ out) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
          i += (size_t)gridDim.x * blockDim.x) {
         const float2 p0 = part[i];
-        double ax = p0.x, ay = p0.y;
+        float hx = p0.x, hy = p0.y, lx = 0.f, ly = 0.f;
         for (int s = 1; s < nsplit; ++s) {
             const float2 b = part[(size_t)s * n + i];
-            ax += b.x;
-            ay += b.y;
+            float ex, ey;
+            two_sum(hx, b.x, hx, ex);
+            two_sum(hy, b.y, hy, ey);
+            lx = __fadd_rn(lx, ex);
+            ly = __fadd_rn(ly, ey);
         }
-        out[i] = make_float2((float)ax, (float)ay);
+        out[i] = make_float2(__fadd_rn(hx, lx), __fadd_rn(hy, ly));
     }
 }
 
