@@ -339,6 +339,9 @@ def test_prefetched_frames_stage_the_same_bits(native_lib):
             p.stage(pinned)
             same(p.compute(*args), plain1)
             p.prefetch(pinned)  # pending when the plan is destroyed
+            arg_error = {name: code for code, name in abi.STATUS.items()}["SASS_ERR_ARG"]
+            assert lib.sass_prefetch_frames(p._h, None) == arg_error
+            assert lib.sass_prefetch_frames(None, pinned.ctypes.data) == arg_error
         finally:
             p.close()
             lib.sass_host_free(hp)
