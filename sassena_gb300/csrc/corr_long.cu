@@ -24,13 +24,97 @@ namespace sassgpu {
 //                conj twiddles, W_L^{-n2 k1}, columns), FP64, normalised as the short path.
 // Spectra stay in (k1, bit-reversed k2) order; K is built in that order by the same passes.
 // ---------------------------------------------------------------------------------------
+
+// ---------------------------------------------------------------------------------------
+// Float-float arithmetic for the FP32 form's long transforms. A value is h + l with
+// |l| <= ulp(h) / 2; additions use Knuth's TwoSum, products the FMA-exact product (Dekker's
+// method with the FMA instruction), each renormalised once ("sloppy" addition: absolute
+// error about 2^-44 (|a| + |b|), the bound FFT butterflies need). These run on the FP32
+// pipe: GB300's FP64 pipe made the FP64 transforms of this path its bound.
+// ---------------------------------------------------------------------------------------
+struct ffs {
+    float h, l;
+    ffs() = default;
+    __device__ __forceinline__ ffs(float v) : h(v), l(0.f) {}
+    __device__ __forceinline__ ffs(float hi, float lo) : h(hi), l(lo) {}
+    __device__ __forceinline__ explicit operator double() const { return (double)h + (double)l; }
+};
+struct __align__(16) ff2 {
+    ffs x, y;
+};
+
+__device__ __forceinline__ ffs ff_renorm(float s, float e) {
+    const float h = __fadd_rn(s, e);
+    return ffs(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
+__device__ __forceinline__ ffs operator+(ffs a, ffs b) {
+    const float s = __fadd_rn(a.h, b.h), bb = __fsub_rn(s, a.h);
+    float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
+    e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+    return ff_renorm(s, e);
+}
+__device__ __forceinline__ ffs operator-(ffs a) { return ffs(-a.h, -a.l); }
+__device__ __forceinline__ ffs operator-(ffs a, ffs b) { return a + (-b); }
+__device__ __forceinline__ ffs operator*(ffs a, ffs b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return ff_renorm(p, e);
+}
+__device__ __forceinline__ ffs& operator+=(ffs& a, ffs b) { return a = a + b; }
+__device__ __forceinline__ ffs ff_from(double v) {
+    const float h = (float)v;
+    return ffs(h, (float)(v - (double)h));
+}
+
+template <>
+struct cplx<ffs> {
+    typedef ff2 type;
+};
+__device__ __forceinline__ ff2 make_ff2(ffs x, ffs y) {
+    ff2 r;
+    r.x = x;
+    r.y = y;
+    return r;
+}
+__device__ __forceinline__ ff2 cadd(ff2 a, ff2 b) { return make_ff2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ ff2 csub(ff2 a, ff2 b) { return make_ff2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ ff2 cmul(ff2 a, ff2 b) {
+    return make_ff2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
 namespace {
+
+template <>
+__device__ __forceinline__ ff2 zero2<ff2>() {
+    return make_ff2(ffs(0.f), ffs(0.f));
+}
+
+// power spectrum accumulator of the float-float transforms (float-float sums)
+template <int MAXR>
+struct PowerAcc<ffs, MAXR> {
+    ffs s[MAXR];
+    __device__ void clear() {
+#pragma unroll
+        for (int r = 0; r < MAXR; ++r) s[r] = ffs(0.f);
+    }
+    __device__ __forceinline__ void add(int r, ffs p) { s[r] += p; }
+    __device__ double get(int r) const { return (double)s[r]; }
+};
+
+// float-float tables from the FP64 ones
+__global__ void to_ff2_kernel(const double2* __restrict__ src, size_t n, ff2* __restrict__ dst) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = make_ff2(ff_from(src[i].x), ff_from(src[i].y));
+}
 
 constexpr int kLongC = 1 << kLongRowLg;
 constexpr int kLongTile = 16;  // columns per CTA in the column passes
 constexpr int kLongNT = 256;
 
 __device__ __forceinline__ float2 cneg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ ff2 cneg(ff2 a) { return make_ff2(-a.x, -a.y); }
+__device__ __forceinline__ ff2 cconj(ff2 a) { return make_ff2(a.x, -a.y); }
 __device__ __forceinline__ double2 cneg(double2 a) { return make_double2(-a.x, -a.y); }
 __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
 __device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
@@ -49,6 +133,8 @@ __device__ __forceinline__ float2 as_t2(float2 x, float2) { return x; }
 __device__ __forceinline__ double2 as_t2(float2 x, double2) { return make_double2(x.x, x.y); }
 __device__ __forceinline__ double2 as_t2(double2 x, double2) { return x; }
 __device__ __forceinline__ float2 as_t2(double2 x, float2) { return make_float2((float)x.x, (float)x.y); }
+__device__ __forceinline__ ff2 as_t2(float2 x, ff2) { return make_ff2(ffs(x.x), ffs(x.y)); }
+__device__ __forceinline__ ff2 as_t2(double2 x, ff2) { return make_ff2(ff_from(x.x), ff_from(x.y)); }
 
 template <class T, class AT2>
 __global__ void __launch_bounds__(kLongNT) long_col_kernel(LongArgs a) {
@@ -251,12 +337,14 @@ __global__ void long_k32_kernel(const double2* k64, int L, float2* k32) {
         k32[i] = make_float2((float)k64[i].x, (float)k64[i].y);
 }
 
+size_t long_elem(int precision) { return precision == PREC_FP32 ? sizeof(float2) : precision == PREC_FF ? sizeof(ff2) : sizeof(double2); }
+
 size_t long_col_smem(int precision, int lg) {
-    return (size_t)kLongTile * ((size_t)1 << (lg - kLongRowLg)) * (precision == PREC_FP32 ? sizeof(float2) : sizeof(double2));
+    return (size_t)kLongTile * ((size_t)1 << (lg - kLongRowLg)) * long_elem(precision);
 }
 
 size_t long_row_smem(int precision) {
-    const size_t e = precision == PREC_FP32 ? sizeof(float2) : sizeof(double2);
+    const size_t e = long_elem(precision);
     return (size_t)kLongC * e + (size_t)(kLongC / 2) * e + (kLongNT / 32) * sizeof(double2);
 }
 
@@ -270,6 +358,7 @@ cudaError_t launch_long_columns(const LongArgs& a, cudaStream_t st) {
     const size_t sm = long_col_smem(a.precision, a.lg);
     dim3 grid(kLongC / kLongTile, (unsigned)a.nseries);
     auto k = a.precision == PREC_FP32 ? (a.amp_f32 ? long_col_kernel<float, float2> : long_col_kernel<float, double2>)
+             : a.precision == PREC_FF ? (a.amp_f32 ? long_col_kernel<ffs, float2> : long_col_kernel<ffs, double2>)
                                       : (a.amp_f32 ? long_col_kernel<double, float2> : long_col_kernel<double, double2>);
     cudaError_t e = set_smem(k, sm);
     if (e != cudaSuccess) return e;
@@ -287,6 +376,10 @@ cudaError_t launch_long_rows(const LongArgs& a, cudaStream_t st) {
         cudaError_t e = set_smem(long_row_kernel<float, 0>, sm);
         if (e != cudaSuccess) return e;
         long_row_kernel<float, 0><<<grid, kLongNT, sm, st>>>(a);
+    } else if (a.precision == PREC_FF) {
+        cudaError_t e = set_smem(long_row_kernel<ffs, 0>, sm);
+        if (e != cudaSuccess) return e;
+        long_row_kernel<ffs, 0><<<grid, kLongNT, sm, st>>>(a);
     } else {
         cudaError_t e = set_smem(long_row_kernel<double, 0>, sm);
         if (e != cudaSuccess) return e;
@@ -343,6 +436,12 @@ cudaError_t launch_long_finalize(const LongFinal& a, cudaStream_t st) {
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     return cudaSuccess;
+}
+
+cudaError_t launch_to_ff2(const double2* src, size_t n, void* dst, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    to_ff2_kernel<<<grid_for(n, 256), 256, 0, st>>>(src, n, static_cast<ff2*>(dst));
+    return cudaGetLastError();
 }
 
 cudaError_t launch_long_store_kernel(const double2* tw64, int lg, int nf, double2* scratch, double2* k64,

@@ -98,6 +98,11 @@ int build_system_tables(SystemState& s, cudaStream_t st, std::string& err) {
         ECK(scratch.ensure((s.nf + L) * sizeof(double2)));
         ECK(launch_long_store_kernel(s.tw64.as<double2>(), s.lg, (int)s.nf, scratch.as<double2>(),
                                      s.k64.as<double2>(), s.k32.as<float2>(), st));
+        // float-float copies for the FP32 form's long transforms
+        ECK(s.twff.ensure(L / 2 * 16));
+        ECK(s.kff.ensure(L * 16));
+        ECK(launch_to_ff2(s.tw64.as<double2>(), L / 2, s.twff.p, st));
+        ECK(launch_to_ff2(s.k64.as<double2>(), L, s.kff.p, st));
         ECK(cudaStreamSynchronize(st));
         return kOk;
     }
@@ -951,7 +956,7 @@ int Engine::prepare_full(const EngineConfig& cfg, const std::vector<WorkItem>& i
         const WorkItem& it = items[i];
         SystemState& s = *it.sys;
         const size_t L = (size_t)1 << s.lg, R = L >> kLongRowLg, nq = it.offs.size() - 1;
-        const size_t esz = sizeof(double2);  // FP64 transforms (see enqueue)
+        const size_t esz = sizeof(double2);  // FP64 or float-float transforms: 16 bytes a value (see enqueue)
         const size_t gsz = f32 ? sizeof(float2) : sizeof(double2);
         // incoherent: the (atom, direction) series are generated per batch next to Y
         const size_t S = std::max<size_t>(1, kLongScratchBytes / (L * esz + (coherent ? 0 : s.nf * gsz)));
@@ -1166,10 +1171,11 @@ int Engine::enqueue(cudaStream_t st, std::string& err, cudaEvent_t* ev) {
         const size_t esz = f32 ? sizeof(float2) : sizeof(double2);
         for (int b = li.batch_begin; b < li.batch_end; ++b) {
             const LongBatch& lb = long_batches_[b];
-            // the transforms run in FP64 in both forms: the 1/(NF - tau) normalisation
-            // amplifies transform rounding at large lags in proportion to NF
+            // The transforms need more than FP32: the 1/(NF - tau) normalisation amplifies
+            // transform rounding at large lags in proportion to NF. The FP64 form runs them in
+            // FP64, the FP32 form in float-float on the FP32 pipe (about 44 bits).
             LongArgs la{};
-            la.precision = PREC_FP64;
+            la.precision = f32 ? PREC_FF : PREC_FP64;
             la.amp_f32 = f32;
             la.lg = s.lg;
             la.nf = (int)s.nf;
@@ -1194,11 +1200,11 @@ int Engine::enqueue(cudaStream_t st, std::string& err, cudaEvent_t* ev) {
             }
             la.Y = long_Y_.p;
             la.nseries = lb.v1 - lb.v0;
-            la.tw = s.tw64.p;
+            la.tw = f32 ? s.twff.p : s.tw64.p;
             la.chunks = d_long_chunks_ + lb.chunk_begin;
             la.nchunks = lb.chunk_end - lb.chunk_begin;
             la.v0 = lb.v0;
-            la.kbr = s.k64.p;
+            la.kbr = f32 ? s.kff.p : s.k64.p;
             la.ppart = ppart_.as<double>();
             la.mpart = long_mpart_.as<double2>() + li.mpart_off;
             ECK(launch_long_columns(la, st));

@@ -46,6 +46,7 @@ struct SystemState {
     int lg = 0;  // padded FFT length 2^lg >= 2 nf
     double center[3] = {0, 0, 0};
     DevBuf raw, xyz, cls, tw64, tw32, k64, k32;
+    DevBuf twff, kff;  // long series: float-float twiddles [L/2] and store kernel [L] (16 B each)
     bool staged = false, classes_set = false;
     uint64_t class_gen = 0;  // counts class assignments (part of a prepared engine's key)
     // frames to copy ahead into `raw` (prefetch_system, issue_prefetch): the host buffer, the

@@ -36,6 +36,9 @@ inline unsigned grid_blocks(size_t n, int threads, int per_sm) {
 }
 
 enum Precision { PREC_FP64 = 0, PREC_FP32 = 1 };
+// Transform arithmetic of the long-series path beyond the two forms: float-float (a value
+// as an unevaluated sum of two floats, about 44 significant bits) on the FP32 pipe.
+constexpr int PREC_FF = 2;
 
 // Device-side error codes written to the plan's error word (first writer wins).
 enum DeviceError : unsigned int {
@@ -258,6 +261,9 @@ struct LongArgs {
     double2* mpart;            // [nv][R] row parts of the series means
     void* xout;                // transform mode: conj(X) in the long order (T2)
 };
+// Float-float copy (16 bytes per complex value) of an FP64 table: the twiddles and the store
+// kernel of the long path's float-float transforms.
+cudaError_t launch_to_ff2(const double2* src, size_t n, void* dst, cudaStream_t st);
 // Column pass over the batch's series; row pass over its chunks (power, means).
 cudaError_t launch_long_columns(const LongArgs& a, cudaStream_t st);
 cudaError_t launch_long_rows(const LongArgs& a, cudaStream_t st);
