@@ -985,7 +985,11 @@ int Engine::prepare_full(const EngineConfig& cfg, const std::vector<WorkItem>& i
             const size_t units = coherent ? nm : s.na * nm;
             const size_t first = coherent ? it.offs[sh] : vbase;
             vbase += units;
-            const size_t len = std::min(S, (units + std::min(per, units) - 1) / std::min(per, units));
+            // chunks short enough that one batch of S series also fills the GPU: the row
+            // pass launches R CTAs per chunk of the batch (at 16,384 frames, chunks of 250
+            // series left 128 CTAs per launch on 152 SMs)
+            const size_t fill = std::max<size_t>(1, S * R / (2 * (size_t)sms));
+            const size_t len = std::min(std::min(S, fill), (units + std::min(per, units) - 1) / std::min(per, units));
             for (size_t u = 0; u < units; u += len) {
                 CorrChunk c{};
                 c.system = (int)i;
